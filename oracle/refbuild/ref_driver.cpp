@@ -1,0 +1,294 @@
+// Driver around the reference's own global-placement sources.
+//
+// TEST INFRASTRUCTURE ONLY (never shipped, never linked into the product).
+// It is compiled together with the reference's unchanged
+// src/placerBase.cpp, src/nesterovBase.cpp, src/nesterovPlace.cpp,
+// src/fft.cpp, src/fftsg.cpp, src/fftsg2d.cpp, src/logger.cpp and
+// src/point.cpp (see Makefile) and an in-memory OpenDB stand-in (opendb/db.h).
+//
+// Modes
+//   place <net.txt> [options]          Replace::doNesterovPlace after the
+//                                      centre placement that
+//                                      InitialPlace::placeInstsCenter does
+//                                      (src/initialPlace.cpp:108-115) when the
+//                                      initial place runs zero iterations.
+//   eval  <net.txt> <out.bin> [opts]   one NesterovBase evaluation at seeded
+//                                      random gcell centres (or the initial
+//                                      density centres with --init-coords):
+//                                      bin areas, density, phi, field, per-gcell
+//                                      WA and density gradients, HPWL.
+//
+// Options: --density d  --bins n  --idp p (init density penalty)  --iwc c
+//          --minphi m --maxphi m --overflow o --maxiter n --incremental
+//          --verbose v --seed s --init-coords --wlcoef c --out-pos file
+//          --reverse-iterms
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <memory>
+#include <random>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "opendb/db.h"
+#include "placerBase.h"
+#include "nesterovBase.h"
+#include "nesterovPlace.h"
+#include "logger.h"
+#include "point.h"
+
+using namespace replace;
+
+struct Opts {
+  float density = 0.7f;
+  int bins = 0;
+  float idp = 0.00008f;
+  float iwc = 0.25f;
+  float minphi = 0.95f, maxphi = 1.05f;
+  float overflow = 0.1f;
+  int maxiter = 2000;
+  bool incremental = false;
+  int verbose = 0;
+  unsigned seed = 1;
+  bool init_coords = false;
+  float wlcoef = -1.0f;
+  std::string out_pos;
+};
+
+static odb::dbDatabase* read_net(const char* path) {
+  std::ifstream in(path);
+  if (!in) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+  std::string tag;
+  auto db = new odb::dbDatabase();
+  db->tech = new odb::dbTech();
+  db->chip = new odb::dbChip();
+  auto blk = new odb::dbBlock();
+  db->chip->block = blk;
+  auto site = new odb::dbSite();
+  int nrows = 0, ninst = 0, nnet = 0;
+  in >> tag;  // REFNET
+  int ver; in >> ver;
+  in >> tag >> db->tech->dbu;                       // DBU
+  in >> tag >> site->w >> site->h;                  // SITE
+  in >> tag >> blk->bbox.xl >> blk->bbox.yl >> blk->bbox.xh >> blk->bbox.yh;  // DIE
+  in >> tag >> nrows;                               // ROWS
+  for (int i = 0; i < nrows; i++) {
+    auto r = new odb::dbRow();
+    in >> r->box.xl_ >> r->box.yl_ >> r->box.xh_ >> r->box.yh_;
+    r->site = site;
+    blk->rows.push_back(r);
+  }
+  in >> tag >> ninst;                               // INSTS
+  std::vector<std::vector<std::pair<int, odb::dbITerm*>>> inst_terms(ninst);
+  for (int i = 0; i < ninst; i++) {
+    auto inst = new odb::dbInst();
+    int st;
+    inst->master = new odb::dbMaster();
+    in >> inst->x >> inst->y >> inst->w >> inst->h >> inst->master->w >> inst->master->h >> st;
+    inst->status = st ? odb::dbPlacementStatus::FIRM : odb::dbPlacementStatus::NONE;
+    inst->bbox = odb::dbBox(inst->x, inst->y, inst->x + inst->w, inst->y + inst->h);
+    blk->insts.push_back(inst);
+  }
+  in >> tag >> nnet;                                // NETS
+  for (int n = 0; n < nnet; n++) {
+    auto net = new odb::dbNet();
+    int sig, ni, nb;
+    in >> sig >> ni >> nb;
+    net->sig = (odb::dbSigType::Value)sig;
+    for (int k = 0; k < ni; k++) {
+      int inst, key, has, xl, yl, xh, yh;
+      in >> inst >> key >> has >> xl >> yl >> xh >> yh;
+      auto it = new odb::dbITerm();
+      it->inst = blk->insts[inst];
+      it->mterm = new odb::dbMTerm();
+      if (has) {
+        auto mp = new odb::dbMPin();
+        mp->boxes.push_back(new odb::dbBox(xl, yl, xh, yh));
+        it->mterm->mpins.push_back(mp);
+      }
+      net->iterms.push_back(it);
+      inst_terms[inst].push_back({key, it});
+    }
+    for (int k = 0; k < nb; k++) {
+      int has, xl, yl, xh, yh;
+      in >> has >> xl >> yl >> xh >> yh;
+      auto bt = new odb::dbBTerm();
+      bt->name = "io" + std::to_string(n) + "_" + std::to_string(k);
+      if (has) {
+        auto bp = new odb::dbBPin();
+        bp->box = odb::dbBox(xl, yl, xh, yh);
+        bt->bpins.push_back(bp);
+      }
+      net->bterms.push_back(bt);
+    }
+    blk->nets.push_back(net);
+  }
+  // instance iterm order = master pin order (stable by key)
+  for (int i = 0; i < ninst; i++) {
+    auto& v = inst_terms[i];
+    std::stable_sort(v.begin(), v.end(),
+                     [](const std::pair<int, odb::dbITerm*>& a,
+                        const std::pair<int, odb::dbITerm*>& b) { return a.first < b.first; });
+    for (auto& p : v) blk->insts[i]->iterms.push_back(p.second);
+  }
+  return db;
+}
+
+static void parse_opts(int argc, char** argv, int start, Opts& o) {
+  for (int i = start; i < argc; i++) {
+    std::string a = argv[i];
+    auto nxt = [&]() { return std::string(argv[++i]); };
+    if (a == "--density") o.density = std::stof(nxt());
+    else if (a == "--bins") o.bins = std::stoi(nxt());
+    else if (a == "--idp") o.idp = std::stof(nxt());
+    else if (a == "--iwc") o.iwc = std::stof(nxt());
+    else if (a == "--minphi") o.minphi = std::stof(nxt());
+    else if (a == "--maxphi") o.maxphi = std::stof(nxt());
+    else if (a == "--overflow") o.overflow = std::stof(nxt());
+    else if (a == "--maxiter") o.maxiter = std::stoi(nxt());
+    else if (a == "--incremental") o.incremental = true;
+    else if (a == "--verbose") o.verbose = std::stoi(nxt());
+    else if (a == "--seed") o.seed = (unsigned)std::stoul(nxt());
+    else if (a == "--init-coords") o.init_coords = true;
+    else if (a == "--wlcoef") o.wlcoef = std::stof(nxt());
+    else if (a == "--out-pos") o.out_pos = nxt();
+    else { fprintf(stderr, "unknown option %s\n", a.c_str()); exit(2); }
+  }
+}
+
+// InitialPlace::placeInstsCenter (src/initialPlace.cpp:108-115)
+static void place_center(PlacerBase& pb) {
+  const int cx = pb.die().coreCx();
+  const int cy = pb.die().coreCy();
+  for (auto& inst : pb.placeInsts()) inst->setCenterLocation(cx, cy);
+}
+
+static NesterovBaseVars nb_vars(const Opts& o) {
+  NesterovBaseVars v;
+  v.targetDensity = o.density;
+  if (o.bins) { v.isSetBinCntX = 1; v.binCntX = o.bins; v.isSetBinCntY = 1; v.binCntY = o.bins; }
+  return v;
+}
+
+template <class T>
+static void put(FILE* f, const char* name, const char* dt, const std::vector<T>& v) {
+  fprintf(f, "%s %s %zu\n", name, dt, v.size());
+  fwrite(v.data(), sizeof(T), v.size(), f);
+  fprintf(f, "\n");
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) { fprintf(stderr, "usage: ref_driver place|eval net.txt ...\n"); return 2; }
+  std::string mode = argv[1];
+  odb::dbDatabase* db = read_net(argv[2]);
+  Opts o;
+  if (mode == "place") {
+    parse_opts(argc, argv, 3, o);
+    auto log = std::make_shared<Logger>("REPL", o.verbose);
+    auto pb = std::make_shared<PlacerBase>(db, log);
+    if (!o.incremental) place_center(*pb);
+    auto nb = std::make_shared<NesterovBase>(nb_vars(o), pb, log);
+    NesterovPlaceVars npv;
+    npv.minPhiCoef = o.minphi;
+    npv.maxPhiCoef = o.maxphi;
+    npv.initDensityPenalty = o.idp;
+    npv.initWireLengthCoef = o.iwc;
+    npv.targetOverflow = o.overflow;
+    npv.maxNesterovIter = o.maxiter;
+    NesterovPlace np(npv, pb, nb, log);
+    np.doNesterovPlace();
+    if (!o.out_pos.empty()) {
+      FILE* f = fopen(o.out_pos.c_str(), "w");
+      for (auto* inst : db->chip->block->insts) fprintf(f, "%d %d\n", inst->x, inst->y);
+      fclose(f);
+    }
+    return 0;
+  }
+  if (mode == "eval") {
+    const char* out = argv[3];
+    parse_opts(argc, argv, 4, o);
+    auto log = std::make_shared<Logger>("REPL", o.verbose);
+    auto pb = std::make_shared<PlacerBase>(db, log);
+    if (!o.incremental) place_center(*pb);
+    auto nb = std::make_shared<NesterovBase>(nb_vars(o), pb, log);
+    const auto& gcells = nb->gCells();
+    const int ng = (int)gcells.size();
+    std::vector<FloatPoint> coords(ng);
+    std::mt19937 rng(o.seed);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    std::vector<int32_t> ginfo;   // per gcell: lx ly ux uy dLx dLy dUx dUy kind
+    std::vector<float> gscale;
+    for (int i = 0; i < ng; i++) {
+      GCell* g = gcells[i];
+      nb->updateDensityCoordiLayoutInside(g);
+      ginfo.insert(ginfo.end(), {g->lx(), g->ly(), g->ux(), g->uy(),
+                                 g->dLx(), g->dLy(), g->dUx(), g->dUy(),
+                                 g->isFiller() ? 2 : (g->isMacroInstance() ? 1 : 0)});
+      gscale.push_back(g->densityScale());
+      if (o.init_coords) {
+        coords[i] = FloatPoint(g->dCx(), g->dCy());
+      } else {
+        const Die& die = pb->die();
+        double ddx = g->dDx(), ddy = g->dDy();
+        double x = die.coreLx() + ddx / 2 + U(rng) * (die.coreDx() - ddx);
+        double y = die.coreLy() + ddy / 2 + U(rng) * (die.coreDy() - ddy);
+        coords[i] = FloatPoint((float)x, (float)y);
+      }
+    }
+    nb->updateGCellDensityCenterLocation(coords);
+    nb->updateDensityForceBin();
+    float wl = o.wlcoef > 0 ? o.wlcoef : 1.0f / (0.5f * (nb->binSizeX() + nb->binSizeY()));
+    nb->updateWireLengthForceWA(wl, wl);
+    std::vector<float> xy(2 * ng), wlg(2 * ng), dg(2 * ng);
+    std::vector<int32_t> drect;
+    for (int i = 0; i < ng; i++) {
+      GCell* g = gcells[i];
+      xy[2 * i] = coords[i].x; xy[2 * i + 1] = coords[i].y;
+      FloatPoint a = nb->getWireLengthGradientWA(g, wl, wl);
+      FloatPoint b = nb->getDensityGradient(g);
+      wlg[2 * i] = a.x; wlg[2 * i + 1] = a.y;
+      dg[2 * i] = b.x; dg[2 * i + 1] = b.y;
+      drect.insert(drect.end(), {g->dLx(), g->dLy(), g->dUx(), g->dUy()});
+    }
+    std::vector<int64_t> inst_a, fill_a, np_a;
+    std::vector<float> dens, phi, ex, ey;
+    for (auto* bin : nb->bins()) {
+      inst_a.push_back(bin->instPlacedArea());
+      fill_a.push_back(bin->fillerArea());
+      np_a.push_back(bin->nonPlaceArea());
+      dens.push_back(bin->density());
+      phi.push_back(bin->electroPhi());
+      ex.push_back(bin->electroForceX());
+      ey.push_back(bin->electroForceY());
+    }
+    std::vector<int32_t> grid = {nb->binCntX(), nb->binCntY(), nb->binSizeX(), nb->binSizeY()};
+    std::vector<int64_t> scal = {nb->overflowArea(), nb->getHpwl(), pb->stdInstsArea(),
+                                 pb->macroInstsArea(), pb->nonPlaceInstsArea(),
+                                 (int64_t)gcells.size(), (int64_t)nb->gCellFillers().size()};
+    std::vector<float> fscal = {nb->sumPhi(), wl};
+    FILE* f = fopen(out, "wb");
+    put(f, "grid", "i4", grid);
+    put(f, "scalars", "i8", scal);
+    put(f, "fscalars", "f4", fscal);
+    put(f, "ginfo", "i4", ginfo);
+    put(f, "gscale", "f4", gscale);
+    put(f, "coords", "f4", xy);
+    put(f, "drect", "i4", drect);
+    put(f, "wl_grad", "f4", wlg);
+    put(f, "density_grad", "f4", dg);
+    put(f, "inst_area", "i8", inst_a);
+    put(f, "filler_area", "i8", fill_a);
+    put(f, "nonplace_area", "i8", np_a);
+    put(f, "density", "f4", dens);
+    put(f, "phi", "f4", phi);
+    put(f, "ex", "f4", ex);
+    put(f, "ey", "f4", ey);
+    fclose(f);
+    return 0;
+  }
+  fprintf(stderr, "unknown mode %s\n", mode.c_str());
+  return 2;
+}
