@@ -1,0 +1,261 @@
+/*
+ * gpl.h - C ABI of the GB300 global-placement core (libgpl_gb300.so).
+ *
+ * The library is a drop-in for RePlAce's electrostatic global placement:
+ * the initial place (B2B + BiCGSTAB) and the Nesterov loop.  Each entry point
+ * below names the reference interface it replaces (paths are relative to the
+ * RePlAce source tree).  Signatures use plain C types and pointers only.
+ *
+ * Ownership: every pointer argument is caller-owned host memory that is read
+ * (or written) during the call only, unless the comment says "device".  A job
+ * owns all the device memory it allocates; gpl_destroy releases it.
+ * Threading: one job must not be used from two threads at once; distinct jobs
+ * are independent.  Errors: every call returns a gpl_status; the reference's
+ * Logger::error exit codes (src/logger.cpp:31-36) become status values with
+ * the same numbers, and gpl_last_error() gives the message.  Nothing here
+ * calls exit().
+ */
+#ifndef GPL_GB300_GPL_H
+#define GPL_GB300_GPL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPL_ABI_VERSION 1
+
+typedef enum gpl_status {
+  GPL_OK = 0,
+  /* Negative filler area: NesterovBase::initFillerGCells, code 1
+   * (src/nesterovBase.cpp:1116-1121). */
+  GPL_ERR_FILLER_AREA = 1,
+  /* NaN/Inf gradient sums during NesterovPlace::init, code 2
+   * (src/nesterovPlace.cpp:280-284). */
+  GPL_ERR_DIVERGED_INIT = 2,
+  /* Back-tracking ran out (maxBackTrack), code 3 (src/nesterovPlace.cpp:404-409). */
+  GPL_ERR_DIVERGED_BACKTRACK = 3,
+  /* Overflow went up while HPWL blew up, code 4 (src/nesterovPlace.cpp:448-456). */
+  GPL_ERR_DIVERGED_PHI = 4,
+  /* Placeable area above 100.1 % of free core area: PlacerBase::printInfo
+   * exits with 1 (src/placerBase.cpp:952-956). */
+  GPL_ERR_UTIL = 5,
+  /* NaN/Inf gradient sums inside the Nesterov loop; the reference reports
+   * this through Logger::error with code 0 (src/nesterovPlace.cpp:371-374,
+   * 469-471). */
+  GPL_ERR_DIVERGED_NAN = 6,
+  GPL_ERR_INVALID_ARG = 16,
+  GPL_ERR_CUDA = 17,
+  GPL_ERR_OUT_OF_MEMORY = 18,
+  GPL_ERR_BAD_STATE = 19,
+  GPL_ERR_NO_DEVICE = 20
+} gpl_status;
+
+/* Instance kinds (PlacerBase::init, src/placerBase.cpp:639-680). */
+enum {
+  GPL_INST_PLACE = 0,    /* movable */
+  GPL_INST_FIXED = 1,    /* fixed, overlaps the core */
+  GPL_INST_DUMMY = 2,    /* fragmented-row dummy (initInstsForFragmentedRow) */
+  GPL_INST_OUTSIDE = 3   /* fixed, outside the core: ignored */
+};
+
+/*
+ * Flat netlist: the data PlacerBase (src/placerBase.h:233-312) builds from
+ * OpenDB.  Pins are net-major: net n owns pins [net_start[n], net_start[n+1]).
+ * Within a net, component pins come first, then IO pins, in
+ * dbNet::getITerms / getBTerms order.
+ */
+typedef struct gpl_netlist_desc {
+  int32_t core_lx, core_ly, core_ux, core_uy;   /* rows' bounding box */
+  int32_t site_w, site_h;
+  int32_t n_insts;
+  const int32_t* inst_lx;      /* [n_insts] bounding boxes (DBU) */
+  const int32_t* inst_ly;
+  const int32_t* inst_ux;
+  const int32_t* inst_uy;
+  const uint8_t* inst_kind;    /* GPL_INST_* */
+  int32_t n_pins;
+  const int32_t* pin_inst;     /* [n_pins] instance index, -1 for an IO port */
+  const int32_t* pin_ox;       /* offset of the pin centre from the instance centre */
+  const int32_t* pin_oy;
+  const int32_t* pin_x;        /* initial absolute pin centre */
+  const int32_t* pin_y;
+  int32_t n_nets;
+  const int32_t* net_start;    /* [n_nets + 1] */
+  /* Optional per-instance pin order (dbInst::getITerms); NULL = ascending
+   * pin index.  [n_insts + 1] and [number of component pins]. */
+  const int32_t* inst_pin_start;
+  const int32_t* inst_pins;
+} gpl_netlist_desc;
+
+/* Placement parameters: the members of replace::Replace
+ * (include/replace/Replace.h:75-93) plus the hidden InitialPlaceVars,
+ * NesterovBaseVars and NesterovPlaceVars fields, plus GB300 knobs. */
+typedef struct gpl_params {
+  /* InitialPlaceVars (src/initialPlace.h:12-23) */
+  int32_t initial_place_max_iter;          /* 20 */
+  int32_t initial_place_min_diff_length;   /* 1500 */
+  int32_t initial_place_max_solver_iter;   /* 100 */
+  int32_t initial_place_max_fanout;        /* 200 */
+  float initial_place_net_weight_scale;    /* 800 */
+  int32_t incremental_place_mode;          /* 0 */
+  /* NesterovBaseVars (src/nesterovBase.h:695-708) */
+  float target_density;                    /* 1.0 (Replace); the Tcl default is 0.7 */
+  int32_t bin_grid_cnt_x;                  /* 0 = bin-count rule */
+  int32_t bin_grid_cnt_y;
+  float min_wire_length_force_bar;         /* -300 */
+  /* NesterovPlaceVars (src/nesterovPlace.h:16-29) */
+  int32_t nesterov_place_max_iter;         /* 2000 */
+  int32_t max_back_track;                  /* 10 */
+  float init_density_penalty;              /* 0.00008 */
+  float init_wire_length_coef;             /* 0.25 */
+  float target_overflow;                   /* 0.1 */
+  float min_phi_coef;                      /* 0.95 */
+  float max_phi_coef;                      /* 1.05 */
+  float min_preconditioner;                /* 1.0 */
+  float initial_prev_coordi_update_coef;   /* 100 */
+  float reference_hpwl;                    /* 446000000 */
+  int32_t verbose_level;                   /* 0: print the reference's default log lines */
+  /* GB300 knobs */
+  int32_t device;                          /* CUDA device ordinal */
+  void* stream;                            /* cudaStream_t to run on; NULL = job-owned stream */
+  int32_t use_graph;                       /* 1 = device-resident Nesterov control in a CUDA graph */
+} gpl_params;
+
+/* Counts and grid chosen by the job (NesterovBase / BinGrid). */
+typedef struct gpl_job_info {
+  int32_t n_place_insts;
+  int32_t n_gcells;          /* movable instances followed by fillers */
+  int32_t n_fillers;
+  int32_t bin_cnt_x, bin_cnt_y;
+  int32_t bin_size_x, bin_size_y;
+  int32_t filler_dx, filler_dy;
+  int64_t place_insts_area, std_insts_area, macro_insts_area, non_place_insts_area;
+  int64_t device_bytes;      /* device memory held by the job */
+} gpl_job_info;
+
+/* One physics evaluation (the work of NesterovBase for one coordinate set). */
+typedef struct gpl_eval_stats {
+  int64_t overflow_area;     /* FP64-accumulated sum of max(0, inst+nonPlace-binArea*td), truncated */
+  double overflow_area_f64;
+  int64_t hpwl;              /* NesterovBase::getHpwl, exact int64 */
+  double sum_phi;            /* FP64 sum of phi * (nonPlace+inst+filler) */
+  double wire_length_grad_sum;   /* sum |dWL/dx| + |dWL/dy| (FP64) */
+  double density_grad_sum;       /* sum |dD/dx| + |dD/dy| (FP64) */
+} gpl_eval_stats;
+
+/* Nesterov progress (NesterovPlace::doNesterovPlace). */
+typedef struct gpl_nesterov_stats {
+  int32_t iterations;        /* iterations completed so far */
+  int32_t evaluations;       /* physics evaluations (back-track tries) so far */
+  int32_t finished;          /* 1 when the loop stopped (converged or diverged) */
+  int32_t status;            /* gpl_status of the loop: GPL_OK or a divergence code */
+  float overflow;            /* sumOverflow_ */
+  float step_length;
+  float density_penalty;
+  float wire_length_coef;
+  int64_t hpwl;              /* prevHpwl_ */
+} gpl_nesterov_stats;
+
+/* Optional per-iteration log (may be NULL); the call appends up to capacity. */
+typedef struct gpl_iter_log {
+  int32_t capacity;
+  int32_t count;
+  float* overflow;           /* [capacity] */
+  int64_t* hpwl;             /* [capacity] */
+  float* step_length;        /* [capacity] */
+  int32_t* backtracks;       /* [capacity] number of tries in the iteration */
+} gpl_iter_log;
+
+/* Initial place progress (InitialPlace::doBicgstabPlace). */
+typedef struct gpl_ip_stats {
+  int32_t iterations;
+  float last_error;          /* max(errorX, errorY) of the last round */
+  int64_t last_hpwl;         /* PlacerBase::hpwl before the last move */
+  int32_t solver_iters_x;    /* BiCGSTAB iterations of the last round */
+  int32_t solver_iters_y;
+} gpl_ip_stats;
+
+/* Library identity and the last error message of the calling thread. */
+const char* gpl_version(void);
+const char* gpl_last_error(void);
+
+/* Defaults of replace::Replace::Replace() (src/replace.cpp:13-33) and of the
+ * Vars constructors (src/initialPlace.cpp:18-24, src/nesterovBase.cpp:875-880,
+ * src/nesterovPlace.cpp:19-29). */
+void gpl_params_default(gpl_params* params);
+
+/* Build the job: PlacerBase-level bookkeeping (areas, utilisation check) and
+ * the device copy of the netlist.  Replaces `std::make_shared<PlacerBase>(db,
+ * log)` in Replace::doInitialPlace / doNesterovPlace (src/replace.cpp:75,96). */
+gpl_status gpl_create(const gpl_netlist_desc* netlist, const gpl_params* params,
+                      struct gpl_job** job);
+void gpl_destroy(struct gpl_job* job);
+
+/* InitialPlace(ipVars, pb, log).doBicgstabPlace() (src/replace.cpp:85-87,
+ * src/initialPlace.cpp:56-105): centre the movable instances (unless
+ * incremental), then up to initial_place_max_iter B2B + BiCGSTAB rounds. */
+gpl_status gpl_initial_place(struct gpl_job* job, gpl_ip_stats* stats);
+
+/* NesterovBase(nbVars, pb, log) + NesterovPlace::init()
+ * (src/replace.cpp:112-125, src/nesterovBase.cpp:917-1062,
+ * src/nesterovPlace.cpp:64-175). */
+gpl_status gpl_nesterov_init(struct gpl_job* job, gpl_job_info* info);
+
+/* NesterovPlace::doNesterovPlace() (src/nesterovPlace.cpp:275-472), run for
+ * at most max_iters further iterations (<= 0: up to nesterov_place_max_iter).
+ * Returns GPL_OK while running or converged, or the divergence code. */
+gpl_status gpl_nesterov_run(struct gpl_job* job, int32_t max_iters,
+                            gpl_nesterov_stats* stats, gpl_iter_log* log);
+
+/* Final locations, NesterovPlace::updateDb (src/nesterovPlace.cpp:585-595):
+ * lx = dCx - dDx/2, ly = dCy - dDy/2 for movable instances; other instances
+ * keep their input location.  Arrays are [n_insts]. */
+gpl_status gpl_get_inst_locations(struct gpl_job* job, int32_t* lx, int32_t* ly);
+
+/* Current Nesterov coordinates (curSLPCoordi_) as float pairs [2 * n_gcells]. */
+gpl_status gpl_get_gcell_coords(struct gpl_job* job, float* xy);
+
+/* Gradient check hook: one evaluation at the given gcell centres
+ * (updateGCellDensityCenterLocation + updateDensityForceBin +
+ * updateWireLengthForceWA + per-gcell getWireLengthGradientWA and
+ * getDensityGradient, src/nesterovBase.cpp:1198-1506).  xy, wl_grad and
+ * density_grad are [2 * n_gcells]; the two outputs may be NULL. */
+gpl_status gpl_eval(struct gpl_job* job, const float* xy, float wl_coef_x,
+                    float wl_coef_y, float* wl_grad, float* density_grad,
+                    gpl_eval_stats* stats);
+
+/* Bin state after the last evaluation, [bin_cnt_x * bin_cnt_y] row-major by y
+ * (bin index j * bin_cnt_x + i, as BinGrid::bins()).  Any pointer may be NULL. */
+gpl_status gpl_get_bins(struct gpl_job* job, int64_t* inst_area, int64_t* filler_area,
+                        int64_t* non_place_area, float* density, float* phi,
+                        float* field_x, float* field_y);
+
+/* Per-gcell density geometry after init: density rectangle [4 * n_gcells]
+ * (dLx, dLy, dUx, dUy), density scale [n_gcells], kind [n_gcells]
+ * (0 standard cell, 1 macro, 2 filler).  Any pointer may be NULL. */
+gpl_status gpl_get_gcells(struct gpl_job* job, int32_t* drect, float* scale, uint8_t* kind);
+
+/* Electrostatic Poisson solve alone (FFT::doFFT, src/fft.cpp:112-177) on
+ * device arrays: density, phi, field_x and field_y are device pointers of
+ * [ny * nx] floats, row-major by y.  nx, ny: powers of two in [2, 4096].
+ * Scratch memory is allocated on first use per device and cached.
+ * stream: cudaStream_t (NULL = default stream). */
+gpl_status gpl_poisson_solve(int32_t nx, int32_t ny, int32_t bin_size_x,
+                             int32_t bin_size_y, const float* density, float* phi,
+                             float* field_x, float* field_y, void* stream);
+
+/* Kernel timing hook used by the benchmark: accumulates CUDA-event time of
+ * the job's kernels by class since the last reset.  names/ms/launches are
+ * [capacity]; returns the number of classes written. */
+int32_t gpl_kernel_times(struct gpl_job* job, const char** names, double* ms,
+                         int64_t* launches, int32_t capacity);
+void gpl_kernel_times_reset(struct gpl_job* job, int32_t enable);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPL_GB300_GPL_H */
