@@ -1,0 +1,283 @@
+"""Benchmark: Nesterov iterations per second on the 1M-cell / 1024x1024-bin
+synthetic placement (the reference's headline workload), one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one Nesterov iteration (all its back-tracking evaluations) of the
+placement of a seeded synthetic netlist: 1,000,000 movable cells, 1,050,000
+nets, 2,000 IO pins, target density 0.75, 1024x1024 bins.  `value` is
+iterations/s with the job resident in HBM, timed with CUDA events on the
+job's stream; `e2e` is the same metric for a whole job through the C ABI from
+host arrays (netlist upload, init, iterations, location read-back).  The
+reference arm times the CPU restatement of the reference's path (the oracle)
+on this host.  Multi-GPU runs are independent replicas (no collectives).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "1m_cells_1024bins"
+METRIC = "Nesterov iters/s @1M cells; placements/h + p99 latency @HPWL within 0.5%"
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.seek(0)
+        rows = [l.strip().split(",") for l in self.f.read().splitlines() if l.strip()]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1])); smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# Algorithmic bytes per launch group (each array touched once), for the
+# roofline of the dominant kernel.  Units: Ng gcells, Np pins, Nn nets, B bins.
+def algorithmic_bytes(kind, ng, npins, nn, nb):
+    return {
+        "density_scatter": 53 * ng + 32 * nb,
+        "poisson_rows_dct": 48 * nb,
+        "poisson_cols_solve": 12 * nb,
+        "poisson_rows_inverse": 16 * nb,
+        "wa_wirelength": 28 * npins + 8 * nn,
+        "gcell_gradient": 57 * ng + 12 * npins + 8 * nb,
+    }.get(kind)
+
+
+def cpu_baseline_sample(nl, td, bins, iters=3):
+    """Oracle (single-threaded CPU restatement) on this host: setup, init,
+    then `iters` Nesterov iterations; returns steady-state iterations/s."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    o = O.Oracle(nl, target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+                 initial_place_max_iter=0)
+    o.initial_place()
+    o.nesterov_init()
+    t1 = time.perf_counter()
+    o.nesterov_run(iters)
+    t2 = time.perf_counter()
+    return iters / (t2 - t1), t2 - t0
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    from replace_gb300 import netlist as N
+    nl, td, bins = N.generate_workload(WORKLOAD, seed=1)
+    from oracle import oracle as O
+    O.build()
+    o = O.Oracle(nl, target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+                 initial_place_max_iter=0)
+    o.initial_place()
+    o.nesterov_init()
+    o.nesterov_run(args.warmup)
+    t0 = time.perf_counter()
+    o.nesterov_run(args.steps)
+    dt = time.perf_counter() - t0
+    v = args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, 1M cells)",
+        "config": {"workload": WORKLOAD, "cells": 1_000_000, "nets": 1_050_000, "bins": "1024x1024",
+                   "target_density": td, "parallelism": "single-threaded CPU"},
+        "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} Nesterov iterations after {args.warmup} warm-up "
+                                   "iterations of the 1M-cell job (oracle restatement; the "
+                                   "reference's own build needs OpenDB/Eigen and is not on this host)"},
+        "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-iters", type=int, default=60)
+    ap.add_argument("--cpu-iters", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from replace_gb300 import Placer, netlist as N
+    from replace_gb300 import _abi
+
+    nl, td, bins = N.generate_workload(WORKLOAD, seed=1 + rank)
+    stream = torch.cuda.Stream()
+    params = _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+                                 initial_place_max_iter=0, device=local_rank,
+                                 stream=stream.cuda_stream)
+    p = Placer(nl, params)
+    p.initial_place()
+    p.nesterov_init()
+    info = p.info
+    p.nesterov_run(args.warmup)
+
+    # timed region: K iterations, resident data, CUDA events on the job stream
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+    barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    launches0 = p.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rc, st, _ = p.nesterov_run(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    launches = p.kernel_launches() - launches0
+    iters_done = st.iterations - args.warmup
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * iters_done / (ms / 1000.0)
+
+    # per-kernel CUDA-event timing over further iterations (same stream)
+    p.kernel_times_reset(True)
+    p.nesterov_run(min(args.steps, 10))
+    kt = p.kernel_times()
+    p.kernel_times_reset(False)
+    hbm, peak_kind = peaks()
+    dom = max((k for k in kt if algorithmic_bytes(k, 1, 1, 1, 1) is not None), key=lambda k: kt[k][0])
+    dom_ms, dom_launches = kt[dom]
+    bytes_per = algorithmic_bytes(dom, info.n_gcells, nl.n_pins, nl.n_nets,
+                                  info.bin_cnt_x * info.bin_cnt_y)
+    achieved = bytes_per * dom_launches / (dom_ms / 1000.0) / 1e9
+    total_ms = sum(v[0] for v in kt.values())
+    kernel_share = {k: round(v[0] / total_ms, 4) for k, v in kt.items() if v[1]}
+    p.close()
+
+    # end to end through the C ABI from host arrays
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    q = Placer(nl, _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+                                      initial_place_max_iter=0, device=local_rank))
+    q.initial_place()
+    q.nesterov_init()
+    rc2, st2, _ = q.nesterov_run(args.e2e_iters)
+    lx, ly = q.inst_locations()
+    t1 = time.perf_counter()
+    q.close()
+    e2e_iters = st2.iterations
+    e2e = e2e_iters / (t1 - t0)
+    h2d = _abi.DescHolder(nl).nbytes
+    d2h = lx.nbytes + ly.nbytes
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v_cpu, t_cpu = cpu_baseline_sample(nl, td, bins, args.cpu_iters)
+        cpu = {"value": v_cpu, "unit": "iters/s", "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_iters} Nesterov iterations of the same 1M-cell job after "
+                         f"setup and init ({t_cpu:.1f} s of single-threaded CPU work; the oracle "
+                         "restatement of the reference's path)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world,
+            "steps": iters_done, "warmup": args.warmup, "ms_per_step": ms / max(iters_done, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, 1M cells)",
+            "config": {"workload": WORKLOAD, "cells": 1_000_000, "nets": 1_050_000, "io_pins": 2000,
+                       "bins": f"{info.bin_cnt_x}x{info.bin_cnt_y}", "gcells": info.n_gcells,
+                       "pins": nl.n_pins, "target_density": td,
+                       "evals_per_iter": round((st.evaluations) / max(st.iterations, 1), 3),
+                       "l2": "inputs larger than L2 (job working set %.0f MB)" % (info.device_bytes / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e, "unit": "iters/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "note": f"one step = a whole job of {e2e_iters} iterations through the C ABI "
+                            "(netlist upload, init, iterations, location read-back)"},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "peak_kind": f"of {peak_kind}",
+                         "traffic": None, "kernel_share": kernel_share},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

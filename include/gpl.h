@@ -253,6 +253,8 @@ gpl_status gpl_poisson_solve(int32_t nx, int32_t ny, int32_t bin_size_x,
 int32_t gpl_kernel_times(struct gpl_job* job, const char** names, double* ms,
                          int64_t* launches, int32_t capacity);
 void gpl_kernel_times_reset(struct gpl_job* job, int32_t enable);
+/* Number of kernels the job has launched since the last reset. */
+int64_t gpl_kernel_launch_count(struct gpl_job* job);
 
 #ifdef __cplusplus
 }

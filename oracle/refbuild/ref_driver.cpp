@@ -21,7 +21,6 @@
 // Options: --density d  --bins n  --idp p (init density penalty)  --iwc c
 //          --minphi m --maxphi m --overflow o --maxiter n --incremental
 //          --verbose v --seed s --init-coords --wlcoef c --out-pos file
-//          --reverse-iterms
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -200,6 +199,8 @@ int main(int argc, char** argv) {
     npv.maxNesterovIter = o.maxiter;
     NesterovPlace np(npv, pb, nb, log);
     np.doNesterovPlace();
+    printf("[REF] FinalHPWL %lld\n", (long long)nb->getHpwl());
+    fflush(stdout);
     if (!o.out_pos.empty()) {
       FILE* f = fopen(o.out_pos.c_str(), "w");
       for (auto* inst : db->chip->block->insts) fprintf(f, "%d %d\n", inst->x, inst->y);

@@ -1,0 +1,11 @@
+"""GB300 global-placement core: a drop-in for RePlAce's initial place and
+Nesterov loop, computed by hand-written sm_103a kernels behind a C ABI
+(include/gpl.h, libgpl_gb300.so)."""
+
+from . import lefdef, netlist  # noqa: F401
+from ._abi import default_params  # noqa: F401
+from ._lib import GplError, load  # noqa: F401
+from .placer import Placer, Replace, global_placement, poisson_solve  # noqa: F401
+
+__all__ = ["Placer", "Replace", "global_placement", "poisson_solve", "GplError", "load",
+           "default_params", "lefdef", "netlist"]

@@ -1,0 +1,427 @@
+// Density scatter (BinGrid::updateBinsGCellDensityArea, src/nesterovBase.cpp:746-798)
+// fused with the Nesterov predictor (src/nesterovPlace.cpp:338-362), the
+// per-gcell gradient kernel (getDensityGradient :1458-1478 + the WA gradient
+// sum :1363-1375 + NesterovPlace::updateGradients src/nesterovPlace.cpp:206-273
+// + the step-length distances :555-571, 598-607), and the FP64 finalize.
+//
+// The scatter adds, per (gcell, covered bin), the truncated int64 value of
+// the float overlap area times the density scale (times the target density
+// for macros) -- the reference's exact per-contribution arithmetic.  Integer
+// addition is associative, so atomics give bit-exact, order-independent bin
+// areas.  Lanes of a warp that hit the same bin are combined first
+// (__match_any_sync), which matters when many cells sit on the same bins
+// (all cells start at the core centre).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "device_common.cuh"
+
+namespace gpl {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kBigBins = 64;        // cells covering more bins go to the big-cell kernels
+
+struct ScatterArgs {
+  BinGeom geo;
+  int n_g;
+  float td;
+  const int2* half;
+  const float* scale;
+  const uint8_t* kind;
+  // predictor
+  int predict;
+  float step, coeff;
+  const float2* cur_slp;
+  const float2* cur_sum;
+  const float2* cur_coordi;
+  float2* next_coordi;
+  float2* slp;
+  unsigned long long* area;   // inst [nb], filler [nb]
+};
+
+__device__ __forceinline__ float2 predict_one(const ScatterArgs& A, int g, int2 h) {
+  const float2 cs = A.cur_slp[g], sg = A.cur_sum[g], cc = A.cur_coordi[g];
+  float nx = __fadd_rn(cs.x, __fmul_rn(A.step, sg.x));
+  float ny = __fadd_rn(cs.y, __fmul_rn(A.step, sg.y));
+  float sx = __fadd_rn(nx, __fmul_rn(A.coeff, __fsub_rn(nx, cc.x)));
+  float sy = __fadd_rn(ny, __fmul_rn(A.coeff, __fsub_rn(ny, cc.y)));
+  const BinGeom& G = A.geo;
+  A.next_coordi[g] = make_float2(inside(nx, h.x, G.core_lx, G.core_ux), inside(ny, h.y, G.core_ly, G.core_uy));
+  float2 s = make_float2(inside(sx, h.x, G.core_lx, G.core_ux), inside(sy, h.y, G.core_ly, G.core_uy));
+  A.slp[g] = s;
+  return s;
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
+  __shared__ long long vals[kBlock];
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const BinGeom& G = A.geo;
+  const int nb = G.cnt_x * G.cnt_y;
+  int x0 = 0, x1 = 0, y0 = 0, y1 = 0, lx = 0, ux = 0, ly = 0, uy = 0;
+  int cnt = 0, k = 0;
+  float sc = 0.0f;
+  if (g < A.n_g) {
+    const int2 h = A.half[g];
+    const float2 c = A.predict ? predict_one(A, g, h) : A.slp[g];
+    k = A.kind[g];
+    density_rect(c, h, lx, ux, ly, uy);
+    G.range(lx, ux, ly, uy, x0, x1, y0, y1);
+    cnt = (x1 > x0 && y1 > y0) ? (x1 - x0) * (y1 - y0) : 0;
+    if (k & 4) cnt = 0;            // big cell: handled by k_scatter_big
+    sc = A.scale[g];
+  }
+  const int nbx = max(x1 - x0, 1);
+  const int maxc = __reduce_max_sync(0xffffffffu, cnt);
+  for (int t = 0; t < maxc; t++) {
+    int key = -1;
+    long long v = 0;
+    if (t < cnt) {
+      const int a = x0 + t % nbx, cc = y0 + t / nbx;
+      const float ov = G.overlap(a, cc, lx, ux, ly, uy);
+      float f = __fmul_rn(ov, sc);
+      if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
+      v = (long long)f;
+      key = ((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    vals[threadIdx.x] = v;
+    __syncwarp();
+    if (key >= 0 && lane == __ffs(peers) - 1) {
+      long long s = 0;
+      for (unsigned m = peers; m; m &= m - 1) s += vals[(threadIdx.x & ~31) + __ffs(m) - 1];
+      if (s) atomicAdd(&A.area[key], (unsigned long long)s);
+    }
+    __syncwarp();
+  }
+}
+
+// One block per big cell (macros): threads stride over its bins.
+__global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int32_t* big, int n_big) {
+  const int g = big[blockIdx.x];
+  const BinGeom& G = A.geo;
+  const int nb = G.cnt_x * G.cnt_y;
+  const int2 h = A.half[g];
+  // k_scatter has already written this cell's predicted coordinates; the
+  // block recomputes them with the same arithmetic instead of reading them
+  float2 c;
+  if (A.predict) {
+    __shared__ float2 cs;
+    if (threadIdx.x == 0) cs = predict_one(A, g, h);
+    __syncthreads();
+    c = cs;
+  } else {
+    c = A.slp[g];
+  }
+  int lx, ux, ly, uy, x0, x1, y0, y1;
+  density_rect(c, h, lx, ux, ly, uy);
+  G.range(lx, ux, ly, uy, x0, x1, y0, y1);
+  if (x1 <= x0 || y1 <= y0) return;
+  const int nbx = x1 - x0, total = nbx * (y1 - y0);
+  const int k = A.kind[g];
+  const float sc = A.scale[g];
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int a = x0 + t % nbx, cc = y0 + t / nbx;
+    float f = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
+    if ((k & 3) == 1) f = __fmul_rn(f, A.td);
+    const long long v = (long long)f;
+    if (v) atomicAdd(&A.area[((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a], (unsigned long long)v);
+  }
+}
+
+struct CellArgs {
+  BinGeom geo;
+  int n_g;
+  const int2* half;
+  const float* scale;
+  const uint8_t* kind;
+  const float2* slp;          // evaluated coordinates
+  const float2* field;        // (Ex, Ey) per bin
+  const int32_t* g_pin_start;
+  const int32_t* g_pins;
+  const float2* pin_grad;
+  const float2* precond;      // (#pins, dx*dy)
+  const int32_t* big_idx;
+  float2* d_big;
+  float density_penalty;
+  float min_precond;
+  float2* sum_out;
+  float2* wl_out;
+  float2* d_out;
+  const float2* ref_slp;
+  const float2* ref_sum;
+  double* part;               // [kPartSlots][stride]
+  int stride;
+};
+
+// Density gradient of one big cell, reduced over a block (fixed tree order).
+__global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t* big, int n_big) {
+  __shared__ float sx[kBlock], sy[kBlock];
+  const int g = big[blockIdx.x];
+  const BinGeom& G = A.geo;
+  int lx, ux, ly, uy, x0, x1, y0, y1;
+  density_rect(A.slp[g], A.half[g], lx, ux, ly, uy);
+  G.range(lx, ux, ly, uy, x0, x1, y0, y1);
+  const int nbx = max(x1 - x0, 0), total = nbx * max(y1 - y0, 0);
+  const float sc = A.scale[g];
+  float ex = 0.0f, ey = 0.0f;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int a = x0 + t % nbx, cc = y0 + t / nbx;
+    const float ov = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
+    const float2 f = A.field[cc * G.cnt_x + a];
+    ex = __fadd_rn(ex, __fmul_rn(ov, f.x));
+    ey = __fadd_rn(ey, __fmul_rn(ov, f.y));
+  }
+  sx[threadIdx.x] = ex; sy[threadIdx.x] = ey;
+  __syncthreads();
+  for (int s = kBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) { sx[threadIdx.x] += sx[threadIdx.x + s]; sy[threadIdx.x] += sy[threadIdx.x + s]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) A.d_big[blockIdx.x] = make_float2(sx[0], sy[0]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
+  __shared__ double sh[32 * 5];
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // |wl|, |d|, coord dist^2, grad dist^2, nan
+  if (g < A.n_g) {
+    const BinGeom& G = A.geo;
+    const float2 c = A.slp[g];
+    const int k = A.kind[g];
+    // density gradient: sum over covered bins of overlap * scale * field
+    float2 d = make_float2(0.0f, 0.0f);
+    if (k & 4) {
+      d = A.d_big[A.big_idx[g]];
+    } else {
+      int lx, ux, ly, uy, x0, x1, y0, y1;
+      density_rect(c, A.half[g], lx, ux, ly, uy);
+      G.range(lx, ux, ly, uy, x0, x1, y0, y1);
+      const float sc = A.scale[g];
+      for (int a = x0; a < x1; a++) {
+        for (int cc = y0; cc < y1; cc++) {
+          const float ov = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
+          const float2 f = __ldg(&A.field[cc * G.cnt_x + a]);
+          d.x = __fadd_rn(d.x, __fmul_rn(ov, f.x));
+          d.y = __fadd_rn(d.y, __fmul_rn(ov, f.y));
+        }
+      }
+    }
+    // WA gradient: the cell's pins in instance pin order
+    float2 w = make_float2(0.0f, 0.0f);
+    const int ps = A.g_pin_start[g], pe = A.g_pin_start[g + 1];
+    for (int t = ps; t < pe; t++) {
+      const float2 pg = A.pin_grad[A.g_pins[t]];
+      w.x = __fadd_rn(w.x, pg.x);
+      w.y = __fadd_rn(w.y, pg.y);
+    }
+    const float lam = A.density_penalty;
+    float2 s = make_float2(__fadd_rn(w.x, __fmul_rn(lam, d.x)), __fadd_rn(w.y, __fmul_rn(lam, d.y)));
+    const float2 pc = A.precond[g];
+    float px = __fadd_rn(pc.x, __fmul_rn(lam, pc.y));
+    float py = px;
+    if (px <= A.min_precond) px = A.min_precond;
+    if (py <= A.min_precond) py = A.min_precond;
+    s.x = __fdiv_rn(s.x, px);
+    s.y = __fdiv_rn(s.y, py);
+    if (A.sum_out) A.sum_out[g] = s;
+    if (A.wl_out) A.wl_out[g] = w;
+    if (A.d_out) A.d_out[g] = d;
+    acc[0] = fabs((double)w.x) + fabs((double)w.y);
+    acc[1] = fabs((double)d.x) + fabs((double)d.y);
+    if (A.ref_slp) {
+      const float2 r = A.ref_slp[g], q = A.ref_sum[g];
+      const double dx = (double)c.x - r.x, dy = (double)c.y - r.y;
+      const double gx = (double)s.x - q.x, gy = (double)s.y - q.y;
+      acc[2] = dx * dx + dy * dy;
+      acc[3] = gx * gx + gy * gy;
+    }
+    if (!isfinite(acc[0]) || !isfinite(acc[1])) acc[4] = 1.0;
+  }
+  block_reduce_n<5>(acc, A.part + (size_t)kPartWl * A.stride, A.stride, sh);
+}
+
+struct FinalArgs {
+  const double* part;
+  const long long* part_i;
+  int stride;
+  int n_ovf_blocks, n_cell_blocks, n_phi_blocks, n_net_blocks;
+  int n_g;
+  EvalResult* out;
+};
+
+// Deterministic FP64 reductions of the per-block partials (fixed order).
+__global__ void __launch_bounds__(1024) k_finalize(FinalArgs F) {
+  __shared__ double sh[32];
+  __shared__ long long shl[32];
+  __shared__ double res[kPartSlots];
+  for (int slot = 0; slot < kPartSlots; slot++) {
+    const int n = slot == kPartOverflow ? F.n_ovf_blocks
+                                        : (slot == kPartPhi ? F.n_phi_blocks : F.n_cell_blocks);
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += F.part[(size_t)slot * F.stride + i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      v = sh[threadIdx.x];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (threadIdx.x == 0) res[slot] = v;
+    }
+    __syncthreads();
+  }
+  long long h = 0;
+  for (int i = threadIdx.x; i < F.n_net_blocks; i += blockDim.x) h += F.part_i[i];
+  for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+  if ((threadIdx.x & 31) == 0) shl[threadIdx.x >> 5] = h;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+    for (int w = 0; w < 32; w++) t += shl[w];
+    EvalResult r;
+    r.overflow = res[kPartOverflow];
+    r.wl_sum = res[kPartWl];
+    r.d_sum = res[kPartD];
+    r.coord_dist = res[kPartCoordDist];
+    r.grad_dist = res[kPartGradDist];
+    r.sum_phi = res[kPartPhi];
+    r.nan_flag = res[kPartNan];
+    r.hpwl = t;
+    // getStepLength / getDistance (src/nesterovPlace.cpp:555-571, 598-607)
+    const float cd = (float)sqrt(r.coord_dist / (2.0 * F.n_g));
+    const float gd = (float)sqrt(r.grad_dist / (2.0 * F.n_g));
+    r.new_step_length = cd / gd;
+    r.pad = 0;
+    *F.out = r;
+  }
+}
+
+// sum over bins of phi * (nonPlace + inst + filler) in FP64
+// (NesterovBase::updateDensityForceBin, src/nesterovBase.cpp:1494-1505)
+__global__ void __launch_bounds__(kBlock) k_sum_phi(const float* phi, const unsigned long long* area,
+                                                   const int64_t* nonplace, int nb, double* part) {
+  __shared__ double sh[32];
+  double v[1] = {0.0};
+  for (int b = blockIdx.x * kBlock + threadIdx.x; b < nb; b += gridDim.x * kBlock)
+    v[0] += (double)phi[b] * (double)(nonplace[b] + (long long)area[b] + (long long)area[nb + b]);
+  block_reduce_n<1>(v, part, 0, sh);
+}
+
+BinGeom geom(const DeviceModel& d) {
+  BinGeom G;
+  G.core_lx = d.core_lx; G.core_ly = d.core_ly; G.core_ux = d.core_ux; G.core_uy = d.core_uy;
+  G.size_x = d.size_x; G.size_y = d.size_y; G.cnt_x = d.cnt_x; G.cnt_y = d.cnt_y;
+  return G;
+}
+
+}  // namespace
+
+int cell_blocks(const DeviceModel& d) { return (d.n_g + kBlock - 1) / kBlock; }
+
+int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+  ScatterArgs A;
+  A.geo = geom(d);
+  A.n_g = d.n_g;
+  A.td = d.target_density;
+  A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
+  A.predict = a.predict ? 1 : 0;
+  A.step = a.step; A.coeff = a.coeff;
+  A.cur_slp = a.cur_slp; A.cur_sum = a.cur_sum; A.cur_coordi = a.cur_coordi;
+  A.next_coordi = a.next_coordi; A.slp = a.slp;
+  A.area = d.area[d.area_cur];
+  t.begin(kKScatter);
+  k_scatter<<<cell_blocks(d), kBlock, 0, s>>>(A);
+  if (d.n_big) k_scatter_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
+  t.end(kKScatter);
+  t.count(d.n_big ? 2 : 1);
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
+int launch_cell(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+  CellArgs A;
+  A.geo = geom(d);
+  A.n_g = d.n_g;
+  A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
+  A.slp = a.slp;
+  A.field = d.field;
+  A.g_pin_start = d.g_pin_start; A.g_pins = d.g_pins;
+  A.pin_grad = d.pin_grad;
+  A.precond = d.g_precond;
+  A.big_idx = d.g_big_idx; A.d_big = d.d_big;
+  A.density_penalty = a.density_penalty;
+  A.min_precond = a.min_precond;
+  A.sum_out = a.sum_out;
+  A.wl_out = d.wl_out; A.d_out = d.d_out;
+  A.ref_slp = a.ref_slp; A.ref_sum = a.ref_sum;
+  A.part = d.part;
+  A.stride = d.part_stride;
+  t.begin(kKCell);
+  if (d.n_big) k_dgrad_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
+  k_cell<<<cell_blocks(d), kBlock, 0, s>>>(A);
+  t.end(kKCell);
+  t.count(d.n_big ? 2 : 1);
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
+int launch_finalize(DeviceModel& d, int n_ovf_blocks, int n_cell_blocks, int n_phi_blocks,
+                    int n_net_blocks, cudaStream_t s, Timer& t) {
+  FinalArgs F;
+  F.part = d.part; F.part_i = d.part_i;
+  F.stride = d.part_stride;
+  F.n_ovf_blocks = n_ovf_blocks; F.n_cell_blocks = n_cell_blocks;
+  F.n_phi_blocks = n_phi_blocks; F.n_net_blocks = n_net_blocks;
+  F.n_g = d.n_g;
+  F.out = d.result;
+  t.begin(kKReduce);
+  k_finalize<<<1, 1024, 0, s>>>(F);
+  t.end(kKReduce);
+  t.count(1);
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
+namespace {
+// updateInitialPrevSLPCoordi (src/nesterovPlace.cpp:492-512):
+// prev = inside(cur + coef * sum), one clamp per axis.
+__global__ void __launch_bounds__(kBlock) k_initial_prev(BinGeom G, int n_g, const int2* half,
+                                                         const float2* cur, const float2* sum, float coef,
+                                                         float2* out) {
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  if (g >= n_g) return;
+  const int2 h = half[g];
+  const float2 c = cur[g], s = sum[g];
+  const float x = __fadd_rn(c.x, __fmul_rn(coef, s.x));
+  const float y = __fadd_rn(c.y, __fmul_rn(coef, s.y));
+  out[g] = make_float2(inside(x, h.x, G.core_lx, G.core_ux), inside(y, h.y, G.core_ly, G.core_uy));
+}
+}  // namespace
+
+int launch_initial_prev(DeviceModel& d, const float2* cur_slp, const float2* cur_sum, float coef,
+                        float2* out, cudaStream_t s, Timer& t) {
+  t.begin(kKOther);
+  k_initial_prev<<<cell_blocks(d), kBlock, 0, s>>>(geom(d), d.n_g, d.g_half, cur_slp, cur_sum, coef, out);
+  t.end(kKOther);
+  t.count(1);
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
+int launch_sum_phi(DeviceModel& d, int area_set, cudaStream_t s, Timer& t, int* n_blocks) {
+  const int nb = d.cnt_x * d.cnt_y;
+  const int blocks = std::min((nb + kBlock - 1) / kBlock, d.part_stride);
+  t.begin(kKOther);
+  k_sum_phi<<<blocks, kBlock, 0, s>>>(d.phi, d.area[area_set], d.nonplace, nb,
+                                     d.part + (size_t)kPartPhi * d.part_stride);
+  t.end(kKOther);
+  t.count(1);
+  GPL_CUDA(cudaGetLastError());
+  *n_blocks = blocks;
+  return GPL_OK;
+}
+
+}  // namespace gpl

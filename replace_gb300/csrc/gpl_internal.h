@@ -1,0 +1,213 @@
+// Internal declarations of libgpl_gb300: host model, device layout, kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gpl.h"
+
+namespace gpl {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string& msg);
+
+#define GPL_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      ::gpl::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));    \
+      return e_ == cudaErrorMemoryAllocation ? GPL_ERR_OUT_OF_MEMORY          \
+                                             : GPL_ERR_CUDA;                  \
+    }                                                                         \
+  } while (0)
+
+// ------------------------------------------------------------- host model
+// Everything NesterovBase / BinGrid / PlacerBase compute once per job on the
+// host (src/placerBase.cpp:606-758, src/nesterovBase.cpp:631-741, 917-1155).
+struct HostModel {
+  gpl_params p;
+  int core_lx, core_ly, core_ux, core_uy, site_w, site_h;
+  int n_insts = 0, n_pins = 0, n_nets = 0;
+  std::vector<int32_t> ilx, ily, iux, iuy;
+  std::vector<uint8_t> ikind;
+  std::vector<int32_t> pin_inst, pin_ox, pin_oy, pin_x, pin_y, net_start;
+  std::vector<int32_t> inst_pin_start, inst_pins;
+  std::vector<int32_t> place_insts, non_place_insts;
+  int64_t place_area = 0, std_area = 0, macro_area = 0, non_place_area = 0;
+  // NesterovBase
+  int n_g = 0, n_place = 0, n_fill = 0, fill_dx = 0, fill_dy = 0;
+  std::vector<int32_t> glx, gly, gux, guy;       // real rectangle
+  std::vector<int32_t> gdlx, gdly, gdux, gduy;   // density rectangle
+  std::vector<float> gscale;
+  std::vector<uint8_t> gkind;                    // 0 std, 1 macro, 2 filler
+  std::vector<int32_t> g_pin_start, g_pins;
+  std::vector<int32_t> pin_g;                    // gcell of each pin or -1
+  // BinGrid
+  int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
+  std::vector<int64_t> bin_nonplace;
+};
+
+int build_placer_base(HostModel& m, const gpl_netlist_desc* d, const gpl_params* p);
+int build_nesterov_base(HostModel& m);
+// InitialPlace::placeInstsCenter + Instance::setCenterLocation
+void host_place_center(HostModel& m);
+void host_set_inst_center(HostModel& m, int inst, int x, int y);
+
+// -------------------------------------------------------------- device model
+struct DeviceModel {
+  // static gcell data
+  int n_g = 0, n_place = 0;
+  int2* g_half = nullptr;          // half density size (dDx/2, dDy/2)
+  float* g_scale = nullptr;
+  uint8_t* g_kind = nullptr;
+  float2* g_precond = nullptr;     // (#pins, real dx*dy)
+  int32_t* g_pin_start = nullptr;
+  int32_t* g_pins = nullptr;
+  int32_t* big_cells = nullptr;    // gcells covering many bins (macros)
+  int n_big = 0;
+  // pins and nets
+  int n_pins = 0, n_nets = 0;
+  int32_t* pin_g = nullptr;        // gcell or -1
+  int2* pin_off = nullptr;         // offset (pin_g >= 0) or absolute position
+  int32_t* net_start = nullptr;
+  int32_t* net_small = nullptr;    // nets with degree <= kSmallNet (thread per net)
+  int32_t* net_large = nullptr;    // other nets (warp per net)
+  int n_net_small = 0, n_net_large = 0;
+  float2* pin_grad = nullptr;      // per-pin WA gradient of the last evaluation
+  // bin grid
+  int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
+  int core_lx, core_ly, core_ux, core_uy;
+  float target_density = 1.0f;
+  unsigned long long* area[2] = {nullptr, nullptr};  // [inst | filler] x nb, double-buffered
+  int area_cur = 0;
+  int64_t* nonplace = nullptr;
+  float* density = nullptr;
+  float* spec = nullptr;           // pass A output (DCT-II along x)
+  float* p1 = nullptr;             // pass B outputs
+  float* p2 = nullptr;
+  float2* field = nullptr;         // (Ex, Ey)
+  float* phi = nullptr;
+  float* wx = nullptr;             // [cnt_x]
+  float* wy = nullptr;             // [cnt_y]
+  float2* w4x = nullptr;           // [cnt_x]
+  float2* w4y = nullptr;           // [cnt_y]
+  float2* twiddle = nullptr;       // exp(-2 pi i k / kFftMax), k < kFftMax/2
+  int32_t* g_big_idx = nullptr;    // index into big_cells or -1
+  float2* d_big = nullptr;         // density gradient of big cells
+  // Nesterov vectors (float2 per gcell)
+  float2* slp[3] = {nullptr, nullptr, nullptr};   // SLP coordinates: prev/cur/next by rotation
+  float2* sum[3] = {nullptr, nullptr, nullptr};   // preconditioned sum gradients
+  float2* coordi[2] = {nullptr, nullptr};         // cur / next coordinates
+  float2* wl_out = nullptr;        // optional per-gcell WL gradient (eval hook)
+  float2* d_out = nullptr;         // optional per-gcell density gradient (eval hook)
+  // reduction partials
+  double* part = nullptr;          // [kPartSlots * part_stride]
+  int part_stride = 0;
+  long long* part_i = nullptr;     // int64 partials (HPWL)
+  struct EvalResult* result = nullptr;     // device
+  struct EvalResult* result_h = nullptr;   // pinned host mirror
+  int64_t bytes = 0;
+};
+
+constexpr int kFftMax = 4096;
+constexpr int kSmallNet = 16;
+
+enum PartSlot {
+  kPartOverflow = 0, kPartWl, kPartD, kPartCoordDist, kPartGradDist, kPartNan,
+  kPartPhi, kPartSlots
+};
+
+struct EvalResult {
+  double overflow;        // FP64 sum of per-bin overflow
+  double wl_sum, d_sum;   // sum |grad|
+  double coord_dist, grad_dist;   // sum of squared differences
+  double sum_phi;
+  double nan_flag;
+  long long hpwl;
+  float new_step_length;
+  int pad;
+};
+
+// kernel-class timing (CUDA events around each launch when enabled)
+enum KernelClass { kKScatter = 0, kKPoissonA, kKPoissonB, kKPoissonC, kKWa, kKCell,
+                   kKReduce, kKOther, kKClasses };
+const char* kernel_class_name(int k);
+
+// Optional CUDA-event timing of kernel classes on the job's stream.  Event
+// pairs are recorded around each launch group and resolved later, so timing
+// adds no host synchronisation to the launch sequence.
+struct TimedPair { int k; cudaEvent_t a, b; };
+struct Timer {
+  bool enabled = false;
+  cudaStream_t stream = nullptr;
+  std::vector<TimedPair> live;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t pending = nullptr;
+  long long kernels = 0;            // kernels launched (always counted)
+  double ms[kKClasses] = {0};
+  long long groups[kKClasses] = {0};
+  void begin(int k);
+  void end(int k);
+  void count(int n) { kernels += n; }
+  int resolve();                    // synchronises the stream, accumulates ms
+  void release();
+};
+
+// ------------------------------------------------------------------ kernels
+struct EvalArgs {
+  // predictor: next = clamp(cur + step*sum), slp = clamp(next + coeff*(next - coordi))
+  bool predict = false;
+  float step = 0.0f, coeff = 0.0f;
+  const float2* cur_slp = nullptr;
+  const float2* cur_sum = nullptr;
+  const float2* cur_coordi = nullptr;
+  float2* next_coordi = nullptr;
+  float2* slp = nullptr;            // coordinates evaluated (written if predict)
+  // gradient combination
+  float density_penalty = 0.0f;
+  float min_precond = 1.0f;
+  float wl_coef_x = 0.0f, wl_coef_y = 0.0f;
+  float min_wl_force_bar = -300.0f;
+  float2* sum_out = nullptr;        // preconditioned sum gradient
+  const float2* ref_slp = nullptr;  // step-length reference (curSLP), may be null
+  const float2* ref_sum = nullptr;
+  bool want_phi = false;
+};
+
+// Bin-grid geometry and transform tables used by the Poisson passes.
+struct PoissonGrid {
+  int nx, ny, size_x, size_y;
+  int core_lx, core_ly, core_ux, core_uy;
+  const float* wx;        // [nx]
+  const float* wy;        // [ny]
+  const float2* w4x;      // exp(-i pi k / 2nx), [nx]
+  const float2* w4y;      // exp(-i pi k / 2ny), [ny]
+  const float2* tw;       // exp(-2 pi i m / kFftMax), [kFftMax/2]
+};
+
+int poisson_passes(const PoissonGrid& g, const unsigned long long* area,
+                   unsigned long long* area_clear, const int64_t* nonplace, float td,
+                   const float* density_in, float* density, double* part_overflow,
+                   float* spec, float* p1, float* p2, float2* field, float* fx, float* fy,
+                   float* phi, cudaStream_t s, Timer* t);
+int poisson_blocks_a(int nx, int ny);
+void make_w4(int n, std::vector<float2>& w);
+
+int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
+int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
+int launch_cell(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
+int launch_finalize(DeviceModel& d, int n_ovf_blocks, int n_cell_blocks, int n_phi_blocks,
+                    int n_net_blocks, cudaStream_t s, Timer& t);
+int launch_sum_phi(DeviceModel& d, int area_set, cudaStream_t s, Timer& t, int* n_blocks);
+int cell_blocks(const DeviceModel& d);
+int bin_blocks(const DeviceModel& d);
+int net_blocks(const DeviceModel& d);
+
+// twiddle / frequency tables (host computed, double precision)
+void make_twiddle(std::vector<float2>& tw);
+void make_freq(int nx, int ny, int bsx, int bsy, std::vector<float>& wx, std::vector<float>& wy);
+
+}  // namespace gpl

@@ -1,0 +1,779 @@
+// libgpl_gb300: job lifecycle, device model upload, one physics evaluation,
+// the Nesterov control loop (NesterovPlace, src/nesterovPlace.cpp:64-607) and
+// the C ABI declared in include/gpl.h.
+//
+// Control stays on the host in this file: each back-track step launches the
+// evaluation kernels and reads back one small result record (overflow, HPWL,
+// gradient sums, step length).  All per-cell and per-bin state stays on the
+// device for the whole job.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gpl_internal.h"
+
+namespace gpl {
+
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+const char* kernel_class_name(int k) {
+  static const char* names[kKClasses] = {"density_scatter", "poisson_rows_dct", "poisson_cols_solve",
+                                         "poisson_rows_inverse", "wa_wirelength", "gcell_gradient",
+                                         "reduce_finalize", "other"};
+  return (k >= 0 && k < kKClasses) ? names[k] : "?";
+}
+
+void Timer::begin(int k) {
+  (void)k;
+  if (!enabled) return;
+  cudaEvent_t a;
+  if (!pool.empty()) { a = pool.back(); pool.pop_back(); } else cudaEventCreate(&a);
+  cudaEventRecord(a, stream);
+  pending = a;
+}
+
+void Timer::end(int k) {
+  if (!enabled || !pending) return;
+  cudaEvent_t b;
+  if (!pool.empty()) { b = pool.back(); pool.pop_back(); } else cudaEventCreate(&b);
+  cudaEventRecord(b, stream);
+  live.push_back({k, pending, b});
+  pending = nullptr;
+}
+
+int Timer::resolve() {
+  if (live.empty()) return GPL_OK;
+  GPL_CUDA(cudaStreamSynchronize(stream));
+  for (auto& p : live) {
+    float ms_ = 0.0f;
+    cudaEventElapsedTime(&ms_, p.a, p.b);
+    ms[p.k] += ms_;
+    groups[p.k]++;
+    pool.push_back(p.a);
+    pool.push_back(p.b);
+  }
+  live.clear();
+  return GPL_OK;
+}
+
+void Timer::release() {
+  for (auto& p : live) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+  for (auto e : pool) cudaEventDestroy(e);
+  live.clear();
+  pool.clear();
+}
+
+int launch_initial_prev(DeviceModel& d, const float2* cur_slp, const float2* cur_sum, float coef,
+                        float2* out, cudaStream_t s, Timer& t);
+
+}  // namespace gpl
+
+using namespace gpl;
+
+struct gpl_job {
+  HostModel m;
+  DeviceModel d;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Timer timer;
+  char* arena = nullptr;
+  bool nb_ready = false, np_ready = false;
+  // NesterovPlace state (src/nesterovPlace.h:76-125)
+  float step_length = 0, density_penalty = 0, base_wl_coef = 0, wl_coef_x = 0, wl_coef_y = 0;
+  float sum_overflow = 0, cur_a = 1.0f, min_sum_overflow = 1e30f, hpwl_with_min = 1e30f;
+  float max_phi_coef = 1.05f;
+  bool max_phi_changed = false, is_diverged = false, finished = false;
+  int64_t prev_hpwl = 0;
+  int iter = 0, evals = 0, diverge_code = 0;
+  int i_prev = 0, i_cur = 1, i_next = 2, c_cur = 0, c_next = 1;
+  const float2* last_slp = nullptr;
+  int last_area = 0;
+  EvalResult last{};
+  float2* eval_xy = nullptr;
+  float2* eval_wl = nullptr;
+  float2* eval_d = nullptr;
+};
+
+namespace {
+
+int upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (!bytes) return GPL_OK;
+  GPL_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  return GPL_OK;
+}
+
+int check_device(int dev) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    set_error("no CUDA device available: the GB300 placement core has no CPU fallback");
+    return GPL_ERR_NO_DEVICE;
+  }
+  if (dev < 0 || dev >= n) { set_error("device ordinal out of range"); return GPL_ERR_INVALID_ARG; }
+  GPL_CUDA(cudaSetDevice(dev));
+  return GPL_OK;
+}
+
+struct Sizer {
+  size_t bytes = 0;
+  void add(size_t n, size_t sz) { size_t b = ((n * sz + 255) / 256) * 256; bytes += b ? b : 256; }
+};
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <class T> T* take(size_t n) {
+    size_t b = ((n * sizeof(T) + 255) / 256) * 256;
+    T* p = reinterpret_cast<T*>(base + off);
+    off += b ? b : 256;
+    return p;
+  }
+};
+
+// NesterovBase on the host, then the device model (one arena).
+int ensure_nb(gpl_job* j) {
+  if (j->nb_ready) return GPL_OK;
+  int rc = build_nesterov_base(j->m);
+  if (rc) return rc;
+  HostModel& m = j->m;
+  DeviceModel& d = j->d;
+  GPL_CUDA(cudaSetDevice(j->device));
+  d.n_g = m.n_g; d.n_place = m.n_place; d.n_pins = m.n_pins; d.n_nets = m.n_nets;
+  d.cnt_x = m.cnt_x; d.cnt_y = m.cnt_y; d.size_x = m.size_x; d.size_y = m.size_y;
+  d.core_lx = m.core_lx; d.core_ly = m.core_ly; d.core_ux = m.core_ux; d.core_uy = m.core_uy;
+  d.target_density = m.p.target_density;
+  const size_t nb = (size_t)m.cnt_x * m.cnt_y;
+  const size_t ng = m.n_g;
+  std::vector<int2> half(ng);
+  std::vector<uint8_t> kind(ng);
+  std::vector<float2> precond(ng);
+  std::vector<int32_t> big, big_idx(ng, -1);
+  for (size_t g = 0; g < ng; g++) {
+    half[g] = make_int2((m.gdux[g] - m.gdlx[g]) / 2, (m.gduy[g] - m.gdly[g]) / 2);
+    kind[g] = m.gkind[g];
+    // bins a cell can touch per axis: its extent in bins plus one for a straddle
+    const long long bx = (2LL * half[g].x) / m.size_x + 2, by = (2LL * half[g].y) / m.size_y + 2;
+    if (bx * by > 64) {
+      kind[g] |= 4;
+      big_idx[g] = (int)big.size();
+      big.push_back((int)g);
+    }
+    // getWireLengthPreconditioner / getDensityPreconditioner (src/nesterovBase.cpp:1442-1454)
+    precond[g] = make_float2((float)(m.g_pin_start[g + 1] - m.g_pin_start[g]),
+                             (float)(m.gux[g] - m.glx[g]) * (float)(m.guy[g] - m.gly[g]));
+  }
+  d.n_big = (int)big.size();
+  std::vector<int2> pin_off(m.n_pins);
+  for (int q = 0; q < m.n_pins; q++)
+    pin_off[q] = m.pin_g[q] >= 0 ? make_int2(m.pin_ox[q], m.pin_oy[q]) : make_int2(m.pin_x[q], m.pin_y[q]);
+  std::vector<int32_t> small_nets, large_nets;
+  for (int n = 0; n < m.n_nets; n++)
+    (m.net_start[n + 1] - m.net_start[n] <= kSmallNet ? small_nets : large_nets).push_back(n);
+  d.n_net_small = (int)small_nets.size();
+  d.n_net_large = (int)large_nets.size();
+  std::vector<float2> tw, w4x, w4y;
+  std::vector<float> wx, wy;
+  make_twiddle(tw);
+  make_w4(m.cnt_x, w4x);
+  make_w4(m.cnt_y, w4y);
+  make_freq(m.cnt_x, m.cnt_y, m.size_x, m.size_y, wx, wy);
+  d.part_stride = std::max(std::max(cell_blocks(d), poisson_blocks_a(m.cnt_x, m.cnt_y)), 1);
+  const size_t nnb = std::max(net_blocks(d), 1);
+  const size_t ps = (size_t)kPartSlots * d.part_stride;
+
+  Sizer S;
+  S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
+  S.add(m.g_pins.size(), 4); S.add(big.size(), 4); S.add(ng, 4); S.add(big.size(), 8);
+  S.add(m.n_pins, 4); S.add(m.n_pins, 8); S.add(m.n_nets + 1, 4); S.add(small_nets.size(), 4);
+  S.add(large_nets.size(), 4); S.add(m.n_pins, 8);
+  S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
+  S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
+  S.add(m.cnt_x, 4); S.add(m.cnt_y, 4); S.add(m.cnt_x, 8); S.add(m.cnt_y, 8); S.add(tw.size(), 8);
+  for (int k = 0; k < 3; k++) { S.add(ng, 8); S.add(ng, 8); }
+  S.add(ng, 8); S.add(ng, 8);                 // coordi
+  S.add(ng, 8); S.add(ng, 8); S.add(ng, 8);   // eval xy / wl / d
+  S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult));
+  cudaError_t e = cudaMalloc(&j->arena, S.bytes);
+  if (e != cudaSuccess) {
+    j->arena = nullptr;
+    set_error(std::string("cudaMalloc of the job arena failed: ") + cudaGetErrorString(e));
+    return GPL_ERR_OUT_OF_MEMORY;
+  }
+  d.bytes = (int64_t)S.bytes;
+  Carver C{j->arena};
+  d.g_half = C.take<int2>(ng); d.g_scale = C.take<float>(ng); d.g_kind = C.take<uint8_t>(ng);
+  d.g_precond = C.take<float2>(ng); d.g_pin_start = C.take<int32_t>(ng + 1);
+  d.g_pins = C.take<int32_t>(m.g_pins.size()); d.big_cells = C.take<int32_t>(big.size());
+  d.g_big_idx = C.take<int32_t>(ng); d.d_big = C.take<float2>(big.size());
+  d.pin_g = C.take<int32_t>(m.n_pins); d.pin_off = C.take<int2>(m.n_pins);
+  d.net_start = C.take<int32_t>(m.n_nets + 1); d.net_small = C.take<int32_t>(small_nets.size());
+  d.net_large = C.take<int32_t>(large_nets.size()); d.pin_grad = C.take<float2>(m.n_pins);
+  d.area[0] = C.take<unsigned long long>(2 * nb); d.area[1] = C.take<unsigned long long>(2 * nb);
+  d.nonplace = C.take<int64_t>(nb);
+  d.density = C.take<float>(nb); d.spec = C.take<float>(nb); d.p1 = C.take<float>(nb);
+  d.p2 = C.take<float>(nb); d.field = C.take<float2>(nb); d.phi = C.take<float>(nb);
+  d.wx = C.take<float>(m.cnt_x); d.wy = C.take<float>(m.cnt_y);
+  d.w4x = C.take<float2>(m.cnt_x); d.w4y = C.take<float2>(m.cnt_y);
+  d.twiddle = C.take<float2>(tw.size());
+  for (int k = 0; k < 3; k++) { d.slp[k] = C.take<float2>(ng); d.sum[k] = C.take<float2>(ng); }
+  d.coordi[0] = C.take<float2>(ng); d.coordi[1] = C.take<float2>(ng);
+  j->eval_xy = C.take<float2>(ng); j->eval_wl = C.take<float2>(ng); j->eval_d = C.take<float2>(ng);
+  d.part = C.take<double>(ps); d.part_i = C.take<long long>(nnb);
+  d.result = C.take<EvalResult>(1);
+  cudaStream_t s = j->stream;
+  int rc2 = GPL_OK;
+  rc2 = rc2 ? rc2 : upload(d.g_half, half.data(), ng * sizeof(int2), s);
+  rc2 = rc2 ? rc2 : upload(d.g_scale, m.gscale.data(), ng * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.g_kind, kind.data(), ng, s);
+  rc2 = rc2 ? rc2 : upload(d.g_precond, precond.data(), ng * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.g_pin_start, m.g_pin_start.data(), (ng + 1) * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.g_pins, m.g_pins.data(), m.g_pins.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.big_cells, big.data(), big.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.g_big_idx, big_idx.data(), ng * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.pin_g, m.pin_g.data(), (size_t)m.n_pins * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.pin_off, pin_off.data(), (size_t)m.n_pins * sizeof(int2), s);
+  rc2 = rc2 ? rc2 : upload(d.net_start, m.net_start.data(), (size_t)(m.n_nets + 1) * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.net_small, small_nets.data(), small_nets.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.net_large, large_nets.data(), large_nets.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.nonplace, m.bin_nonplace.data(), nb * 8, s);
+  rc2 = rc2 ? rc2 : upload(d.wx, wx.data(), wx.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.wy, wy.data(), wy.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.w4x, w4x.data(), w4x.size() * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.w4y, w4y.data(), w4y.size() * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.twiddle, tw.data(), tw.size() * sizeof(float2), s);
+  if (rc2) return rc2;
+  GPL_CUDA(cudaMemsetAsync(d.area[0], 0, 2 * nb * 8, s));
+  GPL_CUDA(cudaMemsetAsync(d.area[1], 0, 2 * nb * 8, s));
+  GPL_CUDA(cudaMemsetAsync(d.part, 0, ps * 8, s));
+  GPL_CUDA(cudaMemsetAsync(d.phi, 0, nb * 4, s));
+  if (!d.result_h) GPL_CUDA(cudaMallocHost(&d.result_h, sizeof(EvalResult)));
+  GPL_CUDA(cudaStreamSynchronize(s));
+  j->nb_ready = true;
+  return GPL_OK;
+}
+
+PoissonGrid grid_of(const DeviceModel& d) {
+  PoissonGrid g;
+  g.nx = d.cnt_x; g.ny = d.cnt_y; g.size_x = d.size_x; g.size_y = d.size_y;
+  g.core_lx = d.core_lx; g.core_ly = d.core_ly; g.core_ux = d.core_ux; g.core_uy = d.core_uy;
+  g.wx = d.wx; g.wy = d.wy; g.w4x = d.w4x; g.w4y = d.w4y; g.tw = d.twiddle;
+  return g;
+}
+
+// Phase 1 of an evaluation: (predictor +) density scatter, then the Poisson
+// solve.  updateGCellDensityCenterLocation + updateDensityForceBin.
+int eval_phase1(gpl_job* j, const EvalArgs& a, bool want_phi) {
+  DeviceModel& d = j->d;
+  int rc = launch_scatter(d, a, j->stream, j->timer);
+  if (rc) return rc;
+  const int cur = d.area_cur;
+  rc = poisson_passes(grid_of(d), d.area[cur], d.area[cur ^ 1], d.nonplace, d.target_density,
+                      nullptr, d.density, d.part + (size_t)kPartOverflow * d.part_stride, d.spec,
+                      d.p1, d.p2, d.field, nullptr, nullptr, want_phi ? d.phi : nullptr, j->stream,
+                      &j->timer);
+  if (rc) return rc;
+  j->last_area = cur;
+  d.area_cur = cur ^ 1;
+  j->last_slp = a.slp;
+  j->evals++;
+  return GPL_OK;
+}
+
+// Phase 2: WA forces, per-gcell gradients, reductions; reads the result back.
+int eval_phase2(gpl_job* j, const EvalArgs& a, bool want_phi) {
+  DeviceModel& d = j->d;
+  int rc = launch_wa(d, a, j->stream, j->timer);
+  if (rc) return rc;
+  rc = launch_cell(d, a, j->stream, j->timer);
+  if (rc) return rc;
+  int phi_blocks = 0;
+  if (want_phi) {
+    rc = launch_sum_phi(d, j->last_area, j->stream, j->timer, &phi_blocks);
+    if (rc) return rc;
+  }
+  rc = launch_finalize(d, poisson_blocks_a(d.cnt_x, d.cnt_y), cell_blocks(d), phi_blocks,
+                       net_blocks(d), j->stream, j->timer);
+  if (rc) return rc;
+  GPL_CUDA(cudaMemcpyAsync(d.result_h, d.result, sizeof(EvalResult), cudaMemcpyDeviceToHost, j->stream));
+  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  j->last = *d.result_h;
+  return GPL_OK;
+}
+
+float overflow_ratio(const gpl_job* j) {
+  // sumOverflow_ (src/nesterovPlace.cpp:112-115, 529-532)
+  const HostModel& m = j->m;
+  return (float)(int64_t)j->last.overflow /
+         (float)(m.std_area + m.macro_area * m.p.target_density);
+}
+
+void update_wl_coef(gpl_job* j, float overflow) {
+  // NesterovPlace::updateWireLengthCoef (src/nesterovPlace.cpp:474-490)
+  float c;
+  if (overflow > 1.0) c = 0.1f;
+  else if (overflow < 0.1) c = 10.0f;
+  else c = (float)(1.0 / pow(10.0, (overflow - 0.1) * 20 / 9.0 - 1.0));
+  j->wl_coef_x = c * j->base_wl_coef;
+  j->wl_coef_y = c * j->base_wl_coef;
+}
+
+EvalArgs base_args(gpl_job* j) {
+  EvalArgs a;
+  a.density_penalty = j->density_penalty;
+  a.min_precond = j->m.p.min_preconditioner;
+  a.wl_coef_x = j->wl_coef_x;
+  a.wl_coef_y = j->wl_coef_y;
+  a.min_wl_force_bar = j->m.p.min_wire_length_force_bar;
+  return a;
+}
+
+bool bad(double v) { return std::isnan(v) || std::isinf(v); }
+
+// NesterovPlace::init (src/nesterovPlace.cpp:64-175)
+int nesterov_init(gpl_job* j) {
+  int rc = ensure_nb(j);
+  if (rc) return rc;
+  HostModel& m = j->m;
+  DeviceModel& d = j->d;
+  const size_t ng = m.n_g;
+  std::vector<float2> c0(ng);
+  for (size_t g = 0; g < ng; g++) {
+    // updateDensityCoordiLayoutInside (src/nesterovBase.cpp:1245-1268)
+    float tlx = (float)m.gdlx[g], tly = (float)m.gdly[g];
+    const int ddx = m.gdux[g] - m.gdlx[g], ddy = m.gduy[g] - m.gdly[g];
+    if (tlx < m.core_lx) tlx = (float)m.core_lx;
+    if (tly < m.core_ly) tly = (float)m.core_ly;
+    if (tlx + ddx > m.core_ux) tlx = (float)(m.core_ux - ddx);
+    if (tly + ddy > m.core_uy) tly = (float)(m.core_uy - ddy);
+    const int nlx = (int)tlx, nly = (int)tly;
+    c0[g] = make_float2((float)((2 * nlx + ddx) / 2), (float)((2 * nly + ddy) / 2));
+  }
+  j->i_prev = 0; j->i_cur = 1; j->i_next = 2; j->c_cur = 0; j->c_next = 1;
+  rc = upload(d.slp[j->i_cur], c0.data(), ng * sizeof(float2), j->stream);
+  if (rc) return rc;
+  GPL_CUDA(cudaMemcpyAsync(d.slp[j->i_prev], d.slp[j->i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
+  GPL_CUDA(cudaMemcpyAsync(d.coordi[j->c_cur], d.slp[j->i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
+  j->density_penalty = 0.0f;
+  j->max_phi_coef = m.p.max_phi_coef;
+  // first evaluation at the initial centres
+  EvalArgs a = base_args(j);
+  a.slp = d.slp[j->i_cur];
+  rc = eval_phase1(j, a, false);
+  if (rc) return rc;
+  rc = eval_phase2(j, a, false);   // overflow and HPWL at curSLP
+  if (rc) return rc;
+  j->prev_hpwl = j->last.hpwl;
+  j->base_wl_coef = (float)(m.p.init_wire_length_coef / ((float)(m.size_x + m.size_y) * 0.5));
+  j->sum_overflow = overflow_ratio(j);
+  update_wl_coef(j, j->sum_overflow);
+  a = base_args(j);
+  a.slp = d.slp[j->i_cur];
+  a.sum_out = d.sum[j->i_cur];
+  rc = eval_phase2(j, a, false);
+  if (rc) return rc;
+  if (bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0) {
+    j->is_diverged = true; j->diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
+    set_error("RePlAce diverged. Please tune the parameters again");
+    return GPL_ERR_DIVERGED_INIT;
+  }
+  // updateInitialPrevSLPCoordi (src/nesterovPlace.cpp:492-512)
+  rc = launch_initial_prev(d, d.slp[j->i_cur], d.sum[j->i_cur], m.p.initial_prev_coordi_update_coef,
+                           d.slp[j->i_prev], j->stream, j->timer);
+  if (rc) return rc;
+  a = base_args(j);
+  a.slp = d.slp[j->i_prev];
+  a.sum_out = d.sum[j->i_prev];
+  a.ref_slp = d.slp[j->i_cur];
+  a.ref_sum = d.sum[j->i_cur];
+  rc = eval_phase1(j, a, false);
+  if (rc) return rc;
+  rc = eval_phase2(j, a, false);
+  if (rc) return rc;
+  if (bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0) {
+    j->is_diverged = true; j->diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
+    set_error("RePlAce diverged. Please tune the parameters again");
+    return GPL_ERR_DIVERGED_INIT;
+  }
+  j->density_penalty = ((float)j->last.wl_sum / (float)j->last.d_sum) * m.p.init_density_penalty;
+  j->sum_overflow = overflow_ratio(j);
+  j->step_length = j->last.new_step_length;
+  j->cur_a = 1.0f;
+  j->min_sum_overflow = 1e30f;
+  j->hpwl_with_min = 1e30f;
+  j->max_phi_changed = false;
+  j->iter = 0;
+  j->finished = false;
+  j->np_ready = true;
+  return GPL_OK;
+}
+
+// NesterovPlace::doNesterovPlace (src/nesterovPlace.cpp:275-472), resumable
+int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
+  HostModel& m = j->m;
+  DeviceModel& d = j->d;
+  const gpl_params& p = m.p;
+  if (j->diverge_code == GPL_ERR_DIVERGED_INIT) { j->finished = true; return j->diverge_code; }
+  int done = 0;
+  while (!j->finished && j->iter < p.nesterov_place_max_iter) {
+    if (max_iters > 0 && done >= max_iters) break;
+    done++;
+    const float prev_a = j->cur_a;
+    j->cur_a = (float)((1.0 + sqrt(4.0 * prev_a * prev_a + 1.0)) * 0.5);
+    const float coeff = (float)((prev_a - 1.0) / j->cur_a);
+    int bt = 0;
+    for (bt = 0; bt < p.max_back_track; bt++) {
+      EvalArgs a = base_args(j);
+      a.predict = true;
+      a.step = j->step_length;
+      a.coeff = coeff;
+      a.cur_slp = d.slp[j->i_cur];
+      a.cur_sum = d.sum[j->i_cur];
+      a.cur_coordi = d.coordi[j->c_cur];
+      a.next_coordi = d.coordi[j->c_next];
+      a.slp = d.slp[j->i_next];
+      a.sum_out = d.sum[j->i_next];
+      a.ref_slp = d.slp[j->i_cur];
+      a.ref_sum = d.sum[j->i_cur];
+      int rc = eval_phase1(j, a, false);
+      if (rc) return rc;
+      rc = eval_phase2(j, a, false);
+      if (rc) return rc;
+      if (bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0) {
+        j->is_diverged = true;
+        break;
+      }
+      const float ns = j->last.new_step_length;
+      if (ns > j->step_length * 0.95) { j->step_length = ns; break; }
+      j->step_length = ns;
+    }
+    if (!j->max_phi_changed && j->sum_overflow < 0.35f) {
+      j->max_phi_changed = true;
+      j->max_phi_coef = (float)(j->max_phi_coef * 0.99);
+    }
+    if (p.max_back_track == bt) {
+      j->diverge_code = GPL_ERR_DIVERGED_BACKTRACK;
+      j->is_diverged = true;
+      set_error("RePlAce divergence detected. Please decrease init_density_penalty value");
+    }
+    if (j->is_diverged) {
+      if (!j->diverge_code) {
+        j->diverge_code = GPL_ERR_DIVERGED_NAN;
+        set_error("RePlAce divergence detected: NaN or Inf in the gradient sums");
+      }
+      j->finished = true;
+      break;
+    }
+    // updateNextIter (src/nesterovPlace.cpp:514-553)
+    const int op = j->i_prev;
+    j->i_prev = j->i_cur; j->i_cur = j->i_next; j->i_next = op;
+    std::swap(j->c_cur, j->c_next);
+    j->sum_overflow = overflow_ratio(j);
+    update_wl_coef(j, j->sum_overflow);
+    const int64_t hpwl = j->last.hpwl;
+    const float sd = (float)(hpwl - j->prev_hpwl) / p.reference_hpwl;
+    float pc = (sd < 0) ? j->max_phi_coef : (float)(j->max_phi_coef * pow(j->max_phi_coef, sd * -1.0));
+    pc = std::max(p.min_phi_coef, pc);
+    j->prev_hpwl = hpwl;
+    j->density_penalty *= pc;
+    if (log && log->count < log->capacity) {
+      const int k = log->count++;
+      if (log->overflow) log->overflow[k] = j->sum_overflow;
+      if (log->hpwl) log->hpwl[k] = j->prev_hpwl;
+      if (log->step_length) log->step_length[k] = j->step_length;
+      if (log->backtracks) log->backtracks[k] = bt + 1;
+    }
+    if (p.verbose_level > 0 && (j->iter == 0 || (j->iter + 1) % 10 == 0)) {
+      printf("[NesterovSolve] Iter: %d overflow: %g HPWL: %lld\n", j->iter + 1, j->sum_overflow,
+             (long long)j->prev_hpwl);
+      fflush(stdout);
+    }
+    const int it = j->iter;
+    j->iter++;
+    if (j->min_sum_overflow > j->sum_overflow) {
+      j->min_sum_overflow = j->sum_overflow;
+      j->hpwl_with_min = (float)j->prev_hpwl;
+    }
+    if (j->sum_overflow < 0.3f && j->sum_overflow - j->min_sum_overflow >= 0.02f &&
+        j->hpwl_with_min * 1.2f < j->prev_hpwl) {
+      j->diverge_code = GPL_ERR_DIVERGED_PHI;
+      j->is_diverged = true;
+      j->finished = true;
+      set_error("RePlAce divergence detected. Please decrease max_phi_cof value");
+      break;
+    }
+    if (it > 50 && j->sum_overflow <= p.target_overflow) {
+      if (p.verbose_level > 0) {
+        printf("[NesterovSolve] Finished with Overflow: %g\n", j->sum_overflow);
+        fflush(stdout);
+      }
+      j->finished = true;
+      break;
+    }
+  }
+  if (j->iter >= p.nesterov_place_max_iter) j->finished = true;
+  return j->diverge_code;
+}
+
+void fill_info(gpl_job* j, gpl_job_info* info) {
+  if (!info) return;
+  memset(info, 0, sizeof(*info));
+  const HostModel& m = j->m;
+  info->n_place_insts = (int)m.place_insts.size();
+  info->n_gcells = m.n_g;
+  info->n_fillers = m.n_fill;
+  info->bin_cnt_x = m.cnt_x; info->bin_cnt_y = m.cnt_y;
+  info->bin_size_x = m.size_x; info->bin_size_y = m.size_y;
+  info->filler_dx = m.fill_dx; info->filler_dy = m.fill_dy;
+  info->place_insts_area = m.place_area; info->std_insts_area = m.std_area;
+  info->macro_insts_area = m.macro_area; info->non_place_insts_area = m.non_place_area;
+  info->device_bytes = j->d.bytes;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+const char* gpl_version(void) { return "gpl_gb300 1.0 (sm_103a)"; }
+
+const char* gpl_last_error(void) { return g_last_error.c_str(); }
+
+void gpl_params_default(gpl_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->initial_place_max_iter = 20;
+  p->initial_place_min_diff_length = 1500;
+  p->initial_place_max_solver_iter = 100;
+  p->initial_place_max_fanout = 200;
+  p->initial_place_net_weight_scale = 800.0f;
+  p->incremental_place_mode = 0;
+  p->target_density = 1.0f;
+  p->bin_grid_cnt_x = 0;
+  p->bin_grid_cnt_y = 0;
+  p->min_wire_length_force_bar = -300.0f;
+  p->nesterov_place_max_iter = 2000;
+  p->max_back_track = 10;
+  p->init_density_penalty = 0.00008f;
+  p->init_wire_length_coef = 0.25f;
+  p->target_overflow = 0.1f;
+  p->min_phi_coef = 0.95f;
+  p->max_phi_coef = 1.05f;
+  p->min_preconditioner = 1.0f;
+  p->initial_prev_coordi_update_coef = 100.0f;
+  p->reference_hpwl = 446000000.0f;
+  p->verbose_level = 0;
+  p->device = 0;
+  p->stream = nullptr;
+  p->use_graph = 0;
+}
+
+gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
+  if (!out) { set_error("null job pointer"); return GPL_ERR_INVALID_ARG; }
+  *out = nullptr;
+  gpl_job* j = new gpl_job();
+  int rc = build_placer_base(j->m, nl, p);
+  if (rc) { delete j; return (gpl_status)rc; }
+  j->device = p->device;
+  rc = check_device(j->device);
+  if (rc) { delete j; return (gpl_status)rc; }
+  if (p->stream) {
+    j->stream = (cudaStream_t)p->stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); delete j; return GPL_ERR_CUDA; }
+    j->own_stream = true;
+  }
+  j->timer.stream = j->stream;
+  *out = j;
+  return GPL_OK;
+}
+
+void gpl_destroy(gpl_job* j) {
+  if (!j) return;
+  cudaSetDevice(j->device);
+  if (j->stream) cudaStreamSynchronize(j->stream);
+  j->timer.release();
+  if (j->arena) cudaFree(j->arena);
+  if (j->d.result_h) cudaFreeHost(j->d.result_h);
+  if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
+  delete j;
+}
+
+gpl_status gpl_nesterov_init(gpl_job* j, gpl_job_info* info) {
+  if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
+  if (j->np_ready) { set_error("Nesterov already initialised"); return GPL_ERR_BAD_STATE; }
+  cudaSetDevice(j->device);
+  int rc = nesterov_init(j);
+  fill_info(j, info);
+  return (gpl_status)rc;
+}
+
+gpl_status gpl_nesterov_run(gpl_job* j, int32_t max_iters, gpl_nesterov_stats* st, gpl_iter_log* log) {
+  if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
+  if (!j->np_ready) { set_error("call gpl_nesterov_init first"); return GPL_ERR_BAD_STATE; }
+  cudaSetDevice(j->device);
+  int rc = nesterov_run(j, max_iters, log);
+  if (st) {
+    st->iterations = j->iter;
+    st->evaluations = j->evals;
+    st->finished = j->finished ? 1 : 0;
+    st->status = j->diverge_code;
+    st->overflow = j->sum_overflow;
+    st->step_length = j->step_length;
+    st->density_penalty = j->density_penalty;
+    st->wire_length_coef = j->wl_coef_x;
+    st->hpwl = j->prev_hpwl;
+  }
+  return (gpl_status)rc;
+}
+
+gpl_status gpl_get_inst_locations(gpl_job* j, int32_t* lx, int32_t* ly) {
+  if (!j || !lx || !ly) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
+  const HostModel& m = j->m;
+  for (int i = 0; i < m.n_insts; i++) { lx[i] = m.ilx[i]; ly[i] = m.ily[i]; }
+  if (j->np_ready && j->last_slp) {
+    // NesterovPlace::updateDb: lx = dCx - dDx/2 at the last evaluated centres
+    std::vector<float2> c(m.n_g);
+    GPL_CUDA(cudaMemcpyAsync(c.data(), j->last_slp, m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+    GPL_CUDA(cudaStreamSynchronize(j->stream));
+    for (int k = 0; k < m.n_place; k++) {
+      const int i = m.place_insts[k];
+      const int hx = (m.gdux[k] - m.gdlx[k]) / 2, hy = (m.gduy[k] - m.gdly[k]) / 2;
+      lx[i] = (int)c[k].x - (2 * hx) / 2;
+      ly[i] = (int)c[k].y - (2 * hy) / 2;
+    }
+  }
+  return GPL_OK;
+}
+
+gpl_status gpl_get_gcell_coords(gpl_job* j, float* xy) {
+  if (!j || !xy) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
+  if (!j->np_ready) { set_error("Nesterov not initialised"); return GPL_ERR_BAD_STATE; }
+  GPL_CUDA(cudaMemcpyAsync(xy, j->d.slp[j->i_cur], (size_t)j->m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  return GPL_OK;
+}
+
+gpl_status gpl_eval(gpl_job* j, const float* xy, float cx, float cy, float* wl_grad,
+                    float* density_grad, gpl_eval_stats* st) {
+  if (!j || !xy) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
+  cudaSetDevice(j->device);
+  int rc = ensure_nb(j);
+  if (rc) return (gpl_status)rc;
+  DeviceModel& d = j->d;
+  const size_t ng = j->m.n_g;
+  rc = upload(j->eval_xy, xy, ng * sizeof(float2), j->stream);
+  if (rc) return (gpl_status)rc;
+  EvalArgs a;
+  a.slp = j->eval_xy;
+  a.wl_coef_x = cx; a.wl_coef_y = cy;
+  a.min_wl_force_bar = j->m.p.min_wire_length_force_bar;
+  a.min_precond = j->m.p.min_preconditioner;
+  rc = eval_phase1(j, a, true);
+  if (rc) return (gpl_status)rc;
+  d.wl_out = j->eval_wl;
+  d.d_out = j->eval_d;
+  rc = eval_phase2(j, a, true);
+  d.wl_out = nullptr;
+  d.d_out = nullptr;
+  if (rc) return (gpl_status)rc;
+  if (wl_grad) GPL_CUDA(cudaMemcpyAsync(wl_grad, j->eval_wl, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+  if (density_grad) GPL_CUDA(cudaMemcpyAsync(density_grad, j->eval_d, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  if (st) {
+    st->overflow_area_f64 = j->last.overflow;
+    st->overflow_area = (int64_t)j->last.overflow;
+    st->hpwl = j->last.hpwl;
+    st->sum_phi = j->last.sum_phi;
+    st->wire_length_grad_sum = j->last.wl_sum;
+    st->density_grad_sum = j->last.d_sum;
+  }
+  return GPL_OK;
+}
+
+gpl_status gpl_get_bins(gpl_job* j, int64_t* inst, int64_t* fill, int64_t* np, float* dens,
+                        float* phi, float* fx, float* fy) {
+  if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
+  if (!j->nb_ready) { set_error("no evaluation yet"); return GPL_ERR_BAD_STATE; }
+  DeviceModel& d = j->d;
+  const size_t nb = (size_t)d.cnt_x * d.cnt_y;
+  cudaStream_t s = j->stream;
+  if (inst) GPL_CUDA(cudaMemcpyAsync(inst, d.area[j->last_area], nb * 8, cudaMemcpyDeviceToHost, s));
+  if (fill) GPL_CUDA(cudaMemcpyAsync(fill, d.area[j->last_area] + nb, nb * 8, cudaMemcpyDeviceToHost, s));
+  if (np) GPL_CUDA(cudaMemcpyAsync(np, d.nonplace, nb * 8, cudaMemcpyDeviceToHost, s));
+  if (dens) GPL_CUDA(cudaMemcpyAsync(dens, d.density, nb * 4, cudaMemcpyDeviceToHost, s));
+  if (phi) GPL_CUDA(cudaMemcpyAsync(phi, d.phi, nb * 4, cudaMemcpyDeviceToHost, s));
+  if (fx || fy) {
+    std::vector<float2> f(nb);
+    GPL_CUDA(cudaMemcpyAsync(f.data(), d.field, nb * 8, cudaMemcpyDeviceToHost, s));
+    GPL_CUDA(cudaStreamSynchronize(s));
+    for (size_t b = 0; b < nb; b++) {
+      if (fx) fx[b] = f[b].x;
+      if (fy) fy[b] = f[b].y;
+    }
+  }
+  GPL_CUDA(cudaStreamSynchronize(s));
+  return GPL_OK;
+}
+
+gpl_status gpl_get_gcells(gpl_job* j, int32_t* drect, float* scale, uint8_t* kind) {
+  if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
+  cudaSetDevice(j->device);
+  int rc = ensure_nb(j);
+  if (rc) return (gpl_status)rc;
+  const HostModel& m = j->m;
+  for (int g = 0; g < m.n_g; g++) {
+    if (drect) {
+      drect[4 * g] = m.gdlx[g]; drect[4 * g + 1] = m.gdly[g];
+      drect[4 * g + 2] = m.gdux[g]; drect[4 * g + 3] = m.gduy[g];
+    }
+    if (scale) scale[g] = m.gscale[g];
+    if (kind) kind[g] = m.gkind[g];
+  }
+  return GPL_OK;
+}
+
+int32_t gpl_kernel_times(gpl_job* j, const char** names, double* ms, int64_t* launches, int32_t cap) {
+  if (!j) return 0;
+  j->timer.resolve();
+  int n = 0;
+  for (int k = 0; k < kKClasses && n < cap; k++) {
+    if (names) names[n] = kernel_class_name(k);
+    if (ms) ms[n] = j->timer.ms[k];
+    if (launches) launches[n] = j->timer.groups[k];
+    n++;
+  }
+  return n;
+}
+
+void gpl_kernel_times_reset(gpl_job* j, int32_t enable) {
+  if (!j) return;
+  j->timer.resolve();
+  for (int k = 0; k < kKClasses; k++) { j->timer.ms[k] = 0; j->timer.groups[k] = 0; }
+  j->timer.kernels = 0;
+  j->timer.enabled = enable != 0;
+}
+
+int64_t gpl_kernel_launch_count(gpl_job* j) { return j ? j->timer.kernels : 0; }
+
+gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
+  if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
+  if (j->nb_ready) { set_error("initial place must run before the Nesterov stage"); return GPL_ERR_BAD_STATE; }
+  // InitialPlace::doBicgstabPlace (src/initialPlace.cpp:56-105): centre the
+  // movable instances unless incremental
+  if (!j->m.p.incremental_place_mode) host_place_center(j->m);
+  if (st) memset(st, 0, sizeof(*st));
+  if (j->m.p.initial_place_max_iter > 0) {
+    set_error("B2B initial place iterations are not available in this build");
+    return GPL_ERR_BAD_STATE;
+  }
+  return GPL_OK;
+}
+
+}  // extern "C"

@@ -287,6 +287,27 @@ def from_lefdef(lib: lefdef.LefLibrary, d: lefdef.DefDesign,
     )
 
 
+_NPZ_ARRAYS = ("inst_lx", "inst_ly", "inst_ux", "inst_uy", "inst_kind", "pin_inst", "pin_ox",
+               "pin_oy", "pin_x", "pin_y", "net_start", "inst_pin_start", "inst_pins")
+
+
+def save_npz(nl: Netlist, path: str) -> None:
+    """Serialise a Netlist (arrays, core/die/site/dbu and row boxes)."""
+    np.savez_compressed(
+        path, core=np.array(nl.core, np.int64), die=np.array(nl.die, np.int64),
+        site=np.array(nl.site, np.int64), dbu=np.array(nl.dbu),
+        rows=np.array(nl.rows, np.int64).reshape(-1, 4),
+        **{k: getattr(nl, k) for k in _NPZ_ARRAYS})
+
+
+def load_npz(path: str) -> Netlist:
+    z = np.load(path)
+    return Netlist(core=tuple(int(v) for v in z["core"]), die=tuple(int(v) for v in z["die"]),
+                   site=tuple(int(v) for v in z["site"]), dbu=int(z["dbu"]),
+                   rows=[tuple(int(v) for v in r) for r in z["rows"]],
+                   **{k: z[k].copy() for k in _NPZ_ARRAYS})
+
+
 def read(lef_paths, def_path, **kw) -> Netlist:
     return from_lefdef(lefdef.read_lef(lef_paths), lefdef.read_def(def_path), **kw)
 

@@ -1,0 +1,77 @@
+"""The C ABI library: builds for sm_103a, loads, exports every declared entry
+point, validates its inputs on the host (no GPU calls here)."""
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from replace_gb300 import _abi, netlist as N
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "gpl.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gpl_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_all_symbols():
+    from replace_gb300 import build
+    path = build.build()
+    lib = C.CDLL(path)
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_params_default_matches_reference_defaults():
+    from replace_gb300 import load
+    lib = load()
+    p = _abi.Params()
+    lib.gpl_params_default(C.byref(p))
+    q = _abi.default_params()
+    for f, _ in _abi.Params._fields_:
+        assert getattr(p, f) == pytest.approx(getattr(q, f)), f
+    # src/nesterovPlace.cpp:19-29 and src/replace.cpp:13-33
+    assert p.max_back_track == 10 and p.initial_prev_coordi_update_coef == 100.0
+    assert p.initial_place_max_fanout == 200 and p.reference_hpwl == 446000000.0
+
+
+def test_invalid_netlists_are_rejected_before_any_device_work():
+    from replace_gb300 import load
+    lib = load()
+    nl = N.generate(200, 210, n_io=5, seed=1)
+    bad = nl.copy()
+    bad.net_start = bad.net_start.copy()
+    bad.net_start[-1] += 1                      # does not end at n_pins
+    for net in (bad,):
+        h = _abi.DescHolder(net)
+        job = C.c_void_p()
+        rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job))
+        assert rc == _abi.GPL_ERR_INVALID_ARG
+        assert b"net_start" in lib.gpl_last_error()
+    # utilisation above 100 %: the reference exits with code 1, here a status
+    tight = nl.copy()
+    tight.core = (0, 0, (nl.core[2] // 3), nl.core[3])
+    h = _abi.DescHolder(tight)
+    job = C.c_void_p()
+    rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job))
+    assert rc == _abi.GPL_ERR_UTIL
+
+
+def test_no_device_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from replace_gb300 import load
+    lib = load()
+    nl = N.generate(200, 210, n_io=5, seed=1)
+    h = _abi.DescHolder(nl)
+    job = C.c_void_p()
+    rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job))
+    assert rc == _abi.GPL_ERR_NO_DEVICE
+    assert b"no CPU fallback" in lib.gpl_last_error()

@@ -1,0 +1,78 @@
+"""GPU parity of the whole Nesterov loop (and the Replace drop-in API) against
+the reference's own runs (golden fixtures) and the oracle."""
+
+import numpy as np
+import pytest
+
+from conftest import case, golden, params_of
+
+pytestmark = pytest.mark.gpu
+
+PLACE_CASES = ["simple01", "simple02", "core01", "ar01", "ar02", "incremental01", "syn10k_b128",
+               "syn_macro", "syn_fixed"]
+
+
+@pytest.mark.parametrize("name", PLACE_CASES)
+def test_place_matches_reference(gpu_lib, name):
+    from replace_gb300 import Placer
+    nl, opts = case(name)
+    ref = golden(f"place_{name}.npz")
+    p = Placer(nl, **params_of(opts))
+    p.initial_place()
+    p.nesterov_init()
+    rc, st, lg = p.nesterov_run(0, log_capacity=4000)
+    assert rc == 0 and st.finished
+    # first logged iteration: before FP32 transform rounding can steer the loop
+    assert abs(lg["overflow"][0] - ref["overflow"][0]) <= 1e-4
+    assert abs(int(lg["hpwl"][0]) - int(ref["hpwl"][0])) <= 1e-4 * int(ref["hpwl"][0])
+    # final result: overflow at target, HPWL within 0.5 % of the reference
+    assert st.overflow <= 0.1
+    assert abs(st.hpwl - int(ref["final_hpwl"])) <= 0.005 * int(ref["final_hpwl"])
+    its = ref["iters"]
+    assert abs(st.iterations - its[-1]) <= max(15, 0.15 * its[-1])
+    lx, ly = p.inst_locations()
+    place = nl.inst_kind == 0
+    c = nl.core
+    assert np.all(lx[place] >= c[0] - 1) and np.all(ly[place] >= c[1] - 1)
+    p.close()
+
+
+def test_diverge01_reports_code_3(gpu_lib):
+    from replace_gb300 import Placer
+    nl, opts = case("diverge01")
+    ref = golden("place_diverge01.npz")
+    assert int(ref["rc"]) == 3
+    p = Placer(nl, **params_of(opts))
+    p.initial_place()
+    p.nesterov_init()
+    rc, st, _ = p.nesterov_run(0, allow_divergence=True)
+    assert rc == 3 and st.status == 3 and st.finished
+
+
+def test_run_is_deterministic_and_resumable(gpu_lib):
+    from replace_gb300 import Placer
+    nl, opts = case("simple01")
+    logs = []
+    for chunks in ((0,), (7, 13, 0)):
+        p = Placer(nl, **params_of(opts))
+        p.initial_place()
+        p.nesterov_init()
+        ov, hp = [], []
+        for c in chunks:
+            rc, st, lg = p.nesterov_run(c, log_capacity=4000)
+            ov += list(lg["overflow"]); hp += list(lg["hpwl"])
+        logs.append((np.array(ov), np.array(hp), st.hpwl))
+        p.close()
+    assert np.array_equal(logs[0][0], logs[1][0]) and np.array_equal(logs[0][1], logs[1][1])
+
+
+def test_replace_api_global_placement(gpu_lib):
+    from replace_gb300 import global_placement
+    nl, _ = case("simple01")
+    ref = golden("place_simple01.npz")
+    r = global_placement(nl, skip_initial_place=True, init_density_penalty=0.01)
+    st = r.np_stats
+    assert st.finished and st.overflow <= 0.1
+    assert abs(st.hpwl - int(ref["final_hpwl"])) <= 0.005 * int(ref["final_hpwl"])
+    lx, ly = r.instLocations()
+    assert lx.shape == (nl.n_insts,)
