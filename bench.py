@@ -50,12 +50,13 @@ class ClockSampler:
 
     def __init__(self, gpu_index: int):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.t0 = time.time()
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except FileNotFoundError:
             self.p = None
@@ -153,12 +154,15 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--e2e-iters", type=int, default=60)
+    ap.add_argument("--e2e-iters", type=int, default=300)
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    help="named synthetic workload (replace_gb300.netlist.WORKLOADS)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -173,7 +177,7 @@ def main():
     from replace_gb300 import Placer, netlist as N
     from replace_gb300 import _abi
 
-    nl, td, bins = N.generate_workload(WORKLOAD, seed=1 + rank)
+    nl, td, bins = N.generate_workload(args.workload, seed=1 + rank)
     stream = torch.cuda.Stream()
     params = _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
                                  initial_place_max_iter=0, device=local_rank,
@@ -224,23 +228,31 @@ def main():
     achieved = bytes_per * dom_launches / (dom_ms / 1000.0) / 1e9
     total_ms = sum(v[0] for v in kt.values())
     kernel_share = {k: round(v[0] / total_ms, 4) for k, v in kt.items() if v[1]}
+    kernel_ms = {k: round(v[0] / v[1], 4) for k, v in kt.items() if v[1]}
     p.close()
 
     # end to end through the C ABI from host arrays
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    q = Placer(nl, _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
-                                      initial_place_max_iter=0, device=local_rank))
-    q.initial_place()
-    q.nesterov_init()
-    rc2, st2, _ = q.nesterov_run(args.e2e_iters)
-    lx, ly = q.inst_locations()
-    t1 = time.perf_counter()
-    q.close()
-    e2e_iters = st2.iterations
-    e2e = e2e_iters / (t1 - t0)
-    h2d = _abi.DescHolder(nl).nbytes
-    d2h = lx.nbytes + ly.nbytes
+    e2e_line = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q = Placer(nl, _abi.default_params(target_density=td, bin_grid_cnt_x=bins,
+                                          bin_grid_cnt_y=bins, initial_place_max_iter=0,
+                                          device=local_rank))
+        q.initial_place()
+        q.nesterov_init()
+        rc2, st2, _ = q.nesterov_run(args.e2e_iters)
+        lx, ly = q.inst_locations()
+        t1 = time.perf_counter()
+        q.close()
+        e2e_iters = st2.iterations
+        e2e_line = {"value": e2e_iters / (t1 - t0), "unit": "iters/s",
+                    "h2d_bytes_per_step": _abi.DescHolder(nl).nbytes,
+                    "d2h_bytes_per_step": lx.nbytes + ly.nbytes,
+                    "note": f"one step = a whole job of {e2e_iters} iterations through the C ABI "
+                            "(netlist upload, host setup, init, iterations, location read-back)",
+                    "job_seconds": t1 - t0, "finished": bool(st2.finished),
+                    "final_overflow": float(st2.overflow), "final_hpwl": int(st2.hpwl)}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -256,20 +268,19 @@ def main():
             "steps": iters_done, "warmup": args.warmup, "ms_per_step": ms / max(iters_done, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, 1M cells)",
-            "config": {"workload": WORKLOAD, "cells": 1_000_000, "nets": 1_050_000, "io_pins": 2000,
+            "config": {"workload": args.workload, "cells": int((nl.inst_kind == 0).sum()),
+                       "nets": nl.n_nets, "io_pins": int((nl.pin_inst < 0).sum()),
                        "bins": f"{info.bin_cnt_x}x{info.bin_cnt_y}", "gcells": info.n_gcells,
                        "pins": nl.n_pins, "target_density": td,
                        "evals_per_iter": round((st.evaluations) / max(st.iterations, 1), 3),
                        "l2": "inputs larger than L2 (job working set %.0f MB)" % (info.device_bytes / 1e6),
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "e2e": {"value": e2e, "unit": "iters/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h,
-                    "note": f"one step = a whole job of {e2e_iters} iterations through the C ABI "
-                            "(netlist upload, init, iterations, location read-back)"},
+            "e2e": e2e_line,
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": f"of {peak_kind}",
-                         "traffic": None, "kernel_share": kernel_share},
+                         "traffic": None, "kernel_share": kernel_share,
+                         "kernel_ms_per_launch": kernel_ms},
             "cpu_baseline": cpu,
             "clocks": clk,
         }
