@@ -130,20 +130,25 @@ def run_reference(args):
                  initial_place_max_iter=0)
     o.initial_place()
     o.nesterov_init()
-    o.nesterov_run(args.warmup)
+    # Each CPU iteration of the 1M-cell job takes about a second: the arm
+    # times a bounded sample (at most 5 iterations after at most 3 warm-up
+    # iterations) so that the run ends within a few minutes.
+    warm = min(args.warmup, 3)
+    steps = max(1, min(args.steps, 5))
+    o.nesterov_run(warm)
     t0 = time.perf_counter()
-    o.nesterov_run(args.steps)
+    o.nesterov_run(steps)
     dt = time.perf_counter() - t0
-    v = args.steps / dt
+    v = steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "steps": steps, "warmup": warm, "ms_per_step": 1000 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, 1M cells)",
         "config": {"workload": WORKLOAD, "cells": 1_000_000, "nets": 1_050_000, "bins": "1024x1024",
                    "target_density": td, "parallelism": "single-threaded CPU"},
         "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} Nesterov iterations after {args.warmup} warm-up "
+                         "sample": f"{steps} Nesterov iterations after {warm} warm-up "
                                    "iterations of the 1M-cell job (oracle restatement; the "
                                    "reference's own build needs OpenDB/Eigen and is not on this host)"},
         "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
