@@ -386,14 +386,20 @@ size_t smem_c(int nx, int ny) { return (size_t)4 * pairs_c(nx, ny) * nx * sizeof
 
 int poisson_blocks_a(int nx, int ny) { int r = pairs_a(nx, ny); return (ny / 2 + r - 1) / r; }
 
+// The dynamic shared-memory limit is a per-device function attribute.
 static int ensure_smem_attrs() {
-  static bool done = false;
-  if (done) return GPL_OK;
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  GPL_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return GPL_ERR_INVALID_ARG; }
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return GPL_OK;
   const int big = 200 * 1024;
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_a, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_b, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  done = true;
+  done[dev] = true;
   return GPL_OK;
 }
 
