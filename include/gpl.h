@@ -247,6 +247,21 @@ gpl_status gpl_poisson_solve(int32_t nx, int32_t ny, int32_t bin_size_x,
                              int32_t bin_size_y, const float* density, float* phi,
                              float* field_x, float* field_y, void* stream);
 
+/* Allocation-free variant of gpl_poisson_solve.  It has no counterpart in
+ * the reference.  It serves callers that must not allocate device memory
+ * during the call (a server that admits jobs against a fixed HBM budget, a
+ * framework whose caching allocator owns the device memory, a loop that
+ * cannot absorb cudaMalloc/cudaFree synchronisation): its scratch is a fixed
+ * static device array (about 3.1 MB, held by every GPU that loads the
+ * library) and the call allocates nothing.  Limit: nx * ny <= 512 * 512
+ * (larger grids return GPL_ERR_INVALID_ARG).  The first call on a device
+ * looks up the array's device address; make that first call before any
+ * stream capture.  All calls share the array, so calls that overlap on the
+ * GPU race; order them (same stream, or events). */
+gpl_status gpl_poisson_solve_noalloc(int32_t nx, int32_t ny, int32_t bin_size_x,
+                                     int32_t bin_size_y, const float* density, float* phi,
+                                     float* field_x, float* field_y, void* stream);
+
 /* Kernel timing hook used by the benchmark: accumulates CUDA-event time of
  * the job's kernels by class since the last reset.  names/ms/launches are
  * [capacity]; returns the number of classes written. */
