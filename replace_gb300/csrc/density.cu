@@ -155,6 +155,10 @@ struct CellArgs {
   const float2* ref_sum;
   double* part;               // [kPartSlots][stride]
   int stride;
+  int n_ovf_blocks, n_phi_blocks;
+  unsigned* counters;
+  const long long* hpwl_total;
+  EvalResult* out;
 };
 
 // Density gradient of one big cell, reduced over a block (fixed tree order).
@@ -184,12 +188,16 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
   if (threadIdx.x == 0) A.d_big[blockIdx.x] = make_float2(sx[0], sy[0]);
 }
 
+// One gcell per thread, grid-stride over a grid sized to the SM count; the
+// block partial sums are reduced by the last block to finish (threadfence +
+// counter), in a fixed order, so there is no separate reduction launch and
+// the result is the same run to run.
 __global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
   __shared__ double sh[32 * 5];
-  const int g = blockIdx.x * kBlock + threadIdx.x;
+  __shared__ bool last;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // |wl|, |d|, coord dist^2, grad dist^2, nan
-  if (g < A.n_g) {
-    const BinGeom& G = A.geo;
+  const BinGeom& G = A.geo;
+  for (int g = blockIdx.x * kBlock + threadIdx.x; g < A.n_g; g += gridDim.x * kBlock) {
     const float2 c = A.slp[g];
     const int k = A.kind[g];
     // density gradient: sum over covered bins of overlap * scale * field
@@ -230,72 +238,50 @@ __global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
     if (A.sum_out) A.sum_out[g] = s;
     if (A.wl_out) A.wl_out[g] = w;
     if (A.d_out) A.d_out[g] = d;
-    acc[0] = fabs((double)w.x) + fabs((double)w.y);
-    acc[1] = fabs((double)d.x) + fabs((double)d.y);
+    const double aw = fabs((double)w.x) + fabs((double)w.y);
+    const double ad = fabs((double)d.x) + fabs((double)d.y);
+    acc[0] += aw;
+    acc[1] += ad;
     if (A.ref_slp) {
       const float2 r = A.ref_slp[g], q = A.ref_sum[g];
       const double dx = (double)c.x - r.x, dy = (double)c.y - r.y;
       const double gx = (double)s.x - q.x, gy = (double)s.y - q.y;
-      acc[2] = dx * dx + dy * dy;
-      acc[3] = gx * gx + gy * gy;
+      acc[2] += dx * dx + dy * dy;
+      acc[3] += gx * gx + gy * gy;
     }
-    if (!isfinite(acc[0]) || !isfinite(acc[1])) acc[4] = 1.0;
+    if (!isfinite(aw) || !isfinite(ad)) acc[4] = 1.0;
   }
   block_reduce_n<5>(acc, A.part + (size_t)kPartWl * A.stride, A.stride, sh);
-}
-
-struct FinalArgs {
-  const double* part;
-  const long long* part_i;
-  int stride;
-  int n_ovf_blocks, n_cell_blocks, n_phi_blocks, n_net_blocks;
-  int n_g;
-  EvalResult* out;
-};
-
-// Deterministic FP64 reductions of the per-block partials (fixed order).
-__global__ void __launch_bounds__(1024) k_finalize(FinalArgs F) {
-  __shared__ double sh[32];
-  __shared__ long long shl[32];
-  __shared__ double res[kPartSlots];
-  for (int slot = 0; slot < kPartSlots; slot++) {
-    const int n = slot == kPartOverflow ? F.n_ovf_blocks
-                                        : (slot == kPartPhi ? F.n_phi_blocks : F.n_cell_blocks);
-    double v = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) v += F.part[(size_t)slot * F.stride + i];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      v = sh[threadIdx.x];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (threadIdx.x == 0) res[slot] = v;
-    }
-    __syncthreads();
-  }
-  long long h = 0;
-  for (int i = threadIdx.x; i < F.n_net_blocks; i += blockDim.x) h += F.part_i[i];
-  for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
-  if ((threadIdx.x & 31) == 0) shl[threadIdx.x >> 5] = h;
-  __syncthreads();
   if (threadIdx.x == 0) {
-    long long t = 0;
-    for (int w = 0; w < 32; w++) t += shl[w];
+    __threadfence();
+    last = atomicAdd(&A.counters[0], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  // final reduction (the last block): every partial is visible after the fence
+  double tot[kPartSlots];
+  for (int slot = 0; slot < kPartSlots; slot++) {
+    const int n = slot == kPartOverflow ? A.n_ovf_blocks
+                                        : (slot == kPartPhi ? A.n_phi_blocks : (int)gridDim.x);
+    tot[slot] = block_sum_ordered(A.part + (size_t)slot * A.stride, n, sh);
+  }
+  if (threadIdx.x == 0) {
     EvalResult r;
-    r.overflow = res[kPartOverflow];
-    r.wl_sum = res[kPartWl];
-    r.d_sum = res[kPartD];
-    r.coord_dist = res[kPartCoordDist];
-    r.grad_dist = res[kPartGradDist];
-    r.sum_phi = res[kPartPhi];
-    r.nan_flag = res[kPartNan];
-    r.hpwl = t;
+    r.overflow = tot[kPartOverflow];
+    r.wl_sum = tot[kPartWl];
+    r.d_sum = tot[kPartD];
+    r.coord_dist = tot[kPartCoordDist];
+    r.grad_dist = tot[kPartGradDist];
+    r.sum_phi = tot[kPartPhi];
+    r.nan_flag = tot[kPartNan];
+    r.hpwl = __ldcg(A.hpwl_total);
     // getStepLength / getDistance (src/nesterovPlace.cpp:555-571, 598-607)
-    const float cd = (float)sqrt(r.coord_dist / (2.0 * F.n_g));
-    const float gd = (float)sqrt(r.grad_dist / (2.0 * F.n_g));
+    const float cd = (float)sqrt(r.coord_dist / (2.0 * A.n_g));
+    const float gd = (float)sqrt(r.grad_dist / (2.0 * A.n_g));
     r.new_step_length = cd / gd;
     r.pad = 0;
-    *F.out = r;
+    *A.out = r;
+    A.counters[0] = 0u;
   }
 }
 
@@ -341,7 +327,9 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   return GPL_OK;
 }
 
-int launch_cell(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+int cell_grid(const DeviceModel& d) { return std::max(1, std::min(cell_blocks(d), d.sm_count * 8)); }
+
+int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t) {
   CellArgs A;
   A.geo = geom(d);
   A.n_g = d.n_g;
@@ -359,28 +347,16 @@ int launch_cell(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.ref_slp = a.ref_slp; A.ref_sum = a.ref_sum;
   A.part = d.part;
   A.stride = d.part_stride;
+  A.n_ovf_blocks = poisson_blocks_a(d.cnt_x, d.cnt_y);
+  A.n_phi_blocks = n_phi_blocks;
+  A.counters = d.counters;
+  A.hpwl_total = d.hpwl_total;
+  A.out = d.result;
   t.begin(kKCell);
   if (d.n_big) k_dgrad_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
-  k_cell<<<cell_blocks(d), kBlock, 0, s>>>(A);
+  k_cell<<<cell_grid(d), kBlock, 0, s>>>(A);
   t.end(kKCell);
   t.count(d.n_big ? 2 : 1);
-  GPL_CUDA(cudaGetLastError());
-  return GPL_OK;
-}
-
-int launch_finalize(DeviceModel& d, int n_ovf_blocks, int n_cell_blocks, int n_phi_blocks,
-                    int n_net_blocks, cudaStream_t s, Timer& t) {
-  FinalArgs F;
-  F.part = d.part; F.part_i = d.part_i;
-  F.stride = d.part_stride;
-  F.n_ovf_blocks = n_ovf_blocks; F.n_cell_blocks = n_cell_blocks;
-  F.n_phi_blocks = n_phi_blocks; F.n_net_blocks = n_net_blocks;
-  F.n_g = d.n_g;
-  F.out = d.result;
-  t.begin(kKReduce);
-  k_finalize<<<1, 1024, 0, s>>>(F);
-  t.end(kKReduce);
-  t.count(1);
   GPL_CUDA(cudaGetLastError());
   return GPL_OK;
 }

@@ -86,6 +86,49 @@ __device__ __forceinline__ void block_reduce_n(double (&v)[N], double* out_base,
   __syncthreads();
 }
 
+// Sum of p[0..n) by one block in a fixed order (thread-strided, then fixed
+// trees); reads bypass L1 because other blocks wrote the values.  The result
+// is returned to every thread.
+__device__ __forceinline__ double block_sum_ordered(const double* p, int n, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v += __ldcg(p + i);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? sh[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[0] = v;
+  }
+  __syncthreads();
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ long long block_sum_ordered_ll(const long long* p, int n, long long* sh) {
+  long long v = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v += __ldcg(p + i);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? sh[lane] : 0ll;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[0] = v;
+  }
+  __syncthreads();
+  const long long r = sh[0];
+  __syncthreads();
+  return r;
+}
+
 __device__ __forceinline__ void block_reduce_ll(long long v, long long* out, long long* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

@@ -73,9 +73,9 @@ struct DeviceModel {
   int32_t* pin_g = nullptr;        // gcell or -1
   int2* pin_off = nullptr;         // offset (pin_g >= 0) or absolute position
   int32_t* net_start = nullptr;
-  int32_t* net_small = nullptr;    // nets with degree <= kSmallNet (thread per net)
-  int32_t* net_large = nullptr;    // other nets (warp per net)
-  int n_net_small = 0, n_net_large = 0;
+  int32_t* net_order = nullptr;    // net ids grouped by WA bucket (degree <= 2, 4, 8, 16, 32, more)
+  int wa_bucket_start[7] = {0};    // offsets of the buckets in net_order
+  int wa_block_start[7] = {0};     // first block of each bucket in the WA launch
   float2* pin_grad = nullptr;      // per-pin WA gradient of the last evaluation
   // bin grid
   int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
@@ -107,13 +107,16 @@ struct DeviceModel {
   double* part = nullptr;          // [kPartSlots * part_stride]
   int part_stride = 0;
   long long* part_i = nullptr;     // int64 partials (HPWL)
+  long long* hpwl_total = nullptr; // HPWL of the last evaluation (device)
+  unsigned* counters = nullptr;    // [2] last-block counters (gcell kernel, WA kernel)
+  int sm_count = 0;
   struct EvalResult* result = nullptr;     // device
   struct EvalResult* result_h = nullptr;   // pinned host mirror
   int64_t bytes = 0;
 };
 
 constexpr int kFftMax = 4096;
-constexpr int kSmallNet = 16;
+constexpr int kWaBuckets = 6;
 
 enum PartSlot {
   kPartOverflow = 0, kPartWl, kPartD, kPartCoordDist, kPartGradDist, kPartNan,
@@ -198,13 +201,13 @@ void make_w4(int n, std::vector<float2>& w);
 
 int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
-int launch_cell(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
-int launch_finalize(DeviceModel& d, int n_ovf_blocks, int n_cell_blocks, int n_phi_blocks,
-                    int n_net_blocks, cudaStream_t s, Timer& t);
+int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t);
+int cell_grid(const DeviceModel& d);
 int launch_sum_phi(DeviceModel& d, int area_set, cudaStream_t s, Timer& t, int* n_blocks);
 int cell_blocks(const DeviceModel& d);
 int bin_blocks(const DeviceModel& d);
 int net_blocks(const DeviceModel& d);
+int wa_nets_per_block(int bucket);
 
 // twiddle / frequency tables (host computed, double precision)
 void make_twiddle(std::vector<float2>& tw);

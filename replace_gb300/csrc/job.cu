@@ -172,33 +172,49 @@ int ensure_nb(gpl_job* j) {
   std::vector<int2> pin_off(m.n_pins);
   for (int q = 0; q < m.n_pins; q++)
     pin_off[q] = m.pin_g[q] >= 0 ? make_int2(m.pin_ox[q], m.pin_oy[q]) : make_int2(m.pin_x[q], m.pin_y[q]);
-  std::vector<int32_t> small_nets, large_nets;
-  for (int n = 0; n < m.n_nets; n++)
-    (m.net_start[n + 1] - m.net_start[n] <= kSmallNet ? small_nets : large_nets).push_back(n);
-  d.n_net_small = (int)small_nets.size();
-  d.n_net_large = (int)large_nets.size();
+  // WA buckets by degree: group widths 2, 4, 8, 16, 32 lanes, then a warp per net
+  std::vector<int32_t> net_order;
+  {
+    std::vector<std::vector<int32_t>> bk(kWaBuckets);
+    for (int n = 0; n < m.n_nets; n++) {
+      const int deg = m.net_start[n + 1] - m.net_start[n];
+      int b = 0;
+      while (b < kWaBuckets - 1 && deg > (2 << b)) b++;
+      bk[b].push_back(n);
+    }
+    net_order.reserve(m.n_nets);
+    d.wa_bucket_start[0] = 0;
+    d.wa_block_start[0] = 0;
+    for (int b = 0; b < kWaBuckets; b++) {
+      net_order.insert(net_order.end(), bk[b].begin(), bk[b].end());
+      d.wa_bucket_start[b + 1] = (int)net_order.size();
+      const int per = wa_nets_per_block(b);
+      d.wa_block_start[b + 1] = d.wa_block_start[b] + ((int)bk[b].size() + per - 1) / per;
+    }
+  }
   std::vector<float2> tw, w4x, w4y;
   std::vector<float> wx, wy;
   make_twiddle(tw);
   make_w4(m.cnt_x, w4x);
   make_w4(m.cnt_y, w4y);
   make_freq(m.cnt_x, m.cnt_y, m.size_x, m.size_y, wx, wy);
-  d.part_stride = std::max(std::max(cell_blocks(d), poisson_blocks_a(m.cnt_x, m.cnt_y)), 1);
+  GPL_CUDA(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, j->device));
+  d.part_stride = std::max(std::max(cell_grid(d), poisson_blocks_a(m.cnt_x, m.cnt_y)), 1);
   const size_t nnb = std::max(net_blocks(d), 1);
   const size_t ps = (size_t)kPartSlots * d.part_stride;
 
   Sizer S;
   S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
   S.add(m.g_pins.size(), 4); S.add(big.size(), 4); S.add(ng, 4); S.add(big.size(), 8);
-  S.add(m.n_pins, 4); S.add(m.n_pins, 8); S.add(m.n_nets + 1, 4); S.add(small_nets.size(), 4);
-  S.add(large_nets.size(), 4); S.add(m.n_pins, 8);
+  S.add(m.n_pins, 4); S.add(m.n_pins, 8); S.add(m.n_nets + 1, 4); S.add(net_order.size(), 4);
+  S.add(m.n_pins, 8);
   S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
   S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
   S.add(m.cnt_x, 4); S.add(m.cnt_y, 4); S.add(m.cnt_x, 8); S.add(m.cnt_y, 8); S.add(tw.size(), 8);
   for (int k = 0; k < 3; k++) { S.add(ng, 8); S.add(ng, 8); }
   S.add(ng, 8); S.add(ng, 8);                 // coordi
   S.add(ng, 8); S.add(ng, 8); S.add(ng, 8);   // eval xy / wl / d
-  S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult));
+  S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
   cudaError_t e = cudaMalloc(&j->arena, S.bytes);
   if (e != cudaSuccess) {
     j->arena = nullptr;
@@ -212,8 +228,8 @@ int ensure_nb(gpl_job* j) {
   d.g_pins = C.take<int32_t>(m.g_pins.size()); d.big_cells = C.take<int32_t>(big.size());
   d.g_big_idx = C.take<int32_t>(ng); d.d_big = C.take<float2>(big.size());
   d.pin_g = C.take<int32_t>(m.n_pins); d.pin_off = C.take<int2>(m.n_pins);
-  d.net_start = C.take<int32_t>(m.n_nets + 1); d.net_small = C.take<int32_t>(small_nets.size());
-  d.net_large = C.take<int32_t>(large_nets.size()); d.pin_grad = C.take<float2>(m.n_pins);
+  d.net_start = C.take<int32_t>(m.n_nets + 1); d.net_order = C.take<int32_t>(net_order.size());
+  d.pin_grad = C.take<float2>(m.n_pins);
   d.area[0] = C.take<unsigned long long>(2 * nb); d.area[1] = C.take<unsigned long long>(2 * nb);
   d.nonplace = C.take<int64_t>(nb);
   d.density = C.take<float>(nb); d.spec = C.take<float>(nb); d.p1 = C.take<float>(nb);
@@ -226,6 +242,8 @@ int ensure_nb(gpl_job* j) {
   j->eval_xy = C.take<float2>(ng); j->eval_wl = C.take<float2>(ng); j->eval_d = C.take<float2>(ng);
   d.part = C.take<double>(ps); d.part_i = C.take<long long>(nnb);
   d.result = C.take<EvalResult>(1);
+  d.hpwl_total = C.take<long long>(1);
+  d.counters = C.take<unsigned>(4);
   cudaStream_t s = j->stream;
   int rc2 = GPL_OK;
   rc2 = rc2 ? rc2 : upload(d.g_half, half.data(), ng * sizeof(int2), s);
@@ -239,8 +257,7 @@ int ensure_nb(gpl_job* j) {
   rc2 = rc2 ? rc2 : upload(d.pin_g, m.pin_g.data(), (size_t)m.n_pins * 4, s);
   rc2 = rc2 ? rc2 : upload(d.pin_off, pin_off.data(), (size_t)m.n_pins * sizeof(int2), s);
   rc2 = rc2 ? rc2 : upload(d.net_start, m.net_start.data(), (size_t)(m.n_nets + 1) * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.net_small, small_nets.data(), small_nets.size() * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.net_large, large_nets.data(), large_nets.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.net_order, net_order.data(), net_order.size() * 4, s);
   rc2 = rc2 ? rc2 : upload(d.nonplace, m.bin_nonplace.data(), nb * 8, s);
   rc2 = rc2 ? rc2 : upload(d.wx, wx.data(), wx.size() * 4, s);
   rc2 = rc2 ? rc2 : upload(d.wy, wy.data(), wy.size() * 4, s);
@@ -252,6 +269,7 @@ int ensure_nb(gpl_job* j) {
   GPL_CUDA(cudaMemsetAsync(d.area[1], 0, 2 * nb * 8, s));
   GPL_CUDA(cudaMemsetAsync(d.part, 0, ps * 8, s));
   GPL_CUDA(cudaMemsetAsync(d.phi, 0, nb * 4, s));
+  GPL_CUDA(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned), s));
   if (!d.result_h) GPL_CUDA(cudaMallocHost(&d.result_h, sizeof(EvalResult)));
   GPL_CUDA(cudaStreamSynchronize(s));
   j->nb_ready = true;
@@ -290,15 +308,12 @@ int eval_phase2(gpl_job* j, const EvalArgs& a, bool want_phi) {
   DeviceModel& d = j->d;
   int rc = launch_wa(d, a, j->stream, j->timer);
   if (rc) return rc;
-  rc = launch_cell(d, a, j->stream, j->timer);
-  if (rc) return rc;
   int phi_blocks = 0;
   if (want_phi) {
     rc = launch_sum_phi(d, j->last_area, j->stream, j->timer, &phi_blocks);
     if (rc) return rc;
   }
-  rc = launch_finalize(d, poisson_blocks_a(d.cnt_x, d.cnt_y), cell_blocks(d), phi_blocks,
-                       net_blocks(d), j->stream, j->timer);
+  rc = launch_cell(d, a, phi_blocks, j->stream, j->timer);
   if (rc) return rc;
   GPL_CUDA(cudaMemcpyAsync(d.result_h, d.result, sizeof(EvalResult), cudaMemcpyDeviceToHost, j->stream));
   GPL_CUDA(cudaStreamSynchronize(j->stream));

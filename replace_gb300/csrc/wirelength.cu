@@ -3,12 +3,14 @@
 // getWireLengthGradientPinWA (:1383-1440, JingWei's thesis eq. 4.13) and the
 // integer HPWL of NesterovBase::getHpwl (:1508-1516).
 //
-// Nets are split once per job by degree: nets of up to kSmallNet pins are
-// processed one per thread (their exponential sums are accumulated in the
-// reference's pin order, so the per-net sums are the reference's values);
-// larger nets are processed one per warp (bounding box by warp min/max, sums
-// by warp shuffles).  Each pin's gradient is written to pin_grad; the gcell
-// kernel sums a cell's pins in the instance's pin order.
+// Nets are bucketed once per job by degree d into group widths G = 2, 4, 8,
+// 16, 32 (the smallest G >= d); a net is handled by G consecutive lanes of a
+// warp, one pin per lane.  The lane keeps its pin's position and four
+// exponentials in registers: bounding box and the eight WA sums are group
+// reductions (xor shuffles inside the aligned G-lane group), and the pin
+// gradient follows without re-reading anything.  Nets of more than 32 pins
+// take a warp each and loop over their pins.  One launch covers all buckets
+// (the block index selects the bucket), so warps never mix net sizes.
 #include <climits>
 
 #include <cuda_runtime.h>
@@ -22,17 +24,19 @@ namespace {
 constexpr int kBlock = 256;
 
 struct WaArgs {
-  const int32_t* nets;        // net list of this launch (small or large)
-  int n_nets;
+  const int32_t* nets;          // net ids ordered by bucket
+  int bucket_start[kWaBuckets + 1];   // offsets into nets
+  int block_start[kWaBuckets + 1];    // first block of each bucket
   const int32_t* net_start;
   const int32_t* pin_g;
   const int2* pin_off;
   const float2* slp;
-  float cx, cy;               // wire-length coefficients (1/gamma)
-  float bar;                  // minWireLengthForceBar
+  float cx, cy;                 // wire-length coefficients (1/gamma)
+  float bar;                    // minWireLengthForceBar
   float2* pin_grad;
-  long long* part_i;          // HPWL partials, this launch's blocks start at part_offset
-  int part_offset;
+  long long* part_i;            // HPWL partial per block
+  unsigned* counter;
+  long long* hpwl_total;        // written by the last block to finish
 };
 
 // Pin centre: gcell pins follow the truncated density centre
@@ -46,112 +50,171 @@ __device__ __forceinline__ int2 pin_pos(const WaArgs& A, int q) {
   return make_int2(__float2int_rz(c.x) + o.x, __float2int_rz(c.y) + o.y);
 }
 
-struct WaSums { float s[8]; };
+// The four WA exponentials of one pin (src/nesterovBase.cpp:1320-1355);
+// a direction whose exponent is not above minWireLengthForceBar contributes 0
+// and has its flag cleared.
+struct PinExp {
+  float e[4];      // min x, max x, min y, max y
+  unsigned flags;  // bit k set: e[k] is used
+};
 
-// getWireLengthGradientPinWA for one pin given its net's sums.
-__device__ __forceinline__ float2 pin_gradient(int2 p, int lx, int ux, int ly, int uy,
-                                               const WaSums& S, float cx, float cy, float bar) {
-  float gminx = 0.f, gmaxx = 0.f, gminy = 0.f, gmaxy = 0.f;
+__device__ __forceinline__ PinExp pin_exps(int2 p, int lx, int ux, int ly, int uy, float cx, float cy,
+                                           float bar) {
+  PinExp r;
+  const float a[4] = {__fmul_rn((float)(lx - p.x), cx), __fmul_rn((float)(p.x - ux), cx),
+                      __fmul_rn((float)(ly - p.y), cy), __fmul_rn((float)(p.y - uy), cy)};
+  r.flags = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    r.e[k] = 0.0f;
+    if (a[k] > bar) { r.e[k] = fast_exp(a[k]); r.flags |= 1u << k; }
+  }
+  return r;
+}
+
+// getWireLengthGradientPinWA for one pin given its net's eight sums S:
+// S[0..3] = (sum e, sum x e) for min x and max x, S[4..7] the same for y.
+__device__ __forceinline__ float2 pin_gradient(int2 p, const PinExp& E, const float* S, float cx,
+                                               float cy) {
   const float x = (float)p.x, y = (float)p.y;
-  const float eminx = __fmul_rn((float)(lx - p.x), cx);
-  const float emaxx = __fmul_rn((float)(p.x - ux), cx);
-  const float eminy = __fmul_rn((float)(ly - p.y), cy);
-  const float emaxy = __fmul_rn((float)(p.y - uy), cy);
-  if (eminx > bar) {
-    const float e = fast_exp(eminx), s0 = S.s[0];
-    gminx = (s0 * (e * (1.0f - cx * x)) + cx * e * S.s[1]) / (s0 * s0);
-  }
-  if (emaxx > bar) {
-    const float e = fast_exp(emaxx), s0 = S.s[2];
-    gmaxx = (s0 * (e * (1.0f + cx * x)) - cx * e * S.s[3]) / (s0 * s0);
-  }
-  if (eminy > bar) {
-    const float e = fast_exp(eminy), s0 = S.s[4];
-    gminy = (s0 * (e * (1.0f - cy * y)) + cy * e * S.s[5]) / (s0 * s0);
-  }
-  if (emaxy > bar) {
-    const float e = fast_exp(emaxy), s0 = S.s[6];
-    gmaxy = (s0 * (e * (1.0f + cy * y)) - cy * e * S.s[7]) / (s0 * s0);
-  }
-  return make_float2(gminx - gmaxx, gminy - gmaxy);
+  float g[4] = {0.f, 0.f, 0.f, 0.f};
+  if (E.flags & 1u) { const float s = S[0]; g[0] = (s * (E.e[0] * (1.0f - cx * x)) + cx * E.e[0] * S[1]) / (s * s); }
+  if (E.flags & 2u) { const float s = S[2]; g[1] = (s * (E.e[1] * (1.0f + cx * x)) - cx * E.e[1] * S[3]) / (s * s); }
+  if (E.flags & 4u) { const float s = S[4]; g[2] = (s * (E.e[2] * (1.0f - cy * y)) + cy * E.e[2] * S[5]) / (s * s); }
+  if (E.flags & 8u) { const float s = S[6]; g[3] = (s * (E.e[3] * (1.0f + cy * y)) - cy * E.e[3] * S[7]) / (s * s); }
+  return make_float2(g[0] - g[1], g[2] - g[3]);
 }
 
-// Accumulate one pin into the eight WA sums (src/nesterovBase.cpp:1320-1355).
-__device__ __forceinline__ void pin_sums(int2 p, int lx, int ux, int ly, int uy, float cx, float cy,
-                                         float bar, WaSums& S) {
-  const float eminx = __fmul_rn((float)(lx - p.x), cx);
-  const float emaxx = __fmul_rn((float)(p.x - ux), cx);
-  const float eminy = __fmul_rn((float)(ly - p.y), cy);
-  const float emaxy = __fmul_rn((float)(p.y - uy), cy);
-  if (eminx > bar) { const float e = fast_exp(eminx); S.s[0] = __fadd_rn(S.s[0], e); S.s[1] = __fadd_rn(S.s[1], __fmul_rn((float)p.x, e)); }
-  if (emaxx > bar) { const float e = fast_exp(emaxx); S.s[2] = __fadd_rn(S.s[2], e); S.s[3] = __fadd_rn(S.s[3], __fmul_rn((float)p.x, e)); }
-  if (eminy > bar) { const float e = fast_exp(eminy); S.s[4] = __fadd_rn(S.s[4], e); S.s[5] = __fadd_rn(S.s[5], __fmul_rn((float)p.y, e)); }
-  if (emaxy > bar) { const float e = fast_exp(emaxy); S.s[6] = __fadd_rn(S.s[6], e); S.s[7] = __fadd_rn(S.s[7], __fmul_rn((float)p.y, e)); }
+__device__ __forceinline__ void sums_of(int2 p, const PinExp& E, float* S) {
+  S[0] = E.e[0]; S[1] = __fmul_rn((float)p.x, E.e[0]);
+  S[2] = E.e[1]; S[3] = __fmul_rn((float)p.x, E.e[1]);
+  S[4] = E.e[2]; S[5] = __fmul_rn((float)p.y, E.e[2]);
+  S[6] = E.e[3]; S[7] = __fmul_rn((float)p.y, E.e[3]);
 }
 
-__global__ void __launch_bounds__(kBlock) k_wa_small(WaArgs A) {
-  __shared__ long long sh[32];
-  const int t = blockIdx.x * kBlock + threadIdx.x;
-  long long hp = 0;
-  if (t < A.n_nets) {
-    const int n = A.nets[t];
-    const int s = A.net_start[n], e = A.net_start[n + 1];
-    int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
-    for (int q = s; q < e; q++) {
-      const int2 p = pin_pos(A, q);
-      lx = min(lx, p.x); ux = max(ux, p.x); ly = min(ly, p.y); uy = max(uy, p.y);
-    }
-    WaSums S;
+// One net per G-lane group, one pin per lane.
+template <int G>
+__device__ __forceinline__ long long wa_group(const WaArgs& A, int bucket, int local_block) {
+  const int per_block = kBlock / G;
+  const int grp = threadIdx.x / G, li = threadIdx.x % G;
+  const int k = A.bucket_start[bucket] + local_block * per_block + grp;
+  const bool net_ok = k < A.bucket_start[bucket + 1];
+  int s = 0, e = 0;
+  if (net_ok) {
+    const int n = __ldg(&A.nets[k]);
+    s = __ldg(&A.net_start[n]);
+    e = __ldg(&A.net_start[n + 1]);
+  }
+  const int q = s + li;
+  const bool valid = net_ok && q < e;
+  const int2 p = valid ? pin_pos(A, q) : make_int2(0, 0);
+  int lx = valid ? p.x : INT_MAX, ux = valid ? p.x : INT_MIN;
+  int ly = valid ? p.y : INT_MAX, uy = valid ? p.y : INT_MIN;
 #pragma unroll
-    for (int k = 0; k < 8; k++) S.s[k] = 0.0f;
-    for (int q = s; q < e; q++) pin_sums(pin_pos(A, q), lx, ux, ly, uy, A.cx, A.cy, A.bar, S);
-    for (int q = s; q < e; q++)
-      A.pin_grad[q] = pin_gradient(pin_pos(A, q), lx, ux, ly, uy, S, A.cx, A.cy, A.bar);
-    hp = (long long)((ux - lx) + (uy - ly));
+  for (int o = G / 2; o > 0; o >>= 1) {
+    lx = min(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+    ux = max(ux, __shfl_xor_sync(0xffffffffu, ux, o));
+    ly = min(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+    uy = max(uy, __shfl_xor_sync(0xffffffffu, uy, o));
   }
-  block_reduce_ll(hp, &A.part_i[A.part_offset + blockIdx.x], sh);
+  PinExp E;
+  float S[8];
+  if (valid) {
+    E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
+    sums_of(p, E, S);
+  } else {
+    E.flags = 0;
+#pragma unroll
+    for (int t = 0; t < 4; t++) E.e[t] = 0.0f;
+#pragma unroll
+    for (int t = 0; t < 8; t++) S[t] = 0.0f;
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int t = 0; t < 8; t++) S[t] += __shfl_xor_sync(0xffffffffu, S[t], o);
+  if (valid) A.pin_grad[q] = pin_gradient(p, E, S, A.cx, A.cy);
+  return (net_ok && li == 0) ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
-// One warp per net.
-__global__ void __launch_bounds__(kBlock) k_wa_large(WaArgs A) {
-  __shared__ long long sh[32];
-  const int w = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+// One warp per net of more than 32 pins; lanes stride over the pins.
+__device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int local_block) {
   const int lane = threadIdx.x & 31;
-  long long hp = 0;
-  if (w < A.n_nets) {
-    const int n = A.nets[w];
-    const int s = A.net_start[n], e = A.net_start[n + 1];
-    int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
-    for (int q = s + lane; q < e; q += 32) {
-      const int2 p = pin_pos(A, q);
-      lx = min(lx, p.x); ux = max(ux, p.x); ly = min(ly, p.y); uy = max(uy, p.y);
-    }
-    lx = __reduce_min_sync(0xffffffffu, lx);
-    ly = __reduce_min_sync(0xffffffffu, ly);
-    ux = __reduce_max_sync(0xffffffffu, ux);
-    uy = __reduce_max_sync(0xffffffffu, uy);
-    WaSums S;
-#pragma unroll
-    for (int k = 0; k < 8; k++) S.s[k] = 0.0f;
-    for (int q = s + lane; q < e; q += 32) pin_sums(pin_pos(A, q), lx, ux, ly, uy, A.cx, A.cy, A.bar, S);
-#pragma unroll
-    for (int k = 0; k < 8; k++)
-      for (int o = 16; o > 0; o >>= 1) S.s[k] += __shfl_xor_sync(0xffffffffu, S.s[k], o);
-    for (int q = s + lane; q < e; q += 32)
-      A.pin_grad[q] = pin_gradient(pin_pos(A, q), lx, ux, ly, uy, S, A.cx, A.cy, A.bar);
-    if (lane == 0) hp = (long long)((ux - lx) + (uy - ly));
+  const int k = A.bucket_start[bucket] + local_block * (kBlock / 32) + (threadIdx.x >> 5);
+  if (k >= A.bucket_start[bucket + 1]) return 0ll;           // warp-uniform
+  const int n = __ldg(&A.nets[k]);
+  const int s = __ldg(&A.net_start[n]), e = __ldg(&A.net_start[n + 1]);
+  int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
+  for (int q = s + lane; q < e; q += 32) {
+    const int2 p = pin_pos(A, q);
+    lx = min(lx, p.x); ux = max(ux, p.x); ly = min(ly, p.y); uy = max(uy, p.y);
   }
-  block_reduce_ll(hp, &A.part_i[A.part_offset + blockIdx.x], sh);
+  lx = __reduce_min_sync(0xffffffffu, lx);
+  ly = __reduce_min_sync(0xffffffffu, ly);
+  ux = __reduce_max_sync(0xffffffffu, ux);
+  uy = __reduce_max_sync(0xffffffffu, uy);
+  float S[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int q = s + lane; q < e; q += 32) {
+    const int2 p = pin_pos(A, q);
+    const PinExp E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
+    float t[8];
+    sums_of(p, E, t);
+#pragma unroll
+    for (int j = 0; j < 8; j++) S[j] = __fadd_rn(S[j], t[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 8; j++)
+    for (int o = 16; o > 0; o >>= 1) S[j] += __shfl_xor_sync(0xffffffffu, S[j], o);
+  for (int q = s + lane; q < e; q += 32) {
+    const int2 p = pin_pos(A, q);
+    const PinExp E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
+    A.pin_grad[q] = pin_gradient(p, E, S, A.cx, A.cy);
+  }
+  return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
+}
+
+__global__ void __launch_bounds__(kBlock) k_wa(WaArgs A) {
+  __shared__ long long sh[32];
+  int bucket = 0;
+  while (bucket < kWaBuckets - 1 && (int)blockIdx.x >= A.block_start[bucket + 1]) bucket++;
+  const int lb = blockIdx.x - A.block_start[bucket];
+  long long hp = 0;
+  switch (bucket) {
+    case 0: hp = wa_group<2>(A, 0, lb); break;
+    case 1: hp = wa_group<4>(A, 1, lb); break;
+    case 2: hp = wa_group<8>(A, 2, lb); break;
+    case 3: hp = wa_group<16>(A, 3, lb); break;
+    case 4: hp = wa_group<32>(A, 4, lb); break;
+    default: hp = wa_huge(A, 5, lb); break;
+  }
+  block_reduce_ll(hp, &A.part_i[blockIdx.x], sh);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(A.counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  const long long total = block_sum_ordered_ll(A.part_i, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *A.hpwl_total = total;
+    *A.counter = 0u;
+  }
 }
 
 }  // namespace
 
-int net_blocks(const DeviceModel& d) {
-  return (d.n_net_small + kBlock - 1) / kBlock + (d.n_net_large * 32 + kBlock - 1) / kBlock;
-}
+int wa_nets_per_block(int bucket) { return bucket < kWaBuckets - 1 ? kBlock / (2 << bucket) : kBlock / 32; }
+
+int net_blocks(const DeviceModel& d) { return d.wa_block_start[kWaBuckets]; }
 
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   WaArgs A;
+  A.nets = d.net_order;
+  for (int b = 0; b <= kWaBuckets; b++) {
+    A.bucket_start[b] = d.wa_bucket_start[b];
+    A.block_start[b] = d.wa_block_start[b];
+  }
   A.net_start = d.net_start;
   A.pin_g = d.pin_g;
   A.pin_off = d.pin_off;
@@ -160,19 +223,13 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.bar = a.min_wl_force_bar;
   A.pin_grad = d.pin_grad;
   A.part_i = d.part_i;
-  const int b_small = (d.n_net_small + kBlock - 1) / kBlock;
-  const int b_large = (d.n_net_large * 32 + kBlock - 1) / kBlock;
+  A.counter = d.counters + 1;
+  A.hpwl_total = d.hpwl_total;
+  const int blocks = d.wa_block_start[kWaBuckets];
   t.begin(kKWa);
-  if (b_small) {
-    A.nets = d.net_small; A.n_nets = d.n_net_small; A.part_offset = 0;
-    k_wa_small<<<b_small, kBlock, 0, s>>>(A);
-  }
-  if (b_large) {
-    A.nets = d.net_large; A.n_nets = d.n_net_large; A.part_offset = b_small;
-    k_wa_large<<<b_large, kBlock, 0, s>>>(A);
-  }
+  if (blocks) k_wa<<<blocks, kBlock, 0, s>>>(A);
   t.end(kKWa);
-  t.count((b_small ? 1 : 0) + (b_large ? 1 : 0));
+  t.count(blocks ? 1 : 0);
   GPL_CUDA(cudaGetLastError());
   return GPL_OK;
 }
