@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgpl_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "job.cu", "density.cu", "poisson.cu", "wirelength.cu", "poisson_noalloc.cu"]
+SOURCES = ["setup.cpp", "job.cu", "density.cu", "poisson.cu", "wirelength.cu", "poisson_noalloc.cu",
+           "initial_place.cu"]
 HEADERS = ["gpl_internal.h", "device_common.cuh", "../../include/gpl.h"]
 
 

@@ -74,18 +74,27 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
     if (k & 4) cnt = 0;            // big cell: handled by k_scatter_big
     sc = A.scale[g];
   }
-  const int nbx = max(x1 - x0, 1);
   const int maxc = __reduce_max_sync(0xffffffffu, cnt);
+  const int base = (k & 3) == 2 ? nb : 0;
+  int a = x0, cc = y0;                 // current bin, walked without division
   for (int t = 0; t < maxc; t++) {
     int key = -1;
     long long v = 0;
     if (t < cnt) {
-      const int a = x0 + t % nbx, cc = y0 + t / nbx;
       const float ov = G.overlap(a, cc, lx, ux, ly, uy);
       float f = __fmul_rn(ov, sc);
       if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
       v = (long long)f;
-      key = ((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a;
+      key = base + cc * G.cnt_x + a;
+      if (++a == x1) { a = x0; cc++; }
+    }
+    // Combine lanes that hit the same bin only when the warp has such lanes
+    // (a cheap neighbour test first); otherwise one atomic per lane.
+    const int up = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned dup = __ballot_sync(0xffffffffu, key >= 0 && lane > 0 && key == up);
+    if (!dup) {
+      if (v) atomicAdd(&A.area[key], (unsigned long long)v);
+      continue;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, key);
     vals[threadIdx.x] = v;
@@ -141,8 +150,8 @@ struct CellArgs {
   const float2* slp;          // evaluated coordinates
   const float2* field;        // (Ex, Ey) per bin
   const int32_t* g_pin_start;
-  const int32_t* g_pins;
-  const float2* pin_grad;
+  const int32_t* g_pins;      // device pin index of each gcell pin slot
+  const float2* pin_grad;     // device pin order
   const float2* precond;      // (#pins, dx*dy)
   const int32_t* big_idx;
   float2* d_big;
@@ -157,7 +166,8 @@ struct CellArgs {
   int stride;
   int n_ovf_blocks, n_phi_blocks;
   unsigned* counters;
-  const long long* hpwl_total;
+  long long* hpwl_total;
+  double* part_total;         // [kPartSlots] scratch of the final reduction
   EvalResult* out;
 };
 
@@ -192,8 +202,8 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
 // block partial sums are reduced by the last block to finish (threadfence +
 // counter), in a fixed order, so there is no separate reduction launch and
 // the result is the same run to run.
-__global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
-  __shared__ double sh[32 * 5];
+__global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
+  __shared__ double sh[32 * kPartSlots];
   __shared__ bool last;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // |wl|, |d|, coord dist^2, grad dist^2, nan
   const BinGeom& G = A.geo;
@@ -222,7 +232,7 @@ __global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
     float2 w = make_float2(0.0f, 0.0f);
     const int ps = A.g_pin_start[g], pe = A.g_pin_start[g + 1];
     for (int t = ps; t < pe; t++) {
-      const float2 pg = A.pin_grad[A.g_pins[t]];
+      const float2 pg = A.pin_grad[__ldg(&A.g_pins[t])];
       w.x = __fadd_rn(w.x, pg.x);
       w.y = __fadd_rn(w.y, pg.y);
     }
@@ -258,14 +268,23 @@ __global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
   }
   __syncthreads();
   if (!last) return;
-  // final reduction (the last block): every partial is visible after the fence
+  // final reduction (the last block): every partial is visible after the
+  // fence; all slots are loaded in one pass so the loads overlap
   double tot[kPartSlots];
-  for (int slot = 0; slot < kPartSlots; slot++) {
-    const int n = slot == kPartOverflow ? A.n_ovf_blocks
-                                        : (slot == kPartPhi ? A.n_phi_blocks : (int)gridDim.x);
-    tot[slot] = block_sum_ordered(A.part + (size_t)slot * A.stride, n, sh);
+#pragma unroll
+  for (int slot = 0; slot < kPartSlots; slot++) tot[slot] = 0.0;
+  const int n_max = max(max((int)gridDim.x, A.n_ovf_blocks), A.n_phi_blocks);
+  for (int i = threadIdx.x; i < n_max; i += blockDim.x) {
+#pragma unroll
+    for (int slot = 0; slot < kPartSlots; slot++) {
+      const int n = slot == kPartOverflow ? A.n_ovf_blocks
+                                          : (slot == kPartPhi ? A.n_phi_blocks : (int)gridDim.x);
+      if (i < n) tot[slot] += __ldcg(A.part + (size_t)slot * A.stride + i);
+    }
   }
+  block_reduce_n<kPartSlots>(tot, A.part_total, 1, sh, 0);   // thread 0 writes part_total[k]
   if (threadIdx.x == 0) {
+    for (int slot = 0; slot < kPartSlots; slot++) tot[slot] = A.part_total[slot];
     EvalResult r;
     r.overflow = tot[kPartOverflow];
     r.wl_sum = tot[kPartWl];
@@ -275,6 +294,7 @@ __global__ void __launch_bounds__(kBlock) k_cell(CellArgs A) {
     r.sum_phi = tot[kPartPhi];
     r.nan_flag = tot[kPartNan];
     r.hpwl = __ldcg(A.hpwl_total);
+    *A.hpwl_total = 0;                      // ready for the next evaluation's WA kernel
     // getStepLength / getDistance (src/nesterovPlace.cpp:555-571, 598-607)
     const float cd = (float)sqrt(r.coord_dist / (2.0 * A.n_g));
     const float gd = (float)sqrt(r.grad_dist / (2.0 * A.n_g));
@@ -336,7 +356,8 @@ int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_
   A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
   A.slp = a.slp;
   A.field = d.field;
-  A.g_pin_start = d.g_pin_start; A.g_pins = d.g_pins;
+  A.g_pin_start = d.g_pin_start;
+  A.g_pins = d.g_pins;
   A.pin_grad = d.pin_grad;
   A.precond = d.g_precond;
   A.big_idx = d.g_big_idx; A.d_big = d.d_big;
@@ -351,6 +372,7 @@ int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_
   A.n_phi_blocks = n_phi_blocks;
   A.counters = d.counters;
   A.hpwl_total = d.hpwl_total;
+  A.part_total = d.part_total;
   A.out = d.result;
   t.begin(kKCell);
   if (d.n_big) k_dgrad_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);

@@ -63,9 +63,12 @@ __device__ __forceinline__ float fast_exp(float a) {
   return a;
 }
 
+// Block sums of N values; thread 0 writes out_base[k * stride + index]
+// (index defaults to the block index).
 template <int N>
 __device__ __forceinline__ void block_reduce_n(double (&v)[N], double* out_base, int stride,
-                                               double* sh /* [32*N] */) {
+                                               double* sh /* [32*N] */, int index = -1) {
+  if (index < 0) index = blockIdx.x;
 #pragma unroll
   for (int k = 0; k < N; k++)
     for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
@@ -80,7 +83,7 @@ __device__ __forceinline__ void block_reduce_n(double (&v)[N], double* out_base,
     for (int k = 0; k < N; k++) {
       double x = lane < nw ? sh[k * 32 + lane] : 0.0;
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (lane == 0) out_base[k * stride + blockIdx.x] = x;
+      if (lane == 0) out_base[k * stride + index] = x;
     }
   }
   __syncthreads();

@@ -64,19 +64,19 @@ struct DeviceModel {
   float* g_scale = nullptr;
   uint8_t* g_kind = nullptr;
   float2* g_precond = nullptr;     // (#pins, real dx*dy)
-  int32_t* g_pin_start = nullptr;
-  int32_t* g_pins = nullptr;
+  int32_t* g_pin_start = nullptr;  // CSR of each gcell's pin slots
+  int32_t* g_pins = nullptr;       // device pin index of each slot
   int32_t* big_cells = nullptr;    // gcells covering many bins (macros)
   int n_big = 0;
   // pins and nets
   int n_pins = 0, n_nets = 0;
-  int32_t* pin_g = nullptr;        // gcell or -1
-  int2* pin_off = nullptr;         // offset (pin_g >= 0) or absolute position
-  int32_t* net_start = nullptr;
-  int32_t* net_order = nullptr;    // net ids grouped by WA bucket (degree <= 2, 4, 8, 16, 32, more)
-  int wa_bucket_start[7] = {0};    // offsets of the buckets in net_order
+  // Pins are renumbered on the device: nets in WA-bucket order (degree <= 2,
+  // 4, 8, 16, 32, more), each net's pins contiguous.
+  int4* pins = nullptr;            // (gcell or -1, x offset or position, y ..., 0)
+  int32_t* net_start = nullptr;    // pin CSR of the bucket-ordered nets
+  int wa_bucket_start[7] = {0};    // first net of each bucket
   int wa_block_start[7] = {0};     // first block of each bucket in the WA launch
-  float2* pin_grad = nullptr;      // per-pin WA gradient of the last evaluation
+  float2* pin_grad = nullptr;      // WA gradient per device pin
   // bin grid
   int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
   int core_lx, core_ly, core_ux, core_uy;
@@ -107,7 +107,8 @@ struct DeviceModel {
   double* part = nullptr;          // [kPartSlots * part_stride]
   int part_stride = 0;
   long long* part_i = nullptr;     // int64 partials (HPWL)
-  long long* hpwl_total = nullptr; // HPWL of the last evaluation (device)
+  long long* hpwl_total = nullptr; // HPWL accumulator (WA blocks add, the gcell kernel reads and clears)
+  double* part_total = nullptr;    // [kPartSlots] final sums
   unsigned* counters = nullptr;    // [2] last-block counters (gcell kernel, WA kernel)
   int sm_count = 0;
   struct EvalResult* result = nullptr;     // device
@@ -208,6 +209,10 @@ int cell_blocks(const DeviceModel& d);
 int bin_blocks(const DeviceModel& d);
 int net_blocks(const DeviceModel& d);
 int wa_nets_per_block(int bucket);
+
+// InitialPlace::doBicgstabPlace rounds on the device (initial_place.cu); on
+// return the host model's movable instances are at the solution.
+int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& t);
 
 // twiddle / frequency tables (host computed, double precision)
 void make_twiddle(std::vector<float2>& tw);

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -169,19 +170,21 @@ int ensure_nb(gpl_job* j) {
                              (float)(m.gux[g] - m.glx[g]) * (float)(m.guy[g] - m.gly[g]));
   }
   d.n_big = (int)big.size();
-  std::vector<int2> pin_off(m.n_pins);
-  for (int q = 0; q < m.n_pins; q++)
-    pin_off[q] = m.pin_g[q] >= 0 ? make_int2(m.pin_ox[q], m.pin_oy[q]) : make_int2(m.pin_x[q], m.pin_y[q]);
   // WA buckets by degree: group widths 2, 4, 8, 16, 32 lanes, then a warp per net
   std::vector<int32_t> net_order;
   {
     std::vector<std::vector<int32_t>> bk(kWaBuckets);
+    std::vector<int32_t> key(m.n_nets, INT32_MAX);   // lowest gcell index on the net
     for (int n = 0; n < m.n_nets; n++) {
       const int deg = m.net_start[n + 1] - m.net_start[n];
       int b = 0;
       while (b < kWaBuckets - 1 && deg > (2 << b)) b++;
       bk[b].push_back(n);
+      for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++)
+        if (m.pin_g[q] >= 0) key[n] = std::min(key[n], m.pin_g[q]);
     }
+    for (auto& v : bk)
+      std::stable_sort(v.begin(), v.end(), [&](int a, int b2) { return key[a] < key[b2]; });
     net_order.reserve(m.n_nets);
     d.wa_bucket_start[0] = 0;
     d.wa_block_start[0] = 0;
@@ -192,6 +195,26 @@ int ensure_nb(gpl_job* j) {
       d.wa_block_start[b + 1] = d.wa_block_start[b] + ((int)bk[b].size() + per - 1) / per;
     }
   }
+  // device pin numbering: the bucket-ordered nets' pins, contiguous per net
+  std::vector<int32_t> dpin_of(m.n_pins, -1);
+  std::vector<int4> pins(m.n_pins);
+  std::vector<int32_t> dnet_start(m.n_nets + 1, 0);
+  {
+    int w = 0;
+    for (int k = 0; k < m.n_nets; k++) {
+      const int n = net_order[k];
+      dnet_start[k] = w;
+      for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++) {
+        const int g = m.pin_g[q];
+        dpin_of[q] = w;
+        pins[w++] = g >= 0 ? make_int4(g, m.pin_ox[q], m.pin_oy[q], 0)
+                           : make_int4(-1, m.pin_x[q], m.pin_y[q], 0);
+      }
+    }
+    dnet_start[m.n_nets] = w;
+  }
+  std::vector<int32_t> g_dpins(m.g_pins.size());
+  for (size_t t = 0; t < m.g_pins.size(); t++) g_dpins[t] = dpin_of[m.g_pins[t]];
   std::vector<float2> tw, w4x, w4y;
   std::vector<float> wx, wy;
   make_twiddle(tw);
@@ -205,9 +228,9 @@ int ensure_nb(gpl_job* j) {
 
   Sizer S;
   S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
-  S.add(m.g_pins.size(), 4); S.add(big.size(), 4); S.add(ng, 4); S.add(big.size(), 8);
-  S.add(m.n_pins, 4); S.add(m.n_pins, 8); S.add(m.n_nets + 1, 4); S.add(net_order.size(), 4);
-  S.add(m.n_pins, 8);
+  S.add(big.size(), 4); S.add(ng, 4); S.add(big.size(), 8);
+  S.add(m.n_pins, 16); S.add(m.n_nets + 1, 4);
+  S.add(m.n_pins, 8); S.add(m.g_pins.size(), 4);
   S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
   S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
   S.add(m.cnt_x, 4); S.add(m.cnt_y, 4); S.add(m.cnt_x, 8); S.add(m.cnt_y, 8); S.add(tw.size(), 8);
@@ -215,6 +238,7 @@ int ensure_nb(gpl_job* j) {
   S.add(ng, 8); S.add(ng, 8);                 // coordi
   S.add(ng, 8); S.add(ng, 8); S.add(ng, 8);   // eval xy / wl / d
   S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
+  S.add(kPartSlots, 8);
   cudaError_t e = cudaMalloc(&j->arena, S.bytes);
   if (e != cudaSuccess) {
     j->arena = nullptr;
@@ -225,11 +249,12 @@ int ensure_nb(gpl_job* j) {
   Carver C{j->arena};
   d.g_half = C.take<int2>(ng); d.g_scale = C.take<float>(ng); d.g_kind = C.take<uint8_t>(ng);
   d.g_precond = C.take<float2>(ng); d.g_pin_start = C.take<int32_t>(ng + 1);
-  d.g_pins = C.take<int32_t>(m.g_pins.size()); d.big_cells = C.take<int32_t>(big.size());
+  d.big_cells = C.take<int32_t>(big.size());
   d.g_big_idx = C.take<int32_t>(ng); d.d_big = C.take<float2>(big.size());
-  d.pin_g = C.take<int32_t>(m.n_pins); d.pin_off = C.take<int2>(m.n_pins);
-  d.net_start = C.take<int32_t>(m.n_nets + 1); d.net_order = C.take<int32_t>(net_order.size());
+  d.pins = C.take<int4>(m.n_pins);
+  d.net_start = C.take<int32_t>(m.n_nets + 1);
   d.pin_grad = C.take<float2>(m.n_pins);
+  d.g_pins = C.take<int32_t>(m.g_pins.size());
   d.area[0] = C.take<unsigned long long>(2 * nb); d.area[1] = C.take<unsigned long long>(2 * nb);
   d.nonplace = C.take<int64_t>(nb);
   d.density = C.take<float>(nb); d.spec = C.take<float>(nb); d.p1 = C.take<float>(nb);
@@ -244,6 +269,7 @@ int ensure_nb(gpl_job* j) {
   d.result = C.take<EvalResult>(1);
   d.hpwl_total = C.take<long long>(1);
   d.counters = C.take<unsigned>(4);
+  d.part_total = C.take<double>(kPartSlots);
   cudaStream_t s = j->stream;
   int rc2 = GPL_OK;
   rc2 = rc2 ? rc2 : upload(d.g_half, half.data(), ng * sizeof(int2), s);
@@ -251,13 +277,11 @@ int ensure_nb(gpl_job* j) {
   rc2 = rc2 ? rc2 : upload(d.g_kind, kind.data(), ng, s);
   rc2 = rc2 ? rc2 : upload(d.g_precond, precond.data(), ng * sizeof(float2), s);
   rc2 = rc2 ? rc2 : upload(d.g_pin_start, m.g_pin_start.data(), (ng + 1) * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.g_pins, m.g_pins.data(), m.g_pins.size() * 4, s);
   rc2 = rc2 ? rc2 : upload(d.big_cells, big.data(), big.size() * 4, s);
   rc2 = rc2 ? rc2 : upload(d.g_big_idx, big_idx.data(), ng * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.pin_g, m.pin_g.data(), (size_t)m.n_pins * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.pin_off, pin_off.data(), (size_t)m.n_pins * sizeof(int2), s);
-  rc2 = rc2 ? rc2 : upload(d.net_start, m.net_start.data(), (size_t)(m.n_nets + 1) * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.net_order, net_order.data(), net_order.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.pins, pins.data(), (size_t)m.n_pins * sizeof(int4), s);
+  rc2 = rc2 ? rc2 : upload(d.g_pins, g_dpins.data(), g_dpins.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.net_start, dnet_start.data(), (size_t)(m.n_nets + 1) * 4, s);
   rc2 = rc2 ? rc2 : upload(d.nonplace, m.bin_nonplace.data(), nb * 8, s);
   rc2 = rc2 ? rc2 : upload(d.wx, wx.data(), wx.size() * 4, s);
   rc2 = rc2 ? rc2 : upload(d.wy, wy.data(), wy.size() * 4, s);
@@ -270,6 +294,7 @@ int ensure_nb(gpl_job* j) {
   GPL_CUDA(cudaMemsetAsync(d.part, 0, ps * 8, s));
   GPL_CUDA(cudaMemsetAsync(d.phi, 0, nb * 4, s));
   GPL_CUDA(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned), s));
+  GPL_CUDA(cudaMemsetAsync(d.hpwl_total, 0, sizeof(long long), s));
   if (!d.result_h) GPL_CUDA(cudaMallocHost(&d.result_h, sizeof(EvalResult)));
   GPL_CUDA(cudaStreamSynchronize(s));
   j->nb_ready = true;
@@ -781,14 +806,14 @@ gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
   if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
   if (j->nb_ready) { set_error("initial place must run before the Nesterov stage"); return GPL_ERR_BAD_STATE; }
   // InitialPlace::doBicgstabPlace (src/initialPlace.cpp:56-105): centre the
-  // movable instances unless incremental
+  // movable instances unless incremental, then the B2B + BiCGSTAB rounds
   if (!j->m.p.incremental_place_mode) host_place_center(j->m);
   if (st) memset(st, 0, sizeof(*st));
-  if (j->m.p.initial_place_max_iter > 0) {
-    set_error("B2B initial place iterations are not available in this build");
-    return GPL_ERR_BAD_STATE;
-  }
-  return GPL_OK;
+  if (j->m.p.initial_place_max_iter <= 0) return GPL_OK;
+  cudaSetDevice(j->device);
+  int sm = 0;
+  GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
+  return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer);
 }
 
 }  // extern "C"

@@ -5,7 +5,11 @@
 //
 // Nets are bucketed once per job by degree d into group widths G = 2, 4, 8,
 // 16, 32 (the smallest G >= d); a net is handled by G consecutive lanes of a
-// warp, one pin per lane.  The lane keeps its pin's position and four
+// warp, one pin per lane.  On the device, nets are numbered in bucket order
+// (within a bucket by their lowest gcell index, so that consecutive warps
+// touch nearby cells) and pins are renumbered so that each net's pins are
+// contiguous in that order: pin records are read and pin gradients written
+// with coalesced accesses.  The lane keeps its pin's position and four
 // exponentials in registers: bounding box and the eight WA sums are group
 // reductions (xor shuffles inside the aligned G-lane group), and the pin
 // gradient follows without re-reading anything.  Nets of more than 32 pins
@@ -24,30 +28,25 @@ namespace {
 constexpr int kBlock = 256;
 
 struct WaArgs {
-  const int32_t* nets;          // net ids ordered by bucket
-  int bucket_start[kWaBuckets + 1];   // offsets into nets
+  int bucket_start[kWaBuckets + 1];   // first (bucket-ordered) net of each bucket
   int block_start[kWaBuckets + 1];    // first block of each bucket
-  const int32_t* net_start;
-  const int32_t* pin_g;
-  const int2* pin_off;
+  const int32_t* net_start;     // pin CSR of the bucket-ordered nets
+  const int4* pins;             // (gcell or -1, x offset or position, y ..., unused)
   const float2* slp;
   float cx, cy;                 // wire-length coefficients (1/gamma)
   float bar;                    // minWireLengthForceBar
-  float2* pin_grad;
+  float2* pin_grad;             // device pin order
   long long* part_i;            // HPWL partial per block
-  unsigned* counter;
-  long long* hpwl_total;        // written by the last block to finish
+  long long* hpwl_total;        // accumulated by every block
 };
 
 // Pin centre: gcell pins follow the truncated density centre
 // (GPin::updateDensityLocation, src/nesterovBase.cpp:411-415); other pins
 // keep their fixed position.
-__device__ __forceinline__ int2 pin_pos(const WaArgs& A, int q) {
-  const int g = __ldg(&A.pin_g[q]);
-  const int2 o = __ldg(&A.pin_off[q]);
-  if (g < 0) return o;
-  const float2 c = __ldg(&A.slp[g]);
-  return make_int2(__float2int_rz(c.x) + o.x, __float2int_rz(c.y) + o.y);
+__device__ __forceinline__ int2 pin_pos(const WaArgs& A, const int4& r) {
+  if (r.x < 0) return make_int2(r.y, r.z);
+  const float2 c = __ldg(&A.slp[r.x]);
+  return make_int2(__float2int_rz(c.x) + r.y, __float2int_rz(c.y) + r.z);
 }
 
 // The four WA exponentials of one pin (src/nesterovBase.cpp:1320-1355);
@@ -101,13 +100,14 @@ __device__ __forceinline__ long long wa_group(const WaArgs& A, int bucket, int l
   const bool net_ok = k < A.bucket_start[bucket + 1];
   int s = 0, e = 0;
   if (net_ok) {
-    const int n = __ldg(&A.nets[k]);
-    s = __ldg(&A.net_start[n]);
-    e = __ldg(&A.net_start[n + 1]);
+    s = __ldg(&A.net_start[k]);
+    e = __ldg(&A.net_start[k + 1]);
   }
   const int q = s + li;
   const bool valid = net_ok && q < e;
-  const int2 p = valid ? pin_pos(A, q) : make_int2(0, 0);
+  int4 r = make_int4(-1, 0, 0, -1);
+  if (valid) r = __ldg(&A.pins[q]);
+  const int2 p = valid ? pin_pos(A, r) : make_int2(0, 0);
   int lx = valid ? p.x : INT_MAX, ux = valid ? p.x : INT_MIN;
   int ly = valid ? p.y : INT_MAX, uy = valid ? p.y : INT_MIN;
 #pragma unroll
@@ -142,11 +142,10 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int lo
   const int lane = threadIdx.x & 31;
   const int k = A.bucket_start[bucket] + local_block * (kBlock / 32) + (threadIdx.x >> 5);
   if (k >= A.bucket_start[bucket + 1]) return 0ll;           // warp-uniform
-  const int n = __ldg(&A.nets[k]);
-  const int s = __ldg(&A.net_start[n]), e = __ldg(&A.net_start[n + 1]);
+  const int s = __ldg(&A.net_start[k]), e = __ldg(&A.net_start[k + 1]);
   int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
   for (int q = s + lane; q < e; q += 32) {
-    const int2 p = pin_pos(A, q);
+    const int2 p = pin_pos(A, __ldg(&A.pins[q]));
     lx = min(lx, p.x); ux = max(ux, p.x); ly = min(ly, p.y); uy = max(uy, p.y);
   }
   lx = __reduce_min_sync(0xffffffffu, lx);
@@ -155,7 +154,7 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int lo
   uy = __reduce_max_sync(0xffffffffu, uy);
   float S[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int q = s + lane; q < e; q += 32) {
-    const int2 p = pin_pos(A, q);
+    const int2 p = pin_pos(A, __ldg(&A.pins[q]));
     const PinExp E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
     float t[8];
     sums_of(p, E, t);
@@ -166,7 +165,8 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int lo
   for (int j = 0; j < 8; j++)
     for (int o = 16; o > 0; o >>= 1) S[j] += __shfl_xor_sync(0xffffffffu, S[j], o);
   for (int q = s + lane; q < e; q += 32) {
-    const int2 p = pin_pos(A, q);
+    const int4 r = __ldg(&A.pins[q]);
+    const int2 p = pin_pos(A, r);
     const PinExp E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
     A.pin_grad[q] = pin_gradient(p, E, S, A.cx, A.cy);
   }
@@ -187,19 +187,11 @@ __global__ void __launch_bounds__(kBlock) k_wa(WaArgs A) {
     case 4: hp = wa_group<32>(A, 4, lb); break;
     default: hp = wa_huge(A, 5, lb); break;
   }
+  // HPWL is an integer sum: one 64-bit atomic per block gives the exact,
+  // order-independent total (the gcell kernel reads and clears it)
   block_reduce_ll(hp, &A.part_i[blockIdx.x], sh);
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    last = atomicAdd(A.counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  const long long total = block_sum_ordered_ll(A.part_i, gridDim.x, sh);
-  if (threadIdx.x == 0) {
-    *A.hpwl_total = total;
-    *A.counter = 0u;
-  }
+  if (threadIdx.x == 0) atomicAdd(reinterpret_cast<unsigned long long*>(A.hpwl_total),
+                                  (unsigned long long)A.part_i[blockIdx.x]);
 }
 
 }  // namespace
@@ -210,20 +202,17 @@ int net_blocks(const DeviceModel& d) { return d.wa_block_start[kWaBuckets]; }
 
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   WaArgs A;
-  A.nets = d.net_order;
   for (int b = 0; b <= kWaBuckets; b++) {
     A.bucket_start[b] = d.wa_bucket_start[b];
     A.block_start[b] = d.wa_block_start[b];
   }
   A.net_start = d.net_start;
-  A.pin_g = d.pin_g;
-  A.pin_off = d.pin_off;
+  A.pins = d.pins;
   A.slp = a.slp;
   A.cx = a.wl_coef_x; A.cy = a.wl_coef_y;
   A.bar = a.min_wl_force_bar;
   A.pin_grad = d.pin_grad;
   A.part_i = d.part_i;
-  A.counter = d.counters + 1;
   A.hpwl_total = d.hpwl_total;
   const int blocks = d.wa_block_start[kWaBuckets];
   t.begin(kKWa);

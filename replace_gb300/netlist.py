@@ -65,6 +65,9 @@ class Netlist:
     inst_names: list = field(default_factory=list)
     net_names: list = field(default_factory=list)
     rows: list = field(default_factory=list)     # row boxes (lx, ly, ux, uy)
+    # IO pin boxes [n_pins, 4] (lx, ly, ux, uy); lx > ux marks "no box"
+    # (component pins and unplaced IO pins)
+    io_box: np.ndarray | None = None
 
     @property
     def n_insts(self):
@@ -108,21 +111,35 @@ class Netlist:
         self.pin_x[m] = (cx + self.pin_ox[m]).astype(np.int32)
         self.pin_y[m] = (cy + self.pin_oy[m]).astype(np.int32)
 
-    def bbox_hpwl(self):
-        """PlacerBase::hpwl (src/placerBase.cpp:868-876) over instance boxes
-        and IO pin centres as boxes (IO pins are points here)."""
-        total = 0
-        for n in range(self.n_nets):
-            s, e = self.net_start[n], self.net_start[n + 1]
-            lx = ly = INT_MAX
-            ux = uy = INT_MIN
-            for p in range(s, e):
-                i = self.pin_inst[p]
-                if i >= 0:
-                    lx = min(lx, self.inst_lx[i]); ly = min(ly, self.inst_ly[i])
-                    ux = max(ux, self.inst_ux[i]); uy = max(uy, self.inst_uy[i])
-            total += (ux - lx) + (uy - ly)
-        return total
+    def bbox_hpwl(self, inst_lx=None, inst_ly=None):
+        """PlacerBase::hpwl (src/placerBase.cpp:868-876, Net::updateBox
+        :480-500): per net, the bounding box of its instances' boxes and its
+        IO pins' boxes.  Instance lower-left corners may be given (their
+        sizes are the netlist's)."""
+        lx0 = self.inst_lx if inst_lx is None else np.asarray(inst_lx)
+        ly0 = self.inst_ly if inst_ly is None else np.asarray(inst_ly)
+        w = (self.inst_ux - self.inst_lx).astype(np.int64)
+        h = (self.inst_uy - self.inst_ly).astype(np.int64)
+        inst = self.pin_inst
+        on = inst >= 0
+        ii = np.where(on, inst, 0)
+        box = np.empty((self.n_pins, 4), np.int64)
+        box[:, 0] = np.where(on, lx0[ii], 0)
+        box[:, 1] = np.where(on, ly0[ii], 0)
+        box[:, 2] = np.where(on, lx0[ii] + w[ii], 0)
+        box[:, 3] = np.where(on, ly0[ii] + h[ii], 0)
+        io = self.io_box if self.io_box is not None else np.stack(
+            [self.pin_x, self.pin_y, self.pin_x, self.pin_y], 1)
+        valid = on | (io[:, 0] <= io[:, 2])
+        box[~on] = io[~on]
+        big = np.iinfo(np.int64).max // 4
+        lo = np.where(valid[:, None], box, [big, big, -big, -big])
+        starts = self.net_start[:-1]
+        mnx = np.minimum.reduceat(lo[:, 0], starts)
+        mny = np.minimum.reduceat(lo[:, 1], starts)
+        mxx = np.maximum.reduceat(lo[:, 2], starts)
+        mxy = np.maximum.reduceat(lo[:, 3], starts)
+        return int(np.sum((mxx - mnx) + (mxy - mny)))
 
 
 def _fragmented_row_dummies(core, site, rows, fixed_boxes):
@@ -220,7 +237,7 @@ def from_lefdef(lib: lefdef.LefLibrary, d: lefdef.DefDesign,
     for p in d.pins:
         if p.net is not None:
             io_by_net.setdefault(p.net, []).append(p)
-    p_inst, p_ox, p_oy, p_x, p_y, p_key = [], [], [], [], [], []
+    p_inst, p_ox, p_oy, p_x, p_y, p_key, p_box = [], [], [], [], [], [], []
     net_start = [0]
     net_names = []
     for net in d.nets:
@@ -239,6 +256,7 @@ def from_lefdef(lib: lefdef.LefLibrary, d: lefdef.DefDesign,
             else:
                 ox = oy = 0
             p_inst.append(k)
+            p_box.append((1, 1, 0, 0))
             p_ox.append(ox); p_oy.append(oy)
             p_x.append(int(lx[k]) + int(_cdiv(m.width, 2)) + ox)
             p_y.append(int(ly[k]) + int(_cdiv(m.height, 2)) + oy)
@@ -252,6 +270,7 @@ def from_lefdef(lib: lefdef.LefLibrary, d: lefdef.DefDesign,
                 y = int(_cdiv(p.box[1] + p.box[3], 2))
             p_inst.append(-1); p_ox.append(0); p_oy.append(0)
             p_x.append(x); p_y.append(y); p_key.append(0)
+            p_box.append(tuple(p.box) if p.box is not None else (1, 1, 0, 0))
         net_start.append(len(p_inst))
         net_names.append(net.name)
 
@@ -284,6 +303,7 @@ def from_lefdef(lib: lefdef.LefLibrary, d: lefdef.DefDesign,
         inst_names=[c.name for c in d.components] + [f"dummy{k}" for k in range(nd)],
         net_names=net_names,
         rows=rows,
+        io_box=np.array(p_box, np.int32).reshape(-1, 4),
     )
 
 
@@ -293,11 +313,12 @@ _NPZ_ARRAYS = ("inst_lx", "inst_ly", "inst_ux", "inst_uy", "inst_kind", "pin_ins
 
 def save_npz(nl: Netlist, path: str) -> None:
     """Serialise a Netlist (arrays, core/die/site/dbu and row boxes)."""
+    extra = {} if nl.io_box is None else {"io_box": nl.io_box}
     np.savez_compressed(
         path, core=np.array(nl.core, np.int64), die=np.array(nl.die, np.int64),
         site=np.array(nl.site, np.int64), dbu=np.array(nl.dbu),
         rows=np.array(nl.rows, np.int64).reshape(-1, 4),
-        **{k: getattr(nl, k) for k in _NPZ_ARRAYS})
+        **{k: getattr(nl, k) for k in _NPZ_ARRAYS}, **extra)
 
 
 def load_npz(path: str) -> Netlist:
@@ -305,6 +326,7 @@ def load_npz(path: str) -> Netlist:
     return Netlist(core=tuple(int(v) for v in z["core"]), die=tuple(int(v) for v in z["die"]),
                    site=tuple(int(v) for v in z["site"]), dbu=int(z["dbu"]),
                    rows=[tuple(int(v) for v in r) for r in z["rows"]],
+                   io_box=z["io_box"].copy() if "io_box" in z.files else None,
                    **{k: z[k].copy() for k in _NPZ_ARRAYS})
 
 

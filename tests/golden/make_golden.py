@@ -14,6 +14,10 @@ It builds the reference's unchanged placement sources with oracle/refbuild
                        and density gradients, overflow area, HPWL
 * place_<case>.npz     the Nesterov run: logged (iteration, overflow, HPWL),
                        exit code, final overflow and HPWL, final locations
+* ip_<case>.npz        for designs placed with the initial place (simple03,
+                       simple04): the rounds and Nesterov lines the
+                       reference logged in test/<case>.ok (its initial place
+                       needs Eigen, so it is not rebuilt here)
 """
 
 from __future__ import annotations
@@ -44,6 +48,9 @@ LEFDEF_CASES = {
 }
 EVAL_CASES = ["simple01", "simple02", "ar01", "syn10k_b128", "syn_macro", "syn_fixed"]
 PLACE_CASES = list(LEFDEF_CASES) + ["syn10k_b128", "syn_macro", "syn_fixed"]
+# designs run with the initial place (netlists only: the reference's IP needs
+# Eigen and does not build here; its logged rounds are in test/<case>.ok)
+IP_CASES = ["simple03", "simple04"]
 
 
 def synthetic(name):
@@ -96,6 +103,22 @@ def main():
     import refnet
     if not refnet.build(args.ref):
         raise SystemExit("reference build unavailable")
+    t = os.path.join(args.ref, "test")
+    for name in IP_CASES:
+        nl = N.read(os.path.join(t, "nangate45.lef"), os.path.join(t, name + ".def"))
+        N.save_npz(nl, os.path.join(HERE, f"netlist_{name}.npz"))
+        rounds = []
+        for l in open(os.path.join(t, name + ".ok")):
+            m = re.match(r"\[InitialPlace\]\s+Iter: (\d+) CG Error: (\S+) HPWL: (\d+)", l)
+            if m:
+                rounds.append((int(m.group(1)), float(m.group(2)), int(m.group(3))))
+        r = np.array(rounds, np.float64)
+        its, ovf, hp, fin, _ = parse_log(open(os.path.join(t, name + ".ok")).read())
+        np.savez_compressed(os.path.join(HERE, f"ip_{name}.npz"), iter=r[:, 0].astype(np.int32),
+                            cg_error=r[:, 1], hpwl=r[:, 2].astype(np.int64),
+                            nesterov_iters=its, nesterov_overflow=ovf, nesterov_hpwl=hp,
+                            final_overflow=np.array(fin))
+        print(name, "ok")
     for name in sorted(set(EVAL_CASES) | set(PLACE_CASES)):
         nl, opts = case_netlist(name, args.ref)
         N.save_npz(nl, os.path.join(HERE, f"netlist_{name}.npz"))

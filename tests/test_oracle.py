@@ -104,3 +104,21 @@ def test_nesterov_loop_matches_reference(oracle_mod, name):
     assert st.overflow <= 0.1
     assert abs(st.hpwl - int(ref["final_hpwl"])) <= 0.005 * int(ref["final_hpwl"])
     assert abs(st.iterations - its[-1]) <= max(10, 0.1 * its[-1])
+
+
+@pytest.mark.parametrize("name", ["simple03", "simple04"])
+def test_initial_place_matches_reference_log(oracle_mod, name):
+    """The reference logs PlacerBase::hpwl (instance and IO-pin boxes) at the
+    start of each initial-place round, i.e. after the previous round's move
+    (test/<case>.ok).  After k oracle rounds the HPWL must match round k+1."""
+    nl, _ = case(name)
+    ref = golden(f"ip_{name}.npz")
+    assert nl.bbox_hpwl() == int(ref["hpwl"][0])          # the DEF positions
+    for k in range(1, len(ref["hpwl"])):
+        o = oracle_mod.Oracle(nl, target_density=0.7, initial_place_max_iter=k)
+        rc, st = o.initial_place()
+        assert rc == 0 and st.iterations == k
+        lx, ly = o.inst_locations()
+        h = nl.bbox_hpwl(lx, ly)
+        assert abs(h - int(ref["hpwl"][k])) <= 1e-4 * int(ref["hpwl"][k]), (k, h)
+        assert st.last_error < 1e-6
