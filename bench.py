@@ -98,7 +98,8 @@ def algorithmic_bytes(kind, ng, npins, nn, nb):
         "poisson_rows_dct": 48 * nb,
         "poisson_cols_solve": 12 * nb,
         "poisson_rows_inverse": 16 * nb,
-        "wa_wirelength": 28 * npins + 8 * nn,
+        # int4 pin record + pin gradient per pin, net CSR, gcell centres once
+        "wa_wirelength": 24 * npins + 4 * nn + 8 * ng,
         "gcell_gradient": 57 * ng + 12 * npins + 8 * nb,
     }.get(kind)
 

@@ -121,7 +121,7 @@ typedef struct gpl_params {
   /* GB300 knobs */
   int32_t device;                          /* CUDA device ordinal */
   void* stream;                            /* cudaStream_t to run on; NULL = job-owned stream */
-  int32_t use_graph;                       /* 1 = device-resident Nesterov control in a CUDA graph */
+  int32_t use_graph;                       /* 1 = each evaluation replays one CUDA graph */
 } gpl_params;
 
 /* Counts and grid chosen by the job (NesterovBase / BinGrid). */

@@ -126,7 +126,7 @@ def default_params(**overrides) -> Params:
         init_density_penalty=0.00008, init_wire_length_coef=0.25,
         target_overflow=0.1, min_phi_coef=0.95, max_phi_coef=1.05,
         min_preconditioner=1.0, initial_prev_coordi_update_coef=100.0,
-        reference_hpwl=446000000.0, verbose_level=0, device=0, stream=None, use_graph=0,
+        reference_hpwl=446000000.0, verbose_level=0, device=0, stream=None, use_graph=1,
     )
     for k, v in overrides.items():
         setattr(p, k, v)

@@ -31,32 +31,30 @@ struct ScatterArgs {
   const int2* half;
   const float* scale;
   const uint8_t* kind;
-  // predictor
-  int predict;
-  float step, coeff;
-  const float2* cur_slp;
-  const float2* cur_sum;
-  const float2* cur_coordi;
-  float2* next_coordi;
-  float2* slp;
-  unsigned long long* area;   // inst [nb], filler [nb]
+  float2* slp[4];
+  float2* sum[4];
+  float2* coordi[2];
+  unsigned long long* area[2];  // two sets of inst [nb], filler [nb]
+  const EvalCtl* ctl;
 };
 
-__device__ __forceinline__ float2 predict_one(const ScatterArgs& A, int g, int2 h) {
-  const float2 cs = A.cur_slp[g], sg = A.cur_sum[g], cc = A.cur_coordi[g];
-  float nx = __fadd_rn(cs.x, __fmul_rn(A.step, sg.x));
-  float ny = __fadd_rn(cs.y, __fmul_rn(A.step, sg.y));
-  float sx = __fadd_rn(nx, __fmul_rn(A.coeff, __fsub_rn(nx, cc.x)));
-  float sy = __fadd_rn(ny, __fmul_rn(A.coeff, __fsub_rn(ny, cc.y)));
+__device__ __forceinline__ float2 predict_one(const ScatterArgs& A, const EvalCtl& C, int g, int2 h) {
+  const float2 cs = A.slp[C.i_src][g], sg = A.sum[C.i_src][g], cc = A.coordi[C.c_cur][g];
+  float nx = __fadd_rn(cs.x, __fmul_rn(C.step, sg.x));
+  float ny = __fadd_rn(cs.y, __fmul_rn(C.step, sg.y));
+  float sx = __fadd_rn(nx, __fmul_rn(C.coeff, __fsub_rn(nx, cc.x)));
+  float sy = __fadd_rn(ny, __fmul_rn(C.coeff, __fsub_rn(ny, cc.y)));
   const BinGeom& G = A.geo;
-  A.next_coordi[g] = make_float2(inside(nx, h.x, G.core_lx, G.core_ux), inside(ny, h.y, G.core_ly, G.core_uy));
+  A.coordi[C.c_next][g] = make_float2(inside(nx, h.x, G.core_lx, G.core_ux), inside(ny, h.y, G.core_ly, G.core_uy));
   float2 s = make_float2(inside(sx, h.x, G.core_lx, G.core_ux), inside(sy, h.y, G.core_ly, G.core_uy));
-  A.slp[g] = s;
+  A.slp[C.i_eval][g] = s;
   return s;
 }
 
 __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
   __shared__ long long vals[kBlock];
+  const EvalCtl C = *A.ctl;
+  unsigned long long* area = A.area[C.area_cur];
   const int g = blockIdx.x * kBlock + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const BinGeom& G = A.geo;
@@ -66,7 +64,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
   float sc = 0.0f;
   if (g < A.n_g) {
     const int2 h = A.half[g];
-    const float2 c = A.predict ? predict_one(A, g, h) : A.slp[g];
+    const float2 c = C.predict ? predict_one(A, C, g, h) : A.slp[C.i_eval][g];
     k = A.kind[g];
     density_rect(c, h, lx, ux, ly, uy);
     G.range(lx, ux, ly, uy, x0, x1, y0, y1);
@@ -93,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
     const int up = __shfl_up_sync(0xffffffffu, key, 1);
     const unsigned dup = __ballot_sync(0xffffffffu, key >= 0 && lane > 0 && key == up);
     if (!dup) {
-      if (v) atomicAdd(&A.area[key], (unsigned long long)v);
+      if (v) atomicAdd(&area[key], (unsigned long long)v);
       continue;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -102,7 +100,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
     if (key >= 0 && lane == __ffs(peers) - 1) {
       long long s = 0;
       for (unsigned m = peers; m; m &= m - 1) s += vals[(threadIdx.x & ~31) + __ffs(m) - 1];
-      if (s) atomicAdd(&A.area[key], (unsigned long long)s);
+      if (s) atomicAdd(&area[key], (unsigned long long)s);
     }
     __syncwarp();
   }
@@ -110,6 +108,8 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
 
 // One block per big cell (macros): threads stride over its bins.
 __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int32_t* big, int n_big) {
+  const EvalCtl C = *A.ctl;
+  unsigned long long* area = A.area[C.area_cur];
   const int g = big[blockIdx.x];
   const BinGeom& G = A.geo;
   const int nb = G.cnt_x * G.cnt_y;
@@ -117,13 +117,13 @@ __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int
   // k_scatter has already written this cell's predicted coordinates; the
   // block recomputes them with the same arithmetic instead of reading them
   float2 c;
-  if (A.predict) {
+  if (C.predict) {
     __shared__ float2 cs;
-    if (threadIdx.x == 0) cs = predict_one(A, g, h);
+    if (threadIdx.x == 0) cs = predict_one(A, C, g, h);
     __syncthreads();
     c = cs;
   } else {
-    c = A.slp[g];
+    c = A.slp[C.i_eval][g];
   }
   int lx, ux, ly, uy, x0, x1, y0, y1;
   density_rect(c, h, lx, ux, ly, uy);
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int
     float f = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
     if ((k & 3) == 1) f = __fmul_rn(f, A.td);
     const long long v = (long long)f;
-    if (v) atomicAdd(&A.area[((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a], (unsigned long long)v);
+    if (v) atomicAdd(&area[((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a], (unsigned long long)v);
   }
 }
 
@@ -147,7 +147,9 @@ struct CellArgs {
   const int2* half;
   const float* scale;
   const uint8_t* kind;
-  const float2* slp;          // evaluated coordinates
+  float2* slp[4];
+  float2* sum[4];
+  const EvalCtl* ctl;
   const float2* field;        // (Ex, Ey) per bin
   const int32_t* g_pin_start;
   const int32_t* g_pins;      // device pin index of each gcell pin slot
@@ -155,13 +157,9 @@ struct CellArgs {
   const float2* precond;      // (#pins, dx*dy)
   const int32_t* big_idx;
   float2* d_big;
-  float density_penalty;
   float min_precond;
-  float2* sum_out;
   float2* wl_out;
   float2* d_out;
-  const float2* ref_slp;
-  const float2* ref_sum;
   double* part;               // [kPartSlots][stride]
   int stride;
   int n_ovf_blocks, n_phi_blocks;
@@ -176,8 +174,9 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
   __shared__ float sx[kBlock], sy[kBlock];
   const int g = big[blockIdx.x];
   const BinGeom& G = A.geo;
+  const EvalCtl C = *A.ctl;
   int lx, ux, ly, uy, x0, x1, y0, y1;
-  density_rect(A.slp[g], A.half[g], lx, ux, ly, uy);
+  density_rect(A.slp[C.i_eval][g], A.half[g], lx, ux, ly, uy);
   G.range(lx, ux, ly, uy, x0, x1, y0, y1);
   const int nbx = max(x1 - x0, 0), total = nbx * max(y1 - y0, 0);
   const float sc = A.scale[g];
@@ -207,8 +206,16 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
   __shared__ bool last;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // |wl|, |d|, coord dist^2, grad dist^2, nan
   const BinGeom& G = A.geo;
+  const EvalCtl C = *A.ctl;
+  const float2* slp = A.slp[C.i_eval];
+  float2* sum_out = C.write_sum ? A.sum[C.i_eval] : nullptr;
+  const float2* ref_slp = C.i_ref >= 0 ? A.slp[C.i_ref] : nullptr;
+  const float2* ref_sum = C.i_ref >= 0 ? A.sum[C.i_ref] : nullptr;
+  float2* wl_out = C.write_wd ? A.wl_out : nullptr;
+  float2* d_out = C.write_wd ? A.d_out : nullptr;
+  const float lam = C.density_penalty;
   for (int g = blockIdx.x * kBlock + threadIdx.x; g < A.n_g; g += gridDim.x * kBlock) {
-    const float2 c = A.slp[g];
+    const float2 c = slp[g];
     const int k = A.kind[g];
     // density gradient: sum over covered bins of overlap * scale * field
     float2 d = make_float2(0.0f, 0.0f);
@@ -236,7 +243,6 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
       w.x = __fadd_rn(w.x, pg.x);
       w.y = __fadd_rn(w.y, pg.y);
     }
-    const float lam = A.density_penalty;
     float2 s = make_float2(__fadd_rn(w.x, __fmul_rn(lam, d.x)), __fadd_rn(w.y, __fmul_rn(lam, d.y)));
     const float2 pc = A.precond[g];
     float px = __fadd_rn(pc.x, __fmul_rn(lam, pc.y));
@@ -245,15 +251,15 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
     if (py <= A.min_precond) py = A.min_precond;
     s.x = __fdiv_rn(s.x, px);
     s.y = __fdiv_rn(s.y, py);
-    if (A.sum_out) A.sum_out[g] = s;
-    if (A.wl_out) A.wl_out[g] = w;
-    if (A.d_out) A.d_out[g] = d;
+    if (sum_out) sum_out[g] = s;
+    if (wl_out) wl_out[g] = w;
+    if (d_out) d_out[g] = d;
     const double aw = fabs((double)w.x) + fabs((double)w.y);
     const double ad = fabs((double)d.x) + fabs((double)d.y);
     acc[0] += aw;
     acc[1] += ad;
-    if (A.ref_slp) {
-      const float2 r = A.ref_slp[g], q = A.ref_sum[g];
+    if (ref_slp) {
+      const float2 r = ref_slp[g], q = ref_sum[g];
       const double dx = (double)c.x - r.x, dy = (double)c.y - r.y;
       const double gx = (double)s.x - q.x, gy = (double)s.y - q.y;
       acc[2] += dx * dx + dy * dy;
@@ -333,11 +339,11 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   A.n_g = d.n_g;
   A.td = d.target_density;
   A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
-  A.predict = a.predict ? 1 : 0;
-  A.step = a.step; A.coeff = a.coeff;
-  A.cur_slp = a.cur_slp; A.cur_sum = a.cur_sum; A.cur_coordi = a.cur_coordi;
-  A.next_coordi = a.next_coordi; A.slp = a.slp;
-  A.area = d.area[d.area_cur];
+  for (int k = 0; k < 4; k++) { A.slp[k] = d.slp[k]; A.sum[k] = d.sum[k]; }
+  A.coordi[0] = d.coordi[0]; A.coordi[1] = d.coordi[1];
+  A.area[0] = d.area[0]; A.area[1] = d.area[1];
+  A.ctl = d.ctl;
+  (void)a;
   t.begin(kKScatter);
   k_scatter<<<cell_blocks(d), kBlock, 0, s>>>(A);
   if (d.n_big) k_scatter_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
@@ -354,18 +360,16 @@ int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_
   A.geo = geom(d);
   A.n_g = d.n_g;
   A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
-  A.slp = a.slp;
+  for (int k = 0; k < 4; k++) { A.slp[k] = d.slp[k]; A.sum[k] = d.sum[k]; }
+  A.ctl = d.ctl;
   A.field = d.field;
   A.g_pin_start = d.g_pin_start;
   A.g_pins = d.g_pins;
   A.pin_grad = d.pin_grad;
   A.precond = d.g_precond;
   A.big_idx = d.g_big_idx; A.d_big = d.d_big;
-  A.density_penalty = a.density_penalty;
   A.min_precond = a.min_precond;
-  A.sum_out = a.sum_out;
   A.wl_out = d.wl_out; A.d_out = d.d_out;
-  A.ref_slp = a.ref_slp; A.ref_sum = a.ref_sum;
   A.part = d.part;
   A.stride = d.part_stride;
   A.n_ovf_blocks = poisson_blocks_a(d.cnt_x, d.cnt_y);

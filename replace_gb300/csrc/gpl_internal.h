@@ -97,10 +97,13 @@ struct DeviceModel {
   float2* twiddle = nullptr;       // exp(-2 pi i k / kFftMax), k < kFftMax/2
   int32_t* g_big_idx = nullptr;    // index into big_cells or -1
   float2* d_big = nullptr;         // density gradient of big cells
-  // Nesterov vectors (float2 per gcell)
-  float2* slp[3] = {nullptr, nullptr, nullptr};   // SLP coordinates: prev/cur/next by rotation
-  float2* sum[3] = {nullptr, nullptr, nullptr};   // preconditioned sum gradients
-  float2* coordi[2] = {nullptr, nullptr};         // cur / next coordinates
+  // Nesterov vectors (float2 per gcell): slots 0-2 rotate as prev/cur/next,
+  // slot 3 holds the coordinates of the gradient-check hook (gpl_eval)
+  float2* slp[4] = {nullptr, nullptr, nullptr, nullptr};   // SLP coordinates
+  float2* sum[4] = {nullptr, nullptr, nullptr, nullptr};   // preconditioned sum gradients
+  float2* coordi[2] = {nullptr, nullptr};                  // cur / next coordinates
+  struct EvalCtl* ctl = nullptr;    // device copy of the evaluation's control record
+  struct EvalCtl* ctl_h = nullptr;  // pinned host staging
   float2* wl_out = nullptr;        // optional per-gcell WL gradient (eval hook)
   float2* d_out = nullptr;         // optional per-gcell density gradient (eval hook)
   // reduction partials
@@ -122,6 +125,21 @@ constexpr int kWaBuckets = 6;
 enum PartSlot {
   kPartOverflow = 0, kPartWl, kPartD, kPartCoordDist, kPartGradDist, kPartNan,
   kPartPhi, kPartSlots
+};
+
+// Everything that changes from one evaluation to the next.  Kernels read it
+// from device memory, so a single captured graph serves every evaluation.
+struct EvalCtl {
+  float step, coeff;            // predictor: x' = clamp(cur + step*sum), y' = clamp(x' + coeff*(x' - coordi))
+  float density_penalty;
+  float wl_coef_x, wl_coef_y;   // 1/gamma
+  int predict;                  // 1: slp[i_eval] is predicted from slot i_src and coordi[c_cur]
+  int i_src, i_eval, i_ref;     // slots of slp/sum; i_ref < 0: no step-length reference
+  int c_cur, c_next;
+  int area_cur;                 // area set scattered into; the other one is cleared
+  int write_sum;                // write sum[i_eval]
+  int write_wd;                 // write the per-gcell WL and density gradients (hook)
+  int pad[2];
 };
 
 struct EvalResult {
@@ -161,24 +179,11 @@ struct Timer {
 };
 
 // ------------------------------------------------------------------ kernels
+// Per-job constants of the evaluation kernels (the per-evaluation values
+// are in EvalCtl).
 struct EvalArgs {
-  // predictor: next = clamp(cur + step*sum), slp = clamp(next + coeff*(next - coordi))
-  bool predict = false;
-  float step = 0.0f, coeff = 0.0f;
-  const float2* cur_slp = nullptr;
-  const float2* cur_sum = nullptr;
-  const float2* cur_coordi = nullptr;
-  float2* next_coordi = nullptr;
-  float2* slp = nullptr;            // coordinates evaluated (written if predict)
-  // gradient combination
-  float density_penalty = 0.0f;
   float min_precond = 1.0f;
-  float wl_coef_x = 0.0f, wl_coef_y = 0.0f;
   float min_wl_force_bar = -300.0f;
-  float2* sum_out = nullptr;        // preconditioned sum gradient
-  const float2* ref_slp = nullptr;  // step-length reference (curSLP), may be null
-  const float2* ref_sum = nullptr;
-  bool want_phi = false;
 };
 
 // Bin-grid geometry and transform tables used by the Poisson passes.
@@ -192,8 +197,8 @@ struct PoissonGrid {
   const float2* tw;       // exp(-2 pi i m / kFftMax), [kFftMax/2]
 };
 
-int poisson_passes(const PoissonGrid& g, const unsigned long long* area,
-                   unsigned long long* area_clear, const int64_t* nonplace, float td,
+int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
+                   const EvalCtl* ctl, const int64_t* nonplace, float td,
                    const float* density_in, float* density, double* part_overflow,
                    float* spec, float* p1, float* p2, float2* field, float* fx, float* fy,
                    float* phi, cudaStream_t s, Timer* t);
@@ -203,6 +208,11 @@ void make_w4(int n, std::vector<float2>& w);
 int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t);
+// the Poisson passes of a job evaluation (area set chosen by EvalCtl)
+int launch_poisson_job(DeviceModel& d, bool want_phi, cudaStream_t s, Timer& t);
+// Sets the Poisson kernels' shared-memory limit on the current device (once
+// per device); called before a stream capture, where it must not run first.
+int poisson_prepare_device();
 int cell_grid(const DeviceModel& d);
 int launch_sum_phi(DeviceModel& d, int area_set, cudaStream_t s, Timer& t, int* n_blocks);
 int cell_blocks(const DeviceModel& d);

@@ -94,12 +94,12 @@ struct gpl_job {
   int64_t prev_hpwl = 0;
   int iter = 0, evals = 0, diverge_code = 0;
   int i_prev = 0, i_cur = 1, i_next = 2, c_cur = 0, c_next = 1;
-  const float2* last_slp = nullptr;
-  int last_area = 0;
+  int last_slot = -1;                   // slp slot of the last evaluation
+  int last_area = 0;                    // area set of the last evaluation
+  int area_next = 0;                    // area set of the next evaluation
   EvalResult last{};
-  float2* eval_xy = nullptr;
-  float2* eval_wl = nullptr;
-  float2* eval_d = nullptr;
+  cudaGraphExec_t graph_exec = nullptr; // one evaluation, replayed
+  long long graph_kernels = 0;
 };
 
 namespace {
@@ -234,9 +234,10 @@ int ensure_nb(gpl_job* j) {
   S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
   S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
   S.add(m.cnt_x, 4); S.add(m.cnt_y, 4); S.add(m.cnt_x, 8); S.add(m.cnt_y, 8); S.add(tw.size(), 8);
-  for (int k = 0; k < 3; k++) { S.add(ng, 8); S.add(ng, 8); }
+  for (int k = 0; k < 4; k++) { S.add(ng, 8); S.add(ng, 8); }
   S.add(ng, 8); S.add(ng, 8);                 // coordi
-  S.add(ng, 8); S.add(ng, 8); S.add(ng, 8);   // eval xy / wl / d
+  S.add(ng, 8); S.add(ng, 8);                 // hook outputs: wl / density gradients
+  S.add(1, sizeof(EvalCtl));
   S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
   S.add(kPartSlots, 8);
   cudaError_t e = cudaMalloc(&j->arena, S.bytes);
@@ -262,9 +263,10 @@ int ensure_nb(gpl_job* j) {
   d.wx = C.take<float>(m.cnt_x); d.wy = C.take<float>(m.cnt_y);
   d.w4x = C.take<float2>(m.cnt_x); d.w4y = C.take<float2>(m.cnt_y);
   d.twiddle = C.take<float2>(tw.size());
-  for (int k = 0; k < 3; k++) { d.slp[k] = C.take<float2>(ng); d.sum[k] = C.take<float2>(ng); }
+  for (int k = 0; k < 4; k++) { d.slp[k] = C.take<float2>(ng); d.sum[k] = C.take<float2>(ng); }
   d.coordi[0] = C.take<float2>(ng); d.coordi[1] = C.take<float2>(ng);
-  j->eval_xy = C.take<float2>(ng); j->eval_wl = C.take<float2>(ng); j->eval_d = C.take<float2>(ng);
+  d.wl_out = C.take<float2>(ng); d.d_out = C.take<float2>(ng);
+  d.ctl = C.take<EvalCtl>(1);
   d.part = C.take<double>(ps); d.part_i = C.take<long long>(nnb);
   d.result = C.take<EvalResult>(1);
   d.hpwl_total = C.take<long long>(1);
@@ -296,54 +298,122 @@ int ensure_nb(gpl_job* j) {
   GPL_CUDA(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned), s));
   GPL_CUDA(cudaMemsetAsync(d.hpwl_total, 0, sizeof(long long), s));
   if (!d.result_h) GPL_CUDA(cudaMallocHost(&d.result_h, sizeof(EvalResult)));
+  if (!d.ctl_h) GPL_CUDA(cudaMallocHost(&d.ctl_h, sizeof(EvalCtl)));
+  memset(d.ctl_h, 0, sizeof(EvalCtl));
   GPL_CUDA(cudaStreamSynchronize(s));
   j->nb_ready = true;
   return GPL_OK;
 }
 
-PoissonGrid grid_of(const DeviceModel& d) {
-  PoissonGrid g;
-  g.nx = d.cnt_x; g.ny = d.cnt_y; g.size_x = d.size_x; g.size_y = d.size_y;
-  g.core_lx = d.core_lx; g.core_ly = d.core_ly; g.core_ux = d.core_ux; g.core_uy = d.core_uy;
-  g.wx = d.wx; g.wy = d.wy; g.w4x = d.w4x; g.w4y = d.w4y; g.tw = d.twiddle;
-  return g;
+EvalArgs base_args(gpl_job* j) {
+  EvalArgs a;
+  a.min_precond = j->m.p.min_preconditioner;
+  a.min_wl_force_bar = j->m.p.min_wire_length_force_bar;
+  return a;
+}
+
+// Copies the control record to the device (stream-ordered).
+int put_ctl(gpl_job* j, const EvalCtl& c) {
+  *j->d.ctl_h = c;
+  GPL_CUDA(cudaMemcpyAsync(j->d.ctl, j->d.ctl_h, sizeof(EvalCtl), cudaMemcpyHostToDevice, j->stream));
+  return GPL_OK;
 }
 
 // Phase 1 of an evaluation: (predictor +) density scatter, then the Poisson
-// solve.  updateGCellDensityCenterLocation + updateDensityForceBin.
-int eval_phase1(gpl_job* j, const EvalArgs& a, bool want_phi) {
-  DeviceModel& d = j->d;
-  int rc = launch_scatter(d, a, j->stream, j->timer);
+// solve -- updateGCellDensityCenterLocation + updateDensityForceBin.
+int launch_phase1(gpl_job* j, bool want_phi) {
+  int rc = launch_scatter(j->d, base_args(j), j->stream, j->timer);
   if (rc) return rc;
-  const int cur = d.area_cur;
-  rc = poisson_passes(grid_of(d), d.area[cur], d.area[cur ^ 1], d.nonplace, d.target_density,
-                      nullptr, d.density, d.part + (size_t)kPartOverflow * d.part_stride, d.spec,
-                      d.p1, d.p2, d.field, nullptr, nullptr, want_phi ? d.phi : nullptr, j->stream,
-                      &j->timer);
-  if (rc) return rc;
-  j->last_area = cur;
-  d.area_cur = cur ^ 1;
-  j->last_slp = a.slp;
-  j->evals++;
-  return GPL_OK;
+  return launch_poisson_job(j->d, want_phi, j->stream, j->timer);
 }
 
-// Phase 2: WA forces, per-gcell gradients, reductions; reads the result back.
-int eval_phase2(gpl_job* j, const EvalArgs& a, bool want_phi) {
+// Phase 2: WA forces, per-gcell gradients and reductions (the gcell kernel's
+// last block writes the result record), then the record's copy to the host.
+int launch_phase2(gpl_job* j, bool want_phi, int area_set) {
   DeviceModel& d = j->d;
-  int rc = launch_wa(d, a, j->stream, j->timer);
+  int rc = launch_wa(d, base_args(j), j->stream, j->timer);
   if (rc) return rc;
   int phi_blocks = 0;
   if (want_phi) {
-    rc = launch_sum_phi(d, j->last_area, j->stream, j->timer, &phi_blocks);
+    rc = launch_sum_phi(d, area_set, j->stream, j->timer, &phi_blocks);
     if (rc) return rc;
   }
-  rc = launch_cell(d, a, phi_blocks, j->stream, j->timer);
+  rc = launch_cell(d, base_args(j), phi_blocks, j->stream, j->timer);
   if (rc) return rc;
   GPL_CUDA(cudaMemcpyAsync(d.result_h, d.result, sizeof(EvalResult), cudaMemcpyDeviceToHost, j->stream));
-  GPL_CUDA(cudaStreamSynchronize(j->stream));
-  j->last = *d.result_h;
   return GPL_OK;
+}
+
+int finish(gpl_job* j) {
+  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  j->last = *j->d.result_h;
+  return GPL_OK;
+}
+
+// The whole evaluation as one CUDA graph (control-record upload, kernels,
+// result download); every evaluation of the job replays it.
+int build_graph(gpl_job* j) {
+  if (!j->m.p.use_graph || j->graph_exec) return GPL_OK;
+  int rc0 = poisson_prepare_device();
+  if (rc0) return rc0;
+  const bool te = j->timer.enabled;
+  j->timer.enabled = false;
+  const long long k0 = j->timer.kernels;
+  cudaGraph_t g = nullptr;
+  int rc = GPL_OK;
+  if (cudaStreamBeginCapture(j->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    j->timer.enabled = te;
+    return GPL_OK;                       // stream cannot be captured: direct launches
+  }
+  cudaMemcpyAsync(j->d.ctl, j->d.ctl_h, sizeof(EvalCtl), cudaMemcpyHostToDevice, j->stream);
+  rc = launch_phase1(j, false);
+  if (!rc) rc = launch_phase2(j, false, 0);
+  cudaError_t e = cudaStreamEndCapture(j->stream, &g);
+  j->graph_kernels = j->timer.kernels - k0;
+  j->timer.kernels = k0;
+  j->timer.enabled = te;
+  if (rc || e != cudaSuccess || !g) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    return GPL_OK;
+  }
+  if (cudaGraphInstantiate(&j->graph_exec, g, 0) != cudaSuccess) {
+    cudaGetLastError();
+    j->graph_exec = nullptr;
+  }
+  cudaGraphDestroy(g);
+  return GPL_OK;
+}
+
+// One evaluation at control record c (area set chosen here).
+int evaluate(gpl_job* j, EvalCtl c, bool want_phi) {
+  c.area_cur = j->area_next;
+  int rc = GPL_OK;
+  if (j->graph_exec && !want_phi && !j->timer.enabled) {
+    *j->d.ctl_h = c;
+    GPL_CUDA(cudaGraphLaunch(j->graph_exec, j->stream));
+    j->timer.count((int)j->graph_kernels);
+  } else {
+    rc = put_ctl(j, c);
+    if (!rc) rc = launch_phase1(j, want_phi);
+    if (!rc) rc = launch_phase2(j, want_phi, c.area_cur);
+  }
+  if (rc) return rc;
+  j->last_area = c.area_cur;
+  j->area_next = c.area_cur ^ 1;
+  j->last_slot = c.i_eval;
+  j->evals++;
+  return finish(j);
+}
+
+// Phase 2 again with a new control record (same coordinates and bins).
+int rerun_phase2(gpl_job* j, EvalCtl c) {
+  c.area_cur = j->last_area;
+  int rc = put_ctl(j, c);
+  if (!rc) rc = launch_phase2(j, false, c.area_cur);
+  if (rc) return rc;
+  return finish(j);
 }
 
 float overflow_ratio(const gpl_job* j) {
@@ -363,21 +433,32 @@ void update_wl_coef(gpl_job* j, float overflow) {
   j->wl_coef_y = c * j->base_wl_coef;
 }
 
-EvalArgs base_args(gpl_job* j) {
-  EvalArgs a;
-  a.density_penalty = j->density_penalty;
-  a.min_precond = j->m.p.min_preconditioner;
-  a.wl_coef_x = j->wl_coef_x;
-  a.wl_coef_y = j->wl_coef_y;
-  a.min_wl_force_bar = j->m.p.min_wire_length_force_bar;
-  return a;
+EvalCtl ctl_of(gpl_job* j, int i_eval, int i_ref, bool write_sum) {
+  EvalCtl c;
+  memset(&c, 0, sizeof(c));
+  c.density_penalty = j->density_penalty;
+  c.wl_coef_x = j->wl_coef_x;
+  c.wl_coef_y = j->wl_coef_y;
+  c.i_src = j->i_cur;
+  c.i_eval = i_eval;
+  c.i_ref = i_ref;
+  c.c_cur = j->c_cur;
+  c.c_next = j->c_next;
+  c.write_sum = write_sum ? 1 : 0;
+  return c;
 }
 
 bool bad(double v) { return std::isnan(v) || std::isinf(v); }
 
+bool diverged(const gpl_job* j) {
+  return bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0;
+}
+
 // NesterovPlace::init (src/nesterovPlace.cpp:64-175)
 int nesterov_init(gpl_job* j) {
   int rc = ensure_nb(j);
+  if (rc) return rc;
+  rc = build_graph(j);
   if (rc) return rc;
   HostModel& m = j->m;
   DeviceModel& d = j->d;
@@ -401,23 +482,18 @@ int nesterov_init(gpl_job* j) {
   GPL_CUDA(cudaMemcpyAsync(d.coordi[j->c_cur], d.slp[j->i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
   j->density_penalty = 0.0f;
   j->max_phi_coef = m.p.max_phi_coef;
-  // first evaluation at the initial centres
-  EvalArgs a = base_args(j);
-  a.slp = d.slp[j->i_cur];
-  rc = eval_phase1(j, a, false);
-  if (rc) return rc;
-  rc = eval_phase2(j, a, false);   // overflow and HPWL at curSLP
+  j->wl_coef_x = j->wl_coef_y = 0.0f;
+  // first evaluation at the initial centres: overflow and HPWL
+  rc = evaluate(j, ctl_of(j, j->i_cur, -1, false), false);
   if (rc) return rc;
   j->prev_hpwl = j->last.hpwl;
   j->base_wl_coef = (float)(m.p.init_wire_length_coef / ((float)(m.size_x + m.size_y) * 0.5));
   j->sum_overflow = overflow_ratio(j);
   update_wl_coef(j, j->sum_overflow);
-  a = base_args(j);
-  a.slp = d.slp[j->i_cur];
-  a.sum_out = d.sum[j->i_cur];
-  rc = eval_phase2(j, a, false);
+  // the WA forces and gradients with the wire-length coefficients set
+  rc = rerun_phase2(j, ctl_of(j, j->i_cur, -1, true));
   if (rc) return rc;
-  if (bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0) {
+  if (diverged(j)) {
     j->is_diverged = true; j->diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
     set_error("RePlAce diverged. Please tune the parameters again");
     return GPL_ERR_DIVERGED_INIT;
@@ -426,16 +502,9 @@ int nesterov_init(gpl_job* j) {
   rc = launch_initial_prev(d, d.slp[j->i_cur], d.sum[j->i_cur], m.p.initial_prev_coordi_update_coef,
                            d.slp[j->i_prev], j->stream, j->timer);
   if (rc) return rc;
-  a = base_args(j);
-  a.slp = d.slp[j->i_prev];
-  a.sum_out = d.sum[j->i_prev];
-  a.ref_slp = d.slp[j->i_cur];
-  a.ref_sum = d.sum[j->i_cur];
-  rc = eval_phase1(j, a, false);
+  rc = evaluate(j, ctl_of(j, j->i_prev, j->i_cur, true), false);
   if (rc) return rc;
-  rc = eval_phase2(j, a, false);
-  if (rc) return rc;
-  if (bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0) {
+  if (diverged(j)) {
     j->is_diverged = true; j->diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
     set_error("RePlAce diverged. Please tune the parameters again");
     return GPL_ERR_DIVERGED_INIT;
@@ -456,7 +525,6 @@ int nesterov_init(gpl_job* j) {
 // NesterovPlace::doNesterovPlace (src/nesterovPlace.cpp:275-472), resumable
 int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
   HostModel& m = j->m;
-  DeviceModel& d = j->d;
   const gpl_params& p = m.p;
   if (j->diverge_code == GPL_ERR_DIVERGED_INIT) { j->finished = true; return j->diverge_code; }
   int done = 0;
@@ -468,23 +536,13 @@ int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
     const float coeff = (float)((prev_a - 1.0) / j->cur_a);
     int bt = 0;
     for (bt = 0; bt < p.max_back_track; bt++) {
-      EvalArgs a = base_args(j);
-      a.predict = true;
-      a.step = j->step_length;
-      a.coeff = coeff;
-      a.cur_slp = d.slp[j->i_cur];
-      a.cur_sum = d.sum[j->i_cur];
-      a.cur_coordi = d.coordi[j->c_cur];
-      a.next_coordi = d.coordi[j->c_next];
-      a.slp = d.slp[j->i_next];
-      a.sum_out = d.sum[j->i_next];
-      a.ref_slp = d.slp[j->i_cur];
-      a.ref_sum = d.sum[j->i_cur];
-      int rc = eval_phase1(j, a, false);
+      EvalCtl c = ctl_of(j, j->i_next, j->i_cur, true);
+      c.predict = 1;
+      c.step = j->step_length;
+      c.coeff = coeff;
+      int rc = evaluate(j, c, false);
       if (rc) return rc;
-      rc = eval_phase2(j, a, false);
-      if (rc) return rc;
-      if (bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0) {
+      if (diverged(j)) {
         j->is_diverged = true;
         break;
       }
@@ -610,7 +668,7 @@ void gpl_params_default(gpl_params* p) {
   p->verbose_level = 0;
   p->device = 0;
   p->stream = nullptr;
-  p->use_graph = 0;
+  p->use_graph = 1;
 }
 
 gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
@@ -639,8 +697,10 @@ void gpl_destroy(gpl_job* j) {
   cudaSetDevice(j->device);
   if (j->stream) cudaStreamSynchronize(j->stream);
   j->timer.release();
+  if (j->graph_exec) cudaGraphExecDestroy(j->graph_exec);
   if (j->arena) cudaFree(j->arena);
   if (j->d.result_h) cudaFreeHost(j->d.result_h);
+  if (j->d.ctl_h) cudaFreeHost(j->d.ctl_h);
   if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
   delete j;
 }
@@ -677,10 +737,10 @@ gpl_status gpl_get_inst_locations(gpl_job* j, int32_t* lx, int32_t* ly) {
   if (!j || !lx || !ly) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
   const HostModel& m = j->m;
   for (int i = 0; i < m.n_insts; i++) { lx[i] = m.ilx[i]; ly[i] = m.ily[i]; }
-  if (j->np_ready && j->last_slp) {
+  if (j->np_ready && j->last_slot >= 0) {
     // NesterovPlace::updateDb: lx = dCx - dDx/2 at the last evaluated centres
     std::vector<float2> c(m.n_g);
-    GPL_CUDA(cudaMemcpyAsync(c.data(), j->last_slp, m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+    GPL_CUDA(cudaMemcpyAsync(c.data(), j->d.slp[j->last_slot], m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
     GPL_CUDA(cudaStreamSynchronize(j->stream));
     for (int k = 0; k < m.n_place; k++) {
       const int i = m.place_insts[k];
@@ -708,23 +768,19 @@ gpl_status gpl_eval(gpl_job* j, const float* xy, float cx, float cy, float* wl_g
   if (rc) return (gpl_status)rc;
   DeviceModel& d = j->d;
   const size_t ng = j->m.n_g;
-  rc = upload(j->eval_xy, xy, ng * sizeof(float2), j->stream);
+  // slot 3 of the coordinate / gradient-sum buffers belongs to this hook
+  rc = upload(d.slp[3], xy, ng * sizeof(float2), j->stream);
   if (rc) return (gpl_status)rc;
-  EvalArgs a;
-  a.slp = j->eval_xy;
-  a.wl_coef_x = cx; a.wl_coef_y = cy;
-  a.min_wl_force_bar = j->m.p.min_wire_length_force_bar;
-  a.min_precond = j->m.p.min_preconditioner;
-  rc = eval_phase1(j, a, true);
+  EvalCtl c;
+  memset(&c, 0, sizeof(c));
+  c.wl_coef_x = cx; c.wl_coef_y = cy;
+  c.i_src = 3; c.i_eval = 3; c.i_ref = -1;
+  c.c_cur = 0; c.c_next = 1;
+  c.write_sum = 1; c.write_wd = 1;
+  rc = evaluate(j, c, true);
   if (rc) return (gpl_status)rc;
-  d.wl_out = j->eval_wl;
-  d.d_out = j->eval_d;
-  rc = eval_phase2(j, a, true);
-  d.wl_out = nullptr;
-  d.d_out = nullptr;
-  if (rc) return (gpl_status)rc;
-  if (wl_grad) GPL_CUDA(cudaMemcpyAsync(wl_grad, j->eval_wl, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
-  if (density_grad) GPL_CUDA(cudaMemcpyAsync(density_grad, j->eval_d, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+  if (wl_grad) GPL_CUDA(cudaMemcpyAsync(wl_grad, d.wl_out, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+  if (density_grad) GPL_CUDA(cudaMemcpyAsync(density_grad, d.d_out, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
   GPL_CUDA(cudaStreamSynchronize(j->stream));
   if (st) {
     st->overflow_area_f64 = j->last.overflow;

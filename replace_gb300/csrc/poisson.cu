@@ -110,8 +110,8 @@ struct PassAArgs {
   int nx, ny, logn, pairs_per_block;
   int core_lx, core_ly, core_ux, core_uy, size_x, size_y;
   float td;
-  const unsigned long long* area;    // inst [nb] then filler [nb]
-  unsigned long long* area_clear;    // other buffer to zero (may be null)
+  unsigned long long* area_pair[2];  // two sets of inst [nb] then filler [nb]
+  const EvalCtl* ctl;                // area_cur: the set to read (the other is zeroed)
   const int64_t* nonplace;
   const float* density_in;           // standalone mode: density given
   float* density;
@@ -130,6 +130,13 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
   float2* buf1 = smem + rp_n * n;
   const int nb = A.nx * A.ny;
   double ovf = 0.0;
+  const unsigned long long* area = nullptr;
+  unsigned long long* area_clear = nullptr;
+  if (A.ctl) {
+    const int cur = A.ctl->area_cur;
+    area = A.area_pair[cur];
+    area_clear = A.area_pair[cur ^ 1];
+  }
   for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
     const int rp = idx / n, i = idx - rp * n;
     const int r = blockIdx.x * rp_n + rp;
@@ -148,13 +155,14 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
           const int buy = min(bly + A.size_y, A.core_uy);
           const long long bin_area = (long long)(bux - blx) * (long long)(buy - bly);
           const float cap = __fmul_rn(__ll2float_rn(bin_area), A.td);
-          const float fi = __ll2float_rn((long long)A.area[b]);
-          const float ff = __ll2float_rn((long long)A.area[nb + b]);
+          const float fi = __ll2float_rn((long long)area[b]);
+          const float ff = __ll2float_rn((long long)area[nb + b]);
           const float fn = __ll2float_rn(A.nonplace[b]);
           // BinGrid::updateBinsGCellDensityArea (src/nesterovBase.cpp:804-818)
           dd[h] = __fdiv_rn(__fadd_rn(__fadd_rn(fi, ff), fn), cap);
           ovf += (double)fmaxf(0.0f, __fsub_rn(__fadd_rn(fi, fn), cap));
-          if (A.area_clear) { A.area_clear[b] = 0ull; A.area_clear[nb + b] = 0ull; }
+          area_clear[b] = 0ull;
+          area_clear[nb + b] = 0ull;
           A.density[b] = dd[h];
         }
       }
@@ -387,7 +395,7 @@ size_t smem_c(int nx, int ny) { return (size_t)4 * pairs_c(nx, ny) * nx * sizeof
 int poisson_blocks_a(int nx, int ny) { int r = pairs_a(nx, ny); return (ny / 2 + r - 1) / r; }
 
 // The dynamic shared-memory limit is a per-device function attribute.
-static int ensure_smem_attrs() {
+int poisson_prepare_device() {
   static std::mutex mu;
   static bool done[64] = {false};
   int dev = 0;
@@ -405,19 +413,21 @@ static int ensure_smem_attrs() {
 
 // The three passes on arbitrary device arrays.  Area mode (area != null):
 // the density comes from the int64 areas; otherwise from density_in.
-int poisson_passes(const PoissonGrid& g, const unsigned long long* area,
-                   unsigned long long* area_clear, const int64_t* nonplace, float td,
+int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
+                   const EvalCtl* ctl, const int64_t* nonplace, float td,
                    const float* density_in, float* density, double* part_overflow,
                    float* spec, float* p1, float* p2, float2* field, float* fx, float* fy,
                    float* phi, cudaStream_t s, Timer* t) {
-  int rc = ensure_smem_attrs();
+  int rc = poisson_prepare_device();
   if (rc) return rc;
   const int nx = g.nx, ny = g.ny;
   PassAArgs A;
   A.nx = nx; A.ny = ny; A.logn = ilog2(nx); A.pairs_per_block = pairs_a(nx, ny);
   A.core_lx = g.core_lx; A.core_ly = g.core_ly; A.core_ux = g.core_ux; A.core_uy = g.core_uy;
   A.size_x = g.size_x; A.size_y = g.size_y; A.td = td;
-  A.area = area; A.area_clear = area_clear; A.nonplace = nonplace;
+  A.area_pair[0] = area_pair ? area_pair[0] : nullptr;
+  A.area_pair[1] = area_pair ? area_pair[1] : nullptr;
+  A.ctl = ctl; A.nonplace = nonplace;
   A.density_in = density_in; A.density = density; A.spec = spec;
   A.part_overflow = part_overflow; A.tw = g.tw; A.w4 = g.w4x;
   if (t) t->begin(kKPoissonA);
@@ -440,6 +450,16 @@ int poisson_passes(const PoissonGrid& g, const unsigned long long* area,
   if (t) t->count(3);
   GPL_CUDA(cudaGetLastError());
   return GPL_OK;
+}
+
+int launch_poisson_job(DeviceModel& d, bool want_phi, cudaStream_t s, Timer& t) {
+  PoissonGrid g;
+  g.nx = d.cnt_x; g.ny = d.cnt_y; g.size_x = d.size_x; g.size_y = d.size_y;
+  g.core_lx = d.core_lx; g.core_ly = d.core_ly; g.core_ux = d.core_ux; g.core_uy = d.core_uy;
+  g.wx = d.wx; g.wy = d.wy; g.w4x = d.w4x; g.w4y = d.w4y; g.tw = d.twiddle;
+  return poisson_passes(g, d.area, d.ctl, d.nonplace, d.target_density, nullptr, d.density,
+                        d.part + (size_t)kPartOverflow * d.part_stride, d.spec, d.p1, d.p2,
+                        d.field, nullptr, nullptr, want_phi ? d.phi : nullptr, s, &t);
 }
 
 void make_w4(int n, std::vector<float2>& w) {

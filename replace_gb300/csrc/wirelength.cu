@@ -32,8 +32,10 @@ struct WaArgs {
   int block_start[kWaBuckets + 1];    // first block of each bucket
   const int32_t* net_start;     // pin CSR of the bucket-ordered nets
   const int4* pins;             // (gcell or -1, x offset or position, y ..., unused)
-  const float2* slp;
-  float cx, cy;                 // wire-length coefficients (1/gamma)
+  float2* slp_all[4];
+  const EvalCtl* ctl;
+  const float2* slp;            // this evaluation's coordinates (set from ctl)
+  float cx, cy;                 // wire-length coefficients (1/gamma, from ctl)
   float bar;                    // minWireLengthForceBar
   float2* pin_grad;             // device pin order
   long long* part_i;            // HPWL partial per block
@@ -175,6 +177,12 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int lo
 
 __global__ void __launch_bounds__(kBlock) k_wa(WaArgs A) {
   __shared__ long long sh[32];
+  {
+    const EvalCtl C = *A.ctl;
+    A.slp = A.slp_all[C.i_eval];
+    A.cx = C.wl_coef_x;
+    A.cy = C.wl_coef_y;
+  }
   int bucket = 0;
   while (bucket < kWaBuckets - 1 && (int)blockIdx.x >= A.block_start[bucket + 1]) bucket++;
   const int lb = blockIdx.x - A.block_start[bucket];
@@ -208,8 +216,10 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   }
   A.net_start = d.net_start;
   A.pins = d.pins;
-  A.slp = a.slp;
-  A.cx = a.wl_coef_x; A.cy = a.wl_coef_y;
+  for (int k = 0; k < 4; k++) A.slp_all[k] = d.slp[k];
+  A.ctl = d.ctl;
+  A.slp = nullptr;
+  A.cx = A.cy = 0.0f;
   A.bar = a.min_wl_force_bar;
   A.pin_grad = d.pin_grad;
   A.part_i = d.part_i;

@@ -66,6 +66,24 @@ def test_run_is_deterministic_and_resumable(gpu_lib):
     assert np.array_equal(logs[0][0], logs[1][0]) and np.array_equal(logs[0][1], logs[1][1])
 
 
+def test_graph_replay_matches_direct_launches(gpu_lib):
+    """An evaluation replayed from the captured CUDA graph and one launched
+    kernel by kernel run the same kernels on the same control record."""
+    from replace_gb300 import Placer
+    nl, opts = case("syn10k_b128")
+    out = []
+    for g in (1, 0):
+        p = Placer(nl, **params_of(opts), use_graph=g)
+        p.initial_place()
+        p.nesterov_init()
+        rc, st, lg = p.nesterov_run(60, log_capacity=100)
+        lx, ly = p.inst_locations()
+        out.append((lg["overflow"], lg["hpwl"], lg["step_length"], lx, ly, st.evaluations))
+        p.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
+
+
 def test_replace_api_global_placement(gpu_lib):
     from replace_gb300 import global_placement
     nl, _ = case("simple01")
