@@ -50,7 +50,9 @@ typedef enum gpl_status {
   GPL_ERR_CUDA = 17,
   GPL_ERR_OUT_OF_MEMORY = 18,
   GPL_ERR_BAD_STATE = 19,
-  GPL_ERR_NO_DEVICE = 20
+  GPL_ERR_NO_DEVICE = 20,
+  /* A server job cancelled before it finished (gpl_server_cancel). */
+  GPL_ERR_CANCELLED = 21
 } gpl_status;
 
 /* Instance kinds (PlacerBase::init, src/placerBase.cpp:639-680). */
@@ -270,6 +272,67 @@ int32_t gpl_kernel_times(struct gpl_job* job, const char** names, double* ms,
 void gpl_kernel_times_reset(struct gpl_job* job, int32_t enable);
 /* Number of kernels the job has launched since the last reset. */
 int64_t gpl_kernel_launch_count(struct gpl_job* job);
+
+/* ------------------------------------------------------------------------
+ * Placement server: continuous batching of independent jobs on one GPU.
+ * No reference counterpart: RePlAce places one design per process.  A
+ * server keeps up to max_active jobs resident and running at once, each on
+ * its own stream with its own CUDA graph, so their kernels overlap on the
+ * device.  Jobs are admitted in submission order as a slot frees and their
+ * device footprint (an upper bound, computed at submission) fits the HBM
+ * budget next to the jobs already resident; a job joins when admitted and
+ * retires when its Nesterov loop ends, between iterations.  Each job runs
+ * the same kernels on its own buffers as gpl_create + gpl_initial_place +
+ * gpl_nesterov_init + gpl_nesterov_run would, so its result does not depend
+ * on the other jobs.
+ * Threading: the server's calls may come from any thread; it runs one host
+ * thread per slot. */
+typedef struct gpl_server gpl_server;
+
+typedef struct gpl_server_params {
+  int32_t device;             /* CUDA device ordinal */
+  int32_t max_active;         /* slots: jobs resident and running at once (8) */
+  int64_t hbm_budget_bytes;   /* device bytes the jobs may hold together;
+                                 0 = 80 % of the free memory at creation */
+  int32_t chunk_iters;        /* Nesterov iterations between cancel checks (64) */
+  int32_t run_initial_place;  /* 1 = gpl_initial_place before the Nesterov loop (1) */
+} gpl_server_params;
+
+typedef struct gpl_server_result {
+  int64_t ticket;
+  int32_t status;             /* gpl_status of the job */
+  int32_t finished;           /* 1 = the Nesterov loop reached its stop rule */
+  int32_t iterations;         /* Nesterov iterations */
+  int32_t ip_rounds;          /* initial-place rounds */
+  float overflow;             /* final overflow */
+  int32_t n_insts;
+  int64_t hpwl;               /* final pin HPWL (DBU) */
+  int64_t device_bytes;       /* footprint reserved at admission */
+  double submit_s, admit_s, finish_s;   /* seconds since the server started */
+  char message[160];          /* gpl_last_error text when status != 0 */
+} gpl_server_result;
+
+void gpl_server_params_default(gpl_server_params* p);
+gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out);
+/* Copies the netlist (the caller's arrays may be freed on return) and queues
+ * the job.  Invalid netlists and jobs whose footprint exceeds the budget are
+ * rejected here.  *ticket identifies the job in the calls below. */
+gpl_status gpl_server_submit(gpl_server* s, const gpl_netlist_desc* nl, const gpl_params* p,
+                             int64_t* ticket);
+/* Up to capacity results of jobs that ended since the last poll, waiting up
+ * to wait_ms for the first one; returns how many were written. */
+int32_t gpl_server_poll(gpl_server* s, gpl_server_result* out, int32_t capacity, int32_t wait_ms);
+/* Final instance locations of an ended job ([n_insts] each), as
+ * gpl_get_inst_locations gives them. */
+gpl_status gpl_server_get_inst_locations(gpl_server* s, int64_t ticket, int32_t* lx, int32_t* ly);
+/* Drops an ended job's result and locations. */
+gpl_status gpl_server_release(gpl_server* s, int64_t ticket);
+/* A queued job ends at once; a running one at its next chunk boundary. */
+gpl_status gpl_server_cancel(gpl_server* s, int64_t ticket);
+/* Numbers of jobs queued, running and ended-but-not-polled. */
+void gpl_server_counts(gpl_server* s, int32_t* queued, int32_t* running, int32_t* ended);
+/* Cancels queued jobs, waits for the running ones, frees everything. */
+void gpl_server_destroy(gpl_server* s);
 
 #ifdef __cplusplus
 }

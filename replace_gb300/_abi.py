@@ -18,6 +18,7 @@ GPL_ERR_CUDA = 17
 GPL_ERR_OUT_OF_MEMORY = 18
 GPL_ERR_BAD_STATE = 19
 GPL_ERR_NO_DEVICE = 20
+GPL_ERR_CANCELLED = 21
 
 _i32p = C.POINTER(C.c_int32)
 _u8p = C.POINTER(C.c_uint8)
@@ -107,6 +108,23 @@ class IpStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int32), ("last_error", C.c_float), ("last_hpwl", C.c_int64),
         ("solver_iters_x", C.c_int32), ("solver_iters_y", C.c_int32),
+    ]
+
+
+class ServerParams(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32), ("max_active", C.c_int32), ("hbm_budget_bytes", C.c_int64),
+        ("chunk_iters", C.c_int32), ("run_initial_place", C.c_int32),
+    ]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [
+        ("ticket", C.c_int64), ("status", C.c_int32), ("finished", C.c_int32),
+        ("iterations", C.c_int32), ("ip_rounds", C.c_int32), ("overflow", C.c_float),
+        ("n_insts", C.c_int32), ("hpwl", C.c_int64), ("device_bytes", C.c_int64),
+        ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double),
+        ("message", C.c_char * 160),
     ]
 
 

@@ -51,6 +51,12 @@ struct HostModel {
 };
 
 int build_placer_base(HostModel& m, const gpl_netlist_desc* d, const gpl_params* p);
+// counts of the NesterovBase and BinGrid that size a job's device memory
+struct NbCounts {
+  int fill_dx = 0, fill_dy = 0, n_fill = 0;
+  int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
+};
+int nb_counts(const HostModel& m, NbCounts* c);
 int build_nesterov_base(HostModel& m);
 // InitialPlace::placeInstsCenter + Instance::setCenterLocation
 void host_place_center(HostModel& m);
@@ -153,6 +159,27 @@ struct EvalResult {
   int pad;
 };
 
+// Pinned host staging of one job: the evaluation's control record and result
+// and the initial place's solver scalars.  A job allocates its own, or a
+// server hands each of its slots one for the life of the server (freeing
+// pinned memory may synchronise the device).
+struct HostPinned {
+  EvalResult result;
+  EvalCtl ctl;
+  alignas(16) unsigned char ip_state[1024];
+};
+
+// Device memory of a job: from a stream-ordered pool when one is given (a
+// server's; allocation and release never synchronise the device), else
+// cudaMalloc / cudaFree.
+inline cudaError_t dev_alloc(void** p, size_t bytes, cudaMemPool_t pool, cudaStream_t s) {
+  return pool ? cudaMallocFromPoolAsync(p, bytes, pool, s) : cudaMalloc(p, bytes);
+}
+inline void dev_free(void* p, cudaMemPool_t pool, cudaStream_t s) {
+  if (!p) return;
+  if (pool) cudaFreeAsync(p, s); else cudaFree(p);
+}
+
 // kernel-class timing (CUDA events around each launch when enabled)
 enum KernelClass { kKScatter = 0, kKPoissonA, kKPoissonB, kKPoissonC, kKWa, kKCell,
                    kKReduce, kKOther, kKClasses };
@@ -222,7 +249,20 @@ int wa_nets_per_block(int bucket);
 
 // InitialPlace::doBicgstabPlace rounds on the device (initial_place.cu); on
 // return the host model's movable instances are at the solution.
-int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& t);
+// `pinned` is the job's ip_state block; `pool` as for dev_alloc.
+int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& t,
+                      void* pinned, cudaMemPool_t pool);
+// device bytes run_initial_place allocates for this model
+size_t initial_place_bytes(const HostModel& m, int sm_count);
+
+// A job's host model without a stream or staging (a server binds those when
+// it admits the job), and the binding: stream, pinned staging and pool stay
+// the caller's.
+int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out);
+void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool);
+// Upper bound of the device bytes the job will hold at once (initial place
+// scratch or the Nesterov arena, whichever is larger).
+int job_device_bytes(gpl_job* j, int64_t* bytes);
 
 // twiddle / frequency tables (host computed, double precision)
 void make_twiddle(std::vector<float2>& tw);

@@ -436,7 +436,45 @@ int blocks_for(int n) { return std::max(1, (n + kB - 1) / kB); }
 
 // Runs the initial place on the device; on return the host model's
 // instances (and pins) are at the solution.  stats may be null.
-int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& timer) {
+struct IpSizes {
+  size_t nnz_cap = 1, bytes = 0;
+  int grid = 1;
+};
+
+// Scratch layout of run_initial_place (the sizes its carving below takes).
+IpSizes ip_sizes(const HostModel& m, int sm_count) {
+  IpSizes z;
+  const size_t nP = m.place_insts.size();
+  size_t n_mp = 0;
+  for (int i : m.place_insts) n_mp += m.inst_pin_start[i + 1] - m.inst_pin_start[i];
+  // an upper bound of the off-diagonal entries: every movable pin of a used
+  // net partners every other pin of that net
+  size_t nnz = 0;
+  for (int n = 0; n < m.n_nets; n++) {
+    const size_t deg = m.net_start[n + 1] - m.net_start[n];
+    if (deg > 1 && (int)deg < m.p.initial_place_max_fanout) nnz += deg * (deg - 1);
+  }
+  z.nnz_cap = std::max<size_t>(nnz, 1);
+  const int nb_mov = blocks_for((int)nP);
+  z.grid = std::max(1, std::min(nb_mov, sm_count * 8));
+  const size_t scan_blocks = nb_mov;
+  size_t bytes = 0;
+  auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
+  add((m.n_nets + 1) * 4); add(m.n_pins * 4); add(m.n_pins * 4); add(m.n_pins * 4);
+  add(m.n_pins * 8); add(m.n_pins * 8); add((nP + 1) * 4); add(n_mp * 4);
+  add(nP * 8); add(m.n_pins * 8); add(m.n_nets * 16); add(2 * nP * 4); add(2 * (nP + 1) * 4);
+  add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 4);
+  for (int k = 0; k < 9; k++) add(2 * nP * 4);
+  add(2 * 2 * (size_t)z.grid * 8); add(16 * 4); add(2 * sizeof(BiState));
+  z.bytes = bytes;
+  return z;
+}
+
+size_t initial_place_bytes(const HostModel& m, int sm_count) { return ip_sizes(m, sm_count).bytes; }
+
+int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& timer,
+                      void* pinned, cudaMemPool_t pool) {
+  static_assert(2 * sizeof(BiState) <= sizeof(HostPinned::ip_state), "pinned solver state too small");
   const gpl_params& prm = m.p;
   IpDev D;
   D.n_mov = (int)m.place_insts.size();
@@ -466,30 +504,16 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     const int i = m.place_insts[k];
     ctr[k] = make_int2((m.ilx[i] + m.iux[i]) / 2, (m.ily[i] + m.iuy[i]) / 2);
   }
-  // an upper bound of the off-diagonal entries: every movable pin of a used
-  // net partners every other pin of that net
-  size_t nnz = 0;
-  for (int n = 0; n < m.n_nets; n++) {
-    const size_t deg = m.net_start[n + 1] - m.net_start[n];
-    if (deg > 1 && (int)deg < prm.initial_place_max_fanout) nnz += deg * (deg - 1);
-  }
-  D.nnz_cap = std::max<size_t>(nnz, 1);
+  const IpSizes z = ip_sizes(m, sm_count);
+  D.nnz_cap = z.nnz_cap;
   const int nb_mov = blocks_for(nP);
-  const int grid = std::max(1, std::min(nb_mov, sm_count * 8));
+  const int grid = z.grid;
   D.parts = grid;
   const int scan_blocks = nb_mov;
-
-  size_t bytes = 0;
-  auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
-  add((m.n_nets + 1) * 4); add(m.n_pins * 4); add(m.n_pins * 4); add(m.n_pins * 4);
-  add(m.n_pins * 8); add(m.n_pins * 8); add((nP + 1) * 4); add(mp.size() * 4);
-  add(nP * 8); add(m.n_pins * 8); add(m.n_nets * 16); add(2 * nP * 4); add(2 * (nP + 1) * 4);
-  add(2 * scan_blocks * 4); add(2 * D.nnz_cap * 4); add(2 * D.nnz_cap * 4);
-  for (int k = 0; k < 9; k++) add(2 * nP * 4);
-  add(2 * 2 * (size_t)D.parts * 8); add(16 * 4); add(2 * sizeof(BiState));
-  cudaError_t e = cudaMalloc(&D.mem, bytes);
+  cudaError_t e = dev_alloc((void**)&D.mem, z.bytes, pool, s);
   if (e != cudaSuccess) {
-    set_error(std::string("initial place: cudaMalloc failed: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    set_error(std::string("initial place: device allocation failed: ") + cudaGetErrorString(e));
     return GPL_ERR_OUT_OF_MEMORY;
   }
   char* cur = D.mem;
@@ -536,12 +560,10 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   up(D.mov_pins, mp.data(), mp.size() * 4);
   up(D.ctr, ctr.data(), nP * 8);
   if (!rc && cudaMemsetAsync(D.counters, 0, 16 * 4, s) != cudaSuccess) rc = GPL_ERR_CUDA;
-  BiState* st_h = nullptr;
-  if (!rc && cudaMallocHost(&st_h, 2 * sizeof(BiState)) != cudaSuccess) rc = GPL_ERR_CUDA;
+  BiState* st_h = static_cast<BiState*>(pinned);
   if (rc) {
     set_error("initial place: upload failed");
-    cudaFree(D.mem);
-    if (st_h) cudaFreeHost(st_h);
+    dev_free(D.mem, pool, s);
     return rc;
   }
   IpParams P;
@@ -600,8 +622,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     if (cudaMemcpyAsync(ctr.data(), D.ctr, nP * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) rc = GPL_ERR_CUDA;
   }
-  cudaFree(D.mem);
-  cudaFreeHost(st_h);
+  dev_free(D.mem, pool, s);
   if (rc) { set_error("initial place: CUDA error"); return rc; }
   if (rounds > 0)
     for (int k = 0; k < nP; k++) host_set_inst_center(m, m.place_insts[k], ctr[k].x, ctr[k].y);

@@ -85,6 +85,9 @@ struct gpl_job {
   bool own_stream = false;
   Timer timer;
   char* arena = nullptr;
+  HostPinned* pinned = nullptr;        // control/result staging
+  bool own_pinned = false;
+  cudaMemPool_t pool = nullptr;         // stream-ordered pool (server jobs)
   bool nb_ready = false, np_ready = false;
   // NesterovPlace state (src/nesterovPlace.h:76-125)
   float step_length = 0, density_penalty = 0, base_wl_coef = 0, wl_coef_x = 0, wl_coef_y = 0;
@@ -136,6 +139,27 @@ struct Carver {
     return p;
   }
 };
+
+// Bytes of a job's arena (the carving in ensure_nb follows the same order).
+size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size_t n_big, size_t nb,
+                   int cnt_x, int cnt_y, size_t part_stride, size_t nnb) {
+  const size_t ps = (size_t)kPartSlots * part_stride;
+  Sizer S;
+  S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
+  S.add(n_big, 4); S.add(ng, 4); S.add(n_big, 8);
+  S.add(n_pins, 16); S.add(n_nets + 1, 4);
+  S.add(n_pins, 8); S.add(n_gpins, 4);
+  S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
+  S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
+  S.add(cnt_x, 4); S.add(cnt_y, 4); S.add(cnt_x, 8); S.add(cnt_y, 8); S.add(kFftMax / 2, 8);
+  for (int k = 0; k < 4; k++) { S.add(ng, 8); S.add(ng, 8); }
+  S.add(ng, 8); S.add(ng, 8);                 // coordi
+  S.add(ng, 8); S.add(ng, 8);                 // hook outputs: wl / density gradients
+  S.add(1, sizeof(EvalCtl));
+  S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
+  S.add(kPartSlots, 8);
+  return S.bytes;
+}
 
 // NesterovBase on the host, then the device model (one arena).
 int ensure_nb(gpl_job* j) {
@@ -226,27 +250,16 @@ int ensure_nb(gpl_job* j) {
   const size_t nnb = std::max(net_blocks(d), 1);
   const size_t ps = (size_t)kPartSlots * d.part_stride;
 
-  Sizer S;
-  S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
-  S.add(big.size(), 4); S.add(ng, 4); S.add(big.size(), 8);
-  S.add(m.n_pins, 16); S.add(m.n_nets + 1, 4);
-  S.add(m.n_pins, 8); S.add(m.g_pins.size(), 4);
-  S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
-  S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
-  S.add(m.cnt_x, 4); S.add(m.cnt_y, 4); S.add(m.cnt_x, 8); S.add(m.cnt_y, 8); S.add(tw.size(), 8);
-  for (int k = 0; k < 4; k++) { S.add(ng, 8); S.add(ng, 8); }
-  S.add(ng, 8); S.add(ng, 8);                 // coordi
-  S.add(ng, 8); S.add(ng, 8);                 // hook outputs: wl / density gradients
-  S.add(1, sizeof(EvalCtl));
-  S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
-  S.add(kPartSlots, 8);
-  cudaError_t e = cudaMalloc(&j->arena, S.bytes);
+  const size_t bytes = arena_bytes(ng, m.n_pins, m.n_nets, m.g_pins.size(), big.size(), nb, m.cnt_x,
+                                   m.cnt_y, d.part_stride, nnb);
+  cudaError_t e = dev_alloc((void**)&j->arena, bytes, j->pool, j->stream);
   if (e != cudaSuccess) {
+    cudaGetLastError();
     j->arena = nullptr;
-    set_error(std::string("cudaMalloc of the job arena failed: ") + cudaGetErrorString(e));
+    set_error(std::string("device allocation of the job arena failed: ") + cudaGetErrorString(e));
     return GPL_ERR_OUT_OF_MEMORY;
   }
-  d.bytes = (int64_t)S.bytes;
+  d.bytes = (int64_t)bytes;
   Carver C{j->arena};
   d.g_half = C.take<int2>(ng); d.g_scale = C.take<float>(ng); d.g_kind = C.take<uint8_t>(ng);
   d.g_precond = C.take<float2>(ng); d.g_pin_start = C.take<int32_t>(ng + 1);
@@ -297,8 +310,8 @@ int ensure_nb(gpl_job* j) {
   GPL_CUDA(cudaMemsetAsync(d.phi, 0, nb * 4, s));
   GPL_CUDA(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned), s));
   GPL_CUDA(cudaMemsetAsync(d.hpwl_total, 0, sizeof(long long), s));
-  if (!d.result_h) GPL_CUDA(cudaMallocHost(&d.result_h, sizeof(EvalResult)));
-  if (!d.ctl_h) GPL_CUDA(cudaMallocHost(&d.ctl_h, sizeof(EvalCtl)));
+  d.result_h = &j->pinned->result;
+  d.ctl_h = &j->pinned->ctl;
   memset(d.ctl_h, 0, sizeof(EvalCtl));
   GPL_CUDA(cudaStreamSynchronize(s));
   j->nb_ready = true;
@@ -635,6 +648,54 @@ void fill_info(gpl_job* j, gpl_job_info* info) {
 
 }  // namespace
 
+namespace gpl {
+
+int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
+  if (!out) { set_error("null job pointer"); return GPL_ERR_INVALID_ARG; }
+  *out = nullptr;
+  if (!p) { set_error("null parameters"); return GPL_ERR_INVALID_ARG; }
+  gpl_job* j = new gpl_job();
+  int rc = build_placer_base(j->m, nl, p);
+  if (rc) { delete j; return rc; }
+  j->device = p->device;
+  rc = check_device(j->device);
+  if (rc) { delete j; return rc; }
+  *out = j;
+  return GPL_OK;
+}
+
+void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool) {
+  j->stream = stream;
+  j->own_stream = false;
+  j->pinned = pinned;
+  j->own_pinned = false;
+  memset(j->pinned, 0, sizeof(HostPinned));
+  j->pool = pool;
+  j->timer.stream = stream;
+}
+
+int job_device_bytes(gpl_job* j, int64_t* bytes) {
+  const HostModel& m = j->m;
+  NbCounts c;
+  int rc = nb_counts(m, &c);
+  if (rc) return rc;
+  int sm = 0;
+  GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
+  size_t n_gpins = 0;
+  for (int i : m.place_insts) n_gpins += m.inst_pin_start[i + 1] - m.inst_pin_start[i];
+  const size_t ng = m.place_insts.size() + (size_t)c.n_fill;
+  const size_t nb = (size_t)c.cnt_x * c.cnt_y;
+  // upper bounds: every gcell big, one WA block per net, the larger partial grid
+  const size_t stride = std::max<size_t>((size_t)sm * 8, (size_t)c.cnt_y);
+  const size_t arena = arena_bytes(ng, m.n_pins, m.n_nets, n_gpins, ng, nb, c.cnt_x, c.cnt_y, stride,
+                                   (size_t)m.n_nets + kWaBuckets);
+  const size_t ip = m.p.initial_place_max_iter > 0 ? initial_place_bytes(m, sm) : 0;
+  *bytes = (int64_t)std::max(arena, ip);
+  return GPL_OK;
+}
+
+}  // namespace gpl
+
 // =================================================================== C ABI
 extern "C" {
 
@@ -672,19 +733,23 @@ void gpl_params_default(gpl_params* p) {
 }
 
 gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
-  if (!out) { set_error("null job pointer"); return GPL_ERR_INVALID_ARG; }
-  *out = nullptr;
-  gpl_job* j = new gpl_job();
-  int rc = build_placer_base(j->m, nl, p);
-  if (rc) { delete j; return (gpl_status)rc; }
-  j->device = p->device;
-  rc = check_device(j->device);
-  if (rc) { delete j; return (gpl_status)rc; }
+  gpl_job* j = nullptr;
+  int rc = job_new(nl, p, &j);
+  if (rc) return (gpl_status)rc;
+  cudaError_t e = cudaMallocHost(&j->pinned, sizeof(HostPinned));
+  if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); delete j; return GPL_ERR_CUDA; }
+  j->own_pinned = true;
+  memset(j->pinned, 0, sizeof(HostPinned));
   if (p->stream) {
     j->stream = (cudaStream_t)p->stream;
   } else {
-    cudaError_t e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); delete j; return GPL_ERR_CUDA; }
+    e = cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      set_error(cudaGetErrorString(e));
+      cudaFreeHost(j->pinned);
+      delete j;
+      return GPL_ERR_CUDA;
+    }
     j->own_stream = true;
   }
   j->timer.stream = j->stream;
@@ -698,9 +763,8 @@ void gpl_destroy(gpl_job* j) {
   if (j->stream) cudaStreamSynchronize(j->stream);
   j->timer.release();
   if (j->graph_exec) cudaGraphExecDestroy(j->graph_exec);
-  if (j->arena) cudaFree(j->arena);
-  if (j->d.result_h) cudaFreeHost(j->d.result_h);
-  if (j->d.ctl_h) cudaFreeHost(j->d.ctl_h);
+  if (j->arena) dev_free(j->arena, j->pool, j->stream);
+  if (j->own_pinned && j->pinned) cudaFreeHost(j->pinned);
   if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
   delete j;
 }
@@ -869,7 +933,7 @@ gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
   cudaSetDevice(j->device);
   int sm = 0;
   GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
-  return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer);
+  return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer, j->pinned->ip_state, j->pool);
 }
 
 }  // extern "C"

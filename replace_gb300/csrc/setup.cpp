@@ -138,19 +138,15 @@ void host_place_center(HostModel& m) {
 
 // NesterovBase::init (src/nesterovBase.cpp:917-1062) with initFillerGCells
 // (:1066-1155) and BinGrid::initBins / updateBinsNonPlaceArea (:631-741).
-int build_nesterov_base(HostModel& m) {
+// Filler size and count (NesterovBase::initFillerGCells, src/nesterovBase.cpp:
+// 1066-1155) and the bin grid (BinGrid::initBins, :631-717): the counts that
+// size a job, independent of the instances' positions.
+int nb_counts(const HostModel& m, NbCounts* c) {
   const gpl_params& p = m.p;
-  m.glx.clear(); m.gly.clear(); m.gux.clear(); m.guy.clear(); m.gkind.clear();
-  m.n_place = (int)m.place_insts.size();
-  for (int i : m.place_insts) {
-    m.glx.push_back(m.ilx[i]); m.gly.push_back(m.ily[i]);
-    m.gux.push_back(m.iux[i]); m.guy.push_back(m.iuy[i]);
-    m.gkind.push_back((m.iuy[i] - m.ily[i]) > m.site_h * 6 ? 1 : 0);
-  }
-  // fillers: trimmed-mean size, count from the white space, mt19937(0) centres
+  const int n_place = (int)m.place_insts.size();
   {
     std::vector<int> dxs, dys;
-    dxs.reserve(m.n_place); dys.reserve(m.n_place);
+    dxs.reserve(n_place); dys.reserve(n_place);
     for (int i : m.place_insts) { dxs.push_back(m.iux[i] - m.ilx[i]); dys.push_back(m.iuy[i] - m.ily[i]); }
     std::sort(dxs.begin(), dxs.end());
     std::sort(dys.begin(), dys.end());
@@ -159,8 +155,8 @@ int build_nesterov_base(HostModel& m) {
     int64_t dx_sum = 0, dy_sum = 0;
     for (int k = min_idx; k < max_idx; k++) { dx_sum += dxs[k]; dy_sum += dys[k]; }
     if (max_idx <= min_idx) { set_error("too few movable instances for the filler size"); return GPL_ERR_INVALID_ARG; }
-    m.fill_dx = (int)(dx_sum / (max_idx - min_idx));
-    m.fill_dy = (int)(dy_sum / (max_idx - min_idx));
+    c->fill_dx = (int)(dx_sum / (max_idx - min_idx));
+    c->fill_dy = (int)(dy_sum / (max_idx - min_idx));
     int64_t core_area = (int64_t)(m.core_ux - m.core_lx) * (int64_t)(m.core_uy - m.core_ly);
     int64_t white = core_area - m.non_place_area;
     int64_t movable = (int64_t)(white * p.target_density);
@@ -169,7 +165,55 @@ int build_nesterov_base(HostModel& m) {
       set_error("Filler area is negative!! Please put higher target density or re-floorplan to have enough coreArea");
       return GPL_ERR_FILLER_AREA;
     }
-    int cnt = (int)(total_filler / (int64_t)(m.fill_dx * m.fill_dy));
+    c->n_fill = (int)(total_filler / (int64_t)(c->fill_dx * c->fill_dy));
+  }
+  int64_t total_bin_area = (int64_t)(m.core_ux - m.core_lx) * (int64_t)(m.core_uy - m.core_ly);
+  int64_t avg_area = m.place_area / (int64_t)n_place;
+  int64_t ideal_bin_area = (int64_t)std::round((float)avg_area / p.target_density);
+  if (ideal_bin_area <= 0) { set_error("degenerate ideal bin area"); return GPL_ERR_INVALID_ARG; }
+  int ideal_bin_cnt = (int)(total_bin_area / ideal_bin_area);
+  int found = 2;
+  for (found = 2; found <= 1024; found *= 2)
+    if (found * found <= ideal_bin_cnt && 4 * found * found > ideal_bin_cnt) break;
+  c->cnt_x = p.bin_grid_cnt_x > 0 ? p.bin_grid_cnt_x : found;
+  c->cnt_y = p.bin_grid_cnt_y > 0 ? p.bin_grid_cnt_y : found;
+  auto pow2 = [](int v) { return v >= 2 && (v & (v - 1)) == 0; };
+  if (!pow2(c->cnt_x) || !pow2(c->cnt_y) || c->cnt_x > kFftMax || c->cnt_y > kFftMax) {
+    // The DCT (Ooura's and ours) needs power-of-two sizes.
+    set_error("bin counts must be powers of two in [2, 4096]");
+    return GPL_ERR_INVALID_ARG;
+  }
+  c->size_x = (int)ceil((float)(m.core_ux - m.core_lx) / c->cnt_x);
+  c->size_y = (int)ceil((float)(m.core_uy - m.core_ly) / c->cnt_y);
+  // BinGrid::initBins lays bins out by walking x in steps of binSize and
+  // wrapping at the core edge; that walk yields cnt bins per row only if
+  // (cnt - 1) * binSize < core width.  Finer grids misalign the reference's
+  // bin indexing, so they are rejected.
+  if ((int64_t)(c->cnt_x - 1) * c->size_x >= (m.core_ux - m.core_lx) ||
+      (int64_t)(c->cnt_y - 1) * c->size_y >= (m.core_uy - m.core_ly)) {
+    set_error("bin grid finer than the core allows (reference bin layout would wrap early)");
+    return GPL_ERR_INVALID_ARG;
+  }
+  return GPL_OK;
+}
+
+int build_nesterov_base(HostModel& m) {
+  const gpl_params& p = m.p;
+  NbCounts nc;
+  int rc = nb_counts(m, &nc);
+  if (rc) return rc;
+  m.glx.clear(); m.gly.clear(); m.gux.clear(); m.guy.clear(); m.gkind.clear();
+  m.n_place = (int)m.place_insts.size();
+  for (int i : m.place_insts) {
+    m.glx.push_back(m.ilx[i]); m.gly.push_back(m.ily[i]);
+    m.gux.push_back(m.iux[i]); m.guy.push_back(m.iuy[i]);
+    m.gkind.push_back((m.iuy[i] - m.ily[i]) > m.site_h * 6 ? 1 : 0);
+  }
+  // fillers: mt19937(0) centres
+  m.fill_dx = nc.fill_dx;
+  m.fill_dy = nc.fill_dy;
+  {
+    const int cnt = nc.n_fill;
     std::mt19937 rv(0);
     const int cdx = m.core_ux - m.core_lx, cdy = m.core_uy - m.core_ly;
     for (int k = 0; k < cnt; k++) {
@@ -199,33 +243,8 @@ int build_nesterov_base(HostModel& m) {
   for (int k = m.n_place; k < m.n_g; k++) m.g_pin_start[k + 1] = m.g_pin_start[k];
 
   // bin grid
-  int64_t total_bin_area = (int64_t)(m.core_ux - m.core_lx) * (int64_t)(m.core_uy - m.core_ly);
-  int64_t avg_area = m.place_area / (int64_t)m.place_insts.size();
-  int64_t ideal_bin_area = (int64_t)std::round((float)avg_area / p.target_density);
-  if (ideal_bin_area <= 0) { set_error("degenerate ideal bin area"); return GPL_ERR_INVALID_ARG; }
-  int ideal_bin_cnt = (int)(total_bin_area / ideal_bin_area);
-  int found = 2;
-  for (found = 2; found <= 1024; found *= 2)
-    if (found * found <= ideal_bin_cnt && 4 * found * found > ideal_bin_cnt) break;
-  m.cnt_x = p.bin_grid_cnt_x > 0 ? p.bin_grid_cnt_x : found;
-  m.cnt_y = p.bin_grid_cnt_y > 0 ? p.bin_grid_cnt_y : found;
-  auto pow2 = [](int v) { return v >= 2 && (v & (v - 1)) == 0; };
-  if (!pow2(m.cnt_x) || !pow2(m.cnt_y) || m.cnt_x > kFftMax || m.cnt_y > kFftMax) {
-    // The DCT (Ooura's and ours) needs power-of-two sizes.
-    set_error("bin counts must be powers of two in [2, 4096]");
-    return GPL_ERR_INVALID_ARG;
-  }
-  m.size_x = (int)ceil((float)(m.core_ux - m.core_lx) / m.cnt_x);
-  m.size_y = (int)ceil((float)(m.core_uy - m.core_ly) / m.cnt_y);
-  // BinGrid::initBins lays bins out by walking x in steps of binSize and
-  // wrapping at the core edge; that walk yields cnt bins per row only if
-  // (cnt - 1) * binSize < core width.  Finer grids misalign the reference's
-  // bin indexing, so they are rejected.
-  if ((int64_t)(m.cnt_x - 1) * m.size_x >= (m.core_ux - m.core_lx) ||
-      (int64_t)(m.cnt_y - 1) * m.size_y >= (m.core_uy - m.core_ly)) {
-    set_error("bin grid finer than the core allows (reference bin layout would wrap early)");
-    return GPL_ERR_INVALID_ARG;
-  }
+  m.cnt_x = nc.cnt_x; m.cnt_y = nc.cnt_y;
+  m.size_x = nc.size_x; m.size_y = nc.size_y;
   const int nb = m.cnt_x * m.cnt_y;
   m.bin_nonplace.assign(nb, 0);
   auto bin_lo_x = [&](int a) { return m.core_lx + a * m.size_x; };

@@ -480,3 +480,51 @@ def generate_workload(name: str, seed: int = 1) -> tuple:
     td = cfg.pop("target_density")
     bins = cfg.pop("bins")
     return generate(seed=seed, **cfg), td, bins
+
+
+def job_batch(n_jobs: int = 64, seed: int = 4, cells=(2_000, 50_000), density=(0.60, 0.85)):
+    """The batched form's instance set: n_jobs netlists from the same
+    generator, cell counts log-uniform in `cells`, target densities uniform
+    in `density`, bin grids left to the reference's bin-count rule.
+
+    The generator's die is sized for 0.60 utilisation; a job whose target
+    density is within 0.02 of that has (almost) no room for fillers and the
+    reference stops with code 1, so such jobs are generated at utilisation
+    target_density - 0.02 instead.  Returns a list of (netlist, td)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_jobs):
+        n = int(round(np.exp(rng.uniform(np.log(cells[0]), np.log(cells[1])))))
+        td = float(rng.uniform(*density))
+        util = min(0.60, td - 0.02)
+        nl = generate(n_cells=n, n_nets=int(round(1.05 * n)), n_io=200, util=util,
+                      seed=seed * 100_003 + k)
+        out.append((nl, td))
+    return out
+
+
+def job_stream_spec(n_jobs: int = 500, rate: float = 2.0, seed: int = 5, cells=(5_000, 500_000),
+                    density=(0.60, 0.90), macro_share: float = 0.10, macros=(10, 40)):
+    """The serving form's request stream: Poisson arrivals at `rate` jobs/s,
+    cell counts log-uniform in `cells`, target densities uniform in
+    `density`, `macro_share` of the jobs mixed-size with a uniform number of
+    macros in `macros`.  Returns a list of dicts (arrival_s, n_cells,
+    n_macros, td, seed); `stream_job` builds a job's netlist."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    spec = []
+    for k in range(n_jobs):
+        t += float(rng.exponential(1.0 / rate))
+        n = int(round(np.exp(rng.uniform(np.log(cells[0]), np.log(cells[1])))))
+        td = float(rng.uniform(*density))
+        nm = int(rng.integers(macros[0], macros[1] + 1)) if rng.random() < macro_share else 0
+        spec.append({"arrival_s": t, "n_cells": n, "n_macros": nm, "td": td,
+                     "seed": seed * 100_003 + k})
+    return spec
+
+
+def stream_job(s: dict) -> Netlist:
+    """Netlist of one `job_stream_spec` entry (utilisation as in job_batch)."""
+    util = min(0.60, s["td"] - 0.02)
+    return generate(n_cells=s["n_cells"], n_nets=int(round(1.05 * s["n_cells"])), n_io=200,
+                    n_macros=s["n_macros"], util=util, seed=s["seed"])

@@ -75,3 +75,31 @@ def test_no_device_fails_loudly():
     rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job))
     assert rc == _abi.GPL_ERR_NO_DEVICE
     assert b"no CPU fallback" in lib.gpl_last_error()
+
+
+def test_server_parameters_and_missing_device():
+    from replace_gb300 import load
+    lib = load()
+    p = _abi.ServerParams()
+    lib.gpl_server_params_default(C.byref(p))
+    assert p.max_active == 8 and p.chunk_iters == 64 and p.run_initial_place == 1
+    h = C.c_void_p()
+    bad = _abi.ServerParams(device=0, max_active=0, hbm_budget_bytes=0, chunk_iters=64,
+                            run_initial_place=1)
+    assert lib.gpl_server_create(C.byref(bad), C.byref(h)) == _abi.GPL_ERR_INVALID_ARG
+    import torch
+    if not torch.cuda.is_available():
+        assert lib.gpl_server_create(C.byref(p), C.byref(h)) == _abi.GPL_ERR_NO_DEVICE
+        assert b"no CPU fallback" in lib.gpl_last_error()
+
+
+def test_job_batch_and_stream_generators():
+    jobs = N.job_batch(n_jobs=4, seed=3, cells=(2_000, 4_000))
+    assert len(jobs) == 4
+    for nl, td in jobs:
+        assert 2_000 <= int((nl.inst_kind == 0).sum()) <= 4_000 and 0.60 <= td <= 0.85
+    spec = N.job_stream_spec(n_jobs=50, rate=2.0, seed=5)
+    t = np.array([s["arrival_s"] for s in spec])
+    assert np.all(np.diff(t) > 0)
+    assert all(5_000 <= s["n_cells"] <= 500_000 for s in spec)
+    assert 0 < sum(s["n_macros"] > 0 for s in spec) < 50
