@@ -11,6 +11,12 @@ job's stream; `e2e` is the same metric for a whole job through the C ABI from
 host arrays (netlist upload, init, iterations, location read-back).  The
 reference arm times the CPU restatement of the reference's path (the oracle)
 on this host.  Multi-GPU runs are independent replicas (no collectives).
+
+At one GPU the line also carries `serving`: the batched form (64 jobs of
+2k-50k cells submitted at once to the placement server, against the same
+jobs placed one at a time) and the serving form (the first --stream-jobs
+requests of a 500-job Poisson stream at 2 jobs/s, 5k-500k cells, against a
+one-job-at-a-time server): placements/h and p50/p99 job latency.
 """
 
 from __future__ import annotations
@@ -119,6 +125,81 @@ def cpu_baseline_sample(nl, td, bins, iters=3):
     return iters / (t2 - t1), t2 - t0
 
 
+def serving_batch(n_jobs, slots, device):
+    """The batched form: n_jobs netlists (2k-50k cells, log-uniform) submitted
+    at once to a server with `slots` slots, against the same jobs placed one
+    at a time through the plain job API.  Netlists are generated before the
+    timed regions; every job runs initial place + Nesterov to its stop rule."""
+    import numpy as np
+    from replace_gb300 import Placer, PlacementServer, netlist as N
+    jobs = N.job_batch(n_jobs, seed=4)
+    t0 = time.perf_counter()
+    seq = []
+    for nl, td in jobs:
+        p = Placer(nl, target_density=td, device=device)
+        p.initial_place()
+        p.nesterov_init()
+        rc, st, _ = p.nesterov_run(0)
+        seq.append((rc, st.iterations, st.hpwl))
+        p.close()
+    t_seq = time.perf_counter() - t0
+    with PlacementServer(device=device, max_active=slots) as srv:
+        t0 = time.perf_counter()
+        ts = [srv.submit(nl, target_density=td) for nl, td in jobs]
+        res = {r["ticket"]: r for r in srv.wait_all(1800)}
+        t_srv = time.perf_counter() - t0
+    lat = np.array([res[t]["latency_s"] for t in ts])
+    same = all(res[t]["hpwl"] == q[2] and res[t]["iterations"] == q[1] for t, q in zip(ts, seq))
+    return {
+        "jobs": n_jobs, "slots": slots, "cells": "2k-50k log-uniform", "td": "0.60-0.85",
+        "placements_per_hour": n_jobs / t_srv * 3600.0, "makespan_s": t_srv,
+        "one_at_a_time_placements_per_hour": n_jobs / t_seq * 3600.0, "one_at_a_time_s": t_seq,
+        "speedup_vs_one_at_a_time": t_seq / t_srv,
+        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+        "converged": int(sum(res[t]["status"] == 0 and res[t]["finished"] and res[t]["overflow"] <= 0.1
+                             for t in ts)),
+        "same_result_alone_and_in_mix": bool(same),
+    }
+
+
+def serving_stream(n_jobs, slots, device):
+    """The serving form on a bounded sample: the first n_jobs requests of the
+    500-job Poisson stream (2 jobs/s; 5k-500k cells; 10 % mixed-size),
+    submitted at their arrival times to a server with `slots` slots and to a
+    one-slot server (one job at a time, FIFO).  Latency = end of the job -
+    its arrival (host netlist conversion and submission included)."""
+    import numpy as np
+    from replace_gb300 import PlacementServer, netlist as N
+    spec = N.job_stream_spec(500, 2.0, seed=5)[:n_jobs]
+    nets = [N.stream_job(s) for s in spec]
+    base = spec[0]["arrival_s"]
+
+    def run(k):
+        with PlacementServer(device=device, max_active=k) as srv:
+            t_create = time.perf_counter()
+            arrive = {}
+            for s, nl in zip(spec, nets):
+                due = t_create + (s["arrival_s"] - base)
+                while time.perf_counter() < due:
+                    time.sleep(min(0.005, max(due - time.perf_counter(), 0)))
+                ta = time.perf_counter()
+                t = srv.submit(nl, target_density=s["td"])
+                arrive[t] = ta - t_create
+            res = srv.wait_all(3600)
+        lat = np.array([r["finish_s"] - arrive[r["ticket"]] for r in res])
+        span = max(r["finish_s"] for r in res)
+        ok = sum(r["status"] == 0 and r["finished"] and r["overflow"] <= 0.1 for r in res)
+        return {"slots": k, "placements_per_hour": len(res) / span * 3600.0, "span_s": span,
+                "p50_latency_s": float(np.percentile(lat, 50)),
+                "p99_latency_s": float(np.percentile(lat, 99)), "converged": int(ok)}
+
+    srv = run(slots)
+    one = run(1)
+    return {"jobs": n_jobs, "of_stream": 500, "rate_per_s": 2.0,
+            "cells": "5k-500k log-uniform", "td": "0.60-0.90", "mixed_size_share": 0.10,
+            "server": srv, "one_at_a_time": one}
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -167,6 +248,10 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--stream-jobs", type=int, default=40)
+    ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--workload", default=WORKLOAD,
                     help="named synthetic workload (replace_gb300.netlist.WORKLOADS)")
     args = ap.parse_args()
@@ -260,6 +345,11 @@ def main():
                     "job_seconds": t1 - t0, "finished": bool(st2.finished),
                     "final_overflow": float(st2.overflow), "final_hpwl": int(st2.hpwl)}
 
+    serving = None
+    if world == 1 and not args.no_serving:
+        serving = {"batch": serving_batch(args.batch_jobs, args.slots, local_rank),
+                   "stream": serving_stream(args.stream_jobs, args.slots, local_rank)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v_cpu, t_cpu = cpu_baseline_sample(nl, td, bins, args.cpu_iters)
@@ -289,6 +379,7 @@ def main():
                          "kernel_ms_per_launch": kernel_ms},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "serving": serving,
         }
         print(json.dumps(line))
     if world > 1:

@@ -124,6 +124,11 @@ typedef struct gpl_params {
   int32_t device;                          /* CUDA device ordinal */
   void* stream;                            /* cudaStream_t to run on; NULL = job-owned stream */
   int32_t use_graph;                       /* 1 = each evaluation replays one CUDA graph */
+  int32_t ip_solver;                       /* BiCGSTAB form: 0 = auto (a thread-block cluster per
+                                              axis for up to 65536 instances, else one
+                                              cooperative grid), 1 = one kernel per phase,
+                                              2 = cooperative grid (same iterates as 1),
+                                              3 = cluster per axis */
 } gpl_params;
 
 /* Counts and grid chosen by the job (NesterovBase / BinGrid). */
@@ -178,6 +183,8 @@ typedef struct gpl_ip_stats {
   int64_t last_hpwl;         /* PlacerBase::hpwl before the last move */
   int32_t solver_iters_x;    /* BiCGSTAB iterations of the last round */
   int32_t solver_iters_y;
+  int32_t cooperative_rounds; /* rounds solved in one launch (cluster or cooperative grid) */
+  int32_t pad;
 } gpl_ip_stats;
 
 /* Library identity and the last error message of the calling thread. */
@@ -296,6 +303,8 @@ typedef struct gpl_server_params {
                                  0 = 80 % of the free memory at creation */
   int32_t chunk_iters;        /* Nesterov iterations between cancel checks (64) */
   int32_t run_initial_place;  /* 1 = gpl_initial_place before the Nesterov loop (1) */
+  int32_t blocking_sync;      /* 1 = slot threads sleep while waiting for the GPU (1) */
+  int32_t pad;
 } gpl_server_params;
 
 typedef struct gpl_server_result {

@@ -65,6 +65,7 @@ class Params(C.Structure):
         ("device", C.c_int32),
         ("stream", C.c_void_p),
         ("use_graph", C.c_int32),
+        ("ip_solver", C.c_int32),
     ]
 
 
@@ -108,6 +109,7 @@ class IpStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int32), ("last_error", C.c_float), ("last_hpwl", C.c_int64),
         ("solver_iters_x", C.c_int32), ("solver_iters_y", C.c_int32),
+        ("cooperative_rounds", C.c_int32), ("pad", C.c_int32),
     ]
 
 
@@ -115,6 +117,7 @@ class ServerParams(C.Structure):
     _fields_ = [
         ("device", C.c_int32), ("max_active", C.c_int32), ("hbm_budget_bytes", C.c_int64),
         ("chunk_iters", C.c_int32), ("run_initial_place", C.c_int32),
+        ("blocking_sync", C.c_int32), ("pad", C.c_int32),
     ]
 
 
@@ -145,6 +148,7 @@ def default_params(**overrides) -> Params:
         target_overflow=0.1, min_phi_coef=0.95, max_phi_coef=1.05,
         min_preconditioner=1.0, initial_prev_coordi_update_coef=100.0,
         reference_hpwl=446000000.0, verbose_level=0, device=0, stream=None, use_graph=1,
+        ip_solver=0,
     )
     for k, v in overrides.items():
         setattr(p, k, v)

@@ -180,6 +180,15 @@ inline void dev_free(void* p, cudaMemPool_t pool, cudaStream_t s) {
   if (pool) cudaFreeAsync(p, s); else cudaFree(p);
 }
 
+// Waits for the stream's work so far: with a blocking-sync event when one is
+// given (the host thread sleeps instead of spinning: a server runs more slot
+// threads than it has cores), else cudaStreamSynchronize.
+inline cudaError_t host_wait(cudaStream_t s, cudaEvent_t ev) {
+  if (!ev) return cudaStreamSynchronize(s);
+  cudaError_t e = cudaEventRecord(ev, s);
+  return e != cudaSuccess ? e : cudaEventSynchronize(ev);
+}
+
 // kernel-class timing (CUDA events around each launch when enabled)
 enum KernelClass { kKScatter = 0, kKPoissonA, kKPoissonB, kKPoissonC, kKWa, kKCell,
                    kKReduce, kKOther, kKClasses };
@@ -251,7 +260,7 @@ int wa_nets_per_block(int bucket);
 // return the host model's movable instances are at the solution.
 // `pinned` is the job's ip_state block; `pool` as for dev_alloc.
 int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& t,
-                      void* pinned, cudaMemPool_t pool);
+                      void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev);
 // device bytes run_initial_place allocates for this model
 size_t initial_place_bytes(const HostModel& m, int sm_count);
 
@@ -259,7 +268,8 @@ size_t initial_place_bytes(const HostModel& m, int sm_count);
 // it admits the job), and the binding: stream, pinned staging and pool stay
 // the caller's.
 int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out);
-void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool);
+void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool,
+              cudaEvent_t sync_ev);
 // Upper bound of the device bytes the job will hold at once (initial place
 // scratch or the Nesterov arena, whichever is larger).
 int job_device_bytes(gpl_job* j, int64_t* bytes);

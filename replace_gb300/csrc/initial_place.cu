@@ -21,10 +21,12 @@
 // products and the rho / alpha / omega scalars are FP64.  Both axes run in
 // the same launches (blockIdx.y = axis).  The scalar steps are done by the
 // last block of each reduction kernel, so the host only polls a done flag.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <climits>
+#include <cstdio>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -57,7 +59,11 @@ struct IpDev {
   int2* ctr;               // movable instance centres
   int2* pos;               // pin positions this round
   int4* bound;             // per net: first min-x, max-x, min-y, max-y pin (or -1)
-  int32_t* cnt;            // [2][n_mov] row lengths (off-diagonal entries)
+  int n_mp = 0;            // movable pin slots (mov_pins)
+  int32_t* cnt;            // [2][n_mp] entries contributed by each movable pin slot
+  int32_t* slot_off;       // [2][n_mp + 1] exclusive prefix of cnt (entry offsets)
+  float* slot_diag;        // [2][n_mp] diagonal and right-hand side parts per slot
+  float* slot_rhs;
   int32_t* rowptr;         // [2][n_mov + 1]
   int32_t* scan_part;      // block sums of the scan
   int32_t* col;            // [2][nnz_cap]
@@ -66,6 +72,8 @@ struct IpDev {
   float* b;                // [2][n_mov]
   float *x, *r, *r0, *p, *v, *s, *t;   // [2][n_mov]
   double* part;            // [2][slots][parts]
+  double* cpart;           // cooperative solve: [4 phases][2 axes][2][parts]
+  struct GridBar* bar;     // cooperative solve: grid barrier
   unsigned* counters;      // [2][8]
   BiState* st;             // [2]
   BiState* st_h;           // pinned mirror
@@ -136,19 +144,65 @@ __device__ __forceinline__ void for_partners(const IpDev& D, int q, int n, int a
   }
 }
 
+// One movable pin slot t of the B2B assembly: pin q of net n.  A bound pin's
+// partners are the other pins of the net (of other instances), a plain pin's
+// the net's two bound pins.  Slots are in instance-pin order, so a row of
+// the matrix is the concatenation of its instance's slots.
+struct Slot {
+  int q, n, inst, s, e;
+  bool used, bound;
+};
+
+__device__ __forceinline__ Slot slot_of(const IpDev& D, const IpParams& P, int t, int axis) {
+  Slot c;
+  c.q = D.mov_pins[t];
+  c.n = D.pin_net[c.q];
+  int deg;
+  c.used = net_used(D, P, c.n, deg);
+  c.s = D.net_start[c.n];
+  c.e = D.net_start[c.n + 1];
+  c.inst = D.pin_inst[c.q];
+  const int4 bd = D.bound[c.n];
+  c.bound = c.q == (axis ? bd.z : bd.x) || c.q == (axis ? bd.w : bd.y);
+  return c;
+}
+
+// Partner lists longer than this (bound pins of large nets) are walked by the
+// whole warp, lanes striding over the net's pins.
+constexpr int kLongList = 32;
+
+// Entries each slot contributes (movable partners); lanes take one slot each,
+// long partner lists are counted by the warp together.
 __global__ void k_ip_count(IpDev D, IpParams P) {
-  const int i = blockIdx.x * kB + threadIdx.x;
-  const int axis = blockIdx.y;
-  if (i >= D.n_mov) return;
-  int c = 0;
-  for (int t = D.mov_pin_start[i]; t < D.mov_pin_start[i + 1]; t++) {
-    const int q = D.mov_pins[t];
-    const int n = D.pin_net[q];
-    int deg;
-    if (!net_used(D, P, n, deg)) continue;
-    for_partners(D, q, n, axis, [&](int r) { if (D.pin_mov[r] >= 0) c++; });
+  const unsigned full = 0xffffffffu;
+  const int axis = blockIdx.y, lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < D.n_mp; w += gridDim.x * kB) {
+    const int t = w + lane;
+    int c = 0;
+    bool lng = false;
+    Slot sl{};
+    if (t < D.n_mp) {
+      sl = slot_of(D, P, t, axis);
+      if (sl.used) {
+        if (sl.bound && sl.e - sl.s > kLongList) lng = true;
+        else for_partners(D, sl.q, sl.n, axis, [&](int r) { if (D.pin_mov[r] >= 0) c++; });
+      }
+    }
+    unsigned longs = __ballot_sync(full, lng);
+    while (longs) {
+      const int src = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const int q = __shfl_sync(full, sl.q, src), inst = __shfl_sync(full, sl.inst, src);
+      const int ls = __shfl_sync(full, sl.s, src), le = __shfl_sync(full, sl.e, src);
+      int part = 0;
+      for (int r = ls + lane; r < le; r += 32)
+        if (r != q && D.pin_inst[r] != inst && D.pin_mov[r] >= 0) part++;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(full, part, o);
+      if (lane == src) c = part;
+    }
+    if (t < D.n_mp) D.cnt[axis * D.n_mp + t] = c;
   }
-  D.cnt[axis * D.n_mov + i] = c;
 }
 
 // exclusive scan of cnt[axis] into rowptr[axis] (three kernels)
@@ -169,17 +223,33 @@ __global__ void k_scan_blocks(const int32_t* in, int32_t* out, int32_t* part, in
   if (threadIdx.x == kB - 1) part[axis * gridDim.x + blockIdx.x] = sh[kB - 1];
 }
 
-__global__ void k_scan_parts(int32_t* part, int nparts, int32_t* rowptr, int n) {
+// Exclusive scan of the block sums (one block of kScanT threads per axis:
+// contiguous chunks per thread, then a scan of the chunk sums); the total
+// goes to out[n].
+constexpr int kScanT = 1024;
+__global__ void __launch_bounds__(kScanT) k_scan_parts(int32_t* part, int nparts, int32_t* out, int n) {
+  __shared__ int32_t sh[kScanT];
   const int axis = blockIdx.x;
-  if (threadIdx.x == 0) {
-    int run = 0;
-    for (int k = 0; k < nparts; k++) {
-      const int v = part[axis * nparts + k];
-      part[axis * nparts + k] = run;
-      run += v;
-    }
-    rowptr[axis * (n + 1) + n] = run;
+  int32_t* pp = part + axis * nparts;
+  const int chunk = (nparts + kScanT - 1) / kScanT;
+  const int lo = min(threadIdx.x * chunk, nparts), hi = min(lo + chunk, nparts);
+  int sum = 0;
+  for (int k = lo; k < hi; k++) sum += pp[k];
+  sh[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < kScanT; o <<= 1) {
+    const int x = threadIdx.x >= o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += x;
+    __syncthreads();
   }
+  int run = sh[threadIdx.x] - sum;
+  for (int k = lo; k < hi; k++) {
+    const int v = pp[k];
+    pp[k] = run;
+    run += v;
+  }
+  if (threadIdx.x == kScanT - 1) out[axis * (n + 1) + n] = sh[kScanT - 1];
 }
 
 __global__ void k_scan_add(int32_t* rowptr, const int32_t* part, int n) {
@@ -188,52 +258,170 @@ __global__ void k_scan_add(int32_t* rowptr, const int32_t* part, int n) {
   if (i < n) rowptr[axis * (n + 1) + i] += part[axis * gridDim.x + blockIdx.x];
 }
 
-// createSparseMatrix, one row per thread (src/initialPlace.cpp:221-374)
+// Row pointers: a row starts at its instance's first slot.
+__global__ void k_ip_rowptr(IpDev D) {
+  const int i = blockIdx.x * kB + threadIdx.x;
+  const int axis = blockIdx.y;
+  if (i > D.n_mov) return;
+  const int t = i < D.n_mov ? D.mov_pin_start[i] : D.n_mp;
+  D.rowptr[axis * (D.n_mov + 1) + i] = D.slot_off[axis * (D.n_mp + 1) + t];
+}
+
+// createSparseMatrix (src/initialPlace.cpp:221-374), one slot per lane: the
+// off-diagonal entries of movable partners at the slot's offset (partner
+// order), and the slot's parts of the diagonal and the right-hand side.  Long
+// partner lists: the warp walks the net 32 pins at a time and compacts the
+// entries in pin order with ballots.
 __global__ void k_ip_fill(IpDev D, IpParams P) {
+  const unsigned full = 0xffffffffu;
+  const int axis = blockIdx.y, lane = threadIdx.x & 31;
+  int32_t* col = D.col + axis * D.nnz_cap;
+  float* val = D.val + axis * D.nnz_cap;
+  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < D.n_mp; w += gridDim.x * kB) {
+    const int t = w + lane;
+    float diag = 0.0f, rhs = 0.0f;
+    bool lng = false;
+    Slot sl{};
+    int at = 0, pq = 0, off_q = 0;
+    float net_w = 0.0f;
+    if (t < D.n_mp) {
+      sl = slot_of(D, P, t, axis);
+      at = D.slot_off[axis * (D.n_mp + 1) + t];
+      const int i = D.pin_mov[sl.q];
+      const int2 ci = D.ctr[i];
+      pq = axis ? D.pos[sl.q].y : D.pos[sl.q].x;
+      off_q = pq - (axis ? ci.y : ci.x);
+      net_w = sl.used ? P.weight_scale / (sl.e - sl.s - 1) : 0.0f;
+      if (sl.used) {
+        if (sl.bound && sl.e - sl.s > kLongList) {
+          lng = true;
+        } else {
+          for_partners(D, sl.q, sl.n, axis, [&](int r) {
+            const int pr = axis ? D.pos[r].y : D.pos[r].x;
+            const float wgt = pair_weight(P, net_w, pq, pr);
+            diag += wgt;
+            const int j = D.pin_mov[r];
+            if (j >= 0) {
+              col[at] = j;
+              val[at] = -wgt;
+              at++;
+              const int2 cj = D.ctr[j];
+              const int off_r = pr - (axis ? cj.y : cj.x);
+              rhs += -wgt * (float)(off_q - off_r);
+            } else {
+              rhs += wgt * (float)(pr - off_q);
+            }
+          });
+        }
+      }
+    }
+    unsigned longs = __ballot_sync(full, lng);
+    while (longs) {
+      const int src = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const int q = __shfl_sync(full, sl.q, src), inst = __shfl_sync(full, sl.inst, src);
+      const int ls = __shfl_sync(full, sl.s, src), le = __shfl_sync(full, sl.e, src);
+      const int spq = __shfl_sync(full, pq, src), soff = __shfl_sync(full, off_q, src);
+      const float snw = __shfl_sync(full, net_w, src);
+      int sat = __shfl_sync(full, at, src);
+      float dg = 0.0f, rh = 0.0f;
+      for (int r0 = ls; r0 < le; r0 += 32) {
+        const int r = r0 + lane;
+        const bool partner = r < le && r != q && D.pin_inst[r] != inst;
+        int j = -1;
+        float wgt = 0.0f;
+        if (partner) {
+          const int pr = axis ? D.pos[r].y : D.pos[r].x;
+          wgt = pair_weight(P, snw, spq, pr);
+          dg += wgt;
+          j = D.pin_mov[r];
+          if (j >= 0) {
+            const int2 cj = D.ctr[j];
+            const int off_r = pr - (axis ? cj.y : cj.x);
+            rh += -wgt * (float)(soff - off_r);
+          } else {
+            rh += wgt * (float)(pr - soff);
+          }
+        }
+        const unsigned mv = __ballot_sync(full, partner && j >= 0);
+        if (partner && j >= 0) {
+          const int k = sat + __popc(mv & ((1u << lane) - 1u));
+          col[k] = j;
+          val[k] = -wgt;
+        }
+        sat += __popc(mv);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        dg += __shfl_xor_sync(full, dg, o);
+        rh += __shfl_xor_sync(full, rh, o);
+      }
+      if (lane == src) { diag = dg; rhs = rh; }
+    }
+    if (t < D.n_mp) {
+      D.slot_diag[axis * D.n_mp + t] = diag;
+      D.slot_rhs[axis * D.n_mp + t] = rhs;
+    }
+  }
+}
+
+// Diagonal and right-hand side of each row: its slots' parts in pin order.
+__global__ void k_ip_rowsum(IpDev D) {
   const int i = blockIdx.x * kB + threadIdx.x;
   const int axis = blockIdx.y;
   if (i >= D.n_mov) return;
-  const int2 ci = D.ctr[i];
-  int w_at = D.rowptr[axis * (D.n_mov + 1) + i];
-  int32_t* col = D.col + axis * D.nnz_cap;
-  float* val = D.val + axis * D.nnz_cap;
   float diag = 0.0f, rhs = 0.0f;
   for (int t = D.mov_pin_start[i]; t < D.mov_pin_start[i + 1]; t++) {
-    const int q = D.mov_pins[t];
-    const int n = D.pin_net[q];
-    int deg;
-    if (!net_used(D, P, n, deg)) continue;
-    const float net_w = P.weight_scale / (deg - 1);
-    const int pq = axis ? D.pos[q].y : D.pos[q].x;
-    const int off_q = pq - (axis ? ci.y : ci.x);
-    for_partners(D, q, n, axis, [&](int r) {
-      const int pr = axis ? D.pos[r].y : D.pos[r].x;
-      const float w = pair_weight(P, net_w, pq, pr);
-      diag += w;
-      const int j = D.pin_mov[r];
-      if (j >= 0) {
-        col[w_at] = j;
-        val[w_at] = -w;
-        w_at++;
-        const int2 cj = D.ctr[j];
-        const int off_r = pr - (axis ? cj.y : cj.x);
-        rhs += -w * (float)(off_q - off_r);
-      } else {
-        rhs += w * (float)(pr - off_q);
-      }
-    });
+    diag += D.slot_diag[axis * D.n_mp + t];
+    rhs += D.slot_rhs[axis * D.n_mp + t];
   }
   D.diag[axis * D.n_mov + i] = diag;
   D.b[axis * D.n_mov + i] = rhs;
 }
 
 // ------------------------------------------------------------ solver
-__device__ __forceinline__ float spmv_row(const IpDev& D, int axis, int i, const float* xv) {
-  const int s = D.rowptr[axis * (D.n_mov + 1) + i], e = D.rowptr[axis * (D.n_mov + 1) + i + 1];
+// Rows of A times xv for the calling warp's 32 consecutive rows (row i of
+// this lane; valid = i < n).  Rows of up to kLongRow entries are summed by
+// their own lane; longer ones (a cell whose pins bound many large nets can
+// have over a thousand) by the whole warp, lanes striding over the entries
+// and then a shuffle tree, so one long row does not hold up the launch.  All
+// 32 lanes must call it together.  kFromL2: read xv through L2 only (in the
+// cooperative solve other blocks wrote it since this block last read it).
+constexpr int kLongRow = 32;
+
+template <bool kFromL2 = false>
+__device__ __forceinline__ float spmv_warp(const IpDev& D, int axis, int i, bool valid,
+                                           const float* xv) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int32_t* rp = D.rowptr + axis * (D.n_mov + 1);
   const int32_t* col = D.col + axis * D.nnz_cap;
   const float* val = D.val + axis * D.nnz_cap;
-  float acc = D.diag[axis * D.n_mov + i] * xv[i];
-  for (int k = s; k < e; k++) acc += val[k] * xv[col[k]];
+  auto ld = [&](int j) { return kFromL2 ? __ldcg(xv + j) : xv[j]; };
+  int s = 0, e = 0;
+  float acc = 0.0f;
+  if (valid) {
+    s = rp[i];
+    e = rp[i + 1];
+    acc = D.diag[axis * D.n_mov + i] * ld(i);
+  }
+  const bool long_row = e - s > kLongRow;
+  if (!long_row) {
+#pragma unroll 4
+    for (int k = s; k < e; k++) acc += val[k] * ld(col[k]);
+  }
+  unsigned longs = __ballot_sync(full, long_row);
+  while (longs) {
+    const int src = __ffs(longs) - 1;
+    longs &= longs - 1;
+    const int ls = __shfl_sync(full, s, src), le = __shfl_sync(full, e, src);
+    float part = 0.0f;
+#pragma unroll 4
+    for (int k = ls + lane; k < le; k += 32) part += val[k] * ld(col[k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(full, part, o);
+    if (lane == src) acc += part;
+  }
   return acc;
 }
 
@@ -289,12 +477,17 @@ __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
   float* r = D.r + axis * n;
   float* r0 = D.r0 + axis * n;
   double v[2] = {0.0, 0.0};
-  for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB) {
-    const float ri = bb[i] - spmv_row(D, axis, i, x);
-    r[i] = ri;
-    r0[i] = ri;
-    v[0] += (double)ri * ri;
-    v[1] += (double)bb[i] * bb[i];
+  const int lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
+    const int i = w + lane;
+    const float ax = spmv_warp(D, axis, i, i < n, x);
+    if (i < n) {
+      const float ri = bb[i] - ax;
+      r[i] = ri;
+      r0[i] = ri;
+      v[0] += (double)ri * ri;
+      v[1] += (double)bb[i] * bb[i];
+    }
   }
   reduce_and_finish<2>(D, 0, v, [&](BiState& s, const double* t) {
     if (init) {
@@ -337,10 +530,14 @@ __global__ void k_bi_v(IpDev D) {
   float* v = D.v + axis * n;
   const float* r0 = D.r0 + axis * n;
   double acc[1] = {0.0};
-  for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB) {
-    const float vi = spmv_row(D, axis, i, p);
-    v[i] = vi;
-    acc[0] += (double)r0[i] * vi;
+  const int lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
+    const int i = w + lane;
+    const float vi = spmv_warp(D, axis, i, i < n, p);
+    if (i < n) {
+      v[i] = vi;
+      acc[0] += (double)r0[i] * vi;
+    }
   }
   reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; });
 }
@@ -365,11 +562,15 @@ __global__ void k_bi_t(IpDev D) {
   const float* s = D.s + axis * n;
   float* t = D.t + axis * n;
   double acc[2] = {0.0, 0.0};
-  for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB) {
-    const float ti = spmv_row(D, axis, i, s);
-    t[i] = ti;
-    acc[0] += (double)ti * ti;
-    acc[1] += (double)ti * s[i];
+  const int lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
+    const int i = w + lane;
+    const float ti = spmv_warp(D, axis, i, i < n, s);
+    if (i < n) {
+      t[i] = ti;
+      acc[0] += (double)ti * ti;
+      acc[1] += (double)ti * s[i];
+    }
   }
   reduce_and_finish<2>(D, 2, acc, [&](BiState& st, const double* tt) {
     st.w = tt[0] > 0.0 ? tt[1] / tt[0] : 0.0;
@@ -402,6 +603,363 @@ __global__ void k_bi_xr(IpDev D, int max_iter) {
     st.i++;
     loop_head(st, max_iter);
   });
+}
+
+// ---------------------------------------------------- cooperative solve
+// The whole BiCGSTAB solve of both axes as one cooperative launch: the
+// phases of k_bi_residual .. k_bi_xr run in the same order with the same
+// block partials, separated by grid barriers instead of kernel boundaries,
+// so the iterates are the same as the kernel-per-phase loop's with the same
+// grid.  Every block reduces the partials of both axes itself (same fixed
+// order), so every block holds the same solver scalars and the loop ends in
+// step across the grid.
+
+struct GridBar {
+  unsigned count, gen;
+  int err, pad;
+};
+
+// At 64 ns per sleep this bounds a wait at about 2 s; a block that gives up
+// sets err, and every block leaves at its next barrier.
+constexpr unsigned long long kBarSpin = 1ull << 25;
+
+__device__ __forceinline__ bool grid_barrier(GridBar* bar) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = &bar->gen;
+    volatile int* err = &bar->err;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned nb = gridDim.x * gridDim.y;
+    if (atomicAdd(&bar->count, 1u) == nb - 1) {
+      atomicExch(&bar->count, 0u);
+      __threadfence();
+      atomicAdd(&bar->gen, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*gen == g && *err == 0) {
+        if (++spins > kBarSpin) { atomicExch(&bar->err, 1); break; }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = (*err == 0);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ double* cpart(const IpDev& D, int phase, int axis) {
+  return D.cpart + (size_t)((phase * 2 + axis) * 2) * D.parts;
+}
+
+// Totals of both axes for one phase, in every block (thread-strided over the
+// block partials, then the block tree), as the last block of a kernel sums.
+template <int N>
+__device__ __forceinline__ void coop_totals(const IpDev& D, int phase, double (&tot)[2][N],
+                                            double* sh, double* tt) {
+  double v[2 * N];
+#pragma unroll
+  for (int k = 0; k < 2 * N; k++) v[k] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int k = 0; k < N; k++) v[a * N + k] += __ldcg(cpart(D, phase, a) + (size_t)k * D.parts + b);
+  block_reduce_n<2 * N>(v, tt, 1, sh, 0);
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int k = 0; k < N; k++) tot[a][k] = tt[a * N + k];
+}
+
+__global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
+  __shared__ double sh[32 * 4];
+  __shared__ double tt[4];
+  __shared__ BiState S[2];
+  const int axis = blockIdx.y;
+  const int n = D.n_mov;
+  if (threadIdx.x < 2) S[threadIdx.x] = D.st[threadIdx.x];
+  __syncthreads();
+  const float* bb = D.b + axis * n;
+  float* x = D.x + axis * n;
+  float* r = D.r + axis * n;
+  float* r0 = D.r0 + axis * n;
+  float* p = D.p + axis * n;
+  float* v = D.v + axis * n;
+  float* sv = D.s + axis * n;
+  float* t = D.t + axis * n;
+  const int i0 = blockIdx.x * kB + threadIdx.x, step = gridDim.x * kB;
+  const int lane = threadIdx.x & 31, w0 = blockIdx.x * kB + (threadIdx.x & ~31);
+  for (int it = 0; it <= 2 * max_iter + 2; it++) {
+    if (S[0].done && S[1].done) break;
+    // restart: r = r0 = b - A x
+    if ((!S[0].done && S[0].need_restart) || (!S[1].done && S[1].need_restart)) {
+      double acc[2] = {0.0, 0.0};
+      if (!S[axis].done && S[axis].need_restart) {
+        for (int w = w0; w < n; w += step) {
+          const int i = w + lane;
+          const float ax = spmv_warp<true>(D, axis, i, i < n, x);
+          if (i < n) {
+            const float ri = bb[i] - ax;
+            r[i] = ri;
+            r0[i] = ri;
+            acc[0] += (double)ri * ri;
+            acc[1] += (double)bb[i] * bb[i];
+          }
+        }
+      }
+      block_reduce_n<2>(acc, cpart(D, 3, axis), D.parts, sh);
+      if (!grid_barrier(D.bar)) return;
+      double tot[2][2];
+      coop_totals<2>(D, 3, tot, sh, tt);
+      if (threadIdx.x == 0)
+        for (int a = 0; a < 2; a++) {
+          BiState& q = S[a];
+          if (q.done || !q.need_restart) continue;
+          q.rho = q.r0sq = q.rr = tot[a][0];
+          if (q.restarts++ == 0) q.i = 0;
+          q.need_restart = 0;
+        }
+      __syncthreads();
+    }
+    const bool live = !S[axis].done;
+    // p = r + beta (p - w v)
+    if (live) {
+      const double beta = (S[axis].rho / S[axis].rho_old) * (S[axis].alpha / S[axis].w);
+      const double w = S[axis].w;
+      for (int i = i0; i < n; i += step) p[i] = (float)(r[i] + beta * (p[i] - w * v[i]));
+    }
+    if (!grid_barrier(D.bar)) return;
+    // v = A p, alpha = rho / (r0 . v)
+    {
+      double acc[1] = {0.0};
+      if (live)
+        for (int w = w0; w < n; w += step) {
+          const int i = w + lane;
+          const float vi = spmv_warp<true>(D, axis, i, i < n, p);
+          if (i < n) {
+            v[i] = vi;
+            acc[0] += (double)r0[i] * vi;
+          }
+        }
+      block_reduce_n<1>(acc, cpart(D, 0, axis), D.parts, sh);
+      if (!grid_barrier(D.bar)) return;
+      double tot[2][1];
+      coop_totals<1>(D, 0, tot, sh, tt);
+      if (threadIdx.x == 0)
+        for (int a = 0; a < 2; a++)
+          if (!S[a].done) S[a].alpha = S[a].rho / tot[a][0];
+      __syncthreads();
+    }
+    // s = r - alpha v
+    if (live) {
+      const double alpha = S[axis].alpha;
+      for (int i = i0; i < n; i += step) sv[i] = (float)(r[i] - alpha * v[i]);
+    }
+    if (!grid_barrier(D.bar)) return;
+    // t = A s, w = (t . s) / (t . t)
+    {
+      double acc[2] = {0.0, 0.0};
+      if (live)
+        for (int w = w0; w < n; w += step) {
+          const int i = w + lane;
+          const float ti = spmv_warp<true>(D, axis, i, i < n, sv);
+          if (i < n) {
+            t[i] = ti;
+            acc[0] += (double)ti * ti;
+            acc[1] += (double)ti * sv[i];
+          }
+        }
+      block_reduce_n<2>(acc, cpart(D, 1, axis), D.parts, sh);
+      if (!grid_barrier(D.bar)) return;
+      double tot[2][2];
+      coop_totals<2>(D, 1, tot, sh, tt);
+      if (threadIdx.x == 0)
+        for (int a = 0; a < 2; a++)
+          if (!S[a].done) S[a].w = tot[a][0] > 0.0 ? tot[a][1] / tot[a][0] : 0.0;
+      __syncthreads();
+    }
+    // x += alpha p + w s; r = s - w t; then the next loop head
+    {
+      double acc[2] = {0.0, 0.0};
+      if (live) {
+        const double alpha = S[axis].alpha, w = S[axis].w;
+        for (int i = i0; i < n; i += step) {
+          x[i] = (float)(x[i] + alpha * p[i] + w * sv[i]);
+          const float ri = (float)(sv[i] - w * t[i]);
+          r[i] = ri;
+          acc[0] += (double)ri * ri;
+          acc[1] += (double)r0[i] * ri;
+        }
+      }
+      block_reduce_n<2>(acc, cpart(D, 2, axis), D.parts, sh);
+      if (!grid_barrier(D.bar)) return;
+      double tot[2][2];
+      coop_totals<2>(D, 2, tot, sh, tt);
+      if (threadIdx.x == 0)
+        for (int a = 0; a < 2; a++) {
+          BiState& q = S[a];
+          if (q.done) continue;
+          q.rr = tot[a][0];
+          q.dot_r0r = tot[a][1];
+          q.i++;
+          loop_head(q, max_iter);
+        }
+      __syncthreads();
+    }
+  }
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 2) D.st[threadIdx.x] = S[threadIdx.x];
+}
+
+// --------------------------------------------------- cluster solve
+// For systems of up to kClMaxRows instances: each axis is solved by one
+// thread-block cluster of kClCtas CTAs.  The phases are those of k_bi_coop;
+// they are separated by the hardware cluster barrier, and the reductions go
+// through distributed shared memory: every CTA stores its block sum in its
+// own shared slot, and after the barrier each CTA adds the slots of all CTAs
+// in rank order, so all CTAs of the cluster hold the same scalars.  Vectors
+// other CTAs wrote are read through L2 (spmv_warp<true>).
+namespace cg = cooperative_groups;
+constexpr int kClCtas = 8;
+constexpr int kClThreads = 1024;
+constexpr int kClMaxRows = 65536;
+
+template <int N>
+__device__ __forceinline__ void cluster_total(cg::cluster_group& cl, double (&v)[N], double* slot,
+                                              double* sh, double* tot_sh, double (&tot)[N]) {
+  block_reduce_n<N>(v, slot, 1, sh, 0);   // slot[k] = this CTA's sum
+  cl.sync();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+      double t = 0.0;
+      for (int r = 0; r < kClCtas; r++) t += cl.map_shared_rank(slot, r)[k];
+      tot_sh[k] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; k++) tot[k] = tot_sh[k];
+}
+
+__global__ void __cluster_dims__(kClCtas, 1, 1) __launch_bounds__(kClThreads, 1)
+k_bi_cluster(IpDev D, int max_iter) {
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ double sh[32 * 2];
+  __shared__ double slot[4][2];
+  __shared__ double tot_sh[2];
+  __shared__ BiState S;
+  const int axis = blockIdx.y;
+  const int n = D.n_mov;
+  if (threadIdx.x == 0) S = D.st[axis];
+  __syncthreads();
+  const float* bb = D.b + axis * n;
+  float* x = D.x + axis * n;
+  float* r = D.r + axis * n;
+  float* r0 = D.r0 + axis * n;
+  float* p = D.p + axis * n;
+  float* v = D.v + axis * n;
+  float* sv = D.s + axis * n;
+  float* t = D.t + axis * n;
+  const int lane = threadIdx.x & 31;
+  const int w0 = (int)cl.block_rank() * kClThreads + (threadIdx.x & ~31);
+  const int step = kClCtas * kClThreads;
+  for (int it = 0; it <= 2 * max_iter + 2 && !S.done; it++) {
+    // restart: r = r0 = b - A x
+    if (S.need_restart) {
+      double acc[2] = {0.0, 0.0};
+      for (int w = w0; w < n; w += step) {
+        const int i = w + lane;
+        const float ax = spmv_warp<true>(D, axis, i, i < n, x);
+        if (i < n) {
+          const float ri = bb[i] - ax;
+          r[i] = ri;
+          r0[i] = ri;
+          acc[0] += (double)ri * ri;
+          acc[1] += (double)bb[i] * bb[i];
+        }
+      }
+      double tot[2];
+      cluster_total<2>(cl, acc, slot[3], sh, tot_sh, tot);
+      if (threadIdx.x == 0) {
+        S.rho = S.r0sq = S.rr = tot[0];
+        if (S.restarts++ == 0) S.i = 0;
+        S.need_restart = 0;
+      }
+      __syncthreads();
+    }
+    // p = r + beta (p - w v)
+    {
+      const double beta = (S.rho / S.rho_old) * (S.alpha / S.w);
+      const double w = S.w;
+      for (int i = w0 + lane; i < n; i += step) p[i] = (float)(r[i] + beta * (p[i] - w * v[i]));
+    }
+    cl.sync();
+    // v = A p, alpha = rho / (r0 . v)
+    {
+      double acc[1] = {0.0};
+      for (int w = w0; w < n; w += step) {
+        const int i = w + lane;
+        const float vi = spmv_warp<true>(D, axis, i, i < n, p);
+        if (i < n) {
+          v[i] = vi;
+          acc[0] += (double)r0[i] * vi;
+        }
+      }
+      double tot[1];
+      cluster_total<1>(cl, acc, slot[0], sh, tot_sh, tot);
+      if (threadIdx.x == 0) S.alpha = S.rho / tot[0];
+      __syncthreads();
+    }
+    // s = r - alpha v
+    {
+      const double alpha = S.alpha;
+      for (int i = w0 + lane; i < n; i += step) sv[i] = (float)(r[i] - alpha * v[i]);
+    }
+    cl.sync();
+    // t = A s, w = (t . s) / (t . t)
+    {
+      double acc[2] = {0.0, 0.0};
+      for (int w = w0; w < n; w += step) {
+        const int i = w + lane;
+        const float ti = spmv_warp<true>(D, axis, i, i < n, sv);
+        if (i < n) {
+          t[i] = ti;
+          acc[0] += (double)ti * ti;
+          acc[1] += (double)ti * sv[i];
+        }
+      }
+      double tot[2];
+      cluster_total<2>(cl, acc, slot[1], sh, tot_sh, tot);
+      if (threadIdx.x == 0) S.w = tot[0] > 0.0 ? tot[1] / tot[0] : 0.0;
+      __syncthreads();
+    }
+    // x += alpha p + w s; r = s - w t; then the next loop head
+    {
+      double acc[2] = {0.0, 0.0};
+      const double alpha = S.alpha, w = S.w;
+      for (int i = w0 + lane; i < n; i += step) {
+        x[i] = (float)(x[i] + alpha * p[i] + w * sv[i]);
+        const float ri = (float)(sv[i] - w * t[i]);
+        r[i] = ri;
+        acc[0] += (double)ri * ri;
+        acc[1] += (double)r0[i] * ri;
+      }
+      double tot[2];
+      cluster_total<2>(cl, acc, slot[2], sh, tot_sh, tot);
+      if (threadIdx.x == 0) {
+        S.rr = tot[0];
+        S.dot_r0r = tot[1];
+        S.i++;
+        loop_head(S, max_iter);
+      }
+      __syncthreads();
+    }
+  }
+  if (cl.block_rank() == 0 && threadIdx.x == 0) D.st[axis] = S;
+  cl.sync();   // no CTA leaves while another may still read its shared memory
 }
 
 // rhs == 0: Eigen sets x = 0; then the instances move to the solution
@@ -442,7 +1000,7 @@ struct IpSizes {
 };
 
 // Scratch layout of run_initial_place (the sizes its carving below takes).
-IpSizes ip_sizes(const HostModel& m, int sm_count) {
+IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   IpSizes z;
   const size_t nP = m.place_insts.size();
   size_t n_mp = 0;
@@ -456,25 +1014,29 @@ IpSizes ip_sizes(const HostModel& m, int sm_count) {
   }
   z.nnz_cap = std::max<size_t>(nnz, 1);
   const int nb_mov = blocks_for((int)nP);
-  z.grid = std::max(1, std::min(nb_mov, sm_count * 8));
-  const size_t scan_blocks = nb_mov;
+  z.grid = std::max(1, std::min(nb_mov, grid_cap));
+  const size_t scan_blocks = blocks_for((int)n_mp);
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
   add((m.n_nets + 1) * 4); add(m.n_pins * 4); add(m.n_pins * 4); add(m.n_pins * 4);
   add(m.n_pins * 8); add(m.n_pins * 8); add((nP + 1) * 4); add(n_mp * 4);
-  add(nP * 8); add(m.n_pins * 8); add(m.n_nets * 16); add(2 * nP * 4); add(2 * (nP + 1) * 4);
+  add(nP * 8); add(m.n_pins * 8); add(m.n_nets * 16); add(2 * n_mp * 4); add(2 * (n_mp + 1) * 4);
+  add(2 * n_mp * 4); add(2 * n_mp * 4); add(2 * (nP + 1) * 4);
   add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 4);
   for (int k = 0; k < 9; k++) add(2 * nP * 4);
-  add(2 * 2 * (size_t)z.grid * 8); add(16 * 4); add(2 * sizeof(BiState));
+  add(2 * 2 * (size_t)z.grid * 8); add(4 * 2 * 2 * (size_t)z.grid * 8); add(sizeof(GridBar));
+  add(16 * 4); add(2 * sizeof(BiState));
   z.bytes = bytes;
   return z;
 }
 
-size_t initial_place_bytes(const HostModel& m, int sm_count) { return ip_sizes(m, sm_count).bytes; }
+// (a cooperative grid has at most 8 blocks of kB threads per SM, 2 axes)
+size_t initial_place_bytes(const HostModel& m, int sm_count) { return ip_sizes(m, sm_count * 8).bytes; }
 
 int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& timer,
-                      void* pinned, cudaMemPool_t pool) {
-  static_assert(2 * sizeof(BiState) <= sizeof(HostPinned::ip_state), "pinned solver state too small");
+                      void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev) {
+  static_assert(2 * sizeof(BiState) + sizeof(GridBar) <= sizeof(HostPinned::ip_state),
+                "pinned solver state too small");
   const gpl_params& prm = m.p;
   IpDev D;
   D.n_mov = (int)m.place_insts.size();
@@ -504,12 +1066,25 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     const int i = m.place_insts[k];
     ctr[k] = make_int2((m.ilx[i] + m.iux[i]) / 2, (m.ily[i] + m.iuy[i]) / 2);
   }
-  const IpSizes z = ip_sizes(m, sm_count);
+  // The cooperative solve needs its whole grid (both axes) resident at once.
+  int dev = 0, coop_attr = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop_attr, cudaDevAttrCooperativeLaunch, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bi_coop, kB, 0);
+  cudaGetLastError();
+  // ip_solver: 0 auto, 1 kernel per phase, 2 cooperative grid, 3 cluster per axis
+  const int mode = prm.ip_solver;
+  bool cluster = mode == 3 || (mode == 0 && nP <= kClMaxRows);
+  bool coop = !cluster && coop_attr != 0 && per_sm > 0 && (mode == 0 || mode == 2);
+  // the same grid either way, so both solvers give the same iterates
+  const int grid_cap = (coop_attr != 0 && per_sm > 0) ? std::max(1, per_sm * sm_count / 2) : sm_count * 8;
+  const IpSizes z = ip_sizes(m, grid_cap);
   D.nnz_cap = z.nnz_cap;
   const int nb_mov = blocks_for(nP);
   const int grid = z.grid;
   D.parts = grid;
-  const int scan_blocks = nb_mov;
+  D.n_mp = (int)mp.size();
+  const int scan_blocks = blocks_for(D.n_mp);
   cudaError_t e = dev_alloc((void**)&D.mem, z.bytes, pool, s);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -529,7 +1104,10 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   D.ctr = (int2*)take(nP * 8);
   D.pos = (int2*)take(m.n_pins * 8);
   D.bound = (int4*)take(m.n_nets * 16);
-  D.cnt = (int32_t*)take(2 * nP * 4);
+  D.cnt = (int32_t*)take(2 * (size_t)D.n_mp * 4);
+  D.slot_off = (int32_t*)take(2 * ((size_t)D.n_mp + 1) * 4);
+  D.slot_diag = (float*)take(2 * (size_t)D.n_mp * 4);
+  D.slot_rhs = (float*)take(2 * (size_t)D.n_mp * 4);
   D.rowptr = (int32_t*)take(2 * (nP + 1) * 4);
   D.scan_part = (int32_t*)take(2 * scan_blocks * 4);
   D.col = (int32_t*)take(2 * D.nnz_cap * 4);
@@ -544,6 +1122,8 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   D.s = (float*)take(2 * nP * 4);
   D.t = (float*)take(2 * nP * 4);
   D.part = (double*)take(2 * 2 * (size_t)D.parts * 8);
+  D.cpart = (double*)take(4 * 2 * 2 * (size_t)D.parts * 8);
+  D.bar = (GridBar*)take(sizeof(GridBar));
   D.counters = (unsigned*)take(16 * 4);
   D.st = (BiState*)take(2 * sizeof(BiState));
   int rc = GPL_OK;
@@ -573,22 +1153,75 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   P.max_iter = prm.initial_place_max_solver_iter;
   const dim3 g2(nb_mov, 2), gs(grid, 2);
   float err = 0.0f;
-  int rounds = 0, iters[2] = {0, 0};
+  int rounds = 0, iters[2] = {0, 0}, coop_rounds = 0;
   for (int round = 1; round <= prm.initial_place_max_iter && !rc; round++) {
     timer.begin(kKOther);
     k_ip_pos<<<blocks_for(m.n_pins), kB, 0, s>>>(D);
     k_ip_bound<<<blocks_for(m.n_nets), kB, 0, s>>>(D);
-    k_ip_count<<<g2, kB, 0, s>>>(D, P);
-    k_scan_blocks<<<dim3(scan_blocks, 2), kB, 0, s>>>(D.cnt, D.rowptr, D.scan_part, nP);
-    k_scan_parts<<<2, 32, 0, s>>>(D.scan_part, scan_blocks, D.rowptr, nP);
-    k_scan_add<<<dim3(scan_blocks, 2), kB, 0, s>>>(D.rowptr, D.scan_part, nP);
-    k_ip_fill<<<g2, kB, 0, s>>>(D, P);
+    k_ip_count<<<dim3(scan_blocks, 2), kB, 0, s>>>(D, P);
+    k_scan_blocks<<<dim3(scan_blocks, 2), kB, 0, s>>>(D.cnt, D.slot_off, D.scan_part, D.n_mp);
+    k_scan_parts<<<2, kScanT, 0, s>>>(D.scan_part, scan_blocks, D.slot_off, D.n_mp);
+    k_scan_add<<<dim3(scan_blocks, 2), kB, 0, s>>>(D.slot_off, D.scan_part, D.n_mp);
+    k_ip_rowptr<<<dim3(blocks_for(nP + 1), 2), kB, 0, s>>>(D);
+    k_ip_fill<<<dim3(scan_blocks, 2), kB, 0, s>>>(D, P);
+    k_ip_rowsum<<<g2, kB, 0, s>>>(D);
     k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
     k_bi_residual<<<gs, kB, 0, s>>>(D, 1, P.max_iter);
     timer.end(kKOther);
-    timer.count(9);
-    // BiCGSTAB: chunks of iterations, then poll the done flags
-    for (int it = 0; it <= 2 * P.max_iter + 2; it += 8) {
+    timer.count(11);
+    bool solved = false;
+    if (cluster) {
+      // the whole solve of each axis in one cluster
+      timer.begin(kKOther);
+      k_bi_cluster<<<dim3(kClCtas, 2), kClThreads, 0, s>>>(D, P.max_iter);
+      timer.end(kKOther);
+      timer.count(1);
+      const cudaError_t ce = cudaGetLastError();
+      if (ce == cudaSuccess) {
+        solved = true;
+        coop_rounds++;
+      } else {
+        // not launched (no room for the cluster): the grid forms below
+        if (prm.verbose_level > 0)
+          printf("[InitialPlace] cluster solve not launched (%s)\n", cudaGetErrorString(ce));
+        cluster = false;
+        coop = coop_attr != 0 && per_sm > 0 && mode != 1;
+      }
+    }
+    if (!solved && coop) {
+      // the whole solve in one cooperative launch
+      int max_iter = P.max_iter;
+      void* args[] = {(void*)&D, (void*)&max_iter};
+      cudaError_t ce = cudaMemsetAsync(D.bar, 0, sizeof(GridBar), s);
+      timer.begin(kKOther);
+      if (ce == cudaSuccess)
+        ce = cudaLaunchCooperativeKernel((const void*)k_bi_coop, dim3(grid, 2), dim3(kB), args, 0, s);
+      timer.end(kKOther);
+      timer.count(1);
+      if (ce != cudaSuccess) {
+        cudaGetLastError();            // not launched: the kernel-per-phase loop below
+        if (prm.verbose_level > 0)
+          printf("[InitialPlace] cooperative solve not launched (%s): one kernel per phase\n",
+                 cudaGetErrorString(ce));
+        coop = false;
+      } else {
+        GridBar* bar_h = reinterpret_cast<GridBar*>(st_h + 2);
+        if (cudaMemcpyAsync(bar_h, D.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            host_wait(s, sync_ev) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+        if (bar_h->err == 0) {
+          solved = true;
+          coop_rounds++;
+        } else {
+          // a barrier wait ran out: solve this round again phase by phase
+          coop = false;
+          k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
+          k_bi_residual<<<gs, kB, 0, s>>>(D, 1, P.max_iter);
+          timer.count(2);
+        }
+      }
+    }
+    // BiCGSTAB phase by phase: chunks of iterations, then poll the done flags
+    for (int it = 0; !solved && it <= 2 * P.max_iter + 2; it += 8) {
       timer.begin(kKOther);
       for (int k = 0; k < 8; k++) {
         k_bi_residual<<<gs, kB, 0, s>>>(D, 0, P.max_iter);
@@ -602,14 +1235,14 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
       timer.count(48);
       if (cudaGetLastError() != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
       if (cudaMemcpyAsync(st_h, D.st, 2 * sizeof(BiState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+          host_wait(s, sync_ev) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
       if (st_h[0].done && st_h[1].done) break;
     }
     if (rc) break;
     k_ip_move<<<nb_mov, kB, 0, s>>>(D);
     timer.count(1);
     if (cudaMemcpyAsync(st_h, D.st, 2 * sizeof(BiState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+        host_wait(s, sync_ev) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
     // solver.error() = sqrt(|r|^2 / |b|^2)
     float ex = st_h[0].rhs_sq > 0 ? (float)sqrt(st_h[0].rr / st_h[0].rhs_sq) : 0.0f;
     float ey = st_h[1].rhs_sq > 0 ? (float)sqrt(st_h[1].rr / st_h[1].rhs_sq) : 0.0f;
@@ -620,7 +1253,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   }
   if (!rc) {
     if (cudaMemcpyAsync(ctr.data(), D.ctr, nP * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) rc = GPL_ERR_CUDA;
+        host_wait(s, sync_ev) != cudaSuccess) rc = GPL_ERR_CUDA;
   }
   dev_free(D.mem, pool, s);
   if (rc) { set_error("initial place: CUDA error"); return rc; }
@@ -632,6 +1265,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     stats->last_hpwl = 0;
     stats->solver_iters_x = iters[0];
     stats->solver_iters_y = iters[1];
+    stats->cooperative_rounds = coop_rounds;
   }
   return GPL_OK;
 }

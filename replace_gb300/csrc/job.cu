@@ -88,6 +88,7 @@ struct gpl_job {
   HostPinned* pinned = nullptr;        // control/result staging
   bool own_pinned = false;
   cudaMemPool_t pool = nullptr;         // stream-ordered pool (server jobs)
+  cudaEvent_t sync_ev = nullptr;        // blocking-sync event (server jobs)
   bool nb_ready = false, np_ready = false;
   // NesterovPlace state (src/nesterovPlace.h:76-125)
   float step_length = 0, density_penalty = 0, base_wl_coef = 0, wl_coef_x = 0, wl_coef_y = 0;
@@ -358,7 +359,7 @@ int launch_phase2(gpl_job* j, bool want_phi, int area_set) {
 }
 
 int finish(gpl_job* j) {
-  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  GPL_CUDA(host_wait(j->stream, j->sync_ev));
   j->last = *j->d.result_h;
   return GPL_OK;
 }
@@ -664,7 +665,9 @@ int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
   return GPL_OK;
 }
 
-void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool) {
+void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool,
+              cudaEvent_t sync_ev) {
+  j->sync_ev = sync_ev;
   j->stream = stream;
   j->own_stream = false;
   j->pinned = pinned;
@@ -730,6 +733,7 @@ void gpl_params_default(gpl_params* p) {
   p->device = 0;
   p->stream = nullptr;
   p->use_graph = 1;
+  p->ip_solver = 0;
 }
 
 gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
@@ -933,7 +937,8 @@ gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
   cudaSetDevice(j->device);
   int sm = 0;
   GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
-  return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer, j->pinned->ip_state, j->pool);
+  return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer, j->pinned->ip_state, j->pool,
+                                       j->sync_ev);
 }
 
 }  // extern "C"

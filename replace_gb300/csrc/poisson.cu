@@ -384,9 +384,16 @@ int ilog2(int v) { int l = 0; while ((1 << l) < v) l++; return l; }
 
 }  // namespace
 
-int pairs_a(int nx, int ny) { return max(1, min(ny / 2, 2048 / nx)); }
-int pairs_b(int nx, int ny) { return max(1, min(nx / 2, min(4, 4096 / ny))); }
-int pairs_c(int nx, int ny) { return max(1, min(ny / 2, 2048 / nx)); }
+// Row (column) pairs per block: enough points per block to keep 256 threads
+// busy on large grids, but at least 64 blocks where the grid has that many
+// pairs, so that small grids are spread over SMs instead of serialised in a
+// few blocks.
+constexpr int kMinPoissonBlocks = 64;
+int pairs_a(int nx, int ny) { return max(1, min(min(ny / 2, 2048 / nx), (ny / 2) / kMinPoissonBlocks)); }
+int pairs_b(int nx, int ny) {
+  return max(1, min(min(nx / 2, min(4, 4096 / ny)), (nx / 2) / kMinPoissonBlocks));
+}
+int pairs_c(int nx, int ny) { return pairs_a(nx, ny); }
 
 size_t smem_a(int nx, int ny) { return (size_t)2 * pairs_a(nx, ny) * nx * sizeof(float2); }
 size_t smem_b(int nx, int ny) { return (size_t)3 * pairs_b(nx, ny) * ny * sizeof(float2); }

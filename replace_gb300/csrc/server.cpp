@@ -55,6 +55,7 @@ struct gpl_server {
   cudaMemPool_t pool = nullptr;
   std::vector<cudaStream_t> streams;
   std::vector<HostPinned*> pinned;
+  std::vector<cudaEvent_t> sync_ev;   // per slot; null = spin-waiting syncs
   std::vector<std::thread> workers;
   std::mutex mu;
   std::condition_variable cv_work;   // queue, budget or stop changed
@@ -77,7 +78,7 @@ namespace {
 // One admitted job on slot `slot`, start to end.
 void run_job(gpl_server* s, int slot, Entry& e) {
   gpl_job* j = e.job;
-  job_bind(j, s->streams[slot], s->pinned[slot], s->pool);
+  job_bind(j, s->streams[slot], s->pinned[slot], s->pool, s->sync_ev[slot]);
   int rc = GPL_OK;
   gpl_ip_stats ip{};
   if (s->p.run_initial_place) rc = gpl_initial_place(j, &ip);
@@ -105,7 +106,7 @@ void run_job(gpl_server* s, int slot, Entry& e) {
   if (e.res.n_insts > 0) gpl_get_inst_locations(j, e.lx.data(), e.ly.data());
   gpl_destroy(j);                               // frees in stream order
   e.job = nullptr;
-  cudaStreamSynchronize(s->streams[slot]);      // the memory is back in the pool
+  host_wait(s->streams[slot], s->sync_ev[slot]); // the memory is back in the pool
 }
 
 void worker(gpl_server* s, int slot) {
@@ -151,6 +152,7 @@ void gpl_server_params_default(gpl_server_params* p) {
   p->hbm_budget_bytes = 0;
   p->chunk_iters = 64;
   p->run_initial_place = 1;
+  p->blocking_sync = 1;
 }
 
 gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out) {
@@ -188,6 +190,10 @@ gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out) {
     HostPinned* hp = nullptr;
     GPL_CUDA(cudaMallocHost(&hp, sizeof(HostPinned)));
     s->pinned.push_back(hp);
+    cudaEvent_t ev = nullptr;
+    if (p->blocking_sync)
+      GPL_CUDA(cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming));
+    s->sync_ev.push_back(ev);
   }
   gpl_server* raw = s.release();
   for (int k = 0; k < p->max_active; k++) raw->workers.emplace_back(worker, raw, k);
@@ -325,6 +331,8 @@ void gpl_server_destroy(gpl_server* s) {
     cudaStreamDestroy(st);
   }
   for (auto hp : s->pinned) cudaFreeHost(hp);
+  for (auto ev : s->sync_ev)
+    if (ev) cudaEventDestroy(ev);
   if (s->pool) cudaMemPoolDestroy(s->pool);
   delete s;
 }

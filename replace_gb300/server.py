@@ -35,12 +35,13 @@ def _result_dict(r: _abi.ServerResult) -> dict:
 
 class PlacementServer:
     def __init__(self, device: int = 0, max_active: int = 8, hbm_budget_bytes: int = 0,
-                 chunk_iters: int = 64, run_initial_place: bool = True):
+                 chunk_iters: int = 64, run_initial_place: bool = True, blocking_sync: bool = True):
         self.lib = load()
         p = _abi.ServerParams()
         self.lib.gpl_server_params_default(C.byref(p))
         p.device, p.max_active, p.hbm_budget_bytes = device, max_active, hbm_budget_bytes
         p.chunk_iters, p.run_initial_place = chunk_iters, 1 if run_initial_place else 0
+        p.blocking_sync = 1 if blocking_sync else 0
         self.params = p
         h = C.c_void_p()
         check(self.lib.gpl_server_create(C.byref(p), C.byref(h)))
