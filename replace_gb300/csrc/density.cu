@@ -214,7 +214,45 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
   float2* wl_out = C.write_wd ? A.wl_out : nullptr;
   float2* d_out = C.write_wd ? A.d_out : nullptr;
   const float lam = C.density_penalty;
-  for (int g = blockIdx.x * kBlock + threadIdx.x; g < A.n_g; g += gridDim.x * kBlock) {
+  const int lane = threadIdx.x & 31;
+  // warp-uniform grid-stride loop: the warps gather the pins of cells with
+  // more than 32 pins (macros) together
+  for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < A.n_g; base += gridDim.x * kBlock) {
+    const int g = base + lane;
+    const bool valid = g < A.n_g;
+    int ps = 0, pe = 0;
+    float2 w = make_float2(0.0f, 0.0f);
+    if (valid) {
+      ps = A.g_pin_start[g];
+      pe = A.g_pin_start[g + 1];
+      if (pe - ps <= 32) {
+        // WA gradient: the cell's pins in instance pin order
+        for (int t = ps; t < pe; t++) {
+          const float2 pg = A.pin_grad[__ldg(&A.g_pins[t])];
+          w.x = __fadd_rn(w.x, pg.x);
+          w.y = __fadd_rn(w.y, pg.y);
+        }
+      }
+    }
+    unsigned many = __ballot_sync(0xffffffffu, pe - ps > 32);
+    while (many) {
+      const int src = __ffs(many) - 1;
+      many &= many - 1;
+      const int s0 = __shfl_sync(0xffffffffu, ps, src), s1 = __shfl_sync(0xffffffffu, pe, src);
+      float2 part = make_float2(0.0f, 0.0f);
+      for (int t = s0 + lane; t < s1; t += 32) {
+        const float2 pg = A.pin_grad[__ldg(&A.g_pins[t])];
+        part.x = __fadd_rn(part.x, pg.x);
+        part.y = __fadd_rn(part.y, pg.y);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        part.x = __fadd_rn(part.x, __shfl_xor_sync(0xffffffffu, part.x, o));
+        part.y = __fadd_rn(part.y, __shfl_xor_sync(0xffffffffu, part.y, o));
+      }
+      if (lane == src) w = part;
+    }
+    if (!valid) continue;
     const float2 c = slp[g];
     const int k = A.kind[g];
     // density gradient: sum over covered bins of overlap * scale * field
@@ -234,14 +272,6 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
           d.y = __fadd_rn(d.y, __fmul_rn(ov, f.y));
         }
       }
-    }
-    // WA gradient: the cell's pins in instance pin order
-    float2 w = make_float2(0.0f, 0.0f);
-    const int ps = A.g_pin_start[g], pe = A.g_pin_start[g + 1];
-    for (int t = ps; t < pe; t++) {
-      const float2 pg = A.pin_grad[__ldg(&A.g_pins[t])];
-      w.x = __fadd_rn(w.x, pg.x);
-      w.y = __fadd_rn(w.y, pg.y);
     }
     float2 s = make_float2(__fadd_rn(w.x, __fmul_rn(lam, d.x)), __fadd_rn(w.y, __fmul_rn(lam, d.y)));
     const float2 pc = A.precond[g];

@@ -391,7 +391,12 @@ def generate(n_cells: int, n_nets: int, n_io: int = 200, n_macros: int = 0,
     rank = np.arange(total) - np.repeat(first, deg)
     off = rng.integers(-window, window + 1, size=total)
     off[rank == 0] = 0                                  # seed instance itself
-    cell = np.clip(seeds[net_of_pin] + off, 0, n_inst - 1)
+    # reflect at both ends of the index range (clipping would pile the pins
+    # of every window that overhangs an end onto the first and last cells)
+    cell = seeds[net_of_pin] + off
+    cell = np.where(cell < 0, -cell, cell)
+    cell = np.where(cell > n_inst - 1, 2 * (n_inst - 1) - cell, cell)
+    cell = np.clip(cell, 0, n_inst - 1)
     pw = w[cell]
     ph = h[cell]
     ox = np.floor((rng.random(total) - 0.5) * pw).astype(np.int64)
