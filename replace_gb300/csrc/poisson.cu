@@ -47,7 +47,6 @@ __device__ float2* block_fft(float2* a, float2* b, int n, int logn, int batch, i
   const int total = half * batch;
   for (int s = 0; s < logn; s++) {
     const int ns = 1 << s;
-    const int twstep = kFftMax / (2 * ns);
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
       const int bi = idx >> (logn - 1);
       const int j = idx & (half - 1);
@@ -56,7 +55,7 @@ __device__ float2* block_fft(float2* a, float2* b, int n, int logn, int batch, i
       const int k = j & (ns - 1);
       float2 u = in[j];
       float2 v = in[j + half];
-      float2 w = __ldg(&tw[k * twstep]);
+      float2 w = tw[k << (logn - 1 - s)];
       if (sign > 0) w.y = -w.y;
       v = cmul(v, w);
       const int o = ((j - k) << 1) + k;
@@ -67,6 +66,13 @@ __device__ float2* block_fft(float2* a, float2* b, int n, int logn, int batch, i
     float2* t = a; a = b; b = t;
   }
   return a;
+}
+
+// The twiddles of a length-n FFT, exp(-2 pi i m / n) for m < n/2, copied into
+// shared memory from the kFftMax table (the same values, read once per block).
+__device__ __forceinline__ void load_twiddles(float2* tws, const float2* __restrict__ tw, int n) {
+  const int stride = kFftMax / n;
+  for (int m = threadIdx.x; m < n / 2; m += blockDim.x) tws[m] = __ldg(&tw[m * stride]);
 }
 
 // Makhoul position of element i of a length-n sequence: v[m] = x[2m],
@@ -128,6 +134,8 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
   const int rp_n = A.pairs_per_block;
   float2* buf0 = smem;
   float2* buf1 = smem + rp_n * n;
+  float2* tws = smem + 2 * rp_n * n;                 // [n/2] twiddles
+  load_twiddles(tws, A.tw, n);
   const int nb = A.nx * A.ny;
   double ovf = 0.0;
   const unsigned long long* area = nullptr;
@@ -171,7 +179,7 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
     buf0[rp * n + makhoul_pos(i, n)] = make_float2(d0, d1);
   }
   __syncthreads();
-  float2* res = block_fft(buf0, buf1, n, A.logn, rp_n, -1, A.tw);
+  float2* res = block_fft(buf0, buf1, n, A.logn, rp_n, -1, tws);
   for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
     const int rp = idx / n, k = idx - rp * n;
     const int r = blockIdx.x * rp_n + rp;
@@ -203,6 +211,8 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
   float2* s0 = smem;                 // [cp][n] work
   float2* s1 = smem + cp * n;        // [cp][n] scratch
   float2* s2 = smem + 2 * cp * n;    // [cp][n] spectrum: (phi^ col u0, phi^ col u1)
+  float2* tws = smem + 3 * cp * n;   // [n/2] twiddles
+  load_twiddles(tws, B.tw, n);
   const int u_base = blockIdx.x * 2 * cp;
   // load: column pair q holds columns u_base + 2q, +1
   for (int idx = threadIdx.x; idx < 2 * cp * n; idx += blockDim.x) {
@@ -214,7 +224,7 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
     slot[c & 1] = val;
   }
   __syncthreads();
-  float2* res = block_fft(s0, s1, n, B.logn, cp, -1, B.tw);
+  float2* res = block_fft(s0, s1, n, B.logn, cp, -1, tws);
   float2* other = (res == s0) ? s1 : s0;
   // DCT-II along y, then the spectral solve (src/fft.cpp:117-166)
   for (int idx = threadIdx.x; idx < cp * n; idx += blockDim.x) {
@@ -250,7 +260,7 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
   }
   __syncthreads();
   float2* scratch = (other == s0) ? s1 : s0;
-  res = block_fft(other, scratch, n, B.logn, cp, +1, B.tw);
+  res = block_fft(other, scratch, n, B.logn, cp, +1, tws);
   for (int idx = threadIdx.x; idx < 2 * cp * n; idx += blockDim.x) {
     const int v = idx / (2 * cp);
     const int c = idx - v * 2 * cp;
@@ -278,7 +288,7 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
   }
   __syncthreads();
   scratch = (other == s0) ? s1 : s0;
-  res = block_fft(other, scratch, n, B.logn, cp, +1, B.tw);
+  res = block_fft(other, scratch, n, B.logn, cp, +1, tws);
   for (int idx = threadIdx.x; idx < 2 * cp * n; idx += blockDim.x) {
     const int v = idx / (2 * cp);
     const int c = idx - v * 2 * cp;
@@ -333,6 +343,8 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
   float* rows = reinterpret_cast<float*>(smem);       // [rp][4][n]: p1 row0, p1 row1, p2 row0, p2 row1
   float2* s0 = smem + rp_n * 2 * n;                    // [rp][n]
   float2* s1 = s0 + rp_n * n;                          // [rp][n]
+  float2* tws = s1 + rp_n * n;                         // [n/2] twiddles
+  load_twiddles(tws, C.tw, n);
   for (int idx = threadIdx.x; idx < rp_n * 2 * n; idx += blockDim.x) {
     const int rp = idx / (2 * n), t = idx - rp * 2 * n;
     const int h = t / n, i = t - h * n;
@@ -355,7 +367,7 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
       build_dct3_pair(a0, a1, tr == 1 ? C.wx : nullptr, tr == 1, s0 + rp * n, n, k, __ldg(&C.w4[k]));
     }
     __syncthreads();
-    float2* res = block_fft(s0, s1, n, C.logn, rp_n, +1, C.tw);
+    float2* res = block_fft(s0, s1, n, C.logn, rp_n, +1, tws);
     for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
       const int rp = idx / n, m = idx - rp * n;
       const int r = blockIdx.x * rp_n + rp;
@@ -384,20 +396,20 @@ int ilog2(int v) { int l = 0; while ((1 << l) < v) l++; return l; }
 
 }  // namespace
 
-// Row (column) pairs per block: enough points per block to keep 256 threads
-// busy on large grids, but at least 64 blocks where the grid has that many
-// pairs, so that small grids are spread over SMs instead of serialised in a
-// few blocks.
-constexpr int kMinPoissonBlocks = 64;
+// Row (column) pairs per block: as few as keep 256 threads busy, so that the
+// grid has up to kMinPoissonBlocks blocks (several per SM) to hide the
+// latency of the loads; small grids are spread over SMs instead of being
+// serialised in a few blocks.
+constexpr int kMinPoissonBlocks = 512;
 int pairs_a(int nx, int ny) { return max(1, min(min(ny / 2, 2048 / nx), (ny / 2) / kMinPoissonBlocks)); }
 int pairs_b(int nx, int ny) {
   return max(1, min(min(nx / 2, min(4, 4096 / ny)), (nx / 2) / kMinPoissonBlocks));
 }
 int pairs_c(int nx, int ny) { return pairs_a(nx, ny); }
 
-size_t smem_a(int nx, int ny) { return (size_t)2 * pairs_a(nx, ny) * nx * sizeof(float2); }
-size_t smem_b(int nx, int ny) { return (size_t)3 * pairs_b(nx, ny) * ny * sizeof(float2); }
-size_t smem_c(int nx, int ny) { return (size_t)4 * pairs_c(nx, ny) * nx * sizeof(float2); }
+size_t smem_a(int nx, int ny) { return ((size_t)2 * pairs_a(nx, ny) * nx + nx / 2) * sizeof(float2); }
+size_t smem_b(int nx, int ny) { return ((size_t)3 * pairs_b(nx, ny) * ny + ny / 2) * sizeof(float2); }
+size_t smem_c(int nx, int ny) { return ((size_t)4 * pairs_c(nx, ny) * nx + nx / 2) * sizeof(float2); }
 
 int poisson_blocks_a(int nx, int ny) { int r = pairs_a(nx, ny); return (ny / 2 + r - 1) / r; }
 
