@@ -39,22 +39,22 @@ struct ScatterArgs {
 };
 
 __device__ __forceinline__ float2 predict_one(const ScatterArgs& A, const EvalCtl& C, int g, int2 h) {
-  const float2 cs = A.slp[C.i_src][g], sg = A.sum[C.i_src][g], cc = A.coordi[C.c_cur][g];
+  const float2 cs = pick4(A.slp, C.i_src)[g], sg = pick4(A.sum, C.i_src)[g], cc = pick2(A.coordi, C.c_cur)[g];
   float nx = __fadd_rn(cs.x, __fmul_rn(C.step, sg.x));
   float ny = __fadd_rn(cs.y, __fmul_rn(C.step, sg.y));
   float sx = __fadd_rn(nx, __fmul_rn(C.coeff, __fsub_rn(nx, cc.x)));
   float sy = __fadd_rn(ny, __fmul_rn(C.coeff, __fsub_rn(ny, cc.y)));
   const BinGeom& G = A.geo;
-  A.coordi[C.c_next][g] = make_float2(inside(nx, h.x, G.core_lx, G.core_ux), inside(ny, h.y, G.core_ly, G.core_uy));
+  pick2(A.coordi, C.c_next)[g] = make_float2(inside(nx, h.x, G.core_lx, G.core_ux), inside(ny, h.y, G.core_ly, G.core_uy));
   float2 s = make_float2(inside(sx, h.x, G.core_lx, G.core_ux), inside(sy, h.y, G.core_ly, G.core_uy));
-  A.slp[C.i_eval][g] = s;
+  pick4(A.slp, C.i_eval)[g] = s;
   return s;
 }
 
 __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
   __shared__ long long vals[kBlock];
   const EvalCtl C = *A.ctl;
-  unsigned long long* area = A.area[C.area_cur];
+  unsigned long long* area = pick2(A.area, C.area_cur);
   const int g = blockIdx.x * kBlock + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const BinGeom& G = A.geo;
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
   float sc = 0.0f;
   if (g < A.n_g) {
     const int2 h = A.half[g];
-    const float2 c = C.predict ? predict_one(A, C, g, h) : A.slp[C.i_eval][g];
+    const float2 c = C.predict ? predict_one(A, C, g, h) : pick4(A.slp, C.i_eval)[g];
     k = A.kind[g];
     density_rect(c, h, lx, ux, ly, uy);
     G.range(lx, ux, ly, uy, x0, x1, y0, y1);
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
 // One block per big cell (macros): threads stride over its bins.
 __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int32_t* big, int n_big) {
   const EvalCtl C = *A.ctl;
-  unsigned long long* area = A.area[C.area_cur];
+  unsigned long long* area = pick2(A.area, C.area_cur);
   const int g = big[blockIdx.x];
   const BinGeom& G = A.geo;
   const int nb = G.cnt_x * G.cnt_y;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int
     __syncthreads();
     c = cs;
   } else {
-    c = A.slp[C.i_eval][g];
+    c = pick4(A.slp, C.i_eval)[g];
   }
   int lx, ux, ly, uy, x0, x1, y0, y1;
   density_rect(c, h, lx, ux, ly, uy);
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
   const BinGeom& G = A.geo;
   const EvalCtl C = *A.ctl;
   int lx, ux, ly, uy, x0, x1, y0, y1;
-  density_rect(A.slp[C.i_eval][g], A.half[g], lx, ux, ly, uy);
+  density_rect(pick4(A.slp, C.i_eval)[g], A.half[g], lx, ux, ly, uy);
   G.range(lx, ux, ly, uy, x0, x1, y0, y1);
   const int nbx = max(x1 - x0, 0), total = nbx * max(y1 - y0, 0);
   const float sc = A.scale[g];
@@ -201,16 +201,16 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
 // block partial sums are reduced by the last block to finish (threadfence +
 // counter), in a fixed order, so there is no separate reduction launch and
 // the result is the same run to run.
-__global__ void __launch_bounds__(kBlock, 5) k_cell(CellArgs A) {
+__global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
   __shared__ double sh[32 * kPartSlots];
   __shared__ bool last;
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // |wl|, |d|, coord dist^2, grad dist^2, nan
   const BinGeom& G = A.geo;
   const EvalCtl C = *A.ctl;
-  const float2* slp = A.slp[C.i_eval];
-  float2* sum_out = C.write_sum ? A.sum[C.i_eval] : nullptr;
-  const float2* ref_slp = C.i_ref >= 0 ? A.slp[C.i_ref] : nullptr;
-  const float2* ref_sum = C.i_ref >= 0 ? A.sum[C.i_ref] : nullptr;
+  const float2* slp = pick4(A.slp, C.i_eval);
+  float2* sum_out = C.write_sum ? pick4(A.sum, C.i_eval) : nullptr;
+  const float2* ref_slp = C.i_ref >= 0 ? pick4(A.slp, C.i_ref) : nullptr;
+  const float2* ref_sum = C.i_ref >= 0 ? pick4(A.sum, C.i_ref) : nullptr;
   float2* wl_out = C.write_wd ? A.wl_out : nullptr;
   float2* d_out = C.write_wd ? A.d_out : nullptr;
   const float lam = C.density_penalty;
@@ -383,7 +383,10 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   return GPL_OK;
 }
 
-int cell_grid(const DeviceModel& d) { return std::max(1, std::min(cell_blocks(d), d.sm_count * 8)); }
+// The gcell kernel's grid-stride loop runs on one wave of resident blocks (4
+// per SM at its register count), so its last-block reduction waits for no
+// second wave.
+int cell_grid(const DeviceModel& d) { return std::max(1, std::min(cell_blocks(d), d.sm_count * 4)); }
 
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t) {
   CellArgs A;

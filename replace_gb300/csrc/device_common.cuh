@@ -56,6 +56,18 @@ __device__ __forceinline__ float inside(float c, int h, int lo, int hi) {
 // fastExp (src/nesterovBase.cpp:1568-1582): (1 + a/1024)^1024 by ten
 // squarings.  The reference's first step is evaluated in double; for a float
 // argument 1 + a/1024 rounded once to float is the same value.
+// Element i of a small pointer array held in kernel parameters, by selects:
+// indexing a parameter array with a run-time index makes the compiler copy
+// the whole parameter block to local memory.
+template <class T>
+__device__ __forceinline__ T pick4(T const (&a)[4], int i) {
+  return i == 0 ? a[0] : i == 1 ? a[1] : i == 2 ? a[2] : a[3];
+}
+template <class T>
+__device__ __forceinline__ T pick2(T const (&a)[2], int i) {
+  return i == 0 ? a[0] : a[1];
+}
+
 __device__ __forceinline__ float fast_exp(float a) {
   a = __fadd_rn(1.0f, __fmul_rn(a, 0.0009765625f));
 #pragma unroll

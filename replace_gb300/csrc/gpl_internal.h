@@ -62,6 +62,10 @@ int build_nesterov_base(HostModel& m);
 void host_place_center(HostModel& m);
 void host_set_inst_center(HostModel& m, int inst, int x, int y);
 
+// WA net buckets by degree: 2, 4, 8, 16, 32 (lane groups), 64, 128 (a warp,
+// two or four pins per lane), more (a warp, looping).
+constexpr int kWaBuckets = 8;
+
 // -------------------------------------------------------------- device model
 struct DeviceModel {
   // static gcell data
@@ -77,11 +81,11 @@ struct DeviceModel {
   // pins and nets
   int n_pins = 0, n_nets = 0;
   // Pins are renumbered on the device: nets in WA-bucket order (degree <= 2,
-  // 4, 8, 16, 32, more), each net's pins contiguous.
+  // 4, 8, 16, 32, 64, 128, more), each net's pins contiguous.
   int4* pins = nullptr;            // (gcell or -1, x offset or position, y ..., 0)
   int32_t* net_start = nullptr;    // pin CSR of the bucket-ordered nets
-  int wa_bucket_start[7] = {0};    // first net of each bucket
-  int wa_block_start[7] = {0};     // first block of each bucket in the WA launch
+  int wa_bucket_start[kWaBuckets + 1] = {0};    // first net of each bucket
+  int wa_block_start[kWaBuckets + 1] = {0};     // first block of each bucket in the WA launch
   float2* pin_grad = nullptr;      // WA gradient per device pin
   // bin grid
   int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
@@ -126,7 +130,6 @@ struct DeviceModel {
 };
 
 constexpr int kFftMax = 4096;
-constexpr int kWaBuckets = 6;
 
 enum PartSlot {
   kPartOverflow = 0, kPartWl, kPartD, kPartCoordDist, kPartGradDist, kPartNan,

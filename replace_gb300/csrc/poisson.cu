@@ -142,8 +142,8 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
   unsigned long long* area_clear = nullptr;
   if (A.ctl) {
     const int cur = A.ctl->area_cur;
-    area = A.area_pair[cur];
-    area_clear = A.area_pair[cur ^ 1];
+    area = cur == 0 ? A.area_pair[0] : A.area_pair[1];
+    area_clear = cur == 0 ? A.area_pair[1] : A.area_pair[0];
   }
   for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
     const int rp = idx / n, i = idx - rp * n;

@@ -5,16 +5,20 @@
 //
 // Nets are bucketed once per job by degree d into group widths G = 2, 4, 8,
 // 16, 32 (the smallest G >= d); a net is handled by G consecutive lanes of a
-// warp, one pin per lane.  On the device, nets are numbered in bucket order
+// warp, one pin per lane.  Nets of up to 64 and 128 pins take a warp with two
+// and four pins per lane, still in registers.  On the device, nets are numbered in bucket order
 // (within a bucket by their lowest gcell index, so that consecutive warps
 // touch nearby cells) and pins are renumbered so that each net's pins are
 // contiguous in that order: pin records are read and pin gradients written
 // with coalesced accesses.  The lane keeps its pin's position and four
 // exponentials in registers: bounding box and the eight WA sums are group
 // reductions (xor shuffles inside the aligned G-lane group), and the pin
-// gradient follows without re-reading anything.  Nets of more than 32 pins
-// take a warp each and loop over their pins.  One launch covers all buckets
-// (the block index selects the bucket), so warps never mix net sizes.
+// gradient follows without re-reading anything.  For groups of 8 lanes or
+// more the eight sums are reduced by halving exchanges (each step sends half
+// of the values still held, so 8 values take 4 + 2 + 1 + ... shuffles instead
+// of 8 per step) and then broadcast.  Nets of more than 128 pins take a warp
+// each and loop over their pins.  One launch covers all buckets (the block
+// index selects the bucket), so warps never mix net sizes.
 #include <climits>
 
 #include <cuda_runtime.h>
@@ -34,20 +38,25 @@ struct WaArgs {
   const int4* pins;             // (gcell or -1, x offset or position, y ..., unused)
   float2* slp_all[4];
   const EvalCtl* ctl;
-  const float2* slp;            // this evaluation's coordinates (set from ctl)
-  float cx, cy;                 // wire-length coefficients (1/gamma, from ctl)
   float bar;                    // minWireLengthForceBar
   float2* pin_grad;             // device pin order
   long long* part_i;            // HPWL partial per block
   long long* hpwl_total;        // accumulated by every block
 };
 
+// This evaluation's coordinates and wire-length coefficients (1/gamma), read
+// from the control record; kept apart from the (constant) kernel parameters.
+struct WaEval {
+  const float2* slp;
+  float cx, cy;
+};
+
 // Pin centre: gcell pins follow the truncated density centre
 // (GPin::updateDensityLocation, src/nesterovBase.cpp:411-415); other pins
 // keep their fixed position.
-__device__ __forceinline__ int2 pin_pos(const WaArgs& A, const int4& r) {
+__device__ __forceinline__ int2 pin_pos(const WaEval& V, const int4& r) {
   if (r.x < 0) return make_int2(r.y, r.z);
-  const float2 c = __ldg(&A.slp[r.x]);
+  const float2 c = __ldg(&V.slp[r.x]);
   return make_int2(__float2int_rz(c.x) + r.y, __float2int_rz(c.y) + r.z);
 }
 
@@ -93,9 +102,54 @@ __device__ __forceinline__ void sums_of(int2 p, const PinExp& E, float* S) {
   S[6] = E.e[3]; S[7] = __fmul_rn((float)p.y, E.e[3]);
 }
 
+// Sums of S[0..7] over each aligned G-lane group (G = 8, 16 or 32), returned
+// to every lane of the group.  Halving exchanges: at offset G/2 a lane keeps
+// the half of its values selected by its own offset bit and sends the other
+// half, so after three steps each lane holds one partial sum (index given by
+// three bits of its lane number); the remaining offsets finish that sum, and
+// eight shuffles broadcast the totals.  The order is fixed, so the result is
+// the same run to run.
+template <int G>
+__device__ __forceinline__ void group_sum8(float (&S)[8]) {
+  static_assert(G == 8 || G == 16 || G == 32, "group width");
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  constexpr int o1 = G / 2, o2 = G / 4, o3 = G / 8;
+  float T[4], U[2], V;
+  {
+    const bool hi = lane & o1;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float keep = hi ? S[4 + j] : S[j], send = hi ? S[j] : S[4 + j];
+      T[j] = keep + __shfl_xor_sync(full, send, o1);
+    }
+  }
+  {
+    const bool hi = lane & o2;
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+      const float keep = hi ? T[2 + j] : T[j], send = hi ? T[j] : T[2 + j];
+      U[j] = keep + __shfl_xor_sync(full, send, o2);
+    }
+  }
+  {
+    const bool hi = lane & o3;
+    const float keep = hi ? U[1] : U[0], send = hi ? U[0] : U[1];
+    V = keep + __shfl_xor_sync(full, send, o3);
+  }
+#pragma unroll
+  for (int o = o3 / 2; o > 0; o >>= 1) V += __shfl_xor_sync(full, V, o);
+  // value index k is held by the lanes whose offset bits o1, o2, o3 spell k
+  const int base = lane & ~(G - 1);
+#pragma unroll
+  for (int k = 0; k < 8; k++)
+    S[k] = __shfl_sync(full, V, base + ((k & 4) ? o1 : 0) + ((k & 2) ? o2 : 0) + ((k & 1) ? o3 : 0));
+}
+
 // One net per G-lane group, one pin per lane.
 template <int G>
-__device__ __forceinline__ long long wa_group(const WaArgs& A, int bucket, int local_block) {
+__device__ __forceinline__ long long wa_group(const WaArgs& A, const WaEval& V, int bucket,
+                                              int local_block) {
   const int per_block = kBlock / G;
   const int grp = threadIdx.x / G, li = threadIdx.x % G;
   const int k = A.bucket_start[bucket] + local_block * per_block + grp;
@@ -109,20 +163,27 @@ __device__ __forceinline__ long long wa_group(const WaArgs& A, int bucket, int l
   const bool valid = net_ok && q < e;
   int4 r = make_int4(-1, 0, 0, -1);
   if (valid) r = __ldg(&A.pins[q]);
-  const int2 p = valid ? pin_pos(A, r) : make_int2(0, 0);
+  const int2 p = valid ? pin_pos(V, r) : make_int2(0, 0);
   int lx = valid ? p.x : INT_MAX, ux = valid ? p.x : INT_MIN;
   int ly = valid ? p.y : INT_MAX, uy = valid ? p.y : INT_MIN;
+  if constexpr (G == 32) {
+    lx = __reduce_min_sync(0xffffffffu, lx);
+    ux = __reduce_max_sync(0xffffffffu, ux);
+    ly = __reduce_min_sync(0xffffffffu, ly);
+    uy = __reduce_max_sync(0xffffffffu, uy);
+  } else {
 #pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    lx = min(lx, __shfl_xor_sync(0xffffffffu, lx, o));
-    ux = max(ux, __shfl_xor_sync(0xffffffffu, ux, o));
-    ly = min(ly, __shfl_xor_sync(0xffffffffu, ly, o));
-    uy = max(uy, __shfl_xor_sync(0xffffffffu, uy, o));
+    for (int o = G / 2; o > 0; o >>= 1) {
+      lx = min(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+      ux = max(ux, __shfl_xor_sync(0xffffffffu, ux, o));
+      ly = min(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+      uy = max(uy, __shfl_xor_sync(0xffffffffu, uy, o));
+    }
   }
   PinExp E;
   float S[8];
   if (valid) {
-    E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
+    E = pin_exps(p, lx, ux, ly, uy, V.cx, V.cy, A.bar);
     sums_of(p, E, S);
   } else {
     E.flags = 0;
@@ -131,23 +192,70 @@ __device__ __forceinline__ long long wa_group(const WaArgs& A, int bucket, int l
 #pragma unroll
     for (int t = 0; t < 8; t++) S[t] = 0.0f;
   }
+  if constexpr (G >= 8) {
+    group_sum8<G>(S);
+  } else {
 #pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1)
+    for (int o = G / 2; o > 0; o >>= 1)
 #pragma unroll
-    for (int t = 0; t < 8; t++) S[t] += __shfl_xor_sync(0xffffffffu, S[t], o);
-  if (valid) A.pin_grad[q] = pin_gradient(p, E, S, A.cx, A.cy);
+      for (int t = 0; t < 8; t++) S[t] += __shfl_xor_sync(0xffffffffu, S[t], o);
+  }
+  if (valid) A.pin_grad[q] = pin_gradient(p, E, S, V.cx, V.cy);
   return (net_ok && li == 0) ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
-// One warp per net of more than 32 pins; lanes stride over the pins.
-__device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int local_block) {
+// One warp per net of up to 32 P pins, P pins per lane kept in registers.
+template <int P>
+__device__ __forceinline__ long long wa_warp(const WaArgs& A, const WaEval& V, int bucket,
+                                             int local_block) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int k = A.bucket_start[bucket] + local_block * (kBlock / 32) + (threadIdx.x >> 5);
+  if (k >= A.bucket_start[bucket + 1]) return 0ll;           // warp-uniform
+  const int s = __ldg(&A.net_start[k]), e = __ldg(&A.net_start[k + 1]);
+  int2 p[P];
+  bool ok[P];
+  int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
+#pragma unroll
+  for (int j = 0; j < P; j++) {
+    const int q = s + lane + 32 * j;
+    ok[j] = q < e;
+    p[j] = ok[j] ? pin_pos(V, __ldg(&A.pins[q])) : make_int2(0, 0);
+    if (ok[j]) { lx = min(lx, p[j].x); ux = max(ux, p[j].x); ly = min(ly, p[j].y); uy = max(uy, p[j].y); }
+  }
+  lx = __reduce_min_sync(full, lx);
+  ly = __reduce_min_sync(full, ly);
+  ux = __reduce_max_sync(full, ux);
+  uy = __reduce_max_sync(full, uy);
+  PinExp E[P];
+  float S[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < P; j++) {
+    if (ok[j]) {
+      E[j] = pin_exps(p[j], lx, ux, ly, uy, V.cx, V.cy, A.bar);
+      float t[8];
+      sums_of(p[j], E[j], t);
+#pragma unroll
+      for (int i = 0; i < 8; i++) S[i] = __fadd_rn(S[i], t[i]);
+    }
+  }
+  group_sum8<32>(S);
+#pragma unroll
+  for (int j = 0; j < P; j++)
+    if (ok[j]) A.pin_grad[s + lane + 32 * j] = pin_gradient(p[j], E[j], S, V.cx, V.cy);
+  return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
+}
+
+// One warp per net of more than 128 pins; lanes stride over the pins.
+__device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval& V, int bucket,
+                                             int local_block) {
   const int lane = threadIdx.x & 31;
   const int k = A.bucket_start[bucket] + local_block * (kBlock / 32) + (threadIdx.x >> 5);
   if (k >= A.bucket_start[bucket + 1]) return 0ll;           // warp-uniform
   const int s = __ldg(&A.net_start[k]), e = __ldg(&A.net_start[k + 1]);
   int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
   for (int q = s + lane; q < e; q += 32) {
-    const int2 p = pin_pos(A, __ldg(&A.pins[q]));
+    const int2 p = pin_pos(V, __ldg(&A.pins[q]));
     lx = min(lx, p.x); ux = max(ux, p.x); ly = min(ly, p.y); uy = max(uy, p.y);
   }
   lx = __reduce_min_sync(0xffffffffu, lx);
@@ -156,8 +264,8 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int lo
   uy = __reduce_max_sync(0xffffffffu, uy);
   float S[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   for (int q = s + lane; q < e; q += 32) {
-    const int2 p = pin_pos(A, __ldg(&A.pins[q]));
-    const PinExp E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
+    const int2 p = pin_pos(V, __ldg(&A.pins[q]));
+    const PinExp E = pin_exps(p, lx, ux, ly, uy, V.cx, V.cy, A.bar);
     float t[8];
     sums_of(p, E, t);
 #pragma unroll
@@ -168,32 +276,36 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, int bucket, int lo
     for (int o = 16; o > 0; o >>= 1) S[j] += __shfl_xor_sync(0xffffffffu, S[j], o);
   for (int q = s + lane; q < e; q += 32) {
     const int4 r = __ldg(&A.pins[q]);
-    const int2 p = pin_pos(A, r);
-    const PinExp E = pin_exps(p, lx, ux, ly, uy, A.cx, A.cy, A.bar);
-    A.pin_grad[q] = pin_gradient(p, E, S, A.cx, A.cy);
+    const int2 p = pin_pos(V, r);
+    const PinExp E = pin_exps(p, lx, ux, ly, uy, V.cx, V.cy, A.bar);
+    A.pin_grad[q] = pin_gradient(p, E, S, V.cx, V.cy);
   }
   return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
-__global__ void __launch_bounds__(kBlock) k_wa(WaArgs A) {
+__global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A) {
   __shared__ long long sh[32];
+  WaEval V;
   {
-    const EvalCtl C = *A.ctl;
-    A.slp = A.slp_all[C.i_eval];
-    A.cx = C.wl_coef_x;
-    A.cy = C.wl_coef_y;
+    const EvalCtl* C = A.ctl;
+    const int i = C->i_eval;
+    V.slp = i == 0 ? A.slp_all[0] : i == 1 ? A.slp_all[1] : i == 2 ? A.slp_all[2] : A.slp_all[3];
+    V.cx = C->wl_coef_x;
+    V.cy = C->wl_coef_y;
   }
   int bucket = 0;
   while (bucket < kWaBuckets - 1 && (int)blockIdx.x >= A.block_start[bucket + 1]) bucket++;
   const int lb = blockIdx.x - A.block_start[bucket];
   long long hp = 0;
   switch (bucket) {
-    case 0: hp = wa_group<2>(A, 0, lb); break;
-    case 1: hp = wa_group<4>(A, 1, lb); break;
-    case 2: hp = wa_group<8>(A, 2, lb); break;
-    case 3: hp = wa_group<16>(A, 3, lb); break;
-    case 4: hp = wa_group<32>(A, 4, lb); break;
-    default: hp = wa_huge(A, 5, lb); break;
+    case 0: hp = wa_group<2>(A, V, 0, lb); break;
+    case 1: hp = wa_group<4>(A, V, 1, lb); break;
+    case 2: hp = wa_group<8>(A, V, 2, lb); break;
+    case 3: hp = wa_group<16>(A, V, 3, lb); break;
+    case 4: hp = wa_group<32>(A, V, 4, lb); break;
+    case 5: hp = wa_warp<2>(A, V, 5, lb); break;
+    case 6: hp = wa_warp<4>(A, V, 6, lb); break;
+    default: hp = wa_huge(A, V, 7, lb); break;
   }
   // HPWL is an integer sum: one 64-bit atomic per block gives the exact,
   // order-independent total (the gcell kernel reads and clears it)
@@ -204,7 +316,8 @@ __global__ void __launch_bounds__(kBlock) k_wa(WaArgs A) {
 
 }  // namespace
 
-int wa_nets_per_block(int bucket) { return bucket < kWaBuckets - 1 ? kBlock / (2 << bucket) : kBlock / 32; }
+// buckets 0-4: lane groups of 2 << bucket; 5-7: a warp per net
+int wa_nets_per_block(int bucket) { return bucket < 5 ? kBlock / (2 << bucket) : kBlock / 32; }
 
 int net_blocks(const DeviceModel& d) { return d.wa_block_start[kWaBuckets]; }
 
@@ -218,8 +331,6 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.pins = d.pins;
   for (int k = 0; k < 4; k++) A.slp_all[k] = d.slp[k];
   A.ctl = d.ctl;
-  A.slp = nullptr;
-  A.cx = A.cy = 0.0f;
   A.bar = a.min_wl_force_bar;
   A.pin_grad = d.pin_grad;
   A.part_i = d.part_i;
