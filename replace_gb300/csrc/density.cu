@@ -75,6 +75,24 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
   const int maxc = __reduce_max_sync(0xffffffffu, cnt);
   const int base = (k & 3) == 2 ? nb : 0;
   int a = x0, cc = y0;                 // current bin, walked without division
+  // Lanes whose cells start in the same bin as the previous lane's: many of
+  // them (cells piled up, as at the start of the placement) and the warp
+  // combines equal bins before its atomics; otherwise each lane adds its
+  // own values with no exchange between lanes.
+  const int key0 = cnt ? base + y0 * G.cnt_x + x0 : -1 - lane;
+  const int key0_up = __shfl_up_sync(0xffffffffu, key0, 1);   // every lane takes part
+  const unsigned same = __ballot_sync(0xffffffffu, lane > 0 && key0 == key0_up);
+  if (__popc(same) < 8) {
+    for (int t = 0; t < cnt; t++) {
+      const float ov = G.overlap(a, cc, lx, ux, ly, uy);
+      float f = __fmul_rn(ov, sc);
+      if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
+      const long long v = (long long)f;
+      if (v) atomicAdd(&area[base + cc * G.cnt_x + a], (unsigned long long)v);
+      if (++a == x1) { a = x0; cc++; }
+    }
+    return;
+  }
   for (int t = 0; t < maxc; t++) {
     int key = -1;
     long long v = 0;
@@ -85,14 +103,6 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
       v = (long long)f;
       key = base + cc * G.cnt_x + a;
       if (++a == x1) { a = x0; cc++; }
-    }
-    // Combine lanes that hit the same bin only when the warp has such lanes
-    // (a cheap neighbour test first); otherwise one atomic per lane.
-    const int up = __shfl_up_sync(0xffffffffu, key, 1);
-    const unsigned dup = __ballot_sync(0xffffffffu, key >= 0 && lane > 0 && key == up);
-    if (!dup) {
-      if (v) atomicAdd(&area[key], (unsigned long long)v);
-      continue;
     }
     const unsigned peers = __match_any_sync(0xffffffffu, key);
     vals[threadIdx.x] = v;
@@ -228,7 +238,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
       if (pe - ps <= 32) {
         // WA gradient: the cell's pins in instance pin order
         for (int t = ps; t < pe; t++) {
-          const float2 pg = A.pin_grad[__ldg(&A.g_pins[t])];
+          const float2 pg = A.pin_grad[A.g_pins[t]];
           w.x = __fadd_rn(w.x, pg.x);
           w.y = __fadd_rn(w.y, pg.y);
         }
@@ -241,7 +251,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
       const int s0 = __shfl_sync(0xffffffffu, ps, src), s1 = __shfl_sync(0xffffffffu, pe, src);
       float2 part = make_float2(0.0f, 0.0f);
       for (int t = s0 + lane; t < s1; t += 32) {
-        const float2 pg = A.pin_grad[__ldg(&A.g_pins[t])];
+        const float2 pg = A.pin_grad[A.g_pins[t]];
         part.x = __fadd_rn(part.x, pg.x);
         part.y = __fadd_rn(part.y, pg.y);
       }
@@ -267,7 +277,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
       for (int a = x0; a < x1; a++) {
         for (int cc = y0; cc < y1; cc++) {
           const float ov = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
-          const float2 f = __ldg(&A.field[cc * G.cnt_x + a]);
+          const float2 f = A.field[cc * G.cnt_x + a];
           d.x = __fadd_rn(d.x, __fmul_rn(ov, f.x));
           d.y = __fadd_rn(d.y, __fmul_rn(ov, f.y));
         }
