@@ -51,68 +51,161 @@ __device__ __forceinline__ float2 predict_one(const ScatterArgs& A, const EvalCt
   return s;
 }
 
-__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A) {
-  __shared__ long long vals[kBlock];
-  const EvalCtl C = *A.ctl;
-  unsigned long long* area = pick2(A.area, C.area_cur);
+// ------------------------------------------------------------ tile order
+// The scatter visits gcells tile by tile: a tile is tile_w x tile_h bins, and
+// the gcells whose centres lie in it (at the last ordering) are consecutive
+// in `order`.  A block takes a chunk of at most kScatterChunk gcells of one
+// tile and accumulates their bin areas in a shared-memory window over the
+// tile and a margin; the window's non-zero bins then go to the global areas
+// with one 64-bit atomic each.  Bins outside the window (cells that moved
+// away, large cells) go to the global areas directly.  The int64 sums do not
+// depend on the order, so the ordering only changes the number of global
+// atomics, never a result.
+
+constexpr int kTileMargin = 2;
+
+struct OrderArgs {
+  BinGeom geo;
+  int n_g, tile_w, tile_h, tiles_x, tiles_y;
+  const float2* slp;
+  int32_t* tile_count;
+  int32_t* tile_start;
+  int32_t* order;
+  int4* chunks;
+  int32_t* n_chunks;
+};
+
+__device__ __forceinline__ int tile_of(const OrderArgs& O, float2 c) {
+  const BinGeom& G = O.geo;
+  const int bx = min(max((__float2int_rz(c.x) - G.core_lx) / G.size_x, 0), G.cnt_x - 1);
+  const int by = min(max((__float2int_rz(c.y) - G.core_ly) / G.size_y, 0), G.cnt_y - 1);
+  return (by / O.tile_h) * O.tiles_x + bx / O.tile_w;
+}
+
+// Lanes of a warp on the same tile add their count with one atomic.
+__global__ void __launch_bounds__(kBlock) k_order_count(OrderArgs O) {
+  const int g = blockIdx.x * kBlock + threadIdx.x;
+  const int t = g < O.n_g ? tile_of(O, O.slp[g]) : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, t);    // every lane takes part
+  if (t >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&O.tile_count[t], __popc(peers));
+}
+
+// One block: exclusive scan of the tile counts into tile_start, fill cursors
+// (tile_count := tile_start), and the chunk table (tiles cut into chunks of
+// at most kScatterChunk gcells).
+constexpr int kOrderScanT = 1024;
+__global__ void __launch_bounds__(kOrderScanT) k_order_scan(OrderArgs O) {
+  __shared__ int32_t sc[kOrderScanT], sk[kOrderScanT];
+  const int nt = O.tiles_x * O.tiles_y;
+  const int per = (nt + kOrderScanT - 1) / kOrderScanT;
+  const int lo = min((int)threadIdx.x * per, nt), hi = min(lo + per, nt);
+  int cells = 0, chunks = 0;
+  for (int t = lo; t < hi; t++) {
+    const int c = O.tile_count[t];
+    cells += c;
+    chunks += (c + kScatterChunk - 1) / kScatterChunk;
+  }
+  sc[threadIdx.x] = cells;
+  sk[threadIdx.x] = chunks;
+  __syncthreads();
+  for (int o = 1; o < kOrderScanT; o <<= 1) {
+    const int x = threadIdx.x >= o ? sc[threadIdx.x - o] : 0;
+    const int y = threadIdx.x >= o ? sk[threadIdx.x - o] : 0;
+    __syncthreads();
+    sc[threadIdx.x] += x;
+    sk[threadIdx.x] += y;
+    __syncthreads();
+  }
+  int at = sc[threadIdx.x] - cells, ck = sk[threadIdx.x] - chunks;
+  for (int t = lo; t < hi; t++) {
+    const int c = O.tile_count[t];
+    O.tile_start[t] = at;
+    O.tile_count[t] = at;
+    for (int f = 0; f < c; f += kScatterChunk) O.chunks[ck++] = make_int4(t, at + f, at + min(f + kScatterChunk, c), 0);
+    at += c;
+  }
+  if (threadIdx.x == kOrderScanT - 1) {
+    O.tile_start[nt] = sc[kOrderScanT - 1];
+    *O.n_chunks = sk[kOrderScanT - 1];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_order_fill(OrderArgs O) {
   const int g = blockIdx.x * kBlock + threadIdx.x;
   const int lane = threadIdx.x & 31;
+  const int t = g < O.n_g ? tile_of(O, O.slp[g]) : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, t);    // every lane takes part
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (t >= 0 && lane == leader) base = atomicAdd(&O.tile_count[t], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);               // every lane takes part
+  if (t >= 0) O.order[base + __popc(peers & ((1u << lane) - 1u))] = g;
+}
+
+struct TileArgs {
+  int tile_w, tile_h, tiles_x;
+  const int32_t* order;
+  const int4* chunks;
+  const int32_t* n_chunks;
+};
+
+// updateGCellDensityCenterLocation + updateBinsGCellDensityArea
+// (src/nesterovBase.cpp:746-819, 1198-1207): one chunk of one tile per block.
+// Per (gcell, bin) the area is (int64)(float overlap * scale [* td for a
+// macro]), added into the inst or filler set.  The predictor runs here for
+// every gcell (big ones included; their bins are left to k_scatter_big).
+__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A, TileArgs T) {
+  extern __shared__ unsigned win[];                // [2][wy][wx] low words, then [2][wy][wx] high words
+  if ((int)blockIdx.x >= *T.n_chunks) return;      // block-uniform
+  const EvalCtl C = *A.ctl;
+  unsigned long long* area = pick2(A.area, C.area_cur);
   const BinGeom& G = A.geo;
   const int nb = G.cnt_x * G.cnt_y;
-  int x0 = 0, x1 = 0, y0 = 0, y1 = 0, lx = 0, ux = 0, ly = 0, uy = 0;
-  int cnt = 0, k = 0;
-  float sc = 0.0f;
-  if (g < A.n_g) {
+  const int4 ch = T.chunks[blockIdx.x];
+  const int ox = (ch.x % T.tiles_x) * T.tile_w - kTileMargin;
+  const int oy = (ch.x / T.tiles_x) * T.tile_h - kTileMargin;
+  const int wx = T.tile_w + 2 * kTileMargin, wy = T.tile_h + 2 * kTileMargin, wn = wx * wy;
+  unsigned* win_hi = win + 2 * wn;
+  for (int i = threadIdx.x; i < 4 * wn; i += blockDim.x) win[i] = 0u;
+  __syncthreads();
+  for (int idx = ch.y + threadIdx.x; idx < ch.z; idx += blockDim.x) {
+    const int g = T.order[idx];
     const int2 h = A.half[g];
     const float2 c = C.predict ? predict_one(A, C, g, h) : pick4(A.slp, C.i_eval)[g];
-    k = A.kind[g];
+    const int k = A.kind[g];
+    if (k & 4) continue;                           // big cell: k_scatter_big
+    int lx, ux, ly, uy, x0, x1, y0, y1;
     density_rect(c, h, lx, ux, ly, uy);
     G.range(lx, ux, ly, uy, x0, x1, y0, y1);
-    cnt = (x1 > x0 && y1 > y0) ? (x1 - x0) * (y1 - y0) : 0;
-    if (k & 4) cnt = 0;            // big cell: handled by k_scatter_big
-    sc = A.scale[g];
+    const float sc = A.scale[g];
+    const int half = (k & 3) == 2 ? 1 : 0;
+    for (int cc = y0; cc < y1; cc++) {
+      for (int a = x0; a < x1; a++) {
+        const float ov = G.overlap(a, cc, lx, ux, ly, uy);
+        float f = __fmul_rn(ov, sc);
+        if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
+        const unsigned long long v = (unsigned long long)(long long)f;
+        if (!v) continue;
+        const int u = a - ox, w = cc - oy;
+        if (u >= 0 && u < wx && w >= 0 && w < wy && v < (1ull << 32)) {
+          // 64-bit sum as two 32-bit words: the low word's wrap-around
+          // (old + v < old) carries into the high word; exact in any order
+          const int i = half * wn + w * wx + u;
+          const unsigned lo = (unsigned)v;
+          if (atomicAdd(&win[i], lo) + lo < lo) atomicAdd(&win_hi[i], 1u);
+        } else {
+          atomicAdd(&area[half * nb + cc * G.cnt_x + a], v);
+        }
+      }
+    }
   }
-  const int maxc = __reduce_max_sync(0xffffffffu, cnt);
-  const int base = (k & 3) == 2 ? nb : 0;
-  int a = x0, cc = y0;                 // current bin, walked without division
-  // Lanes whose cells start in the same bin as the previous lane's: many of
-  // them (cells piled up, as at the start of the placement) and the warp
-  // combines equal bins before its atomics; otherwise each lane adds its
-  // own values with no exchange between lanes.
-  const int key0 = cnt ? base + y0 * G.cnt_x + x0 : -1 - lane;
-  const int key0_up = __shfl_up_sync(0xffffffffu, key0, 1);   // every lane takes part
-  const unsigned same = __ballot_sync(0xffffffffu, lane > 0 && key0 == key0_up);
-  if (__popc(same) < 8) {
-    for (int t = 0; t < cnt; t++) {
-      const float ov = G.overlap(a, cc, lx, ux, ly, uy);
-      float f = __fmul_rn(ov, sc);
-      if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
-      const long long v = (long long)f;
-      if (v) atomicAdd(&area[base + cc * G.cnt_x + a], (unsigned long long)v);
-      if (++a == x1) { a = x0; cc++; }
-    }
-    return;
-  }
-  for (int t = 0; t < maxc; t++) {
-    int key = -1;
-    long long v = 0;
-    if (t < cnt) {
-      const float ov = G.overlap(a, cc, lx, ux, ly, uy);
-      float f = __fmul_rn(ov, sc);
-      if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
-      v = (long long)f;
-      key = base + cc * G.cnt_x + a;
-      if (++a == x1) { a = x0; cc++; }
-    }
-    const unsigned peers = __match_any_sync(0xffffffffu, key);
-    vals[threadIdx.x] = v;
-    __syncwarp();
-    if (key >= 0 && lane == __ffs(peers) - 1) {
-      long long s = 0;
-      for (unsigned m = peers; m; m &= m - 1) s += vals[(threadIdx.x & ~31) + __ffs(m) - 1];
-      if (s) atomicAdd(&area[key], (unsigned long long)s);
-    }
-    __syncwarp();
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * wn; i += blockDim.x) {
+    const unsigned long long v = ((unsigned long long)win_hi[i] << 32) | win[i];
+    if (!v) continue;
+    const int half = i >= wn ? 1 : 0, r = i - half * wn;
+    const int a = ox + r % wx, cc = oy + r / wx;      // inside the grid: only in-grid bins were added
+    atomicAdd(&area[half * nb + cc * G.cnt_x + a], v);
   }
 }
 
@@ -384,11 +477,45 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   A.area[0] = d.area[0]; A.area[1] = d.area[1];
   A.ctl = d.ctl;
   (void)a;
+  TileArgs T;
+  T.tile_w = d.tile_w; T.tile_h = d.tile_h; T.tiles_x = d.tiles_x;
+  T.order = d.order; T.chunks = d.chunks; T.n_chunks = d.n_chunks;
+  const size_t smem = (size_t)4 * (d.tile_w + 2 * kTileMargin) * (d.tile_h + 2 * kTileMargin) * 4;
   t.begin(kKScatter);
-  k_scatter<<<cell_blocks(d), kBlock, 0, s>>>(A);
+  k_scatter<<<d.max_chunks, kBlock, smem, s>>>(A, T);
   if (d.n_big) k_scatter_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
   t.end(kKScatter);
   t.count(d.n_big ? 2 : 1);
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
+void tile_grid(int cnt_x, int cnt_y, int* tw, int* th, int* tx, int* ty) {
+  *tw = std::min(32, cnt_x);
+  *th = std::min(32, cnt_y);
+  *tx = (cnt_x + *tw - 1) / *tw;
+  *ty = (cnt_y + *th - 1) / *th;
+}
+
+// every tile's chunks: one per kScatterChunk gcells, plus one per tile for
+// the partial last chunks
+int scatter_max_chunks(int n_g, int tiles) { return tiles + (n_g + kScatterChunk - 1) / kScatterChunk; }
+
+int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t) {
+  OrderArgs O;
+  O.geo = geom(d);
+  O.n_g = d.n_g;
+  O.tile_w = d.tile_w; O.tile_h = d.tile_h; O.tiles_x = d.tiles_x; O.tiles_y = d.tiles_y;
+  O.slp = d.slp[slot];
+  O.tile_count = d.tile_count; O.tile_start = d.tile_start; O.order = d.order;
+  O.chunks = d.chunks; O.n_chunks = d.n_chunks;
+  t.begin(kKOther);
+  GPL_CUDA(cudaMemsetAsync(d.tile_count, 0, sizeof(int32_t) * d.tiles_x * d.tiles_y, s));
+  k_order_count<<<cell_blocks(d), kBlock, 0, s>>>(O);
+  k_order_scan<<<1, kOrderScanT, 0, s>>>(O);
+  k_order_fill<<<cell_blocks(d), kBlock, 0, s>>>(O);
+  t.end(kKOther);
+  t.count(3);
   GPL_CUDA(cudaGetLastError());
   return GPL_OK;
 }

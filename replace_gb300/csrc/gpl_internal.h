@@ -124,6 +124,14 @@ struct DeviceModel {
   double* part_total = nullptr;    // [kPartSlots] final sums
   unsigned* counters = nullptr;    // [2] last-block counters (gcell kernel, WA kernel)
   int sm_count = 0;
+  // gcells ordered by bin tile for the scatter (refreshed every few
+  // evaluations; any order gives the same int64 areas)
+  int tile_w = 32, tile_h = 32, tiles_x = 1, tiles_y = 1, max_chunks = 1;
+  int32_t* order = nullptr;        // [n_g] gcell indices, tile by tile
+  int32_t* tile_count = nullptr;   // [tiles] counts, then fill cursors
+  int32_t* tile_start = nullptr;   // [tiles + 1]
+  int4* chunks = nullptr;          // [max_chunks] (tile, first, end, 0) of <= kScatterChunk gcells
+  int32_t* n_chunks = nullptr;     // [1]
   struct EvalResult* result = nullptr;     // device
   struct EvalResult* result_h = nullptr;   // pinned host mirror
   int64_t bytes = 0;
@@ -245,6 +253,13 @@ int poisson_blocks_a(int nx, int ny);
 void make_w4(int n, std::vector<float2>& w);
 
 int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
+// Orders the gcells by the bin tile of their centres in slp[slot] (counting
+// sort) and builds the scatter's chunk table.
+int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t);
+// Tile grid of a bin grid, and the chunk-table bound, for sizing.
+constexpr int kScatterChunk = 2048;
+void tile_grid(int cnt_x, int cnt_y, int* tw, int* th, int* tx, int* ty);
+int scatter_max_chunks(int n_g, int tiles);
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t);
 // the Poisson passes of a job evaluation (area set chosen by EvalCtl)

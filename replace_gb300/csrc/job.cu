@@ -145,7 +145,12 @@ struct Carver {
 size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size_t n_big, size_t nb,
                    int cnt_x, int cnt_y, size_t part_stride, size_t nnb) {
   const size_t ps = (size_t)kPartSlots * part_stride;
+  int tw, th, tx, ty;
+  tile_grid(cnt_x, cnt_y, &tw, &th, &tx, &ty);
+  const size_t tiles = (size_t)tx * ty;
   Sizer S;
+  S.add(ng, 4); S.add(tiles, 4); S.add(tiles + 1, 4);
+  S.add(scatter_max_chunks((int)ng, (int)tiles), 16); S.add(1, 4);
   S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
   S.add(n_big, 4); S.add(ng, 4); S.add(n_big, 8);
   S.add(n_pins, 16); S.add(n_nets + 1, 4);
@@ -262,6 +267,13 @@ int ensure_nb(gpl_job* j) {
   }
   d.bytes = (int64_t)bytes;
   Carver C{j->arena};
+  tile_grid(m.cnt_x, m.cnt_y, &d.tile_w, &d.tile_h, &d.tiles_x, &d.tiles_y);
+  d.max_chunks = scatter_max_chunks((int)ng, d.tiles_x * d.tiles_y);
+  d.order = C.take<int32_t>(ng);
+  d.tile_count = C.take<int32_t>((size_t)d.tiles_x * d.tiles_y);
+  d.tile_start = C.take<int32_t>((size_t)d.tiles_x * d.tiles_y + 1);
+  d.chunks = C.take<int4>(d.max_chunks);
+  d.n_chunks = C.take<int32_t>(1);
   d.g_half = C.take<int2>(ng); d.g_scale = C.take<float>(ng); d.g_kind = C.take<uint8_t>(ng);
   d.g_precond = C.take<float2>(ng); d.g_pin_start = C.take<int32_t>(ng + 1);
   d.big_cells = C.take<int32_t>(big.size());
@@ -318,6 +330,9 @@ int ensure_nb(gpl_job* j) {
   j->nb_ready = true;
   return GPL_OK;
 }
+
+// Iterations between refreshes of the scatter's tile order.
+constexpr int kTileOrderEvery = 8;
 
 EvalArgs base_args(gpl_job* j) {
   EvalArgs a;
@@ -498,6 +513,8 @@ int nesterov_init(gpl_job* j) {
   j->max_phi_coef = m.p.max_phi_coef;
   j->wl_coef_x = j->wl_coef_y = 0.0f;
   // first evaluation at the initial centres: overflow and HPWL
+  rc = launch_tile_order(d, j->i_cur, j->stream, j->timer);
+  if (rc) return rc;
   rc = evaluate(j, ctl_of(j, j->i_cur, -1, false), false);
   if (rc) return rc;
   j->prev_hpwl = j->last.hpwl;
@@ -549,6 +566,11 @@ int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
     j->cur_a = (float)((1.0 + sqrt(4.0 * prev_a * prev_a + 1.0)) * 0.5);
     const float coeff = (float)((prev_a - 1.0) / j->cur_a);
     int bt = 0;
+    // refresh the scatter's tile order now and then (cells move slowly)
+    if (j->iter % kTileOrderEvery == 0) {
+      int rc = launch_tile_order(j->d, j->i_cur, j->stream, j->timer);
+      if (rc) return rc;
+    }
     for (bt = 0; bt < p.max_back_track; bt++) {
       EvalCtl c = ctl_of(j, j->i_next, j->i_cur, true);
       c.predict = 1;
@@ -845,6 +867,8 @@ gpl_status gpl_eval(gpl_job* j, const float* xy, float cx, float cy, float* wl_g
   c.i_src = 3; c.i_eval = 3; c.i_ref = -1;
   c.c_cur = 0; c.c_next = 1;
   c.write_sum = 1; c.write_wd = 1;
+  rc = launch_tile_order(d, 3, j->stream, j->timer);
+  if (rc) return (gpl_status)rc;
   rc = evaluate(j, c, true);
   if (rc) return (gpl_status)rc;
   if (wl_grad) GPL_CUDA(cudaMemcpyAsync(wl_grad, d.wl_out, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
