@@ -145,38 +145,54 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
     area = cur == 0 ? A.area_pair[0] : A.area_pair[1];
     area_clear = cur == 0 ? A.area_pair[1] : A.area_pair[0];
   }
-  for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
-    const int rp = idx / n, i = idx - rp * n;
-    const int r = blockIdx.x * rp_n + rp;
-    float d0 = 0.0f, d1 = 0.0f;
-    if (r < A.ny / 2) {
-      float dd[2];
-      for (int h = 0; h < 2; h++) {
-        const int j = 2 * r + h;
-        const int b = j * n + i;
-        if (A.density_in) {
-          dd[h] = A.density_in[b];
-        } else {
-          const int blx = A.core_lx + i * A.size_x;
-          const int bux = min(blx + A.size_x, A.core_ux);
+  if (A.density_in) {
+    for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
+      const int rp = idx / n, i = idx - rp * n;
+      const int r = blockIdx.x * rp_n + rp;
+      float d0 = 0.0f, d1 = 0.0f;
+      if (r < A.ny / 2) {
+        d0 = A.density_in[(2 * r) * n + i];
+        d1 = A.density_in[(2 * r + 1) * n + i];
+      }
+      buf0[rp * n + makhoul_pos(i, n)] = make_float2(d0, d1);
+    }
+  } else {
+    // restrict-qualified views: the areas read and the set cleared (and the
+    // density written) are distinct arrays, so the loads of later elements
+    // can be issued before the stores of earlier ones
+    const unsigned long long* __restrict__ ar = area;
+    unsigned long long* __restrict__ ac = area_clear;
+    const int64_t* __restrict__ np = A.nonplace;
+    float* __restrict__ dens = A.density;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
+      const int rp = idx / n, i = idx - rp * n;
+      const int r = blockIdx.x * rp_n + rp;
+      float dd[2] = {0.0f, 0.0f};
+      if (r < A.ny / 2) {
+        const int blx = A.core_lx + i * A.size_x;
+        const int bux = min(blx + A.size_x, A.core_ux);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int j = 2 * r + h;
+          const int b = j * n + i;
           const int bly = A.core_ly + j * A.size_y;
           const int buy = min(bly + A.size_y, A.core_uy);
           const long long bin_area = (long long)(bux - blx) * (long long)(buy - bly);
           const float cap = __fmul_rn(__ll2float_rn(bin_area), A.td);
-          const float fi = __ll2float_rn((long long)area[b]);
-          const float ff = __ll2float_rn((long long)area[nb + b]);
-          const float fn = __ll2float_rn(A.nonplace[b]);
+          const float fi = __ll2float_rn((long long)ar[b]);
+          const float ff = __ll2float_rn((long long)ar[nb + b]);
+          const float fn = __ll2float_rn(np[b]);
           // BinGrid::updateBinsGCellDensityArea (src/nesterovBase.cpp:804-818)
           dd[h] = __fdiv_rn(__fadd_rn(__fadd_rn(fi, ff), fn), cap);
           ovf += (double)fmaxf(0.0f, __fsub_rn(__fadd_rn(fi, fn), cap));
-          area_clear[b] = 0ull;
-          area_clear[nb + b] = 0ull;
-          A.density[b] = dd[h];
+          ac[b] = 0ull;
+          ac[nb + b] = 0ull;
+          dens[b] = dd[h];
         }
       }
-      d0 = dd[0]; d1 = dd[1];
+      buf0[rp * n + makhoul_pos(i, n)] = make_float2(dd[0], dd[1]);
     }
-    buf0[rp * n + makhoul_pos(i, n)] = make_float2(d0, d1);
   }
   __syncthreads();
   float2* res = block_fft(buf0, buf1, n, A.logn, rp_n, -1, tws);
@@ -215,6 +231,7 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
   load_twiddles(tws, B.tw, n);
   const int u_base = blockIdx.x * 2 * cp;
   // load: column pair q holds columns u_base + 2q, +1
+#pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * cp * n; idx += blockDim.x) {
     const int v = idx / (2 * cp);           // row (y) index: consecutive threads read one row
     const int c = idx - v * 2 * cp;         // column within block
@@ -345,6 +362,7 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
   float2* s1 = s0 + rp_n * n;                          // [rp][n]
   float2* tws = s1 + rp_n * n;                         // [n/2] twiddles
   load_twiddles(tws, C.tw, n);
+#pragma unroll 4
   for (int idx = threadIdx.x; idx < rp_n * 2 * n; idx += blockDim.x) {
     const int rp = idx / (2 * n), t = idx - rp * 2 * n;
     const int h = t / n, i = t - h * n;
@@ -379,9 +397,15 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
       if (tr == 0) {
         C.phi[b0] = v0; C.phi[b1] = v1;
       } else if (C.field) {
-        float* f0 = reinterpret_cast<float*>(&C.field[b0]);
-        float* f1 = reinterpret_cast<float*>(&C.field[b1]);
-        f0[tr - 1] = v0; f1[tr - 1] = v1;
+        // Ex waits in the P1 rows (no longer read) and goes out with Ey as
+        // one float2 per bin
+        float* ex = rows + (rp * 4) * n;
+        if (tr == 1) {
+          ex[m] = v0; ex[n + m] = v1;
+        } else {
+          C.field[b0] = make_float2(ex[m], v0);
+          C.field[b1] = make_float2(ex[n + m], v1);
+        }
       } else {
         float* dst = tr == 1 ? C.fx : C.fy;
         dst[b0] = v0; dst[b1] = v1;
