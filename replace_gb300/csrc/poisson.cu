@@ -37,30 +37,70 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
 
-// Radix-2 Stockham FFT over `batch` sequences of length n = 2^logn stored
-// back to back in smem buffer a; b is a same-size scratch buffer.  Returns
-// the buffer that holds the result.  sign -1: forward, +1: unnormalised
-// inverse.  tw[m] = exp(-2 pi i m / kFftMax).
+// exp(sign * 2 pi i m / n) for 0 <= m < n from the half table tw[m] =
+// exp(-2 pi i m / n), m < n/2 (the second half is the negated first half).
+__device__ __forceinline__ float2 twiddle(const float2* tw, int m, int n, int sign) {
+  const int h = n >> 1;
+  float2 w = m < h ? tw[m] : make_float2(-tw[m - h].x, -tw[m - h].y);
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+// Stockham FFT over `batch` sequences of length n = 2^logn stored back to
+// back in the shared buffer a; b is a same-size scratch buffer.  Returns the
+// buffer that holds the result.  sign -1: forward, +1: unnormalised inverse.
+// tw: the half table of this n in shared memory.  Radix-4 passes (one radix-2
+// pass first when logn is odd): half as many passes, barriers and shared
+// round trips as radix 2.  Pass with sub-transform size ns: element j of
+// quarter r is multiplied by exp(sign 2 pi i r k / 4ns), k = j mod ns, and the
+// 4-point DFT's outputs go to (j - k) * 4 + k + r ns.
 __device__ float2* block_fft(float2* a, float2* b, int n, int logn, int batch, int sign,
                              const float2* __restrict__ tw) {
-  const int half = n >> 1;
-  const int total = half * batch;
-  for (int s = 0; s < logn; s++) {
-    const int ns = 1 << s;
+  int ns = 1, lns = 0;
+  if (logn & 1) {
+    const int half = n >> 1;
+    const int total = half * batch;
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
       const int bi = idx >> (logn - 1);
       const int j = idx & (half - 1);
       const float2* in = a + bi * n;
       float2* out = b + bi * n;
+      const float2 u = in[j], v = in[j + half];
+      out[2 * j] = cadd(u, v);
+      out[2 * j + 1] = csub(u, v);
+    }
+    __syncthreads();
+    float2* t = a; a = b; b = t;
+    ns = 2;
+    lns = 1;
+  }
+  if (logn < 2) return a;
+  const int lq = logn - 2, q = 1 << lq;
+  const int total = q * batch;
+  for (; ns < n; ns <<= 2, lns += 2) {
+    const int tstep_log = logn - 2 - lns;       // n / (4 ns) = 2^tstep_log
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      const int bi = idx >> lq;
+      const int j = idx & (q - 1);
+      const float2* in = a + bi * n;
+      float2* out = b + bi * n;
       const int k = j & (ns - 1);
-      float2 u = in[j];
-      float2 v = in[j + half];
-      float2 w = tw[k << (logn - 1 - s)];
-      if (sign > 0) w.y = -w.y;
-      v = cmul(v, w);
-      const int o = ((j - k) << 1) + k;
-      out[o] = cadd(u, v);
-      out[o + ns] = csub(u, v);
+      float2 x0 = in[j], x1 = in[j + q], x2 = in[j + 2 * q], x3 = in[j + 3 * q];
+      if (ns > 1) {
+        const int m = k << tstep_log;
+        x1 = cmul(x1, twiddle(tw, m, n, sign));
+        x2 = cmul(x2, twiddle(tw, 2 * m, n, sign));
+        x3 = cmul(x3, twiddle(tw, 3 * m, n, sign));
+      }
+      // 4-point DFT with W = exp(sign 2 pi i / 4) = sign * i
+      const float2 a0 = cadd(x0, x2), a1 = csub(x0, x2);
+      const float2 b0 = cadd(x1, x3), b1 = csub(x1, x3);
+      const float2 wb1 = sign > 0 ? make_float2(-b1.y, b1.x) : make_float2(b1.y, -b1.x);
+      const int o = ((j - k) << 2) + k;
+      out[o] = cadd(a0, b0);
+      out[o + ns] = cadd(a1, wb1);
+      out[o + 2 * ns] = csub(a0, b0);
+      out[o + 3 * ns] = csub(a1, wb1);
     }
     __syncthreads();
     float2* t = a; a = b; b = t;
