@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A, TileArgs T) {
         const float ov = G.overlap(a, cc, lx, ux, ly, uy);
         float f = __fmul_rn(ov, sc);
         if ((k & 3) == 1) f = __fmul_rn(f, A.td);          // macro: scale down by target density
-        const unsigned long long v = (unsigned long long)(long long)f;
+        const unsigned long long v = trunc_u64(f);
         if (!v) continue;
         const int u = a - ox, w = cc - oy;
         if (u >= 0 && u < wx && w >= 0 && w < wy && v < (1ull << 32)) {
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int
     const int a = x0 + t % nbx, cc = y0 + t / nbx;
     float f = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
     if ((k & 3) == 1) f = __fmul_rn(f, A.td);
-    const long long v = (long long)f;
+    const long long v = (long long)trunc_u64(f);
     if (v) atomicAdd(&area[((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a], (unsigned long long)v);
   }
 }
@@ -307,7 +307,10 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
 __global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
   __shared__ double sh[32 * kPartSlots];
   __shared__ bool last;
-  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};   // |wl|, |d|, coord dist^2, grad dist^2, nan
+  // per-thread sums in float over the thread's few gcells; FP64 from the
+  // warp sums on (the FP64 pipe is narrow on this part)
+  float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};      // |wl|, |d|, coord dist^2, grad dist^2
+  int bad = 0;
   const BinGeom& G = A.geo;
   const EvalCtl C = *A.ctl;
   const float2* slp = pick4(A.slp, C.i_eval);
@@ -387,20 +390,41 @@ __global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
     if (sum_out) sum_out[g] = s;
     if (wl_out) wl_out[g] = w;
     if (d_out) d_out[g] = d;
-    const double aw = fabs((double)w.x) + fabs((double)w.y);
-    const double ad = fabs((double)d.x) + fabs((double)d.y);
+    const float aw = fabsf(w.x) + fabsf(w.y);
+    const float ad = fabsf(d.x) + fabsf(d.y);
     acc[0] += aw;
     acc[1] += ad;
     if (ref_slp) {
       const float2 r = ref_slp[g], q = ref_sum[g];
-      const double dx = (double)c.x - r.x, dy = (double)c.y - r.y;
-      const double gx = (double)s.x - q.x, gy = (double)s.y - q.y;
+      // getDistance (src/nesterovPlace.cpp:598-607): float differences
+      const float dx = c.x - r.x, dy = c.y - r.y;
+      const float gx = s.x - q.x, gy = s.y - q.y;
       acc[2] += dx * dx + dy * dy;
       acc[3] += gx * gx + gy * gy;
     }
-    if (!isfinite(aw) || !isfinite(ad)) acc[4] = 1.0;
+    if (!isfinite(aw) || !isfinite(ad)) bad = 1;
   }
-  block_reduce_n<5>(acc, A.part + (size_t)kPartWl * A.stride, A.stride, sh);
+  {
+    // warp sums (float, fixed xor tree), then the block's warps in order in FP64
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+    const int any_bad = __any_sync(0xffffffffu, bad);
+    const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) sh[k * 32 + wid] = (double)acc[k];
+      sh[4 * 32 + wid] = any_bad ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+      double t = 0.0;
+      for (int w8 = 0; w8 < nw; w8++) t += sh[threadIdx.x * 32 + w8];
+      A.part[(size_t)(kPartWl + threadIdx.x) * A.stride + blockIdx.x] = t;
+    }
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
     __threadfence();
     last = atomicAdd(&A.counters[0], 1u) == gridDim.x - 1;

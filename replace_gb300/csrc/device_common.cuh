@@ -68,6 +68,16 @@ __device__ __forceinline__ T pick2(T const (&a)[2], int i) {
   return i == 0 ? a[0] : a[1];
 }
 
+// float -> int64 truncation and int64 -> float rounding through 32-bit
+// conversions when the value fits (the same results; the 64-bit conversions
+// run on the FP64 pipe, which is narrow on this part).
+__device__ __forceinline__ unsigned long long trunc_u64(float f) {   // f >= 0
+  return f < 4294967296.0f ? (unsigned long long)__float2uint_rz(f) : (unsigned long long)(long long)f;
+}
+__device__ __forceinline__ float ll_to_float(long long v) {
+  return (v >= 0 && v < 2147483648ll) ? __int2float_rn((int)v) : __ll2float_rn(v);
+}
+
 __device__ __forceinline__ float fast_exp(float a) {
   a = __fadd_rn(1.0f, __fmul_rn(a, 0.0009765625f));
 #pragma unroll

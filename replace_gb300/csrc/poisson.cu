@@ -24,6 +24,7 @@
 #include <mutex>
 #include <vector>
 
+#include "device_common.cuh"
 #include "gpl_internal.h"
 
 namespace gpl {
@@ -177,7 +178,7 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
   float2* tws = smem + 2 * rp_n * n;                 // [n/2] twiddles
   load_twiddles(tws, A.tw, n);
   const int nb = A.nx * A.ny;
-  double ovf = 0.0;
+  float ovf_f = 0.0f;          // the thread's few bins in float; FP64 across threads
   const unsigned long long* area = nullptr;
   unsigned long long* area_clear = nullptr;
   if (A.ctl) {
@@ -219,13 +220,13 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
           const int bly = A.core_ly + j * A.size_y;
           const int buy = min(bly + A.size_y, A.core_uy);
           const long long bin_area = (long long)(bux - blx) * (long long)(buy - bly);
-          const float cap = __fmul_rn(__ll2float_rn(bin_area), A.td);
-          const float fi = __ll2float_rn((long long)ar[b]);
-          const float ff = __ll2float_rn((long long)ar[nb + b]);
-          const float fn = __ll2float_rn(np[b]);
+          const float cap = __fmul_rn(ll_to_float(bin_area), A.td);
+          const float fi = ll_to_float((long long)ar[b]);
+          const float ff = ll_to_float((long long)ar[nb + b]);
+          const float fn = ll_to_float(np[b]);
           // BinGrid::updateBinsGCellDensityArea (src/nesterovBase.cpp:804-818)
           dd[h] = __fdiv_rn(__fadd_rn(__fadd_rn(fi, ff), fn), cap);
-          ovf += (double)fmaxf(0.0f, __fsub_rn(__fadd_rn(fi, fn), cap));
+          ovf_f += fmaxf(0.0f, __fsub_rn(__fadd_rn(fi, fn), cap));
           ac[b] = 0ull;
           ac[nb + b] = 0ull;
           dens[b] = dd[h];
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
     A.spec[(2 * r) * n + k] = c.x;
     A.spec[(2 * r + 1) * n + k] = c.y;
   }
-  if (A.part_overflow) block_reduce_add(ovf, &A.part_overflow[blockIdx.x], red);
+  if (A.part_overflow) block_reduce_add((double)ovf_f, &A.part_overflow[blockIdx.x], red);
 }
 
 struct PassBArgs {
