@@ -428,11 +428,14 @@ __device__ __forceinline__ float spmv_warp(const IpDev& D, int axis, int i, bool
 // block partial sums of up to 2 products, then the last block of this axis
 // runs `fin` with the totals (fixed-order reduction)
 template <int N, class Fin>
-__device__ __forceinline__ void reduce_and_finish(IpDev& D, int kernel_id, double (&v)[N], Fin fin) {
+__device__ __forceinline__ void reduce_and_finish(IpDev& D, int kernel_id, const float (&vf)[N], Fin fin) {
   __shared__ double sh[32 * N];
   __shared__ bool last;
   const int axis = blockIdx.y;
   double* part = D.part + (size_t)(axis * 2) * D.parts;
+  double v[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) v[k] = vf[k];      // the thread's rows in float, FP64 across threads
   block_reduce_n<N>(v, part, D.parts, sh);
   if (threadIdx.x == 0) {
     __threadfence();
@@ -476,7 +479,7 @@ __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
   float* x = D.x + axis * n;
   float* r = D.r + axis * n;
   float* r0 = D.r0 + axis * n;
-  double v[2] = {0.0, 0.0};
+  float v[2] = {0.0f, 0.0f};
   const int lane = threadIdx.x & 31;
   for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
     const int i = w + lane;
@@ -485,8 +488,8 @@ __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
       const float ri = bb[i] - ax;
       r[i] = ri;
       r0[i] = ri;
-      v[0] += (double)ri * ri;
-      v[1] += (double)bb[i] * bb[i];
+      v[0] += ri * ri;
+      v[1] += bb[i] * bb[i];
     }
   }
   reduce_and_finish<2>(D, 0, v, [&](BiState& s, const double* t) {
@@ -517,8 +520,9 @@ __global__ void k_bi_p(IpDev D) {
   float* p = D.p + axis * n;
   const float* r = D.r + axis * n;
   const float* v = D.v + axis * n;
+  const float bf = (float)beta, wf = (float)S.w;   // Eigen's scalars are float
   for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB)
-    p[i] = (float)(r[i] + beta * (p[i] - S.w * v[i]));
+    p[i] = r[i] + bf * (p[i] - wf * v[i]);
 }
 
 // v = A p, alpha = rho / (r0 . v)
@@ -529,14 +533,14 @@ __global__ void k_bi_v(IpDev D) {
   const float* p = D.p + axis * n;
   float* v = D.v + axis * n;
   const float* r0 = D.r0 + axis * n;
-  double acc[1] = {0.0};
+  float acc[1] = {0.0f};
   const int lane = threadIdx.x & 31;
   for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
     const int i = w + lane;
     const float vi = spmv_warp(D, axis, i, i < n, p);
     if (i < n) {
       v[i] = vi;
-      acc[0] += (double)r0[i] * vi;
+      acc[0] += r0[i] * vi;
     }
   }
   reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; });
@@ -550,8 +554,9 @@ __global__ void k_bi_s(IpDev D) {
   const float* r = D.r + axis * n;
   const float* v = D.v + axis * n;
   float* s = D.s + axis * n;
+  const float af = (float)S.alpha;
   for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB)
-    s[i] = (float)(r[i] - S.alpha * v[i]);
+    s[i] = r[i] - af * v[i];
 }
 
 // t = A s, omega = (t . s) / (t . t)
@@ -561,15 +566,15 @@ __global__ void k_bi_t(IpDev D) {
   const int n = D.n_mov;
   const float* s = D.s + axis * n;
   float* t = D.t + axis * n;
-  double acc[2] = {0.0, 0.0};
+  float acc[2] = {0.0f, 0.0f};
   const int lane = threadIdx.x & 31;
   for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
     const int i = w + lane;
     const float ti = spmv_warp(D, axis, i, i < n, s);
     if (i < n) {
       t[i] = ti;
-      acc[0] += (double)ti * ti;
-      acc[1] += (double)ti * s[i];
+      acc[0] += ti * ti;
+      acc[1] += ti * s[i];
     }
   }
   reduce_and_finish<2>(D, 2, acc, [&](BiState& st, const double* tt) {
@@ -589,13 +594,14 @@ __global__ void k_bi_xr(IpDev D, int max_iter) {
   const float* s = D.s + axis * n;
   const float* t = D.t + axis * n;
   const float* r0 = D.r0 + axis * n;
-  double acc[2] = {0.0, 0.0};
+  const float af = (float)S.alpha, wf = (float)S.w;
+  float acc[2] = {0.0f, 0.0f};
   for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB) {
-    x[i] = (float)(x[i] + S.alpha * p[i] + S.w * s[i]);
-    const float ri = (float)(s[i] - S.w * t[i]);
+    x[i] = x[i] + (af * p[i] + wf * s[i]);
+    const float ri = s[i] - wf * t[i];
     r[i] = ri;
-    acc[0] += (double)ri * ri;
-    acc[1] += (double)r0[i] * ri;
+    acc[0] += ri * ri;
+    acc[1] += r0[i] * ri;
   }
   reduce_and_finish<2>(D, 3, acc, [&](BiState& st, const double* tt) {
     st.rr = tt[0];
@@ -650,6 +656,15 @@ __device__ __forceinline__ bool grid_barrier(GridBar* bar) {
   return s_ok != 0;
 }
 
+// Block sums of float per-thread partials, in FP64 (block_reduce_n).
+template <int N>
+__device__ __forceinline__ void block_partials(const float (&vf)[N], double* out, int stride, double* sh) {
+  double v[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) v[k] = vf[k];
+  block_reduce_n<N>(v, out, stride, sh);
+}
+
 __device__ __forceinline__ double* cpart(const IpDev& D, int phase, int axis) {
   return D.cpart + (size_t)((phase * 2 + axis) * 2) * D.parts;
 }
@@ -696,7 +711,7 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     if (S[0].done && S[1].done) break;
     // restart: r = r0 = b - A x
     if ((!S[0].done && S[0].need_restart) || (!S[1].done && S[1].need_restart)) {
-      double acc[2] = {0.0, 0.0};
+      float acc[2] = {0.0f, 0.0f};
       if (!S[axis].done && S[axis].need_restart) {
         for (int w = w0; w < n; w += step) {
           const int i = w + lane;
@@ -705,12 +720,12 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
             const float ri = bb[i] - ax;
             r[i] = ri;
             r0[i] = ri;
-            acc[0] += (double)ri * ri;
-            acc[1] += (double)bb[i] * bb[i];
+            acc[0] += ri * ri;
+            acc[1] += bb[i] * bb[i];
           }
         }
       }
-      block_reduce_n<2>(acc, cpart(D, 3, axis), D.parts, sh);
+      block_partials<2>(acc, cpart(D, 3, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][2];
       coop_totals<2>(D, 3, tot, sh, tt);
@@ -727,24 +742,24 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     const bool live = !S[axis].done;
     // p = r + beta (p - w v)
     if (live) {
-      const double beta = (S[axis].rho / S[axis].rho_old) * (S[axis].alpha / S[axis].w);
-      const double w = S[axis].w;
-      for (int i = i0; i < n; i += step) p[i] = (float)(r[i] + beta * (p[i] - w * v[i]));
+      const float beta = (float)((S[axis].rho / S[axis].rho_old) * (S[axis].alpha / S[axis].w));
+      const float w = (float)S[axis].w;
+      for (int i = i0; i < n; i += step) p[i] = r[i] + beta * (p[i] - w * v[i]);
     }
     if (!grid_barrier(D.bar)) return;
     // v = A p, alpha = rho / (r0 . v)
     {
-      double acc[1] = {0.0};
+      float acc[1] = {0.0f};
       if (live)
         for (int w = w0; w < n; w += step) {
           const int i = w + lane;
           const float vi = spmv_warp<true>(D, axis, i, i < n, p);
           if (i < n) {
             v[i] = vi;
-            acc[0] += (double)r0[i] * vi;
+            acc[0] += r0[i] * vi;
           }
         }
-      block_reduce_n<1>(acc, cpart(D, 0, axis), D.parts, sh);
+      block_partials<1>(acc, cpart(D, 0, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][1];
       coop_totals<1>(D, 0, tot, sh, tt);
@@ -755,24 +770,24 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     }
     // s = r - alpha v
     if (live) {
-      const double alpha = S[axis].alpha;
-      for (int i = i0; i < n; i += step) sv[i] = (float)(r[i] - alpha * v[i]);
+      const float alpha = (float)S[axis].alpha;
+      for (int i = i0; i < n; i += step) sv[i] = r[i] - alpha * v[i];
     }
     if (!grid_barrier(D.bar)) return;
     // t = A s, w = (t . s) / (t . t)
     {
-      double acc[2] = {0.0, 0.0};
+      float acc[2] = {0.0f, 0.0f};
       if (live)
         for (int w = w0; w < n; w += step) {
           const int i = w + lane;
           const float ti = spmv_warp<true>(D, axis, i, i < n, sv);
           if (i < n) {
             t[i] = ti;
-            acc[0] += (double)ti * ti;
-            acc[1] += (double)ti * sv[i];
+            acc[0] += ti * ti;
+            acc[1] += ti * sv[i];
           }
         }
-      block_reduce_n<2>(acc, cpart(D, 1, axis), D.parts, sh);
+      block_partials<2>(acc, cpart(D, 1, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][2];
       coop_totals<2>(D, 1, tot, sh, tt);
@@ -783,18 +798,18 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     }
     // x += alpha p + w s; r = s - w t; then the next loop head
     {
-      double acc[2] = {0.0, 0.0};
+      float acc[2] = {0.0f, 0.0f};
       if (live) {
-        const double alpha = S[axis].alpha, w = S[axis].w;
+        const float alpha = (float)S[axis].alpha, w = (float)S[axis].w;
         for (int i = i0; i < n; i += step) {
-          x[i] = (float)(x[i] + alpha * p[i] + w * sv[i]);
-          const float ri = (float)(sv[i] - w * t[i]);
+          x[i] = x[i] + (alpha * p[i] + w * sv[i]);
+          const float ri = sv[i] - w * t[i];
           r[i] = ri;
-          acc[0] += (double)ri * ri;
-          acc[1] += (double)r0[i] * ri;
+          acc[0] += ri * ri;
+          acc[1] += r0[i] * ri;
         }
       }
-      block_reduce_n<2>(acc, cpart(D, 2, axis), D.parts, sh);
+      block_partials<2>(acc, cpart(D, 2, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][2];
       coop_totals<2>(D, 2, tot, sh, tt);
@@ -827,8 +842,11 @@ constexpr int kClThreads = 1024;
 constexpr int kClMaxRows = 65536;
 
 template <int N>
-__device__ __forceinline__ void cluster_total(cg::cluster_group& cl, double (&v)[N], double* slot,
+__device__ __forceinline__ void cluster_total(cg::cluster_group& cl, const float (&vf)[N], double* slot,
                                               double* sh, double* tot_sh, double (&tot)[N]) {
+  double v[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) v[k] = vf[k];
   block_reduce_n<N>(v, slot, 1, sh, 0);   // slot[k] = this CTA's sum
   cl.sync();
   if (threadIdx.x == 0) {
@@ -869,7 +887,7 @@ k_bi_cluster(IpDev D, int max_iter) {
   for (int it = 0; it <= 2 * max_iter + 2 && !S.done; it++) {
     // restart: r = r0 = b - A x
     if (S.need_restart) {
-      double acc[2] = {0.0, 0.0};
+      float acc[2] = {0.0f, 0.0f};
       for (int w = w0; w < n; w += step) {
         const int i = w + lane;
         const float ax = spmv_warp<true>(D, axis, i, i < n, x);
@@ -877,8 +895,8 @@ k_bi_cluster(IpDev D, int max_iter) {
           const float ri = bb[i] - ax;
           r[i] = ri;
           r0[i] = ri;
-          acc[0] += (double)ri * ri;
-          acc[1] += (double)bb[i] * bb[i];
+          acc[0] += ri * ri;
+          acc[1] += bb[i] * bb[i];
         }
       }
       double tot[2];
@@ -892,20 +910,20 @@ k_bi_cluster(IpDev D, int max_iter) {
     }
     // p = r + beta (p - w v)
     {
-      const double beta = (S.rho / S.rho_old) * (S.alpha / S.w);
-      const double w = S.w;
-      for (int i = w0 + lane; i < n; i += step) p[i] = (float)(r[i] + beta * (p[i] - w * v[i]));
+      const float beta = (float)((S.rho / S.rho_old) * (S.alpha / S.w));
+      const float w = (float)S.w;
+      for (int i = w0 + lane; i < n; i += step) p[i] = r[i] + beta * (p[i] - w * v[i]);
     }
     cl.sync();
     // v = A p, alpha = rho / (r0 . v)
     {
-      double acc[1] = {0.0};
+      float acc[1] = {0.0f};
       for (int w = w0; w < n; w += step) {
         const int i = w + lane;
         const float vi = spmv_warp<true>(D, axis, i, i < n, p);
         if (i < n) {
           v[i] = vi;
-          acc[0] += (double)r0[i] * vi;
+          acc[0] += r0[i] * vi;
         }
       }
       double tot[1];
@@ -915,20 +933,20 @@ k_bi_cluster(IpDev D, int max_iter) {
     }
     // s = r - alpha v
     {
-      const double alpha = S.alpha;
-      for (int i = w0 + lane; i < n; i += step) sv[i] = (float)(r[i] - alpha * v[i]);
+      const float alpha = (float)S.alpha;
+      for (int i = w0 + lane; i < n; i += step) sv[i] = r[i] - alpha * v[i];
     }
     cl.sync();
     // t = A s, w = (t . s) / (t . t)
     {
-      double acc[2] = {0.0, 0.0};
+      float acc[2] = {0.0f, 0.0f};
       for (int w = w0; w < n; w += step) {
         const int i = w + lane;
         const float ti = spmv_warp<true>(D, axis, i, i < n, sv);
         if (i < n) {
           t[i] = ti;
-          acc[0] += (double)ti * ti;
-          acc[1] += (double)ti * sv[i];
+          acc[0] += ti * ti;
+          acc[1] += ti * sv[i];
         }
       }
       double tot[2];
@@ -938,14 +956,14 @@ k_bi_cluster(IpDev D, int max_iter) {
     }
     // x += alpha p + w s; r = s - w t; then the next loop head
     {
-      double acc[2] = {0.0, 0.0};
-      const double alpha = S.alpha, w = S.w;
+      float acc[2] = {0.0f, 0.0f};
+      const float alpha = (float)S.alpha, w = (float)S.w;
       for (int i = w0 + lane; i < n; i += step) {
-        x[i] = (float)(x[i] + alpha * p[i] + w * sv[i]);
-        const float ri = (float)(sv[i] - w * t[i]);
+        x[i] = x[i] + (alpha * p[i] + w * sv[i]);
+        const float ri = sv[i] - w * t[i];
         r[i] = ri;
-        acc[0] += (double)ri * ri;
-        acc[1] += (double)r0[i] * ri;
+        acc[0] += ri * ri;
+        acc[1] += r0[i] * ri;
       }
       double tot[2];
       cluster_total<2>(cl, acc, slot[2], sh, tot_sh, tot);
