@@ -88,10 +88,13 @@ __device__ __forceinline__ float2 pin_gradient(int2 p, const PinExp& E, const fl
                                                float cy) {
   const float x = (float)p.x, y = (float)p.y;
   float g[4] = {0.f, 0.f, 0.f, 0.f};
-  if (E.flags & 1u) { const float s = S[0]; g[0] = (s * (E.e[0] * (1.0f - cx * x)) + cx * E.e[0] * S[1]) / (s * s); }
-  if (E.flags & 2u) { const float s = S[2]; g[1] = (s * (E.e[1] * (1.0f + cx * x)) - cx * E.e[1] * S[3]) / (s * s); }
-  if (E.flags & 4u) { const float s = S[4]; g[2] = (s * (E.e[2] * (1.0f - cy * y)) + cy * E.e[2] * S[5]) / (s * s); }
-  if (E.flags & 8u) { const float s = S[6]; g[3] = (s * (E.e[3] * (1.0f + cy * y)) - cy * E.e[3] * S[7]) / (s * s); }
+  // The sums of exponentials are in [1, degree]: the net's extreme pin
+  // contributes exp(0) = 1 and every term is at most 1, so s*s lies in
+  // [1, degree^2] and the fast division (2 ulp) is exact enough and safe.
+  if (E.flags & 1u) { const float s = S[0]; g[0] = __fdividef(s * (E.e[0] * (1.0f - cx * x)) + cx * E.e[0] * S[1], s * s); }
+  if (E.flags & 2u) { const float s = S[2]; g[1] = __fdividef(s * (E.e[1] * (1.0f + cx * x)) - cx * E.e[1] * S[3], s * s); }
+  if (E.flags & 4u) { const float s = S[4]; g[2] = __fdividef(s * (E.e[2] * (1.0f - cy * y)) + cy * E.e[2] * S[5], s * s); }
+  if (E.flags & 8u) { const float s = S[6]; g[3] = __fdividef(s * (E.e[3] * (1.0f + cy * y)) - cy * E.e[3] * S[7], s * s); }
   return make_float2(g[0] - g[1], g[2] - g[3]);
 }
 
@@ -283,6 +286,12 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval& V, i
   return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
+// Buckets 0-5 (nets of up to 64 pins) in one launch; buckets 6-7 (larger
+// nets, rare) in a second one, so that their larger register footprint does
+// not lower the occupancy of the common case.
+constexpr int kWaSplit = 6;
+
+template <bool kLarge>
 __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A) {
   __shared__ long long sh[32];
   WaEval V;
@@ -293,25 +302,30 @@ __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A)
     V.cx = C->wl_coef_x;
     V.cy = C->wl_coef_y;
   }
-  int bucket = 0;
-  while (bucket < kWaBuckets - 1 && (int)blockIdx.x >= A.block_start[bucket + 1]) bucket++;
-  const int lb = blockIdx.x - A.block_start[bucket];
+  const int gb = (int)blockIdx.x + (kLarge ? A.block_start[kWaSplit] : 0);
+  int bucket = kLarge ? kWaSplit : 0;
+  const int last = kLarge ? kWaBuckets - 1 : kWaSplit - 1;
+  while (bucket < last && gb >= A.block_start[bucket + 1]) bucket++;
+  const int lb = gb - A.block_start[bucket];
   long long hp = 0;
-  switch (bucket) {
-    case 0: hp = wa_group<2>(A, V, 0, lb); break;
-    case 1: hp = wa_group<4>(A, V, 1, lb); break;
-    case 2: hp = wa_group<8>(A, V, 2, lb); break;
-    case 3: hp = wa_group<16>(A, V, 3, lb); break;
-    case 4: hp = wa_group<32>(A, V, 4, lb); break;
-    case 5: hp = wa_warp<2>(A, V, 5, lb); break;
-    case 6: hp = wa_warp<4>(A, V, 6, lb); break;
-    default: hp = wa_huge(A, V, 7, lb); break;
+  if constexpr (!kLarge) {
+    switch (bucket) {
+      case 0: hp = wa_group<2>(A, V, 0, lb); break;
+      case 1: hp = wa_group<4>(A, V, 1, lb); break;
+      case 2: hp = wa_group<8>(A, V, 2, lb); break;
+      case 3: hp = wa_group<16>(A, V, 3, lb); break;
+      case 4: hp = wa_group<32>(A, V, 4, lb); break;
+      default: hp = wa_warp<2>(A, V, 5, lb); break;
+    }
+  } else {
+    if (bucket == 6) hp = wa_warp<4>(A, V, 6, lb);
+    else hp = wa_huge(A, V, 7, lb);
   }
   // HPWL is an integer sum: one 64-bit atomic per block gives the exact,
   // order-independent total (the gcell kernel reads and clears it)
-  block_reduce_ll(hp, &A.part_i[blockIdx.x], sh);
+  block_reduce_ll(hp, &A.part_i[gb], sh);
   if (threadIdx.x == 0) atomicAdd(reinterpret_cast<unsigned long long*>(A.hpwl_total),
-                                  (unsigned long long)A.part_i[blockIdx.x]);
+                                  (unsigned long long)A.part_i[gb]);
 }
 
 }  // namespace
@@ -335,11 +349,13 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.pin_grad = d.pin_grad;
   A.part_i = d.part_i;
   A.hpwl_total = d.hpwl_total;
-  const int blocks = d.wa_block_start[kWaBuckets];
+  const int small = d.wa_block_start[kWaSplit];
+  const int large = d.wa_block_start[kWaBuckets] - small;
   t.begin(kKWa);
-  if (blocks) k_wa<<<blocks, kBlock, 0, s>>>(A);
+  if (small) k_wa<false><<<small, kBlock, 0, s>>>(A);
+  if (large) k_wa<true><<<large, kBlock, 0, s>>>(A);
   t.end(kKWa);
-  t.count(blocks ? 1 : 0);
+  t.count((small ? 1 : 0) + (large ? 1 : 0));
   GPL_CUDA(cudaGetLastError());
   return GPL_OK;
 }
