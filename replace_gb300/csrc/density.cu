@@ -154,8 +154,8 @@ struct TileArgs {
 // Per (gcell, bin) the area is (int64)(float overlap * scale [* td for a
 // macro]), added into the inst or filler set.  The predictor runs here for
 // every gcell (big ones included; their bins are left to k_scatter_big).
-__global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A, TileArgs T) {
-  extern __shared__ unsigned win[];                // [2][wy][wx] low words, then [2][wy][wx] high words
+__global__ void __launch_bounds__(kBlock, 5) k_scatter(ScatterArgs A, TileArgs T) {
+  extern __shared__ unsigned win[];                // [2][wy][wx] low 16-bit sums, then high 16-bit sums
   if ((int)blockIdx.x >= *T.n_chunks) return;      // block-uniform
   const EvalCtl C = *A.ctl;
   unsigned long long* area = pick2(A.area, C.area_cur);
@@ -188,11 +188,12 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A, TileArgs T) {
         if (!v) continue;
         const int u = a - ox, w = cc - oy;
         if (u >= 0 && u < wx && w >= 0 && w < wy && v < (1ull << 32)) {
-          // 64-bit sum as two 32-bit words: the low word's wrap-around
-          // (old + v < old) carries into the high word; exact in any order
+          // v < 2^32 split into 16-bit halves added to two 32-bit words: a
+          // chunk has at most kScatterChunk (< 2^16) gcells, one addition
+          // each per bin, so neither word can wrap; the adds return nothing
           const int i = half * wn + w * wx + u;
-          const unsigned lo = (unsigned)v;
-          if (atomicAdd(&win[i], lo) + lo < lo) atomicAdd(&win_hi[i], 1u);
+          atomicAdd(&win[i], (unsigned)(v & 0xffffu));
+          atomicAdd(&win_hi[i], (unsigned)(v >> 16));
         } else {
           atomicAdd(&area[half * nb + cc * G.cnt_x + a], v);
         }
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(kBlock) k_scatter(ScatterArgs A, TileArgs T) {
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 2 * wn; i += blockDim.x) {
-    const unsigned long long v = ((unsigned long long)win_hi[i] << 32) | win[i];
+    const unsigned long long v = (unsigned long long)win[i] + ((unsigned long long)win_hi[i] << 16);
     if (!v) continue;
     const int half = i >= wn ? 1 : 0, r = i - half * wn;
     const int a = ox + r % wx, cc = oy + r / wx;      // inside the grid: only in-grid bins were added

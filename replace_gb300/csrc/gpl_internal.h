@@ -258,6 +258,7 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t);
 // Tile grid of a bin grid, and the chunk-table bound, for sizing.
 constexpr int kScatterChunk = 2048;
+static_assert(kScatterChunk < 65536, "the scatter's 16-bit split window sums need < 2^16 gcells per chunk");
 void tile_grid(int cnt_x, int cnt_y, int* tw, int* th, int* tx, int* ty);
 int scatter_max_chunks(int n_g, int tiles);
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);

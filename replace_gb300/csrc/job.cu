@@ -332,7 +332,7 @@ int ensure_nb(gpl_job* j) {
 }
 
 // Iterations between refreshes of the scatter's tile order.
-constexpr int kTileOrderEvery = 8;
+constexpr int kTileOrderEvery = 16;
 
 EvalArgs base_args(gpl_job* j) {
   EvalArgs a;

@@ -476,6 +476,10 @@ WORKLOADS = {
                                         bins=512),
     "1m_cells_1024bins": dict(n_cells=1_000_000, n_nets=1_050_000, n_io=2_000,
                               n_macros=0, util=0.60, target_density=0.75, bins=1024),
+    # the 1M workload's bin grid with 40 % of its cells: the case kernel
+    # profiles are captured on (working set above L2, a few hundred MB)
+    "400k_cells_1024bins": dict(n_cells=400_000, n_nets=420_000, n_io=1_000,
+                                n_macros=0, util=0.60, target_density=0.75, bins=1024),
 }
 
 
