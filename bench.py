@@ -110,6 +110,17 @@ def algorithmic_bytes(kind, ng, npins, nn, nb):
     }.get(kind)
 
 
+# DRAM bytes per launch (read + write) measured with ncu on the 1M-cell
+# workload (profiles/traffic_1m_cells_1024bins.md): the `traffic` of the
+# roofline object when the dominant kernel is one of these.
+NCU_TRAFFIC = {
+    "1m_cells_1024bins": {
+        "wa_wirelength": 104.6e6, "gcell_gradient": 131.1e6, "density_scatter": 64.7e6,
+        "poisson_rows_dct": 25.2e6, "poisson_cols_solve": 4.3e6, "poisson_rows_inverse": 8.4e6,
+    },
+}
+
+
 def max_over_ranks(ms: float, world: int, device: str) -> float:
     """The slowest rank's timed region (replicas: one job per GPU)."""
     if world == 1:
@@ -394,7 +405,10 @@ def main():
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": f"of {peak_kind}",
-                         "traffic": None, "kernel_share": kernel_share,
+                         "traffic": NCU_TRAFFIC.get(args.workload, {}).get(dom),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                                           "(profiles/traffic_1m_cells_1024bins.md)",
+                         "algorithmic_bytes": bytes_per, "kernel_share": kernel_share,
                          "kernel_ms_per_launch": kernel_ms},
             "cpu_baseline": cpu,
             "clocks": clk,
