@@ -280,6 +280,15 @@ void gpl_kernel_times_reset(struct gpl_job* job, int32_t enable);
 /* Number of kernels the job has launched since the last reset. */
 int64_t gpl_kernel_launch_count(struct gpl_job* job);
 
+/* Tensor-core GEMM (no reference counterpart; the building block of the
+ * DCT-as-GEMM Poisson path): D (m x n, fp32, row-major) = A (m x k, bf16,
+ * row-major) * B (n x k, bf16, row-major)^T on tcgen05 with TMA-fed shared
+ * memory.  All pointers are device memory, 16-byte aligned; m and n must be
+ * multiples of 128 and k of 64.  *error_flag (device int, may be NULL) is
+ * set to 1 if a pipeline wait timed out (the result is then invalid). */
+gpl_status gpl_tc_gemm_bf16(const void* a, const void* b, float* d, int32_t m, int32_t n, int32_t k,
+                            int32_t* error_flag, void* stream);
+
 /* ------------------------------------------------------------------------
  * Placement server: continuous batching of independent jobs on one GPU.
  * No reference counterpart: RePlAce places one design per process.  A
