@@ -129,6 +129,10 @@ typedef struct gpl_params {
                                               cooperative grid), 1 = one kernel per phase,
                                               2 = cooperative grid (same iterates as 1),
                                               3 = cluster per axis */
+  int32_t poisson_path;                    /* Poisson solve: 0 = auto (times both forms on the job's
+                                              grid and keeps the faster), 1 = shared-memory FFT,
+                                              2 = tensor-core GEMMs (bf16 three-term split; grids
+                                              with both counts multiples of 128) */
 } gpl_params;
 
 /* Counts and grid chosen by the job (NesterovBase / BinGrid). */
@@ -141,6 +145,10 @@ typedef struct gpl_job_info {
   int32_t filler_dx, filler_dy;
   int64_t place_insts_area, std_insts_area, macro_insts_area, non_place_insts_area;
   int64_t device_bytes;      /* device memory held by the job */
+  int32_t poisson_path;      /* the form the job runs: 1 FFT, 2 tensor-core GEMMs */
+  float poisson_fft_us;      /* the timings auto mode compared (0 if not timed) */
+  float poisson_gemm_us;
+  int32_t pad;
 } gpl_job_info;
 
 /* One physics evaluation (the work of NesterovBase for one coordinate set). */
@@ -283,8 +291,8 @@ int64_t gpl_kernel_launch_count(struct gpl_job* job);
 /* Tensor-core GEMM (no reference counterpart; the building block of the
  * DCT-as-GEMM Poisson path): D (m x n, fp32, row-major) = A (m x k, bf16,
  * row-major) * B (n x k, bf16, row-major)^T on tcgen05 with TMA-fed shared
- * memory.  All pointers are device memory, 16-byte aligned; m and n must be
- * multiples of 128 and k of 64.  *error_flag (device int, may be NULL) is
+ * memory.  All pointers are device memory, 16-byte aligned; m must be a
+ * multiple of 128, n and k of 64.  *error_flag (device int, may be NULL) is
  * set to 1 if a pipeline wait timed out (the result is then invalid). */
 gpl_status gpl_tc_gemm_bf16(const void* a, const void* b, float* d, int32_t m, int32_t n, int32_t k,
                             int32_t* error_flag, void* stream);

@@ -132,6 +132,9 @@ struct DeviceModel {
   int32_t* tile_start = nullptr;   // [tiles + 1]
   int4* chunks = nullptr;          // [max_chunks] (tile, first, end, 0) of <= kScatterChunk gcells
   int32_t* n_chunks = nullptr;     // [1]
+  // Poisson solve: 1 = shared-memory FFT passes, 2 = tensor-core GEMMs
+  int poisson_path = 1;
+  struct PoissonGemm* pg = nullptr;
   struct EvalResult* result = nullptr;     // device
   struct EvalResult* result_h = nullptr;   // pinned host mirror
   int64_t bytes = 0;
@@ -265,6 +268,14 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t);
 // the Poisson passes of a job evaluation (area set chosen by EvalCtl)
 int launch_poisson_job(DeviceModel& d, bool want_phi, cudaStream_t s, Timer& t);
+// The tensor-core GEMM form of the Poisson solve (poisson_gemm.cu).
+struct PoissonGemm;
+bool poisson_gemm_eligible(int nx, int ny);
+int64_t poisson_gemm_bytes(int nx, int ny);
+int poisson_gemm_setup(DeviceModel& d, PoissonGemm** out, cudaMemPool_t pool, cudaStream_t s);
+void poisson_gemm_free(PoissonGemm* pg, cudaMemPool_t pool, cudaStream_t s);
+int poisson_gemm_error(const PoissonGemm* pg, cudaStream_t s, int* flag);
+int launch_poisson_gemm(DeviceModel& d, PoissonGemm* pg, bool want_phi, cudaStream_t s, Timer& t);
 // Sets the Poisson kernels' shared-memory limit on the current device (once
 // per device); called before a stream capture, where it must not run first.
 int poisson_prepare_device();

@@ -104,6 +104,8 @@ struct gpl_job {
   EvalResult last{};
   cudaGraphExec_t graph_exec = nullptr; // one evaluation, replayed
   long long graph_kernels = 0;
+  float poisson_fft_us = 0.0f, poisson_gemm_us = 0.0f;   // auto mode's timings
+  bool poisson_chosen = false;
 };
 
 namespace {
@@ -379,6 +381,66 @@ int finish(gpl_job* j) {
   return GPL_OK;
 }
 
+// Mean time of `reps` Poisson solves on the job's stream (after one warm-up).
+float time_poisson(gpl_job* j, int reps) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  Timer quiet;
+  launch_poisson_job(j->d, false, j->stream, quiet);
+  cudaEventRecord(a, j->stream);
+  for (int r = 0; r < reps; r++) launch_poisson_job(j->d, false, j->stream, quiet);
+  cudaEventRecord(b, j->stream);
+  float ms = 0.0f;
+  if (cudaEventSynchronize(b) == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaGetLastError();
+  return 1000.0f * ms / reps;
+}
+
+// The form of the Poisson solve (gpl_params.poisson_path): auto times the
+// shared-memory FFT passes and the tensor-core GEMMs on this job's grid and
+// keeps the faster.  Runs before the first evaluation (the areas are still
+// zero, so the trial solves change nothing the evaluation reads).
+int choose_poisson_path(gpl_job* j) {
+  DeviceModel& d = j->d;
+  if (j->poisson_chosen) return GPL_OK;
+  j->poisson_chosen = true;
+  const int want = j->m.p.poisson_path;
+  d.poisson_path = 1;
+  if (want == 1) return GPL_OK;
+  if (!poisson_gemm_eligible(d.cnt_x, d.cnt_y)) {
+    if (want == 2) {
+      set_error("tensor-core Poisson path: both bin counts must be multiples of 128");
+      return GPL_ERR_INVALID_ARG;
+    }
+    return GPL_OK;
+  }
+  int rc = poisson_gemm_setup(d, &d.pg, j->pool, j->stream);
+  if (rc) {
+    if (want == 2) return rc;
+    cudaGetLastError();
+    return GPL_OK;                 // auto: the FFT form
+  }
+  if (want == 2) { d.poisson_path = 2; return GPL_OK; }
+  EvalCtl c;
+  memset(&c, 0, sizeof(c));
+  rc = put_ctl(j, c);
+  if (rc) return rc;
+  j->poisson_fft_us = time_poisson(j, 5);
+  d.poisson_path = 2;
+  j->poisson_gemm_us = time_poisson(j, 5);
+  int flag = 0;
+  poisson_gemm_error(d.pg, j->stream, &flag);
+  if (flag || !(j->poisson_gemm_us > 0.0f) || j->poisson_gemm_us >= j->poisson_fft_us) {
+    d.poisson_path = 1;
+    poisson_gemm_free(d.pg, j->pool, j->stream);
+    d.pg = nullptr;
+  }
+  return GPL_OK;
+}
+
 // The whole evaluation as one CUDA graph (control-record upload, kernels,
 // result download); every evaluation of the job replays it.
 int build_graph(gpl_job* j) {
@@ -486,6 +548,8 @@ bool diverged(const gpl_job* j) {
 // NesterovPlace::init (src/nesterovPlace.cpp:64-175)
 int nesterov_init(gpl_job* j) {
   int rc = ensure_nb(j);
+  if (rc) return rc;
+  rc = choose_poisson_path(j);
   if (rc) return rc;
   rc = build_graph(j);
   if (rc) return rc;
@@ -651,6 +715,15 @@ int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
     }
   }
   if (j->iter >= p.nesterov_place_max_iter) j->finished = true;
+  if (j->d.poisson_path == 2) {
+    int flag = 0;
+    int rc = poisson_gemm_error(j->d.pg, j->stream, &flag);
+    if (rc) return rc;
+    if (flag) {
+      set_error("tensor-core Poisson path: a pipeline wait timed out; results are invalid");
+      return GPL_ERR_CUDA;
+    }
+  }
   return j->diverge_code;
 }
 
@@ -667,6 +740,9 @@ void fill_info(gpl_job* j, gpl_job_info* info) {
   info->place_insts_area = m.place_area; info->std_insts_area = m.std_area;
   info->macro_insts_area = m.macro_area; info->non_place_insts_area = m.non_place_area;
   info->device_bytes = j->d.bytes;
+  info->poisson_path = j->d.poisson_path;
+  info->poisson_fft_us = j->poisson_fft_us;
+  info->poisson_gemm_us = j->poisson_gemm_us;
 }
 
 }  // namespace
@@ -715,7 +791,9 @@ int job_device_bytes(gpl_job* j, int64_t* bytes) {
   const size_t arena = arena_bytes(ng, m.n_pins, m.n_nets, n_gpins, ng, nb, c.cnt_x, c.cnt_y, stride,
                                    (size_t)m.n_nets + kWaBuckets);
   const size_t ip = m.p.initial_place_max_iter > 0 ? initial_place_bytes(m, sm) : 0;
-  *bytes = (int64_t)std::max(arena, ip);
+  const size_t pg = (m.p.poisson_path != 1 && poisson_gemm_eligible(c.cnt_x, c.cnt_y))
+                        ? (size_t)poisson_gemm_bytes(c.cnt_x, c.cnt_y) : 0;
+  *bytes = (int64_t)std::max(arena + pg, ip);
   return GPL_OK;
 }
 
@@ -756,6 +834,7 @@ void gpl_params_default(gpl_params* p) {
   p->stream = nullptr;
   p->use_graph = 1;
   p->ip_solver = 0;
+  p->poisson_path = 0;
 }
 
 gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
@@ -789,6 +868,7 @@ void gpl_destroy(gpl_job* j) {
   if (j->stream) cudaStreamSynchronize(j->stream);
   j->timer.release();
   if (j->graph_exec) cudaGraphExecDestroy(j->graph_exec);
+  if (j->d.pg) poisson_gemm_free(j->d.pg, j->pool, j->stream);
   if (j->arena) dev_free(j->arena, j->pool, j->stream);
   if (j->own_pinned && j->pinned) cudaFreeHost(j->pinned);
   if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
@@ -858,6 +938,8 @@ gpl_status gpl_eval(gpl_job* j, const float* xy, float cx, float cy, float* wl_g
   if (rc) return (gpl_status)rc;
   DeviceModel& d = j->d;
   const size_t ng = j->m.n_g;
+  rc = choose_poisson_path(j);
+  if (rc) return (gpl_status)rc;
   // slot 3 of the coordinate / gradient-sum buffers belongs to this hook
   rc = upload(d.slp[3], xy, ng * sizeof(float2), j->stream);
   if (rc) return (gpl_status)rc;

@@ -537,6 +537,7 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
 }
 
 int launch_poisson_job(DeviceModel& d, bool want_phi, cudaStream_t s, Timer& t) {
+  if (d.poisson_path == 2 && d.pg) return launch_poisson_gemm(d, d.pg, want_phi, s, t);
   PoissonGrid g;
   g.nx = d.cnt_x; g.ny = d.cnt_y; g.size_x = d.size_x; g.size_y = d.size_y;
   g.core_lx = d.core_lx; g.core_ly = d.core_ly; g.core_ux = d.core_ux; g.core_uy = d.core_uy;

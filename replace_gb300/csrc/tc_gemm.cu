@@ -1,143 +1,9 @@
-// Tensor-core GEMM on the fifth-generation (tcgen05) path:
-//   D (M x N, fp32) = A (M x K, bf16) * B (N x K, bf16)^T
-// with A and B stored K-contiguous (row-major M x K and N x K), the layout
-// the DCT-as-GEMM Poisson path uses.  One CTA computes a 128 x 128 tile of D:
-//   * a TMA producer thread streams 128 x 64 tiles of A and B into a
-//     four-stage shared-memory ring (128-byte swizzle, the layout the MMA
-//     descriptors expect), one mbarrier per stage for "full";
-//   * an MMA thread issues tcgen05.mma (kind::f16, bf16 inputs, fp32
-//     accumulator in tensor memory, M = 128, N = 128, K = 16 per
-//     instruction) and commits each stage back to its "empty" mbarrier;
-//   * after the last commit all four warps read the accumulator from tensor
-//     memory (tcgen05.ld, 32 rows per warp) and hand it to the epilogue.
-// Every mbarrier wait is bounded: on time-out the CTA records an error,
-// drains the copies it issued (again bounded), frees its tensor memory and
-// returns, so a fault in the pipeline can never hang the GPU.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-#include <cuda_bf16.h>
-#include <cuda_runtime.h>
-
-#include <cstdint>
-#include <mutex>
-
-#include "gpl_internal.h"
+// The diagnostic entry point of the tensor-core GEMM (gpl_tc_gemm_bf16):
+// row-major fp32 output.
+#include "tc_gemm.cuh"
 
 namespace gpl {
-
 namespace {
-
-constexpr int kTcM = 128;
-constexpr int kTcN = 128;
-constexpr int kTcK = 64;                 // one 128-byte swizzle row of bf16
-constexpr int kTcStages = 4;
-constexpr int kTcThreads = 128;
-constexpr uint32_t kTileBytes = kTcM * kTcK * 2;   // 16 KB, A and B alike
-constexpr long long kWaitPolls = 1ll << 24;        // bounded mbarrier polls
-
-struct TcSmem {
-  __nv_bfloat16 a[kTcStages][kTcM * kTcK];
-  __nv_bfloat16 b[kTcStages][kTcN * kTcK];
-  uint64_t full[kTcStages];
-  uint64_t empty[kTcStages];
-  uint64_t done;
-  uint32_t tmem_base;
-};
-constexpr size_t kTcSmemBytes = sizeof(TcSmem) + 1024;   // + alignment slack
-
-__device__ __forceinline__ uint32_t saddr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(saddr(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// Waits for the phase of the given parity; false after kWaitPolls polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
-  for (long long i = 0; i < kWaitPolls; i++)
-    if (mbar_try(b, parity)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-          "r"(saddr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major operand with 128-byte swizzle,
-// rows of 128 B, 8-row atoms 1024 B apart (stride byte offset), descriptor
-// version 1, layout type 2 (128-byte swizzle).
-__device__ __forceinline__ uint64_t smem_desc(const void* p) {
-  const uint32_t a = saddr(p);
-  uint64_t d = 0;
-  d |= (uint64_t)((a & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;                 // leading byte offset (unused for this layout)
-  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
-  d |= (uint64_t)1 << 46;                 // descriptor version
-  d |= (uint64_t)2 << 61;                 // 128-byte swizzle
-  return d;
-}
-
-// Instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both
-// K-major, N = kTcN, M = kTcM.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
-                            ((uint32_t)(kTcM >> 4) << 24);
-
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
-               : "memory");
-}
-
-// 32 consecutive fp32 columns of this warp's 32 accumulator rows.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
 
 // Row-major fp32 output (the diagnostic GEMM).
 struct EpiStore {
@@ -150,141 +16,7 @@ struct EpiStore {
   }
 };
 
-template <class Epi>
-__global__ void __launch_bounds__(kTcThreads, 1)
-    k_tc_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int K, Epi epi,
-              int* err) {
-  extern __shared__ unsigned char smem_raw[];
-  TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
-  const int kt_n = K / kTcK;
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kTcStages; s++) {
-      mbar_init(&S.full[s], 1);
-      mbar_init(&S.empty[s], 1);
-    }
-    mbar_init(&S.done, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {   // tensor memory: kTcN fp32 columns x 128 lanes
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&S.tmem_base)),
-                 "r"((uint32_t)kTcN)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem = S.tmem_base;
-  bool ok = true;
-  if (warp == 0 && lane == 0) {
-    // producer: stage s holds k-tile kt while kt % kTcStages == s
-    int issued = 0;
-    for (int kt = 0; kt < kt_n; kt++) {
-      const int s = kt % kTcStages;
-      if (kt >= kTcStages && !mbar_wait(&S.empty[s], ((kt / kTcStages) - 1) & 1)) { ok = false; break; }
-      mbar_expect_tx(&S.full[s], 2 * kTileBytes);
-      tma_load_2d(S.a[s], &ta, kt * kTcK, m0, &S.full[s]);
-      tma_load_2d(S.b[s], &tb, kt * kTcK, n0, &S.full[s]);
-      issued = kt + 1;
-    }
-    if (!ok) {
-      // drain: the copies of the last stages issued must land before the
-      // CTA releases its shared memory
-      for (int kt = (issued > kTcStages ? issued - kTcStages : 0); kt < issued; kt++)
-        mbar_wait(&S.full[kt % kTcStages], (kt / kTcStages) & 1);
-    }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    for (int kt = 0; kt < kt_n; kt++) {
-      const int s = kt % kTcStages;
-      if (!mbar_wait(&S.full[s], (kt / kTcStages) & 1)) { ok = false; break; }
-      tc_fence_after();
-      const uint64_t da = smem_desc(S.a[s]), db = smem_desc(S.b[s]);
-#pragma unroll
-      for (int kk = 0; kk < kTcK / 16; kk++)   // 16 bf16 = 32 bytes = 2 descriptor units
-        tc_mma(tmem, da + 2 * kk, db + 2 * kk, (kt | kk) ? 1u : 0u);
-      tc_commit(&S.empty[s]);
-    }
-    tc_commit(&S.done);   // arrives when every MMA issued above has completed
-  }
-  __syncwarp();
-  // warp-uniform: tcgen05.ld below is a warp-collective instruction
-  const bool got = __all_sync(0xffffffffu, mbar_wait(&S.done, 0));
-  tc_fence_after();
-  if (got) {
-    float v[32];
-    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-#pragma unroll 1
-    for (int c = 0; c < kTcN; c += 32) {
-      tmem_ld32(tmem + lane_base + (uint32_t)c, v);
-      epi(m0 + warp * 32 + lane, n0 + c, v);
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)kTcN)
-                 : "memory");
-  if ((!ok || !got) && err) atomicExch(err, 1);
-}
-
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static std::mutex mu;
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  std::lock_guard<std::mutex> lk(mu);
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    else
-      cudaGetLastError();
-  }
-  return fn;
-}
-
-// K-major bf16 operand of `rows` x K as a TMA map with 64 x 128 boxes.
-int encode_operand(CUtensorMap* map, const void* base, int rows, int K) {
-  auto fn = encode_fn();
-  if (!fn) { set_error("cuTensorMapEncodeTiled is not available"); return GPL_ERR_CUDA; }
-  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM};
-  const cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed"); return GPL_ERR_CUDA; }
-  return GPL_OK;
-}
-
-template <class Epi>
-int launch_tc_gemm(const void* a, const void* b, int M, int N, int K, const Epi& epi, int* err,
-                   cudaStream_t s) {
-  if (M <= 0 || N <= 0 || K <= 0 || M % kTcM || N % kTcN || K % kTcK) {
-    set_error("tensor-core GEMM: M and N must be multiples of 128 and K of 64");
-    return GPL_ERR_INVALID_ARG;
-  }
-  if ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) {
-    set_error("tensor-core GEMM: operands must be 16-byte aligned");
-    return GPL_ERR_INVALID_ARG;
-  }
-  CUtensorMap ta, tb;
-  int rc = encode_operand(&ta, a, M, K);
-  if (!rc) rc = encode_operand(&tb, b, N, K);
-  if (rc) return rc;
-  GPL_CUDA(cudaFuncSetAttribute(k_tc_gemm<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemBytes));
-  k_tc_gemm<Epi><<<dim3(N / kTcN, M / kTcM), kTcThreads, kTcSmemBytes, s>>>(ta, tb, K, epi, err);
-  GPL_CUDA(cudaGetLastError());
-  return GPL_OK;
-}
-
 }  // namespace
-
 }  // namespace gpl
 
 using namespace gpl;
@@ -293,5 +25,8 @@ extern "C" gpl_status gpl_tc_gemm_bf16(const void* a, const void* b, float* d, i
                                        int32_t* error_flag, void* stream) {
   if (!a || !b || !d) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
   EpiStore e{d, n};
-  return (gpl_status)launch_tc_gemm(a, b, m, n, k, e, error_flag, (cudaStream_t)stream);
+  // a 64-wide N tile where a 128-wide one would leave SMs idle
+  if (n % 128 == 0 && (int64_t)(m / 128) * (n / 128) >= 148)
+    return (gpl_status)tc::launch_tc_gemm<128>(a, k, b, k, m, n, k, e, error_flag, (cudaStream_t)stream);
+  return (gpl_status)tc::launch_tc_gemm<64>(a, k, b, k, m, n, k, e, error_flag, (cudaStream_t)stream);
 }

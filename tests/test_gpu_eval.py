@@ -105,3 +105,31 @@ def test_poisson_solve_matches_fp64(gpu_lib, oracle_mod, nx, ny):
     assert rel_l2(phi.cpu().numpy(), p64) < 1e-5
     assert rel_l2(fx.cpu().numpy(), x64) < 1e-5
     assert rel_l2(fy.cpu().numpy(), y64) < 1e-5
+
+
+def test_eval_parity_tensor_core_poisson(gpu_lib, oracle_mod):
+    """The Poisson solve as tensor-core GEMMs (bf16 three-term split): bin
+    areas, density and HPWL are untouched and bit-exact; potential, field and
+    density gradient are within the split's error (about 1e-5 of the
+    field; bar 2e-4 relative L2)."""
+    from replace_gb300 import Placer
+    nl, opts = case("syn10k_b128")
+    ref = golden("eval_syn10k_b128.npz")
+    p = Placer(nl, **params_of(opts), poisson_path=2)
+    p.initial_place()
+    o = oracle_mod.Oracle(nl, **params_of(opts))
+    o.initial_place()
+    o.nesterov_base()
+    wlc = float(ref["fscalars"][1])
+    wl, dg, st = p.eval(ref["coords"], wlc)
+    owl, odg, ost, _ = o.eval(ref["coords"], wlc)
+    info = o.info
+    b = p.bins(info.bin_cnt_x, info.bin_cnt_y)
+    for k in ("inst_area", "filler_area", "nonplace_area", "density"):
+        assert np.array_equal(b[k], ref[k]), k
+    assert st.hpwl == ost.hpwl
+    assert rel_l2(wl, ref["wl_grad"]) < TOL
+    for k in ("phi", "ex", "ey"):
+        assert rel_l2(b[k], ref[k]) < 2e-4, (k, rel_l2(b[k], ref[k]))
+    assert rel_l2(dg, odg) < 2e-4
+    p.close()

@@ -94,3 +94,40 @@ def test_replace_api_global_placement(gpu_lib):
     assert abs(st.hpwl - int(ref["final_hpwl"])) <= 0.005 * int(ref["final_hpwl"])
     lx, ly = r.instLocations()
     assert lx.shape == (nl.n_insts,)
+
+
+def test_place_with_tensor_core_poisson(gpu_lib):
+    """The whole loop with the tensor-core Poisson solve meets the same bar
+    as the FFT form: final HPWL within 0.5 % of the reference, overflow at
+    target, iteration count within 15 %."""
+    from replace_gb300 import Placer
+    nl, opts = case("syn10k_b128")
+    ref = golden("place_syn10k_b128.npz")
+    p = Placer(nl, **params_of(opts), poisson_path=2)
+    p.initial_place()
+    p.nesterov_init()
+    assert p.info.poisson_path == 2
+    rc, st, lg = p.nesterov_run(0, log_capacity=4000)
+    assert rc == 0 and st.finished and st.overflow <= 0.1
+    assert abs(st.hpwl - int(ref["final_hpwl"])) <= 0.005 * int(ref["final_hpwl"])
+    its = ref["iters"]
+    assert abs(st.iterations - its[-1]) <= max(15, 0.15 * its[-1])
+    p.close()
+
+
+def test_poisson_form_autotuned_per_grid(gpu_lib):
+    from replace_gb300 import Placer
+    nl, opts = case("syn10k_b128")
+    p = Placer(nl, **params_of(opts))            # auto
+    p.initial_place()
+    p.nesterov_init()
+    info = p.info
+    assert info.poisson_path in (1, 2)
+    assert info.poisson_fft_us > 0 and info.poisson_gemm_us > 0
+    assert (info.poisson_path == 2) == (info.poisson_gemm_us < info.poisson_fft_us)
+    p.close()
+    q = Placer(nl, **params_of(opts), poisson_path=1)
+    q.initial_place()
+    q.nesterov_init()
+    assert q.info.poisson_path == 1 and q.info.poisson_gemm_us == 0
+    q.close()
