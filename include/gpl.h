@@ -130,9 +130,10 @@ typedef struct gpl_params {
                                               2 = cooperative grid (same iterates as 1),
                                               3 = cluster per axis */
   int32_t poisson_path;                    /* Poisson solve: 0 = auto (times both forms on the job's
-                                              grid and keeps the faster), 1 = shared-memory FFT,
-                                              2 = tensor-core GEMMs (bf16 three-term split; grids
-                                              with both counts multiples of 128) */
+                                              grid and keeps the faster; the GEMM form only up to
+                                              512 bins per axis, for precision), 1 = shared-memory
+                                              FFT, 2 = tensor-core GEMMs (bf16 three-term split;
+                                              grids with both counts multiples of 128) */
 } gpl_params;
 
 /* Counts and grid chosen by the job (NesterovBase / BinGrid). */

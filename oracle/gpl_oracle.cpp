@@ -1170,6 +1170,7 @@ int orc_get_gcells(void* h, int32_t* drect, float* scale, uint8_t* kind) {
 
 int orc_get_gcell_coords(void* h, float* xy) {
   Oracle* o = (Oracle*)h;
+  if ((int)o->curSLP.size() < o->nG) return GPL_ERR_BAD_STATE;   // before nesterov_init
   for (int g = 0; g < o->nG; g++) { xy[2 * g] = o->curSLP[g].x; xy[2 * g + 1] = o->curSLP[g].y; }
   return GPL_OK;
 }
