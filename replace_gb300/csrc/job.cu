@@ -106,6 +106,10 @@ struct gpl_job {
   long long graph_kernels = 0;
   float poisson_fft_us = 0.0f, poisson_gemm_us = 0.0f;   // auto mode's timings
   bool poisson_chosen = false;
+  // WA runs beside the Poisson passes on a second stream (fork after the
+  // scatter, join before the gcell kernel)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -177,6 +181,11 @@ int ensure_nb(gpl_job* j) {
   HostModel& m = j->m;
   DeviceModel& d = j->d;
   GPL_CUDA(cudaSetDevice(j->device));
+  if (!j->side) {
+    GPL_CUDA(cudaStreamCreateWithFlags(&j->side, cudaStreamNonBlocking));
+    GPL_CUDA(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
+    GPL_CUDA(cudaEventCreateWithFlags(&j->ev_join, cudaEventDisableTiming));
+  }
   d.n_g = m.n_g; d.n_place = m.n_place; d.n_pins = m.n_pins; d.n_nets = m.n_nets;
   d.cnt_x = m.cnt_x; d.cnt_y = m.cnt_y; d.size_x = m.size_x; d.size_y = m.size_y;
   d.core_lx = m.core_lx; d.core_ly = m.core_ly; d.core_ux = m.core_ux; d.core_uy = m.core_uy;
@@ -350,20 +359,44 @@ int put_ctl(gpl_job* j, const EvalCtl& c) {
   return GPL_OK;
 }
 
-// Phase 1 of an evaluation: (predictor +) density scatter, then the Poisson
-// solve -- updateGCellDensityCenterLocation + updateDensityForceBin.
-int launch_phase1(gpl_job* j, bool want_phi) {
-  int rc = launch_scatter(j->d, base_args(j), j->stream, j->timer);
-  if (rc) return rc;
-  return launch_poisson_job(j->d, want_phi, j->stream, j->timer);
-}
-
-// Phase 2: WA forces, per-gcell gradients and reductions (the gcell kernel's
-// last block writes the result record), then the record's copy to the host.
+// WA forces, per-gcell gradients and reductions again (the gcell kernel's
+// last block writes the result record), then the record's copy to the host:
+// a second pass over the same coordinates and bins with new coefficients.
 int launch_phase2(gpl_job* j, bool want_phi, int area_set) {
   DeviceModel& d = j->d;
   int rc = launch_wa(d, base_args(j), j->stream, j->timer);
   if (rc) return rc;
+  int phi_blocks = 0;
+  if (want_phi) {
+    rc = launch_sum_phi(d, area_set, j->stream, j->timer, &phi_blocks);
+    if (rc) return rc;
+  }
+  rc = launch_cell(d, base_args(j), phi_blocks, j->stream, j->timer);
+  if (rc) return rc;
+  GPL_CUDA(cudaMemcpyAsync(d.result_h, d.result, sizeof(EvalResult), cudaMemcpyDeviceToHost, j->stream));
+  return GPL_OK;
+}
+
+// One evaluation's launches: scatter (with the predictor), then the WA
+// kernel on the side stream beside the Poisson passes (WA needs only the
+// predicted coordinates, Poisson only the areas), joined before the gcell
+// kernel, and the result record's copy to the host.  With kernel timing on,
+// everything stays on the job's stream so that each class is timed alone.
+int launch_eval(gpl_job* j, bool want_phi, int area_set) {
+  DeviceModel& d = j->d;
+  int rc = launch_scatter(d, base_args(j), j->stream, j->timer);
+  if (rc) return rc;
+  const bool fork = j->side && !j->timer.enabled;
+  if (fork) {
+    GPL_CUDA(cudaEventRecord(j->ev_fork, j->stream));
+    GPL_CUDA(cudaStreamWaitEvent(j->side, j->ev_fork, 0));
+  }
+  rc = launch_wa(d, base_args(j), fork ? j->side : j->stream, j->timer);
+  if (rc) return rc;
+  if (fork) GPL_CUDA(cudaEventRecord(j->ev_join, j->side));
+  rc = launch_poisson_job(d, want_phi, j->stream, j->timer);
+  if (rc) return rc;
+  if (fork) GPL_CUDA(cudaStreamWaitEvent(j->stream, j->ev_join, 0));
   int phi_blocks = 0;
   if (want_phi) {
     rc = launch_sum_phi(d, area_set, j->stream, j->timer, &phi_blocks);
@@ -463,8 +496,7 @@ int build_graph(gpl_job* j) {
     return GPL_OK;                       // stream cannot be captured: direct launches
   }
   cudaMemcpyAsync(j->d.ctl, j->d.ctl_h, sizeof(EvalCtl), cudaMemcpyHostToDevice, j->stream);
-  rc = launch_phase1(j, false);
-  if (!rc) rc = launch_phase2(j, false, 0);
+  rc = launch_eval(j, false, 0);
   cudaError_t e = cudaStreamEndCapture(j->stream, &g);
   j->graph_kernels = j->timer.kernels - k0;
   j->timer.kernels = k0;
@@ -492,8 +524,7 @@ int evaluate(gpl_job* j, EvalCtl c, bool want_phi) {
     j->timer.count((int)j->graph_kernels);
   } else {
     rc = put_ctl(j, c);
-    if (!rc) rc = launch_phase1(j, want_phi);
-    if (!rc) rc = launch_phase2(j, want_phi, c.area_cur);
+    if (!rc) rc = launch_eval(j, want_phi, c.area_cur);
   }
   if (rc) return rc;
   j->last_area = c.area_cur;
@@ -876,6 +907,12 @@ void gpl_destroy(gpl_job* j) {
   if (j->d.pg) poisson_gemm_free(j->d.pg, j->pool, j->stream);
   if (j->arena) dev_free(j->arena, j->pool, j->stream);
   if (j->own_pinned && j->pinned) cudaFreeHost(j->pinned);
+  if (j->side) {
+    cudaStreamSynchronize(j->side);
+    cudaStreamDestroy(j->side);
+  }
+  if (j->ev_fork) cudaEventDestroy(j->ev_fork);
+  if (j->ev_join) cudaEventDestroy(j->ev_join);
   if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
   delete j;
 }
