@@ -22,7 +22,8 @@ namespace gpl {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kBigBins = 64;        // cells covering more bins go to the big-cell kernels
+constexpr int kBigBins = 64;
+constexpr int kCellBlocksPerSm = 5;   // the gcell kernel's residency (48 registers)        // cells covering more bins go to the big-cell kernels
 
 struct ScatterArgs {
   BinGeom geo;
@@ -305,7 +306,7 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
 // block partial sums are reduced by the last block to finish (threadfence +
 // counter), in a fixed order, so there is no separate reduction launch and
 // the result is the same run to run.
-__global__ void __launch_bounds__(kBlock, 4) k_cell(CellArgs A) {
+__global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
   __shared__ double sh[32 * kPartSlots];
   __shared__ bool last;
   // per-thread sums in float over the thread's few gcells; FP64 from the
@@ -545,10 +546,10 @@ int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t) {
   return GPL_OK;
 }
 
-// The gcell kernel's grid-stride loop runs on one wave of resident blocks (4
-// per SM at its register count), so its last-block reduction waits for no
-// second wave.
-int cell_grid(const DeviceModel& d) { return std::max(1, std::min(cell_blocks(d), d.sm_count * 4)); }
+// The gcell kernel's grid-stride loop runs on one wave of resident blocks
+// (kCellBlocksPerSm per SM at its register count), so its last-block
+// reduction waits for no second wave.
+int cell_grid(const DeviceModel& d) { return std::max(1, std::min(cell_blocks(d), d.sm_count * kCellBlocksPerSm)); }
 
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t) {
   CellArgs A;

@@ -343,7 +343,7 @@ int ensure_nb(gpl_job* j) {
 }
 
 // Iterations between refreshes of the scatter's tile order.
-constexpr int kTileOrderEvery = 16;
+constexpr int kTileOrderEvery = 32;
 
 EvalArgs base_args(gpl_job* j) {
   EvalArgs a;
