@@ -315,28 +315,40 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
   int bad = 0;
   const BinGeom& G = A.geo;
   const EvalCtl C = *A.ctl;
-  const float2* slp = pick4(A.slp, C.i_eval);
-  float2* sum_out = C.write_sum ? pick4(A.sum, C.i_eval) : nullptr;
-  const float2* ref_slp = C.i_ref >= 0 ? pick4(A.slp, C.i_ref) : nullptr;
-  const float2* ref_sum = C.i_ref >= 0 ? pick4(A.sum, C.i_ref) : nullptr;
-  float2* wl_out = C.write_wd ? A.wl_out : nullptr;
-  float2* d_out = C.write_wd ? A.d_out : nullptr;
+  // restrict-qualified views (inputs and outputs are distinct arrays), so
+  // the loads of a thread's next gcell can be issued before the stores of
+  // its previous one
+  const float2* __restrict__ slp = pick4(A.slp, C.i_eval);
+  float2* __restrict__ sum_out = C.write_sum ? pick4(A.sum, C.i_eval) : nullptr;
+  const float2* __restrict__ ref_slp = C.i_ref >= 0 ? pick4(A.slp, C.i_ref) : nullptr;
+  const float2* __restrict__ ref_sum = C.i_ref >= 0 ? pick4(A.sum, C.i_ref) : nullptr;
+  float2* __restrict__ wl_out = C.write_wd ? A.wl_out : nullptr;
+  float2* __restrict__ d_out = C.write_wd ? A.d_out : nullptr;
+  const float2* __restrict__ pin_grad = A.pin_grad;
+  const int32_t* __restrict__ g_pins = A.g_pins;
+  const int32_t* __restrict__ g_pin_start = A.g_pin_start;
+  const float2* __restrict__ field = A.field;
+  const int2* __restrict__ half = A.half;
+  const uint8_t* __restrict__ kind = A.kind;
+  const float* __restrict__ scale = A.scale;
+  const float2* __restrict__ precond = A.precond;
   const float lam = C.density_penalty;
   const int lane = threadIdx.x & 31;
   // warp-uniform grid-stride loop: the warps gather the pins of cells with
   // more than 32 pins (macros) together
+#pragma unroll 2
   for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < A.n_g; base += gridDim.x * kBlock) {
     const int g = base + lane;
     const bool valid = g < A.n_g;
     int ps = 0, pe = 0;
     float2 w = make_float2(0.0f, 0.0f);
     if (valid) {
-      ps = A.g_pin_start[g];
-      pe = A.g_pin_start[g + 1];
+      ps = g_pin_start[g];
+      pe = g_pin_start[g + 1];
       if (pe - ps <= 32) {
         // WA gradient: the cell's pins in instance pin order
         for (int t = ps; t < pe; t++) {
-          const float2 pg = A.pin_grad[A.g_pins[t]];
+          const float2 pg = pin_grad[g_pins[t]];
           w.x = __fadd_rn(w.x, pg.x);
           w.y = __fadd_rn(w.y, pg.y);
         }
@@ -349,7 +361,7 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
       const int s0 = __shfl_sync(0xffffffffu, ps, src), s1 = __shfl_sync(0xffffffffu, pe, src);
       float2 part = make_float2(0.0f, 0.0f);
       for (int t = s0 + lane; t < s1; t += 32) {
-        const float2 pg = A.pin_grad[A.g_pins[t]];
+        const float2 pg = pin_grad[g_pins[t]];
         part.x = __fadd_rn(part.x, pg.x);
         part.y = __fadd_rn(part.y, pg.y);
       }
@@ -362,27 +374,27 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
     }
     if (!valid) continue;
     const float2 c = slp[g];
-    const int k = A.kind[g];
+    const int k = kind[g];
     // density gradient: sum over covered bins of overlap * scale * field
     float2 d = make_float2(0.0f, 0.0f);
     if (k & 4) {
       d = A.d_big[A.big_idx[g]];
     } else {
       int lx, ux, ly, uy, x0, x1, y0, y1;
-      density_rect(c, A.half[g], lx, ux, ly, uy);
+      density_rect(c, half[g], lx, ux, ly, uy);
       G.range(lx, ux, ly, uy, x0, x1, y0, y1);
-      const float sc = A.scale[g];
+      const float sc = scale[g];
       for (int a = x0; a < x1; a++) {
         for (int cc = y0; cc < y1; cc++) {
           const float ov = __fmul_rn(G.overlap(a, cc, lx, ux, ly, uy), sc);
-          const float2 f = A.field[cc * G.cnt_x + a];
+          const float2 f = field[cc * G.cnt_x + a];
           d.x = __fadd_rn(d.x, __fmul_rn(ov, f.x));
           d.y = __fadd_rn(d.y, __fmul_rn(ov, f.y));
         }
       }
     }
     float2 s = make_float2(__fadd_rn(w.x, __fmul_rn(lam, d.x)), __fadd_rn(w.y, __fmul_rn(lam, d.y)));
-    const float2 pc = A.precond[g];
+    const float2 pc = precond[g];
     float px = __fadd_rn(pc.x, __fmul_rn(lam, pc.y));
     float py = px;
     if (px <= A.min_precond) px = A.min_precond;
