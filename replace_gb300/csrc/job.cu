@@ -214,18 +214,27 @@ int ensure_nb(gpl_job* j) {
   // WA buckets by degree: group widths 2, 4, 8, 16, 32 lanes, then a warp per net
   std::vector<int32_t> net_order;
   {
-    std::vector<std::vector<int32_t>> bk(kWaBuckets);
-    std::vector<int32_t> key(m.n_nets, INT32_MAX);   // lowest gcell index on the net
+    // key = lowest gcell index on the net (ng for nets without a movable
+    // pin); a stable counting sort by key, then a stable split by bucket,
+    // orders each bucket by key with ties in net order
+    std::vector<int32_t> key(m.n_nets), cnt(ng + 2, 0);
+    std::vector<uint8_t> bucket(m.n_nets);
     for (int n = 0; n < m.n_nets; n++) {
       const int deg = m.net_start[n + 1] - m.net_start[n];
       int b = 0;
       while (b < kWaBuckets - 1 && deg > (2 << b)) b++;
-      bk[b].push_back(n);
+      bucket[n] = (uint8_t)b;
+      int k = (int)ng;
       for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++)
-        if (m.pin_g[q] >= 0) key[n] = std::min(key[n], m.pin_g[q]);
+        if (m.pin_g[q] >= 0) k = std::min(k, m.pin_g[q]);
+      key[n] = k;
+      cnt[k + 1]++;
     }
-    for (auto& v : bk)
-      std::stable_sort(v.begin(), v.end(), [&](int a, int b2) { return key[a] < key[b2]; });
+    for (size_t k = 0; k <= ng; k++) cnt[k + 1] += cnt[k];
+    std::vector<int32_t> by_key(m.n_nets);
+    for (int n = 0; n < m.n_nets; n++) by_key[cnt[key[n]]++] = n;
+    std::vector<std::vector<int32_t>> bk(kWaBuckets);
+    for (int n : by_key) bk[bucket[n]].push_back(n);
     net_order.reserve(m.n_nets);
     d.wa_bucket_start[0] = 0;
     d.wa_block_start[0] = 0;
@@ -456,11 +465,15 @@ int choose_poisson_path(gpl_job* j) {
     cudaGetLastError();
     return GPL_OK;                 // auto: the FFT form
   }
-  if (want == 2) { d.poisson_path = 2; return GPL_OK; }
   EvalCtl c;
   memset(&c, 0, sizeof(c));
   rc = put_ctl(j, c);
   if (rc) return rc;
+  if (want == 2) {
+    d.poisson_path = 2;
+    j->poisson_gemm_us = time_poisson(j, 5);
+    return GPL_OK;
+  }
   j->poisson_fft_us = time_poisson(j, 5);
   d.poisson_path = 2;
   j->poisson_gemm_us = time_poisson(j, 5);

@@ -67,12 +67,21 @@ int build_placer_base(HostModel& m, const gpl_netlist_desc* d, const gpl_params*
     int np = m.inst_pin_start[m.n_insts];
     if (np < 0 || np > m.n_pins) { set_error("inst_pin_start out of range"); return GPL_ERR_INVALID_ARG; }
     m.inst_pins.assign(d->inst_pins, d->inst_pins + np);
+    // every instance pin listed exactly once, under its own instance
+    std::vector<uint64_t> seen(((size_t)m.n_pins + 63) / 64, 0);
     for (int i = 0; i < m.n_insts; i++) {
+      if (m.inst_pin_start[i + 1] < m.inst_pin_start[i]) { set_error("inst_pin_start not monotone"); return GPL_ERR_INVALID_ARG; }
       for (int k = m.inst_pin_start[i]; k < m.inst_pin_start[i + 1]; k++) {
         int q = m.inst_pins[k];
         if (q < 0 || q >= m.n_pins || m.pin_inst[q] != i) { set_error("inst_pins inconsistent with pin_inst"); return GPL_ERR_INVALID_ARG; }
+        const uint64_t bit = 1ull << (q & 63);
+        if (seen[q >> 6] & bit) { set_error("inst_pins lists a pin twice"); return GPL_ERR_INVALID_ARG; }
+        seen[q >> 6] |= bit;
       }
     }
+    int64_t inst_owned = 0;
+    for (int q = 0; q < m.n_pins; q++) inst_owned += m.pin_inst[q] >= 0;
+    if (inst_owned != np) { set_error("inst_pins must list every pin of every instance"); return GPL_ERR_INVALID_ARG; }
   } else {
     m.inst_pin_start.assign(m.n_insts + 1, 0);
     for (int q = 0; q < m.n_pins; q++) if (m.pin_inst[q] >= 0) m.inst_pin_start[m.pin_inst[q] + 1]++;
@@ -148,13 +157,20 @@ int nb_counts(const HostModel& m, NbCounts* c) {
     std::vector<int> dxs, dys;
     dxs.reserve(n_place); dys.reserve(n_place);
     for (int i : m.place_insts) { dxs.push_back(m.iux[i] - m.ilx[i]); dys.push_back(m.iuy[i] - m.ily[i]); }
-    std::sort(dxs.begin(), dxs.end());
-    std::sort(dys.begin(), dys.end());
     int min_idx = (int)(dxs.size() * 0.05);
     int max_idx = (int)(dxs.size() * 0.95);
-    int64_t dx_sum = 0, dy_sum = 0;
-    for (int k = min_idx; k < max_idx; k++) { dx_sum += dxs[k]; dy_sum += dys[k]; }
     if (max_idx <= min_idx) { set_error("too few movable instances for the filler size"); return GPL_ERR_INVALID_ARG; }
+    // The reference sums ranks [min_idx, max_idx) of the sorted sizes.  Two
+    // selections put exactly those ranks' values into [min_idx, max_idx)
+    // (in some order), so the sum is the same without a full sort.
+    auto mid_sum = [&](std::vector<int>& v) {
+      std::nth_element(v.begin(), v.begin() + min_idx, v.end());
+      std::nth_element(v.begin() + min_idx, v.begin() + max_idx, v.end());
+      int64_t s = 0;
+      for (int k = min_idx; k < max_idx; k++) s += v[k];
+      return s;
+    };
+    const int64_t dx_sum = mid_sum(dxs), dy_sum = mid_sum(dys);
     c->fill_dx = (int)(dx_sum / (max_idx - min_idx));
     c->fill_dy = (int)(dy_sum / (max_idx - min_idx));
     int64_t core_area = (int64_t)(m.core_ux - m.core_lx) * (int64_t)(m.core_uy - m.core_ly);
@@ -228,17 +244,30 @@ int build_nesterov_base(HostModel& m) {
     m.n_fill = cnt;
   }
   m.n_g = (int)m.glx.size();
-  // gcell -> pins in instance pin order; pin -> gcell
+  // gcell -> pins in instance pin order; pin -> gcell (inst_pins lists
+  // every pin of an instance exactly once, checked by build_placer_base)
   m.g_pin_start.assign(m.n_g + 1, 0);
-  m.pin_g.assign(m.n_pins, -1);
   m.g_pins.clear();
-  for (int k = 0; k < m.n_place; k++) {
-    int i = m.place_insts[k];
-    for (int t = m.inst_pin_start[i]; t < m.inst_pin_start[i + 1]; t++) {
-      m.g_pins.push_back(m.inst_pins[t]);
-      m.pin_g[m.inst_pins[t]] = k;
+  {
+    std::vector<int32_t> g_of_inst(m.n_insts, -1);
+    size_t total = 0;
+    for (int k = 0; k < m.n_place; k++) {
+      const int i = m.place_insts[k];
+      g_of_inst[i] = k;
+      total += m.inst_pin_start[i + 1] - m.inst_pin_start[i];
     }
-    m.g_pin_start[k + 1] = (int)m.g_pins.size();
+    m.g_pins.reserve(total);
+    for (int k = 0; k < m.n_place; k++) {
+      const int i = m.place_insts[k];
+      m.g_pins.insert(m.g_pins.end(), m.inst_pins.begin() + m.inst_pin_start[i],
+                      m.inst_pins.begin() + m.inst_pin_start[i + 1]);
+      m.g_pin_start[k + 1] = (int)m.g_pins.size();
+    }
+    m.pin_g.resize(m.n_pins);
+    for (int q = 0; q < m.n_pins; q++) {
+      const int i = m.pin_inst[q];
+      m.pin_g[q] = i >= 0 ? g_of_inst[i] : -1;
+    }
   }
   for (int k = m.n_place; k < m.n_g; k++) m.g_pin_start[k + 1] = m.g_pin_start[k];
 
@@ -274,16 +303,23 @@ int build_nesterov_base(HostModel& m) {
   // and the size are evaluated in long double as in the reference
   m.gdlx = m.glx; m.gdly = m.gly; m.gdux = m.gux; m.gduy = m.guy;
   m.gscale.assign(m.n_g, 0.0f);
+  // The long double terms depend on the bin size only, so they are formed
+  // once (long double is a software type on some hosts).  For an integer d,
+  // d < sqrt2 * size  <=>  d < ceil(sqrt2 * size).
+  const long double thx = kSqrt2 * m.size_x, thy = kSqrt2 * m.size_y;
+  const int64_t lim_x = (int64_t)ceill(thx), lim_y = (int64_t)ceill(thy);
+  const float den_x = (float)thx, den_y = (float)thy;
+  const float small_dsx = (float)(kSqrt2 * (float)m.size_x), small_dsy = (float)(kSqrt2 * (float)m.size_y);
   for (int g = 0; g < m.n_g; g++) {
     int dx = m.gux[g] - m.glx[g], dy = m.guy[g] - m.gly[g];
     float sx, sy, dsx, dsy;
-    if (dx < kSqrt2 * m.size_x) {
-      sx = (float)dx / (float)(kSqrt2 * m.size_x);
-      dsx = (float)(kSqrt2 * (float)m.size_x);
+    if (dx < lim_x) {
+      sx = (float)dx / den_x;
+      dsx = small_dsx;
     } else { sx = 1.0f; dsx = (float)dx; }
-    if (dy < kSqrt2 * m.size_y) {
-      sy = (float)dy / (float)(kSqrt2 * m.size_y);
-      dsy = (float)(kSqrt2 * (float)m.size_y);
+    if (dy < lim_y) {
+      sy = (float)dy / den_y;
+      dsy = small_dsy;
     } else { sy = 1.0f; dsy = (float)dy; }
     int ddx = (int)dsx, ddy = (int)dsy;   // GCell::setDensitySize(int, int)
     int cx = (m.gdux[g] + m.gdlx[g]) / 2, cy = (m.gduy[g] + m.gdly[g]) / 2;

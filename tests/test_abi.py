@@ -63,6 +63,29 @@ def test_invalid_netlists_are_rejected_before_any_device_work():
     assert rc == _abi.GPL_ERR_UTIL
 
 
+def test_instance_pin_lists_must_cover_each_pin_once():
+    """inst_pins (the instance pin order) must list every pin of every
+    instance exactly once: a repeated or a missing pin is rejected."""
+    from replace_gb300 import load
+    lib = load()
+    nl = N.generate(200, 210, n_io=5, seed=1)
+    s, e = int(nl.inst_pin_start[3]), int(nl.inst_pin_start[4])
+    assert e - s >= 2
+    dup = nl.copy()
+    dup.inst_pins = dup.inst_pins.copy()
+    dup.inst_pins[s + 1] = dup.inst_pins[s]               # one pin twice, one missing
+    short = nl.copy()
+    short.inst_pin_start = short.inst_pin_start.copy()
+    short.inst_pins = np.delete(short.inst_pins, s)       # one pin missing
+    short.inst_pin_start[4:] -= 1
+    for net, msg in ((dup, b"twice"), (short, b"every pin")):
+        h = _abi.DescHolder(net)
+        job = C.c_void_p()
+        rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job))
+        assert rc == _abi.GPL_ERR_INVALID_ARG
+        assert msg in lib.gpl_last_error()
+
+
 def test_no_device_fails_loudly():
     import torch
     if torch.cuda.is_available():
