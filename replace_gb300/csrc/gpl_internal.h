@@ -56,7 +56,18 @@ struct NbCounts {
   int fill_dx = 0, fill_dy = 0, n_fill = 0;
   int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
 };
-int nb_counts(const HostModel& m, NbCounts* c);
+// the movable instances' rectangles (in place_insts order)
+struct PlaceRects {
+  std::vector<int32_t> lx, ly, ux, uy;
+};
+PlaceRects place_rects(const HostModel& m);
+// rects: the movable instances' rectangles to use (default: the model's)
+int nb_counts(const HostModel& m, NbCounts* c, const PlaceRects* rects = nullptr);
+// NesterovBase in two parts: the position-independent part (may run beside
+// an initial place, from a copy of the movable rectangles), then the movable
+// gcells at the instances' current positions
+int build_nesterov_static(HostModel& m, const PlaceRects& rects);
+void place_gcells(HostModel& m);
 int build_nesterov_base(HostModel& m);
 // InitialPlace::placeInstsCenter + Instance::setCenterLocation
 void host_place_center(HostModel& m);
@@ -301,8 +312,9 @@ int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out);
 void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t pool,
               cudaEvent_t sync_ev);
 // Upper bound of the device bytes the job will hold at once (initial place
-// scratch or the Nesterov arena, whichever is larger).
-int job_device_bytes(gpl_job* j, int64_t* bytes);
+// scratch or the Nesterov arena, whichever is larger).  centred: the job's
+// movable instances will be centred first (InitialPlace::placeInstsCenter).
+int job_device_bytes(gpl_job* j, int64_t* bytes, bool centred);
 
 // twiddle / frequency tables (host computed, double precision)
 void make_twiddle(std::vector<float2>& tw);

@@ -9,11 +9,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gpl_internal.h"
@@ -77,6 +81,20 @@ int launch_initial_prev(DeviceModel& d, const float2* cur_slp, const float2* cur
 
 using namespace gpl;
 
+// Host arrays of a job's device model (see stage_device_model).
+struct DevStage {
+  std::vector<int2> half;
+  std::vector<uint8_t> kind;
+  std::vector<float2> precond;
+  std::vector<int32_t> big, big_idx;
+  std::vector<int4> pins;
+  std::vector<int32_t> dnet_start, g_dpins;
+  std::vector<float2> tw, w4x, w4y;
+  std::vector<float> wx, wy;
+  int wa_bucket_start[kWaBuckets + 1] = {0};
+  int wa_block_start[kWaBuckets + 1] = {0};
+};
+
 struct gpl_job {
   HostModel m;
   DeviceModel d;
@@ -110,6 +128,12 @@ struct gpl_job {
   // scatter, join before the gcell kernel)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // position-independent Nesterov setup, built beside the initial place
+  std::thread prep;
+  std::unique_ptr<DevStage> stage;
+  int prep_rc = 0;
+  std::string prep_err;
+  bool static_done = false;
 };
 
 namespace {
@@ -118,6 +142,11 @@ int upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
   if (!bytes) return GPL_OK;
   GPL_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
   return GPL_OK;
+}
+
+// wall clock in ms (verbose_level >= 2 timings)
+double wall_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
 int check_device(int dev) {
@@ -173,44 +202,29 @@ size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size
   return S.bytes;
 }
 
-// NesterovBase on the host, then the device model (one arena).
-int ensure_nb(gpl_job* j) {
-  if (j->nb_ready) return GPL_OK;
-  int rc = build_nesterov_base(j->m);
-  if (rc) return rc;
-  HostModel& m = j->m;
-  DeviceModel& d = j->d;
-  GPL_CUDA(cudaSetDevice(j->device));
-  if (!j->side) {
-    GPL_CUDA(cudaStreamCreateWithFlags(&j->side, cudaStreamNonBlocking));
-    GPL_CUDA(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
-    GPL_CUDA(cudaEventCreateWithFlags(&j->ev_join, cudaEventDisableTiming));
-  }
-  d.n_g = m.n_g; d.n_place = m.n_place; d.n_pins = m.n_pins; d.n_nets = m.n_nets;
-  d.cnt_x = m.cnt_x; d.cnt_y = m.cnt_y; d.size_x = m.size_x; d.size_y = m.size_y;
-  d.core_lx = m.core_lx; d.core_ly = m.core_ly; d.core_ux = m.core_ux; d.core_uy = m.core_uy;
-  d.target_density = m.p.target_density;
-  const size_t nb = (size_t)m.cnt_x * m.cnt_y;
+// The device model's host arrays: everything but the movable gcells'
+// positions, so that it can be built beside the initial place.
+int stage_device_model(const HostModel& m, DevStage& st) {
   const size_t ng = m.n_g;
-  std::vector<int2> half(ng);
-  std::vector<uint8_t> kind(ng);
-  std::vector<float2> precond(ng);
-  std::vector<int32_t> big, big_idx(ng, -1);
+  st.half.resize(ng);
+  st.kind.resize(ng);
+  st.precond.resize(ng);
+  st.big.clear();
+  st.big_idx.assign(ng, -1);
   for (size_t g = 0; g < ng; g++) {
-    half[g] = make_int2((m.gdux[g] - m.gdlx[g]) / 2, (m.gduy[g] - m.gdly[g]) / 2);
-    kind[g] = m.gkind[g];
+    st.half[g] = make_int2((m.gdux[g] - m.gdlx[g]) / 2, (m.gduy[g] - m.gdly[g]) / 2);
+    st.kind[g] = m.gkind[g];
     // bins a cell can touch per axis: its extent in bins plus one for a straddle
-    const long long bx = (2LL * half[g].x) / m.size_x + 2, by = (2LL * half[g].y) / m.size_y + 2;
+    const long long bx = (2LL * st.half[g].x) / m.size_x + 2, by = (2LL * st.half[g].y) / m.size_y + 2;
     if (bx * by > 64) {
-      kind[g] |= 4;
-      big_idx[g] = (int)big.size();
-      big.push_back((int)g);
+      st.kind[g] |= 4;
+      st.big_idx[g] = (int)st.big.size();
+      st.big.push_back((int)g);
     }
     // getWireLengthPreconditioner / getDensityPreconditioner (src/nesterovBase.cpp:1442-1454)
-    precond[g] = make_float2((float)(m.g_pin_start[g + 1] - m.g_pin_start[g]),
-                             (float)(m.gux[g] - m.glx[g]) * (float)(m.guy[g] - m.gly[g]));
+    st.precond[g] = make_float2((float)(m.g_pin_start[g + 1] - m.g_pin_start[g]),
+                                (float)(m.gux[g] - m.glx[g]) * (float)(m.guy[g] - m.gly[g]));
   }
-  d.n_big = (int)big.size();
   // WA buckets by degree: group widths 2, 4, 8, 16, 32 lanes, then a warp per net
   std::vector<int32_t> net_order;
   {
@@ -236,47 +250,128 @@ int ensure_nb(gpl_job* j) {
     std::vector<std::vector<int32_t>> bk(kWaBuckets);
     for (int n : by_key) bk[bucket[n]].push_back(n);
     net_order.reserve(m.n_nets);
-    d.wa_bucket_start[0] = 0;
-    d.wa_block_start[0] = 0;
+    st.wa_bucket_start[0] = 0;
+    st.wa_block_start[0] = 0;
     for (int b = 0; b < kWaBuckets; b++) {
       net_order.insert(net_order.end(), bk[b].begin(), bk[b].end());
-      d.wa_bucket_start[b + 1] = (int)net_order.size();
+      st.wa_bucket_start[b + 1] = (int)net_order.size();
       const int per = wa_nets_per_block(b);
-      d.wa_block_start[b + 1] = d.wa_block_start[b] + ((int)bk[b].size() + per - 1) / per;
+      st.wa_block_start[b + 1] = st.wa_block_start[b] + ((int)bk[b].size() + per - 1) / per;
     }
   }
   // device pin numbering: the bucket-ordered nets' pins, contiguous per net
+  // (the pins are visited in host order, each net written at its rank's slot)
   std::vector<int32_t> dpin_of(m.n_pins, -1);
-  std::vector<int4> pins(m.n_pins);
-  std::vector<int32_t> dnet_start(m.n_nets + 1, 0);
+  std::vector<int4>& pins = st.pins;
+  std::vector<int32_t>& dnet_start = st.dnet_start;
+  pins.resize(m.n_pins);
+  dnet_start.assign(m.n_nets + 1, 0);
   {
+    std::vector<int32_t> rank(m.n_nets);
     int w = 0;
     for (int k = 0; k < m.n_nets; k++) {
       const int n = net_order[k];
+      rank[n] = k;
       dnet_start[k] = w;
-      for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++) {
-        const int g = m.pin_g[q];
-        dpin_of[q] = w;
-        pins[w++] = g >= 0 ? make_int4(g, m.pin_ox[q], m.pin_oy[q], 0)
-                           : make_int4(-1, m.pin_x[q], m.pin_y[q], 0);
-      }
+      w += m.net_start[n + 1] - m.net_start[n];
     }
     dnet_start[m.n_nets] = w;
+    for (int n = 0; n < m.n_nets; n++) {
+      int t = dnet_start[rank[n]];
+      for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++, t++) {
+        const int g = m.pin_g[q];
+        dpin_of[q] = t;
+        pins[t] = g >= 0 ? make_int4(g, m.pin_ox[q], m.pin_oy[q], 0)
+                         : make_int4(-1, m.pin_x[q], m.pin_y[q], 0);
+      }
+    }
   }
-  std::vector<int32_t> g_dpins(m.g_pins.size());
-  for (size_t t = 0; t < m.g_pins.size(); t++) g_dpins[t] = dpin_of[m.g_pins[t]];
-  std::vector<float2> tw, w4x, w4y;
-  std::vector<float> wx, wy;
-  make_twiddle(tw);
-  make_w4(m.cnt_x, w4x);
-  make_w4(m.cnt_y, w4y);
-  make_freq(m.cnt_x, m.cnt_y, m.size_x, m.size_y, wx, wy);
+  st.g_dpins.resize(m.g_pins.size());
+  for (size_t t = 0; t < m.g_pins.size(); t++) st.g_dpins[t] = dpin_of[m.g_pins[t]];
+  make_twiddle(st.tw);
+  make_w4(m.cnt_x, st.w4x);
+  make_w4(m.cnt_y, st.w4y);
+  make_freq(m.cnt_x, m.cnt_y, m.size_x, m.size_y, st.wx, st.wy);
+  return GPL_OK;
+}
+
+// Runs the position-independent setup (NesterovBase and the device model's
+// host arrays); on a worker thread its error message is kept for the caller.
+void prepare_static(gpl_job* j, const PlaceRects& rects) {
+  int rc = GPL_OK;
+  try {
+    rc = build_nesterov_static(j->m, rects);
+    if (!rc) {
+      j->stage.reset(new DevStage());
+      rc = stage_device_model(j->m, *j->stage);
+    }
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed in the Nesterov setup");
+    rc = GPL_ERR_OUT_OF_MEMORY;
+  }
+  if (rc) j->prep_err = gpl_last_error();
+  j->prep_rc = rc;
+}
+
+// Starts the position-independent setup beside the initial place (the
+// movable instances' sizes are final once the initial place has centred
+// them; only their positions change).
+void start_static_prep(gpl_job* j) {
+  if (j->static_done || j->prep.joinable()) return;
+  PlaceRects rects = place_rects(j->m);
+  j->prep = std::thread([j, rects = std::move(rects)]() { prepare_static(j, rects); });
+}
+
+// Waits for (or runs) the position-independent setup.
+int finish_static_prep(gpl_job* j) {
+  if (j->static_done) return GPL_OK;
+  if (j->prep.joinable()) {
+    j->prep.join();
+  } else {
+    prepare_static(j, place_rects(j->m));
+  }
+  if (j->prep_rc) {
+    set_error(j->prep_err);
+    return j->prep_rc;
+  }
+  j->static_done = true;
+  return GPL_OK;
+}
+
+// NesterovBase, then the device model (one arena).
+int ensure_nb(gpl_job* j) {
+  if (j->nb_ready) return GPL_OK;
+  const double t0 = wall_ms();
+  int rc = finish_static_prep(j);
+  if (rc) return rc;
+  HostModel& m = j->m;
+  place_gcells(m);
+  if (m.p.verbose_level >= 2) printf("[NesterovInit] host NesterovBase (wait) %.2f ms\n", wall_ms() - t0);
+  DeviceModel& d = j->d;
+  const DevStage& st = *j->stage;
+  GPL_CUDA(cudaSetDevice(j->device));
+  if (!j->side) {
+    GPL_CUDA(cudaStreamCreateWithFlags(&j->side, cudaStreamNonBlocking));
+    GPL_CUDA(cudaEventCreateWithFlags(&j->ev_fork, cudaEventDisableTiming));
+    GPL_CUDA(cudaEventCreateWithFlags(&j->ev_join, cudaEventDisableTiming));
+  }
+  d.n_g = m.n_g; d.n_place = m.n_place; d.n_pins = m.n_pins; d.n_nets = m.n_nets;
+  d.cnt_x = m.cnt_x; d.cnt_y = m.cnt_y; d.size_x = m.size_x; d.size_y = m.size_y;
+  d.core_lx = m.core_lx; d.core_ly = m.core_ly; d.core_ux = m.core_ux; d.core_uy = m.core_uy;
+  d.target_density = m.p.target_density;
+  d.n_big = (int)st.big.size();
+  for (int b = 0; b <= kWaBuckets; b++) {
+    d.wa_bucket_start[b] = st.wa_bucket_start[b];
+    d.wa_block_start[b] = st.wa_block_start[b];
+  }
+  const size_t nb = (size_t)m.cnt_x * m.cnt_y;
+  const size_t ng = m.n_g;
   GPL_CUDA(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, j->device));
   d.part_stride = std::max(std::max(cell_grid(d), poisson_blocks_a(m.cnt_x, m.cnt_y)), 1);
   const size_t nnb = std::max(net_blocks(d), 1);
   const size_t ps = (size_t)kPartSlots * d.part_stride;
 
-  const size_t bytes = arena_bytes(ng, m.n_pins, m.n_nets, m.g_pins.size(), big.size(), nb, m.cnt_x,
+  const size_t bytes = arena_bytes(ng, m.n_pins, m.n_nets, m.g_pins.size(), st.big.size(), nb, m.cnt_x,
                                    m.cnt_y, d.part_stride, nnb);
   cudaError_t e = dev_alloc((void**)&j->arena, bytes, j->pool, j->stream);
   if (e != cudaSuccess) {
@@ -296,8 +391,8 @@ int ensure_nb(gpl_job* j) {
   d.n_chunks = C.take<int32_t>(1);
   d.g_half = C.take<int2>(ng); d.g_scale = C.take<float>(ng); d.g_kind = C.take<uint8_t>(ng);
   d.g_precond = C.take<float2>(ng); d.g_pin_start = C.take<int32_t>(ng + 1);
-  d.big_cells = C.take<int32_t>(big.size());
-  d.g_big_idx = C.take<int32_t>(ng); d.d_big = C.take<float2>(big.size());
+  d.big_cells = C.take<int32_t>(st.big.size());
+  d.g_big_idx = C.take<int32_t>(ng); d.d_big = C.take<float2>(st.big.size());
   d.pins = C.take<int4>(m.n_pins);
   d.net_start = C.take<int32_t>(m.n_nets + 1);
   d.pin_grad = C.take<float2>(m.n_pins);
@@ -308,7 +403,7 @@ int ensure_nb(gpl_job* j) {
   d.p2 = C.take<float>(nb); d.field = C.take<float2>(nb); d.phi = C.take<float>(nb);
   d.wx = C.take<float>(m.cnt_x); d.wy = C.take<float>(m.cnt_y);
   d.w4x = C.take<float2>(m.cnt_x); d.w4y = C.take<float2>(m.cnt_y);
-  d.twiddle = C.take<float2>(tw.size());
+  d.twiddle = C.take<float2>(st.tw.size());
   for (int k = 0; k < 4; k++) { d.slp[k] = C.take<float2>(ng); d.sum[k] = C.take<float2>(ng); }
   d.coordi[0] = C.take<float2>(ng); d.coordi[1] = C.take<float2>(ng);
   d.wl_out = C.take<float2>(ng); d.d_out = C.take<float2>(ng);
@@ -320,22 +415,22 @@ int ensure_nb(gpl_job* j) {
   d.part_total = C.take<double>(kPartSlots);
   cudaStream_t s = j->stream;
   int rc2 = GPL_OK;
-  rc2 = rc2 ? rc2 : upload(d.g_half, half.data(), ng * sizeof(int2), s);
+  rc2 = rc2 ? rc2 : upload(d.g_half, st.half.data(), ng * sizeof(int2), s);
   rc2 = rc2 ? rc2 : upload(d.g_scale, m.gscale.data(), ng * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.g_kind, kind.data(), ng, s);
-  rc2 = rc2 ? rc2 : upload(d.g_precond, precond.data(), ng * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.g_kind, st.kind.data(), ng, s);
+  rc2 = rc2 ? rc2 : upload(d.g_precond, st.precond.data(), ng * sizeof(float2), s);
   rc2 = rc2 ? rc2 : upload(d.g_pin_start, m.g_pin_start.data(), (ng + 1) * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.big_cells, big.data(), big.size() * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.g_big_idx, big_idx.data(), ng * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.pins, pins.data(), (size_t)m.n_pins * sizeof(int4), s);
-  rc2 = rc2 ? rc2 : upload(d.g_pins, g_dpins.data(), g_dpins.size() * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.net_start, dnet_start.data(), (size_t)(m.n_nets + 1) * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.big_cells, st.big.data(), st.big.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.g_big_idx, st.big_idx.data(), ng * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.pins, st.pins.data(), (size_t)m.n_pins * sizeof(int4), s);
+  rc2 = rc2 ? rc2 : upload(d.g_pins, st.g_dpins.data(), st.g_dpins.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.net_start, st.dnet_start.data(), (size_t)(m.n_nets + 1) * 4, s);
   rc2 = rc2 ? rc2 : upload(d.nonplace, m.bin_nonplace.data(), nb * 8, s);
-  rc2 = rc2 ? rc2 : upload(d.wx, wx.data(), wx.size() * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.wy, wy.data(), wy.size() * 4, s);
-  rc2 = rc2 ? rc2 : upload(d.w4x, w4x.data(), w4x.size() * sizeof(float2), s);
-  rc2 = rc2 ? rc2 : upload(d.w4y, w4y.data(), w4y.size() * sizeof(float2), s);
-  rc2 = rc2 ? rc2 : upload(d.twiddle, tw.data(), tw.size() * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.wx, st.wx.data(), st.wx.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.wy, st.wy.data(), st.wy.size() * 4, s);
+  rc2 = rc2 ? rc2 : upload(d.w4x, st.w4x.data(), st.w4x.size() * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.w4y, st.w4y.data(), st.w4y.size() * sizeof(float2), s);
+  rc2 = rc2 ? rc2 : upload(d.twiddle, st.tw.data(), st.tw.size() * sizeof(float2), s);
   if (rc2) return rc2;
   GPL_CUDA(cudaMemsetAsync(d.area[0], 0, 2 * nb * 8, s));
   GPL_CUDA(cudaMemsetAsync(d.area[1], 0, 2 * nb * 8, s));
@@ -347,6 +442,7 @@ int ensure_nb(gpl_job* j) {
   d.ctl_h = &j->pinned->ctl;
   memset(d.ctl_h, 0, sizeof(EvalCtl));
   GPL_CUDA(cudaStreamSynchronize(s));
+  j->stage.reset();     // the host copies are no longer needed
   j->nb_ready = true;
   return GPL_OK;
 }
@@ -596,12 +692,19 @@ bool diverged(const gpl_job* j) {
 
 // NesterovPlace::init (src/nesterovPlace.cpp:64-175)
 int nesterov_init(gpl_job* j) {
+  const bool tell = j->m.p.verbose_level >= 2;
+  const double t0 = wall_ms();
   int rc = ensure_nb(j);
   if (rc) return rc;
+  const double t1 = wall_ms();
   rc = choose_poisson_path(j);
   if (rc) return rc;
+  const double t2 = wall_ms();
   rc = build_graph(j);
   if (rc) return rc;
+  if (tell)
+    printf("[NesterovInit] base and device model %.2f ms, Poisson form %.2f ms, graph %.2f ms\n", t1 - t0,
+           t2 - t1, wall_ms() - t2);
   HostModel& m = j->m;
   DeviceModel& d = j->d;
   const size_t ng = m.n_g;
@@ -824,10 +927,17 @@ void job_bind(gpl_job* j, cudaStream_t stream, HostPinned* pinned, cudaMemPool_t
   j->timer.stream = stream;
 }
 
-int job_device_bytes(gpl_job* j, int64_t* bytes) {
+int job_device_bytes(gpl_job* j, int64_t* bytes, bool centred) {
   const HostModel& m = j->m;
   NbCounts c;
-  int rc = nb_counts(m, &c);
+  // sizes as the job will see them: centring keeps 2 * (size / 2)
+  PlaceRects rects = place_rects(m);
+  if (centred)
+    for (size_t k = 0; k < rects.lx.size(); k++) {
+      rects.ux[k] = rects.lx[k] + 2 * ((rects.ux[k] - rects.lx[k]) / 2);
+      rects.uy[k] = rects.ly[k] + 2 * ((rects.uy[k] - rects.ly[k]) / 2);
+    }
+  int rc = nb_counts(m, &c, &rects);
   if (rc) return rc;
   int sm = 0;
   GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
@@ -913,6 +1023,7 @@ gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job**
 
 void gpl_destroy(gpl_job* j) {
   if (!j) return;
+  if (j->prep.joinable()) j->prep.join();
   cudaSetDevice(j->device);
   if (j->stream) cudaStreamSynchronize(j->stream);
   j->timer.release();
@@ -1096,6 +1207,8 @@ gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
   if (st) memset(st, 0, sizeof(*st));
   if (j->m.p.initial_place_max_iter <= 0) return GPL_OK;
   cudaSetDevice(j->device);
+  // the Nesterov setup's host part runs on a worker thread meanwhile
+  start_static_prep(j);
   int sm = 0;
   GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
   return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer, j->pinned->ip_state, j->pool,

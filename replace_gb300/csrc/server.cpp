@@ -209,7 +209,7 @@ gpl_status gpl_server_submit(gpl_server* s, const gpl_netlist_desc* nl, const gp
   int rc = job_new(nl, p, &j);
   if (rc) return (gpl_status)rc;
   int64_t bytes = 0;
-  rc = job_device_bytes(j, &bytes);
+  rc = job_device_bytes(j, &bytes, s->p.run_initial_place && !p->incremental_place_mode);
   if (rc) { gpl_destroy(j); return (gpl_status)rc; }
   bytes += kJobSlack;
   if (bytes > s->budget) {

@@ -150,13 +150,17 @@ void host_place_center(HostModel& m) {
 // Filler size and count (NesterovBase::initFillerGCells, src/nesterovBase.cpp:
 // 1066-1155) and the bin grid (BinGrid::initBins, :631-717): the counts that
 // size a job, independent of the instances' positions.
-int nb_counts(const HostModel& m, NbCounts* c) {
+int nb_counts(const HostModel& m, NbCounts* c, const PlaceRects* rects) {
   const gpl_params& p = m.p;
   const int n_place = (int)m.place_insts.size();
   {
     std::vector<int> dxs, dys;
     dxs.reserve(n_place); dys.reserve(n_place);
-    for (int i : m.place_insts) { dxs.push_back(m.iux[i] - m.ilx[i]); dys.push_back(m.iuy[i] - m.ily[i]); }
+    if (rects) {
+      for (int k = 0; k < n_place; k++) { dxs.push_back(rects->ux[k] - rects->lx[k]); dys.push_back(rects->uy[k] - rects->ly[k]); }
+    } else {
+      for (int i : m.place_insts) { dxs.push_back(m.iux[i] - m.ilx[i]); dys.push_back(m.iuy[i] - m.ily[i]); }
+    }
     int min_idx = (int)(dxs.size() * 0.05);
     int max_idx = (int)(dxs.size() * 0.95);
     if (max_idx <= min_idx) { set_error("too few movable instances for the filler size"); return GPL_ERR_INVALID_ARG; }
@@ -213,17 +217,35 @@ int nb_counts(const HostModel& m, NbCounts* c) {
   return GPL_OK;
 }
 
-int build_nesterov_base(HostModel& m) {
+PlaceRects place_rects(const HostModel& m) {
+  PlaceRects r;
+  const size_t n = m.place_insts.size();
+  r.lx.resize(n); r.ly.resize(n); r.ux.resize(n); r.uy.resize(n);
+  for (size_t k = 0; k < n; k++) {
+    const int i = m.place_insts[k];
+    r.lx[k] = m.ilx[i]; r.ly[k] = m.ily[i]; r.ux[k] = m.iux[i]; r.uy[k] = m.iuy[i];
+  }
+  return r;
+}
+
+// Everything of NesterovBase but the movable gcells' positions.  The
+// movable instances' rectangles come from `rects` (a copy taken when their
+// sizes are final: the initial place moves instances but keeps their sizes),
+// so that this can run beside an initial place that moves the instances; it
+// reads no other per-instance state that the initial place writes.
+int build_nesterov_static(HostModel& m, const PlaceRects& rects) {
   const gpl_params& p = m.p;
   NbCounts nc;
-  int rc = nb_counts(m, &nc);
+  int rc = nb_counts(m, &nc, &rects);
   if (rc) return rc;
   m.glx.clear(); m.gly.clear(); m.gux.clear(); m.guy.clear(); m.gkind.clear();
   m.n_place = (int)m.place_insts.size();
-  for (int i : m.place_insts) {
-    m.glx.push_back(m.ilx[i]); m.gly.push_back(m.ily[i]);
-    m.gux.push_back(m.iux[i]); m.guy.push_back(m.iuy[i]);
-    m.gkind.push_back((m.iuy[i] - m.ily[i]) > m.site_h * 6 ? 1 : 0);
+  const size_t n_all = (size_t)m.n_place + (size_t)std::max(nc.n_fill, 0);
+  m.glx.reserve(n_all); m.gly.reserve(n_all); m.gux.reserve(n_all); m.guy.reserve(n_all); m.gkind.reserve(n_all);
+  for (int k = 0; k < m.n_place; k++) {
+    m.glx.push_back(rects.lx[k]); m.gly.push_back(rects.ly[k]);
+    m.gux.push_back(rects.ux[k]); m.guy.push_back(rects.uy[k]);
+    m.gkind.push_back((rects.uy[k] - rects.ly[k]) > m.site_h * 6 ? 1 : 0);
   }
   // fillers: mt19937(0) centres
   m.fill_dx = nc.fill_dx;
@@ -327,6 +349,27 @@ int build_nesterov_base(HostModel& m) {
     m.gdux[g] = cx + ddx / 2; m.gduy[g] = cy + ddy / 2;
     m.gscale[g] = sx * sy;
   }
+  return GPL_OK;
+}
+
+// The movable gcells' real and density rectangles at the instances' current
+// positions (GCell(Instance*) and setDensityCenterLocation: the density
+// rectangle keeps its size and the real rectangle's centre).
+void place_gcells(HostModel& m) {
+  for (int k = 0; k < m.n_place; k++) {
+    const int i = m.place_insts[k];
+    const int hx = (m.gdux[k] - m.gdlx[k]) / 2, hy = (m.gduy[k] - m.gdly[k]) / 2;
+    m.glx[k] = m.ilx[i]; m.gly[k] = m.ily[i]; m.gux[k] = m.iux[i]; m.guy[k] = m.iuy[i];
+    const int cx = (m.gux[k] + m.glx[k]) / 2, cy = (m.guy[k] + m.gly[k]) / 2;
+    m.gdlx[k] = cx - hx; m.gdly[k] = cy - hy;
+    m.gdux[k] = cx + hx; m.gduy[k] = cy + hy;
+  }
+}
+
+int build_nesterov_base(HostModel& m) {
+  int rc = build_nesterov_static(m, place_rects(m));
+  if (rc) return rc;
+  place_gcells(m);
   return GPL_OK;
 }
 
