@@ -33,6 +33,8 @@ struct HostModel {
   int n_insts = 0, n_pins = 0, n_nets = 0;
   std::vector<int32_t> ilx, ily, iux, iuy;
   std::vector<uint8_t> ikind;
+  // pin_x / pin_y: positions of pins off movable instances (IO pins, pins of
+  // fixed instances); a movable instance's pin is its centre plus (pin_ox, pin_oy)
   std::vector<int32_t> pin_inst, pin_ox, pin_oy, pin_x, pin_y, net_start;
   std::vector<int32_t> inst_pin_start, inst_pins;
   std::vector<int32_t> place_insts, non_place_insts;

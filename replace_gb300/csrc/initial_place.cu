@@ -273,6 +273,11 @@ __global__ void k_ip_rowptr(IpDev D) {
 // order), and the slot's parts of the diagonal and the right-hand side.  Long
 // partner lists: the warp walks the net 32 pins at a time and compacts the
 // entries in pin order with ballots.
+// counters[kFillOverflow]: set if an entry fell outside the entry bound of
+// ip_sizes (never expected: the bound is exact for the partner rule); the
+// entry is dropped and the initial place reports an error.
+constexpr int kFillOverflow = 7;
+
 __global__ void k_ip_fill(IpDev D, IpParams P) {
   const unsigned full = 0xffffffffu;
   const int axis = blockIdx.y, lane = threadIdx.x & 31;
@@ -303,8 +308,12 @@ __global__ void k_ip_fill(IpDev D, IpParams P) {
             diag += wgt;
             const int j = D.pin_mov[r];
             if (j >= 0) {
-              col[at] = j;
-              val[at] = -wgt;
+              if ((size_t)at < D.nnz_cap) {
+                col[at] = j;
+                val[at] = -wgt;
+              } else {
+                D.counters[kFillOverflow] = 1u;
+              }
               at++;
               const int2 cj = D.ctr[j];
               const int off_r = pr - (axis ? cj.y : cj.x);
@@ -347,8 +356,12 @@ __global__ void k_ip_fill(IpDev D, IpParams P) {
         const unsigned mv = __ballot_sync(full, partner && j >= 0);
         if (partner && j >= 0) {
           const int k = sat + __popc(mv & ((1u << lane) - 1u));
-          col[k] = j;
-          val[k] = -wgt;
+          if ((size_t)k < D.nnz_cap) {
+            col[k] = j;
+            val[k] = -wgt;
+          } else {
+            D.counters[kFillOverflow] = 1u;
+          }
         }
         sat += __popc(mv);
       }
@@ -1134,12 +1147,15 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   const size_t nP = m.place_insts.size();
   size_t n_mp = 0;
   for (int i : m.place_insts) n_mp += m.inst_pin_start[i + 1] - m.inst_pin_start[i];
-  // an upper bound of the off-diagonal entries: every movable pin of a used
-  // net partners every other pin of that net
+  // An upper bound of the off-diagonal entries per axis (see for_partners):
+  // a net of degree d has at most two bound pins, each partnering at most
+  // d - 1 pins, and every other pin partners at most the two bound pins, so
+  // the net contributes at most 2 (d - 1) + 2 (d - 2) = 4 d - 6 entries (one
+  // bound pin for both ends: (d - 1) + (d - 1) <= 4 d - 6 for d >= 2).
   size_t nnz = 0;
   for (int n = 0; n < m.n_nets; n++) {
     const size_t deg = m.net_start[n + 1] - m.net_start[n];
-    if (deg > 1 && (int)deg < m.p.initial_place_max_fanout) nnz += deg * (deg - 1);
+    if (deg > 1 && (int)deg < m.p.initial_place_max_fanout) nnz += 4 * deg - 6;
   }
   z.nnz_cap = std::max<size_t>(nnz, 1);
   const int nb_mov = blocks_for((int)nP);
@@ -1400,14 +1416,20 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     }
     if (err <= 1e-5 && round >= 5) break;
   }
+  const double t_end = wall();
+  unsigned fill_overflow = 0;
   if (!rc) {
     if (cudaMemcpyAsync(ctr.data(), D.ctr, nP * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&fill_overflow, D.counters + kFillOverflow, sizeof(unsigned), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
         host_wait(s, sync_ev) != cudaSuccess) rc = GPL_ERR_CUDA;
   }
   dev_free(D.mem, pool, s);
   if (rc) { set_error("initial place: CUDA error"); return rc; }
+  if (fill_overflow) { set_error("initial place: B2B entries exceeded their bound"); return GPL_ERR_CUDA; }
   if (rounds > 0)
     for (int k = 0; k < nP; k++) host_set_inst_center(m, m.place_insts[k], ctr[k].x, ctr[k].y);
+  if (prm.verbose_level >= 2) printf("[InitialPlace] read-back and release %.2f ms\n", wall() - t_end);
   if (stats) {
     stats->iterations = rounds;
     stats->last_error = err;

@@ -1203,12 +1203,14 @@ gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
   if (j->nb_ready) { set_error("initial place must run before the Nesterov stage"); return GPL_ERR_BAD_STATE; }
   // InitialPlace::doBicgstabPlace (src/initialPlace.cpp:56-105): centre the
   // movable instances unless incremental, then the B2B + BiCGSTAB rounds
+  const double t0 = wall_ms();
   if (!j->m.p.incremental_place_mode) host_place_center(j->m);
   if (st) memset(st, 0, sizeof(*st));
   if (j->m.p.initial_place_max_iter <= 0) return GPL_OK;
   cudaSetDevice(j->device);
   // the Nesterov setup's host part runs on a worker thread meanwhile
   start_static_prep(j);
+  if (j->m.p.verbose_level >= 2) printf("[InitialPlace] centring and worker start %.2f ms\n", wall_ms() - t0);
   int sm = 0;
   GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, j->device));
   return (gpl_status)run_initial_place(j->m, j->stream, sm, st, j->timer, j->pinned->ip_state, j->pool,

@@ -128,15 +128,10 @@ int build_placer_base(HostModel& m, const gpl_netlist_desc* d, const gpl_params*
 
 void host_set_inst_center(HostModel& m, int i, int x, int y) {
   // Instance::setCenterLocation (src/placerBase.cpp:127-140): the box keeps
-  // 2*(dx/2) width; pins follow (Pin::updateLocation).
+  // 2*(dx/2) width.  The instance's pins are not stored: a movable
+  // instance's pin is always its centre plus the pin offset.
   const int hx = (m.iux[i] - m.ilx[i]) / 2, hy = (m.iuy[i] - m.ily[i]) / 2;
   m.ilx[i] = x - hx; m.ily[i] = y - hy; m.iux[i] = x + hx; m.iuy[i] = y + hy;
-  const int cx = (m.ilx[i] + m.iux[i]) / 2, cy = (m.ily[i] + m.iuy[i]) / 2;
-  for (int k = m.inst_pin_start[i]; k < m.inst_pin_start[i + 1]; k++) {
-    int q = m.inst_pins[k];
-    m.pin_x[q] = cx + m.pin_ox[q];
-    m.pin_y[q] = cy + m.pin_oy[q];
-  }
 }
 
 void host_place_center(HostModel& m) {
