@@ -123,8 +123,11 @@ __global__ void __launch_bounds__(kPgThreads) k_pg_density(PgArgs A) {
   }
 }
 
-// G1 epilogue: T[j][u0 + t] -> T^T[u][j] as an A operand (rows u, width ny).
+// G1 epilogue: T[j][u0 + t] -> T^T[u][j] as an A operand (rows u, width ny);
+// each thread's row j is a column of the output, so the lanes' stores of one
+// output row are consecutive.
 struct EpiT {
+  static constexpr bool kRowMajor = false;
   __nv_bfloat16* out;
   int ny;
   __device__ __forceinline__ void operator()(int j, int u0, const float (&v)[32]) const {
@@ -136,50 +139,41 @@ struct EpiT {
 // G2 epilogue: the spectral solve of FFT::doFFT (src/fft.cpp:117-166) on
 // S[u][v] (x frequency u, y frequency v), stored as phi^T[u][v], a B operand.
 struct EpiS {
+  static constexpr bool kRowMajor = true;
   __nv_bfloat16* out;
   int nx, ny;
   const float* wx;
   const float* wy;
   float scale;
-  __device__ __forceinline__ void operator()(int u, int v0, const float (&v)[32]) const {
-    __nv_bfloat16* row = out + (size_t)u * 3 * ny;
-    const float wxu = wx[u];
-#pragma unroll
-    for (int t = 0; t < 32; t++) {
-      const int vv = v0 + t;
-      float d = v[t];
-      if (u == 0) d *= 0.5f;
-      if (vv == 0) d *= 0.5f;
-      d *= scale;
-      float ph = 0.0f;
-      if (u != 0 || vv != 0) {
-        const float wyv = wy[vv];
-        ph = __fdiv_rn(d, __fadd_rn(__fmul_rn(wxu, wxu), __fmul_rn(wyv, wyv)));
-      }
-      put_b(row, ny, vv, ph);
+  __device__ __forceinline__ void at(int u, int vv, float s) const {
+    float d = s;
+    if (u == 0) d *= 0.5f;
+    if (vv == 0) d *= 0.5f;
+    d *= scale;
+    float ph = 0.0f;
+    if (u != 0 || vv != 0) {
+      const float wxu = __ldg(wx + u), wyv = __ldg(wy + vv);
+      ph = __fdiv_rn(d, __fadd_rn(__fmul_rn(wxu, wxu), __fmul_rn(wyv, wyv)));
     }
+    put_b(out + (size_t)u * 3 * ny, ny, vv, ph);
   }
 };
 
 // G34 epilogue: P[y'][u] stored as an A operand (rows y', width nx).
 struct EpiP {
+  static constexpr bool kRowMajor = true;
   __nv_bfloat16* out;
   int nx;
-  __device__ __forceinline__ void operator()(int y, int u0, const float (&v)[32]) const {
-    __nv_bfloat16* row = out + (size_t)y * 3 * nx;
-#pragma unroll
-    for (int t = 0; t < 32; t++) put_a(row, nx, u0 + t, v[t]);
-  }
+  __device__ __forceinline__ void at(int y, int u, float v) const { put_a(out + (size_t)y * 3 * nx, nx, u, v); }
 };
 
 // G5/G6/G7 epilogue: one component of the field (or phi) at [y][x].
 struct EpiF {
+  static constexpr bool kRowMajor = true;
   float* base;        // field as floats (component c of bin b at 2 b + c), or phi
   int nx, stride, comp;
-  __device__ __forceinline__ void operator()(int y, int x0, const float (&v)[32]) const {
-    float* p = base + ((size_t)y * nx + x0) * stride + comp;
-#pragma unroll
-    for (int t = 0; t < 32; t++) p[(size_t)t * stride] = v[t];
+  __device__ __forceinline__ void at(int y, int x, float v) const {
+    base[((size_t)y * nx + x) * stride + comp] = v;
   }
 };
 
@@ -195,7 +189,7 @@ struct PoissonGemm {
   int* err = nullptr;
   tc::TcPlan<64, EpiT> g1;
   tc::TcPlan<64, EpiS> g2;
-  tc::TcPlan<64, EpiP> g34;
+  tc::TcPlan<128, EpiP> g34;   // M = 2 ny: 128-wide N tiles keep it to one wave
   tc::TcPlan<64, EpiF> g6, g7, g5;
 };
 

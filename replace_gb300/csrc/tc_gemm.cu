@@ -5,15 +5,12 @@
 namespace gpl {
 namespace {
 
-// Row-major fp32 output (the diagnostic GEMM).
+// Row-major fp32 output (the diagnostic GEMM): lanes on consecutive columns.
 struct EpiStore {
+  static constexpr bool kRowMajor = true;
   float* d;
   int ldd;
-  __device__ __forceinline__ void operator()(int row, int col0, const float (&v)[32]) const {
-    float4* p = reinterpret_cast<float4*>(d + (size_t)row * ldd + col0);
-#pragma unroll
-    for (int i = 0; i < 8; i++) p[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-  }
+  __device__ __forceinline__ void at(int row, int col, float v) const { d[(size_t)row * ldd + col] = v; }
 };
 
 }  // namespace

@@ -5,14 +5,18 @@
 // with A and B stored K-contiguous (row-major M x K and N x K).  One CTA
 // computes a 128 x BN tile of D:
 //   * a TMA producer thread streams 128 x 64 tiles of A and BN x 64 tiles of
-//     B into a four-stage shared-memory ring (128-byte swizzle, the layout
-//     the MMA descriptors expect), one mbarrier per stage for "full";
+//     B into a shared-memory ring of 192 KB (eight stages at BN = 64, six at
+//     128, four at 256; 128-byte swizzle, the layout the MMA descriptors
+//     expect), one mbarrier per stage for "full";
 //   * an MMA thread issues tcgen05.mma (kind::f16, bf16 inputs, fp32
 //     accumulator in tensor memory, M = 128, N = BN, K = 16 per
 //     instruction) and commits each stage back to its "empty" mbarrier;
 //   * after the last commit all four warps read the accumulator from tensor
-//     memory (tcgen05.ld, 32 rows per warp) and hand it to the epilogue,
-//     32 consecutive columns of one row per call.
+//     memory (tcgen05.ld, 32 rows per warp, 32 columns at a time) and hand
+//     it to the epilogue: a row-major epilogue (Epi::kRowMajor) gets one
+//     element per lane with the lanes on 32 consecutive columns of one row
+//     (the warp's 32 x 32 block goes through a shared-memory transpose), so
+//     its stores coalesce; otherwise each thread gets its row's 32 columns.
 // Every mbarrier wait is bounded: on time-out the CTA records an error,
 // drains the copies it issued (again bounded), frees its tensor memory and
 // returns, so a fault in the pipeline can never hang the GPU.
@@ -33,16 +37,22 @@ namespace tc {
 
 constexpr int kTcM = 128;
 constexpr int kTcK = 64;                 // one 128-byte swizzle row of bf16
-constexpr int kTcStages = 4;
 constexpr int kTcThreads = 128;
 constexpr long long kWaitPolls = 1ll << 24;        // bounded mbarrier polls
 
+// Ring depth: 192 KB of stages.  Each k-tile is little MMA work, so the
+// loads in flight (not the tensor pipe) set the pace.
+template <int BN>
+constexpr int tc_stages() { return (192 * 1024) / ((kTcM + BN) * kTcK * 2); }
+
 template <int BN>
 struct TcSmem {
-  __nv_bfloat16 a[kTcStages][kTcM * kTcK];
-  __nv_bfloat16 b[kTcStages][BN * kTcK];
-  uint64_t full[kTcStages];
-  uint64_t empty[kTcStages];
+  static constexpr int ST = tc_stages<BN>();
+  __nv_bfloat16 a[ST][kTcM * kTcK];
+  __nv_bfloat16 b[ST][BN * kTcK];
+  float scratch[kTcThreads / 32][32 * 33];   // the epilogue's per-warp transpose
+  uint64_t full[ST];
+  uint64_t empty[ST];
   uint64_t done;
   uint32_t tmem_base;
 };
@@ -151,6 +161,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int K, Epi epi,
               int* err) {
   static_assert(BN == 64 || BN == 128 || BN == 256, "N tile");
+  constexpr int kTcStages = TcSmem<BN>::ST;
+  static_assert(kTcStages >= 2, "ring depth");
   constexpr uint32_t kBytesA = kTcM * kTcK * 2, kBytesB = BN * kTcK * 2;
   extern __shared__ unsigned char smem_raw[];
   TcSmem<BN>& S =
@@ -215,10 +227,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   if (got) {
     float v[32];
     const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    float* scr = S.scratch[warp];
 #pragma unroll 1
     for (int c = 0; c < BN; c += 32) {
       tmem_ld32(tmem + lane_base + (uint32_t)c, v);
-      epi(m0 + warp * 32 + lane, n0 + c, v);
+      if constexpr (Epi::kRowMajor) {
+#pragma unroll
+        for (int i = 0; i < 32; i++) scr[lane * 33 + i] = v[i];
+        __syncwarp();
+#pragma unroll 4
+        for (int r = 0; r < 32; r++) epi.at(m0 + warp * 32 + r, n0 + c + lane, scr[r * 33 + lane]);
+        __syncwarp();
+      } else {
+        epi(m0 + warp * 32 + lane, n0 + c, v);
+      }
     }
   }
   tc_fence_before();
