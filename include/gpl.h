@@ -133,6 +133,11 @@ typedef struct gpl_params {
                                               512 bins per axis, for precision), 1 = shared-memory
                                               FFT, 2 = tensor-core GEMMs (bf16 three-term split;
                                               grids with both counts multiples of 128) */
+  int32_t device_loop;                     /* 0 = the host drives the Nesterov loop, one
+                                              evaluation graph at a time (default); 1 = the loop
+                                              runs on the device (a CUDA graph with a conditional
+                                              WHILE node: evaluation, then a one-thread control
+                                              kernel).  Same control arithmetic and results. */
 } gpl_params;
 
 /* Counts and grid chosen by the job (NesterovBase / BinGrid). */

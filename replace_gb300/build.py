@@ -17,8 +17,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgpl_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["setup.cpp", "job.cu", "density.cu", "poisson.cu", "wirelength.cu", "poisson_noalloc.cu",
-           "initial_place.cu", "server.cpp", "tc_gemm.cu", "poisson_gemm.cu"]
-HEADERS = ["gpl_internal.h", "device_common.cuh", "tc_gemm.cuh", "../../include/gpl.h"]
+           "initial_place.cu", "server.cpp", "tc_gemm.cu", "poisson_gemm.cu", "control.cu"]
+HEADERS = ["gpl_internal.h", "device_common.cuh", "tc_gemm.cuh", "control.h", "../../include/gpl.h"]
 
 
 def nvcc() -> str:

@@ -68,7 +68,9 @@ constexpr int kTileMargin = 2;
 struct OrderArgs {
   BinGeom geo;
   int n_g, tile_w, tile_h, tiles_x, tiles_y;
-  const float2* slp;
+  const float2* slp;            // the coordinates to order by, or (slp == nullptr)
+  const float2* slp_all[4];     // slot ctl->i_src of these (the device loop)
+  const EvalCtl* ctl;
   int32_t* tile_count;
   int32_t* tile_start;
   int32_t* order;
@@ -83,10 +85,15 @@ __device__ __forceinline__ int tile_of(const OrderArgs& O, float2 c) {
   return (by / O.tile_h) * O.tiles_x + bx / O.tile_w;
 }
 
+__device__ __forceinline__ const float2* order_coords(const OrderArgs& O) {
+  return O.slp ? O.slp : pick4(O.slp_all, O.ctl->i_src);
+}
+
 // Lanes of a warp on the same tile add their count with one atomic.
 __global__ void __launch_bounds__(kBlock) k_order_count(OrderArgs O) {
   const int g = blockIdx.x * kBlock + threadIdx.x;
-  const int t = g < O.n_g ? tile_of(O, O.slp[g]) : -1;
+  const float2* slp = order_coords(O);
+  const int t = g < O.n_g ? tile_of(O, slp[g]) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, t);    // every lane takes part
   if (t >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&O.tile_count[t], __popc(peers));
 }
@@ -134,7 +141,8 @@ __global__ void __launch_bounds__(kOrderScanT) k_order_scan(OrderArgs O) {
 __global__ void __launch_bounds__(kBlock) k_order_fill(OrderArgs O) {
   const int g = blockIdx.x * kBlock + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  const int t = g < O.n_g ? tile_of(O, O.slp[g]) : -1;
+  const float2* slp = order_coords(O);
+  const int t = g < O.n_g ? tile_of(O, slp[g]) : -1;
   const unsigned peers = __match_any_sync(0xffffffffu, t);    // every lane takes part
   const int leader = __ffs(peers) - 1;
   int base = 0;
@@ -544,7 +552,10 @@ int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t) {
   O.geo = geom(d);
   O.n_g = d.n_g;
   O.tile_w = d.tile_w; O.tile_h = d.tile_h; O.tiles_x = d.tiles_x; O.tiles_y = d.tiles_y;
-  O.slp = d.slp[slot];
+  // slot < 0: the slot the control record's predictor starts from
+  O.slp = slot >= 0 ? d.slp[slot] : nullptr;
+  for (int k = 0; k < 4; k++) O.slp_all[k] = d.slp[k];
+  O.ctl = d.ctl;
   O.tile_count = d.tile_count; O.tile_start = d.tile_start; O.order = d.order;
   O.chunks = d.chunks; O.n_chunks = d.n_chunks;
   t.begin(kKOther);

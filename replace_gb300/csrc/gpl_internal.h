@@ -186,6 +186,37 @@ struct EvalResult {
   int pad;
 };
 
+// Everything the Nesterov loop carries from one evaluation to the next.  The
+// job keeps a host copy; the device loop works on a device copy and the two
+// are exchanged around each device chunk.
+struct NesterovState {
+  // parameters
+  int max_back_track, max_iter;
+  float target_overflow, min_phi_coef, reference_hpwl;
+  float ovf_den;            // std area + macro area * target density (float, as the reference)
+  float base_wl_coef;
+  // NesterovPlace state (src/nesterovPlace.h:76-125)
+  float cur_a, coeff, step_length, density_penalty, wl_coef_x, wl_coef_y;
+  float sum_overflow, min_sum_overflow, hpwl_with_min, max_phi_coef;
+  int max_phi_changed, is_diverged, finished, diverge_code;
+  long long prev_hpwl;
+  int iter, evals, attempts;
+  // buffer slots (rotated by index), area set alternation
+  int i_prev, i_cur, i_next, c_cur, c_next;
+  int area_next, last_area, last_slot;
+  // device loop: iterations this chunk may run (0 = to the stop rule), done,
+  // evaluations, log entries, tile-order refreshes
+  int chunk_limit, chunk_done, chunk_evals, log_count, refreshes, pad;
+  EvalResult last;          // the last evaluation's result
+};
+
+// One logged iteration.
+struct IterEntry {
+  long long hpwl;
+  float overflow, step_length;
+  int backtracks, pad;
+};
+
 // Pinned host staging of one job: the evaluation's control record and result
 // and the initial place's solver scalars.  A job allocates its own, or a
 // server hands each of its slots one for the life of the server (freeing
@@ -193,6 +224,7 @@ struct EvalResult {
 struct HostPinned {
   EvalResult result;
   EvalCtl ctl;
+  NesterovState state;
   alignas(16) unsigned char ip_state[1024];
 };
 
@@ -270,8 +302,15 @@ void make_w4(int n, std::vector<float2>& w);
 
 int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 // Orders the gcells by the bin tile of their centres in slp[slot] (counting
-// sort) and builds the scatter's chunk table.
+// sort) and builds the scatter's chunk table; slot < 0: the slot the device
+// control record's predictor starts from (ctl->i_src).
 int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t);
+
+// Device loop of the Nesterov iteration (control.cu, control.h).
+int launch_loop_head(NesterovState* S, EvalCtl* ctl, cudaGraphConditionalHandle h_loop,
+                     cudaGraphConditionalHandle h_order, cudaStream_t s);
+int launch_loop_step(NesterovState* S, EvalCtl* ctl, const EvalResult* res, IterEntry* log, int log_cap,
+                     cudaGraphConditionalHandle h_loop, cudaGraphConditionalHandle h_order, cudaStream_t s);
 // Tile grid of a bin grid, and the chunk-table bound, for sizing.
 constexpr int kScatterChunk = 2048;
 static_assert(kScatterChunk < 65536, "the scatter's 16-bit split window sums need < 2^16 gcells per chunk");

@@ -20,6 +20,7 @@
 #include <thread>
 #include <vector>
 
+#include "control.h"
 #include "gpl_internal.h"
 
 namespace gpl {
@@ -108,20 +109,18 @@ struct gpl_job {
   cudaMemPool_t pool = nullptr;         // stream-ordered pool (server jobs)
   cudaEvent_t sync_ev = nullptr;        // blocking-sync event (server jobs)
   bool nb_ready = false, np_ready = false;
-  // NesterovPlace state (src/nesterovPlace.h:76-125)
-  float step_length = 0, density_penalty = 0, base_wl_coef = 0, wl_coef_x = 0, wl_coef_y = 0;
-  float sum_overflow = 0, cur_a = 1.0f, min_sum_overflow = 1e30f, hpwl_with_min = 1e30f;
-  float max_phi_coef = 1.05f;
-  bool max_phi_changed = false, is_diverged = false, finished = false;
-  int64_t prev_hpwl = 0;
-  int iter = 0, evals = 0, diverge_code = 0;
-  int i_prev = 0, i_cur = 1, i_next = 2, c_cur = 0, c_next = 1;
-  int last_slot = -1;                   // slp slot of the last evaluation
-  int last_area = 0;                    // area set of the last evaluation
-  int area_next = 0;                    // area set of the next evaluation
-  EvalResult last{};
+  // NesterovPlace state (src/nesterovPlace.h:76-125), the host copy; the
+  // device loop works on d_state and the two are exchanged around a chunk
+  NesterovState S{};
   cudaGraphExec_t graph_exec = nullptr; // one evaluation, replayed
   long long graph_kernels = 0;
+  // device loop: head kernel, then WHILE { [IF tile order] evaluation, step }
+  cudaGraphExec_t loop_exec = nullptr;
+  bool loop_tried = false;
+  NesterovState* d_state = nullptr;
+  IterEntry* d_log = nullptr;
+  int log_cap = 0;
+  long long order_kernels = 0;
   float poisson_fft_us = 0.0f, poisson_gemm_us = 0.0f;   // auto mode's timings
   bool poisson_chosen = false;
   // WA runs beside the Poisson passes on a second stream (fork after the
@@ -178,7 +177,7 @@ struct Carver {
 
 // Bytes of a job's arena (the carving in ensure_nb follows the same order).
 size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size_t n_big, size_t nb,
-                   int cnt_x, int cnt_y, size_t part_stride, size_t nnb) {
+                   int cnt_x, int cnt_y, size_t part_stride, size_t nnb, size_t log_cap) {
   const size_t ps = (size_t)kPartSlots * part_stride;
   int tw, th, tx, ty;
   tile_grid(cnt_x, cnt_y, &tw, &th, &tx, &ty);
@@ -199,6 +198,7 @@ size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size
   S.add(1, sizeof(EvalCtl));
   S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
   S.add(kPartSlots, 8);
+  S.add(1, sizeof(NesterovState)); S.add(log_cap, sizeof(IterEntry));   // device loop
   return S.bytes;
 }
 
@@ -371,8 +371,9 @@ int ensure_nb(gpl_job* j) {
   const size_t nnb = std::max(net_blocks(d), 1);
   const size_t ps = (size_t)kPartSlots * d.part_stride;
 
+  const size_t log_cap = (size_t)std::max(1, m.p.nesterov_place_max_iter);
   const size_t bytes = arena_bytes(ng, m.n_pins, m.n_nets, m.g_pins.size(), st.big.size(), nb, m.cnt_x,
-                                   m.cnt_y, d.part_stride, nnb);
+                                   m.cnt_y, d.part_stride, nnb, log_cap);
   cudaError_t e = dev_alloc((void**)&j->arena, bytes, j->pool, j->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -413,6 +414,9 @@ int ensure_nb(gpl_job* j) {
   d.hpwl_total = C.take<long long>(1);
   d.counters = C.take<unsigned>(4);
   d.part_total = C.take<double>(kPartSlots);
+  j->d_state = C.take<NesterovState>(1);
+  j->d_log = C.take<IterEntry>(log_cap);
+  j->log_cap = (int)log_cap;
   cudaStream_t s = j->stream;
   int rc2 = GPL_OK;
   rc2 = rc2 ? rc2 : upload(d.g_half, st.half.data(), ng * sizeof(int2), s);
@@ -446,9 +450,6 @@ int ensure_nb(gpl_job* j) {
   j->nb_ready = true;
   return GPL_OK;
 }
-
-// Iterations between refreshes of the scatter's tile order.
-constexpr int kTileOrderEvery = 32;
 
 EvalArgs base_args(gpl_job* j) {
   EvalArgs a;
@@ -487,7 +488,7 @@ int launch_phase2(gpl_job* j, bool want_phi, int area_set) {
 // predicted coordinates, Poisson only the areas), joined before the gcell
 // kernel, and the result record's copy to the host.  With kernel timing on,
 // everything stays on the job's stream so that each class is timed alone.
-int launch_eval(gpl_job* j, bool want_phi, int area_set) {
+int launch_eval(gpl_job* j, bool want_phi, int area_set, bool copy_result = true) {
   DeviceModel& d = j->d;
   int rc = launch_scatter(d, base_args(j), j->stream, j->timer);
   if (rc) return rc;
@@ -509,13 +510,14 @@ int launch_eval(gpl_job* j, bool want_phi, int area_set) {
   }
   rc = launch_cell(d, base_args(j), phi_blocks, j->stream, j->timer);
   if (rc) return rc;
-  GPL_CUDA(cudaMemcpyAsync(d.result_h, d.result, sizeof(EvalResult), cudaMemcpyDeviceToHost, j->stream));
+  if (copy_result)
+    GPL_CUDA(cudaMemcpyAsync(d.result_h, d.result, sizeof(EvalResult), cudaMemcpyDeviceToHost, j->stream));
   return GPL_OK;
 }
 
 int finish(gpl_job* j) {
   GPL_CUDA(host_wait(j->stream, j->sync_ev));
-  j->last = *j->d.result_h;
+  j->S.last = *j->d.result_h;
   return GPL_OK;
 }
 
@@ -625,7 +627,7 @@ int build_graph(gpl_job* j) {
 
 // One evaluation at control record c (area set chosen here).
 int evaluate(gpl_job* j, EvalCtl c, bool want_phi) {
-  c.area_cur = j->area_next;
+  c.area_cur = j->S.area_next;
   int rc = GPL_OK;
   if (j->graph_exec && !want_phi && !j->timer.enabled) {
     *j->d.ctl_h = c;
@@ -636,59 +638,42 @@ int evaluate(gpl_job* j, EvalCtl c, bool want_phi) {
     if (!rc) rc = launch_eval(j, want_phi, c.area_cur);
   }
   if (rc) return rc;
-  j->last_area = c.area_cur;
-  j->area_next = c.area_cur ^ 1;
-  j->last_slot = c.i_eval;
-  j->evals++;
+  j->S.last_area = c.area_cur;
+  j->S.area_next = c.area_cur ^ 1;
+  j->S.last_slot = c.i_eval;
+  j->S.evals++;
   return finish(j);
 }
 
 // Phase 2 again with a new control record (same coordinates and bins).
 int rerun_phase2(gpl_job* j, EvalCtl c) {
-  c.area_cur = j->last_area;
+  c.area_cur = j->S.last_area;
   int rc = put_ctl(j, c);
   if (!rc) rc = launch_phase2(j, false, c.area_cur);
   if (rc) return rc;
   return finish(j);
 }
 
-float overflow_ratio(const gpl_job* j) {
-  // sumOverflow_ (src/nesterovPlace.cpp:112-115, 529-532)
-  const HostModel& m = j->m;
-  return (float)(int64_t)j->last.overflow /
-         (float)(m.std_area + m.macro_area * m.p.target_density);
-}
+float overflow_ratio(const gpl_job* j) { return overflow_ratio_of(j->S, j->S.last.overflow); }
 
-void update_wl_coef(gpl_job* j, float overflow) {
-  // NesterovPlace::updateWireLengthCoef (src/nesterovPlace.cpp:474-490)
-  float c;
-  if (overflow > 1.0) c = 0.1f;
-  else if (overflow < 0.1) c = 10.0f;
-  else c = (float)(1.0 / pow(10.0, (overflow - 0.1) * 20 / 9.0 - 1.0));
-  j->wl_coef_x = c * j->base_wl_coef;
-  j->wl_coef_y = c * j->base_wl_coef;
-}
+void update_wl_coef(gpl_job* j, float overflow) { update_wl_coef_of(j->S, overflow); }
 
 EvalCtl ctl_of(gpl_job* j, int i_eval, int i_ref, bool write_sum) {
   EvalCtl c;
   memset(&c, 0, sizeof(c));
-  c.density_penalty = j->density_penalty;
-  c.wl_coef_x = j->wl_coef_x;
-  c.wl_coef_y = j->wl_coef_y;
-  c.i_src = j->i_cur;
+  c.density_penalty = j->S.density_penalty;
+  c.wl_coef_x = j->S.wl_coef_x;
+  c.wl_coef_y = j->S.wl_coef_y;
+  c.i_src = j->S.i_cur;
   c.i_eval = i_eval;
   c.i_ref = i_ref;
-  c.c_cur = j->c_cur;
-  c.c_next = j->c_next;
+  c.c_cur = j->S.c_cur;
+  c.c_next = j->S.c_next;
   c.write_sum = write_sum ? 1 : 0;
   return c;
 }
 
-bool bad(double v) { return std::isnan(v) || std::isinf(v); }
-
-bool diverged(const gpl_job* j) {
-  return bad((float)j->last.wl_sum) || bad((float)j->last.d_sum) || j->last.nan_flag != 0.0;
-}
+bool diverged(const gpl_job* j) { return diverged_result(j->S.last); }
 
 // NesterovPlace::init (src/nesterovPlace.cpp:64-175)
 int nesterov_init(gpl_job* j) {
@@ -707,6 +692,13 @@ int nesterov_init(gpl_job* j) {
            t2 - t1, wall_ms() - t2);
   HostModel& m = j->m;
   DeviceModel& d = j->d;
+  NesterovState& S = j->S;
+  S.max_back_track = m.p.max_back_track;
+  S.max_iter = m.p.nesterov_place_max_iter;
+  S.target_overflow = m.p.target_overflow;
+  S.min_phi_coef = m.p.min_phi_coef;
+  S.reference_hpwl = m.p.reference_hpwl;
+  S.ovf_den = (float)(m.std_area + m.macro_area * m.p.target_density);
   const size_t ng = m.n_g;
   std::vector<float2> c0(ng);
   for (size_t g = 0; g < ng; g++) {
@@ -720,153 +712,241 @@ int nesterov_init(gpl_job* j) {
     const int nlx = (int)tlx, nly = (int)tly;
     c0[g] = make_float2((float)((2 * nlx + ddx) / 2), (float)((2 * nly + ddy) / 2));
   }
-  j->i_prev = 0; j->i_cur = 1; j->i_next = 2; j->c_cur = 0; j->c_next = 1;
-  rc = upload(d.slp[j->i_cur], c0.data(), ng * sizeof(float2), j->stream);
+  j->S.i_prev = 0; j->S.i_cur = 1; j->S.i_next = 2; j->S.c_cur = 0; j->S.c_next = 1;
+  rc = upload(d.slp[j->S.i_cur], c0.data(), ng * sizeof(float2), j->stream);
   if (rc) return rc;
-  GPL_CUDA(cudaMemcpyAsync(d.slp[j->i_prev], d.slp[j->i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
-  GPL_CUDA(cudaMemcpyAsync(d.coordi[j->c_cur], d.slp[j->i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
-  j->density_penalty = 0.0f;
-  j->max_phi_coef = m.p.max_phi_coef;
-  j->wl_coef_x = j->wl_coef_y = 0.0f;
+  GPL_CUDA(cudaMemcpyAsync(d.slp[j->S.i_prev], d.slp[j->S.i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
+  GPL_CUDA(cudaMemcpyAsync(d.coordi[j->S.c_cur], d.slp[j->S.i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
+  j->S.density_penalty = 0.0f;
+  j->S.max_phi_coef = m.p.max_phi_coef;
+  j->S.wl_coef_x = j->S.wl_coef_y = 0.0f;
   // first evaluation at the initial centres: overflow and HPWL
-  rc = launch_tile_order(d, j->i_cur, j->stream, j->timer);
+  rc = launch_tile_order(d, j->S.i_cur, j->stream, j->timer);
   if (rc) return rc;
-  rc = evaluate(j, ctl_of(j, j->i_cur, -1, false), false);
+  rc = evaluate(j, ctl_of(j, j->S.i_cur, -1, false), false);
   if (rc) return rc;
-  j->prev_hpwl = j->last.hpwl;
-  j->base_wl_coef = (float)(m.p.init_wire_length_coef / ((float)(m.size_x + m.size_y) * 0.5));
-  j->sum_overflow = overflow_ratio(j);
-  update_wl_coef(j, j->sum_overflow);
+  j->S.prev_hpwl = j->S.last.hpwl;
+  j->S.base_wl_coef = (float)(m.p.init_wire_length_coef / ((float)(m.size_x + m.size_y) * 0.5));
+  j->S.sum_overflow = overflow_ratio(j);
+  update_wl_coef(j, j->S.sum_overflow);
   // the WA forces and gradients with the wire-length coefficients set
-  rc = rerun_phase2(j, ctl_of(j, j->i_cur, -1, true));
+  rc = rerun_phase2(j, ctl_of(j, j->S.i_cur, -1, true));
   if (rc) return rc;
   if (diverged(j)) {
-    j->is_diverged = true; j->diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
+    j->S.is_diverged = true; j->S.diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
     set_error("RePlAce diverged. Please tune the parameters again");
     return GPL_ERR_DIVERGED_INIT;
   }
   // updateInitialPrevSLPCoordi (src/nesterovPlace.cpp:492-512)
-  rc = launch_initial_prev(d, d.slp[j->i_cur], d.sum[j->i_cur], m.p.initial_prev_coordi_update_coef,
-                           d.slp[j->i_prev], j->stream, j->timer);
+  rc = launch_initial_prev(d, d.slp[j->S.i_cur], d.sum[j->S.i_cur], m.p.initial_prev_coordi_update_coef,
+                           d.slp[j->S.i_prev], j->stream, j->timer);
   if (rc) return rc;
-  rc = evaluate(j, ctl_of(j, j->i_prev, j->i_cur, true), false);
+  rc = evaluate(j, ctl_of(j, j->S.i_prev, j->S.i_cur, true), false);
   if (rc) return rc;
   if (diverged(j)) {
-    j->is_diverged = true; j->diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
+    j->S.is_diverged = true; j->S.diverge_code = GPL_ERR_DIVERGED_INIT; j->np_ready = true;
     set_error("RePlAce diverged. Please tune the parameters again");
     return GPL_ERR_DIVERGED_INIT;
   }
-  j->density_penalty = ((float)j->last.wl_sum / (float)j->last.d_sum) * m.p.init_density_penalty;
-  j->sum_overflow = overflow_ratio(j);
-  j->step_length = j->last.new_step_length;
-  j->cur_a = 1.0f;
-  j->min_sum_overflow = 1e30f;
-  j->hpwl_with_min = 1e30f;
-  j->max_phi_changed = false;
-  j->iter = 0;
-  j->finished = false;
+  j->S.density_penalty = ((float)j->S.last.wl_sum / (float)j->S.last.d_sum) * m.p.init_density_penalty;
+  j->S.sum_overflow = overflow_ratio(j);
+  j->S.step_length = j->S.last.new_step_length;
+  j->S.cur_a = 1.0f;
+  j->S.min_sum_overflow = 1e30f;
+  j->S.hpwl_with_min = 1e30f;
+  j->S.max_phi_changed = false;
+  j->S.iter = 0;
+  j->S.finished = false;
   j->np_ready = true;
   return GPL_OK;
 }
 
-// NesterovPlace::doNesterovPlace (src/nesterovPlace.cpp:275-472), resumable
-int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
-  HostModel& m = j->m;
-  const gpl_params& p = m.p;
-  if (j->diverge_code == GPL_ERR_DIVERGED_INIT) { j->finished = true; return j->diverge_code; }
-  int done = 0;
-  while (!j->finished && j->iter < p.nesterov_place_max_iter) {
-    if (max_iters > 0 && done >= max_iters) break;
-    done++;
-    const float prev_a = j->cur_a;
-    j->cur_a = (float)((1.0 + sqrt(4.0 * prev_a * prev_a + 1.0)) * 0.5);
-    const float coeff = (float)((prev_a - 1.0) / j->cur_a);
-    int bt = 0;
-    // refresh the scatter's tile order now and then (cells move slowly)
-    if (j->iter % kTileOrderEvery == 0) {
-      int rc = launch_tile_order(j->d, j->i_cur, j->stream, j->timer);
-      if (rc) return rc;
-    }
-    for (bt = 0; bt < p.max_back_track; bt++) {
-      EvalCtl c = ctl_of(j, j->i_next, j->i_cur, true);
-      c.predict = 1;
-      c.step = j->step_length;
-      c.coeff = coeff;
-      int rc = evaluate(j, c, false);
-      if (rc) return rc;
-      if (diverged(j)) {
-        j->is_diverged = true;
-        break;
-      }
-      const float ns = j->last.new_step_length;
-      if (ns > j->step_length * 0.95) { j->step_length = ns; break; }
-      j->step_length = ns;
-    }
-    if (!j->max_phi_changed && j->sum_overflow < 0.35f) {
-      j->max_phi_changed = true;
-      j->max_phi_coef = (float)(j->max_phi_coef * 0.99);
-    }
-    if (p.max_back_track == bt) {
-      j->diverge_code = GPL_ERR_DIVERGED_BACKTRACK;
-      j->is_diverged = true;
-      set_error("RePlAce divergence detected. Please decrease init_density_penalty value");
-    }
-    if (j->is_diverged) {
-      if (!j->diverge_code) {
-        j->diverge_code = GPL_ERR_DIVERGED_NAN;
-        set_error("RePlAce divergence detected: NaN or Inf in the gradient sums");
-      }
-      j->finished = true;
-      break;
-    }
-    // updateNextIter (src/nesterovPlace.cpp:514-553)
-    const int op = j->i_prev;
-    j->i_prev = j->i_cur; j->i_cur = j->i_next; j->i_next = op;
-    std::swap(j->c_cur, j->c_next);
-    j->sum_overflow = overflow_ratio(j);
-    update_wl_coef(j, j->sum_overflow);
-    const int64_t hpwl = j->last.hpwl;
-    const float sd = (float)(hpwl - j->prev_hpwl) / p.reference_hpwl;
-    float pc = (sd < 0) ? j->max_phi_coef : (float)(j->max_phi_coef * pow(j->max_phi_coef, sd * -1.0));
-    pc = std::max(p.min_phi_coef, pc);
-    j->prev_hpwl = hpwl;
-    j->density_penalty *= pc;
-    if (log && log->count < log->capacity) {
-      const int k = log->count++;
-      if (log->overflow) log->overflow[k] = j->sum_overflow;
-      if (log->hpwl) log->hpwl[k] = j->prev_hpwl;
-      if (log->step_length) log->step_length[k] = j->step_length;
-      if (log->backtracks) log->backtracks[k] = bt + 1;
-    }
-    if (p.verbose_level > 0 && (j->iter == 0 || (j->iter + 1) % 10 == 0)) {
-      printf("[NesterovSolve] Iter: %d overflow: %g HPWL: %lld\n", j->iter + 1, j->sum_overflow,
-             (long long)j->prev_hpwl);
-      fflush(stdout);
-    }
-    const int it = j->iter;
-    j->iter++;
-    if (j->min_sum_overflow > j->sum_overflow) {
-      j->min_sum_overflow = j->sum_overflow;
-      j->hpwl_with_min = (float)j->prev_hpwl;
-    }
-    if (j->sum_overflow < 0.3f && j->sum_overflow - j->min_sum_overflow >= 0.02f &&
-        j->hpwl_with_min * 1.2f < j->prev_hpwl) {
-      j->diverge_code = GPL_ERR_DIVERGED_PHI;
-      j->is_diverged = true;
-      j->finished = true;
-      set_error("RePlAce divergence detected. Please decrease max_phi_cof value");
-      break;
-    }
-    if (it > 50 && j->sum_overflow <= p.target_overflow) {
-      if (p.verbose_level > 0) {
-        printf("[NesterovSolve] Finished with Overflow: %g\n", j->sum_overflow);
-        fflush(stdout);
-      }
-      j->finished = true;
-      break;
+// The job's loop graph: a head kernel, then WHILE (condition set by the
+// kernels) { IF (refresh) the tile order; one evaluation; the step kernel }.
+// Built once per job after the evaluation graph; a failure leaves the host
+// loop in charge (same kernels, same control arithmetic).
+int build_loop_graph(gpl_job* j) {
+  if (j->loop_tried) return GPL_OK;
+  j->loop_tried = true;
+  if (!j->m.p.use_graph || !j->m.p.device_loop || !j->d_state || !j->d_log) return GPL_OK;
+  int rc0 = poisson_prepare_device();
+  if (rc0) return rc0;
+  DeviceModel& d = j->d;
+  const bool te = j->timer.enabled;
+  j->timer.enabled = false;
+  const long long k0 = j->timer.kernels;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+  cudaGraphConditionalHandle h_loop = 0, h_order = 0;
+  ok = ok && cudaGraphConditionalHandleCreate(&h_loop, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+  ok = ok && cudaGraphConditionalHandleCreate(&h_order, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+  // head
+  cudaGraphNode_t head = nullptr;
+  if (ok) {
+    cudaGraph_t cap = nullptr;
+    ok = cudaStreamBeginCaptureToGraph(j->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    int rc = ok ? launch_loop_head(j->d_state, d.ctl, h_loop, h_order, j->stream) : GPL_OK;
+    if (ok) ok = cudaStreamEndCapture(j->stream, &cap) == cudaSuccess && !rc;
+    size_t n = 1;
+    ok = ok && cudaGraphGetNodes(g, &head, &n) == cudaSuccess && n == 1;
+  }
+  // WHILE node and its body
+  cudaGraph_t body = nullptr;
+  if (ok) {
+    cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+    wp.conditional.handle = h_loop;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    ok = cudaGraphAddNode(&wnode, g, &head, nullptr, 1, &wp) == cudaSuccess;
+    if (ok) body = wp.conditional.phGraph_out[0];
+  }
+  cudaGraphNode_t inode = nullptr;
+  long long order_kernels = 0;
+  if (ok) {
+    cudaGraphNodeParams ip = {cudaGraphNodeTypeConditional};
+    ip.conditional.handle = h_order;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    ok = cudaGraphAddNode(&inode, body, nullptr, nullptr, 0, &ip) == cudaSuccess;
+    if (ok) {
+      cudaGraph_t obody = ip.conditional.phGraph_out[0], cap = nullptr;
+      const long long o0 = j->timer.kernels;
+      ok = cudaStreamBeginCaptureToGraph(j->stream, obody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+           cudaSuccess;
+      int rc = ok ? launch_tile_order(d, -1, j->stream, j->timer) : GPL_OK;
+      if (ok) ok = cudaStreamEndCapture(j->stream, &cap) == cudaSuccess && !rc;
+      order_kernels = j->timer.kernels - o0;
     }
   }
-  if (j->iter >= p.nesterov_place_max_iter) j->finished = true;
+  if (ok) {
+    cudaGraph_t cap = nullptr;
+    ok = cudaStreamBeginCaptureToGraph(j->stream, body, &inode, nullptr, 1, cudaStreamCaptureModeThreadLocal) ==
+         cudaSuccess;
+    int rc = ok ? launch_eval(j, false, 0, false) : GPL_OK;
+    if (ok && !rc)
+      rc = launch_loop_step(j->d_state, d.ctl, d.result, j->d_log, j->log_cap, h_loop, h_order, j->stream);
+    if (ok) ok = cudaStreamEndCapture(j->stream, &cap) == cudaSuccess && !rc;
+  }
+  ok = ok && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+  j->timer.kernels = k0;
+  j->timer.enabled = te;
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+  if (!ok) {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (j->m.p.verbose_level > 0) printf("[NesterovSolve] device loop not built: the host drives the loop\n");
+    return GPL_OK;
+  }
+  j->loop_exec = exec;
+  j->order_kernels = order_kernels;
+  return GPL_OK;
+}
+
+// Appends a finished iteration to the caller's log and prints the
+// reference's progress line.
+void record_iteration(gpl_job* j, const IterEntry& e, int iter_number, gpl_iter_log* log) {
+  if (log && log->count < log->capacity) {
+    const int k = log->count++;
+    if (log->overflow) log->overflow[k] = e.overflow;
+    if (log->hpwl) log->hpwl[k] = e.hpwl;
+    if (log->step_length) log->step_length[k] = e.step_length;
+    if (log->backtracks) log->backtracks[k] = e.backtracks;
+  }
+  if (j->m.p.verbose_level > 0 && (iter_number == 1 || iter_number % 10 == 0)) {
+    printf("[NesterovSolve] Iter: %d overflow: %g HPWL: %lld\n", iter_number, e.overflow, (long long)e.hpwl);
+    fflush(stdout);
+  }
+}
+
+// Up to max_iters iterations (0: to the stop rule) on the device loop.
+int run_device_chunk(gpl_job* j, int max_iters, gpl_iter_log* log) {
+  NesterovState& S = j->S;
+  const int iter0 = S.iter, evals0 = S.evals, refreshes0 = S.refreshes;
+  S.chunk_limit = max_iters;
+  NesterovState* hs = &j->pinned->state;
+  *hs = S;
+  GPL_CUDA(cudaMemcpyAsync(j->d_state, hs, sizeof(NesterovState), cudaMemcpyHostToDevice, j->stream));
+  GPL_CUDA(cudaGraphLaunch(j->loop_exec, j->stream));
+  GPL_CUDA(cudaMemcpyAsync(hs, j->d_state, sizeof(NesterovState), cudaMemcpyDeviceToHost, j->stream));
+  GPL_CUDA(host_wait(j->stream, j->sync_ev));
+  S = *hs;
+  const int n_log = std::min(S.log_count, j->log_cap);
+  if (n_log > 0) {
+    std::vector<IterEntry> entries(n_log);
+    GPL_CUDA(cudaMemcpyAsync(entries.data(), j->d_log, n_log * sizeof(IterEntry), cudaMemcpyDeviceToHost, j->stream));
+    GPL_CUDA(cudaStreamSynchronize(j->stream));
+    for (int k = 0; k < n_log; k++) record_iteration(j, entries[k], iter0 + k + 1, log);
+  }
+  // launches: the head, per evaluation its kernels and the step kernel, per
+  // refresh the tile-order kernels
+  j->timer.count((int)(1 + (long long)(S.evals - evals0) * (j->graph_kernels + 1) +
+                       (long long)(S.refreshes - refreshes0) * j->order_kernels));
+  return GPL_OK;
+}
+
+// The same loop driven from the host, one evaluation at a time.
+int run_host_loop(gpl_job* j, int max_iters, gpl_iter_log* log) {
+  NesterovState& S = j->S;
+  int done = 0;
+  while (!S.finished && S.iter < S.max_iter) {
+    if (max_iters > 0 && done >= max_iters) break;
+    done++;
+    start_iteration(S);
+    if (S.iter % kTileOrderEvery == 0) {
+      int rc = launch_tile_order(j->d, S.i_cur, j->stream, j->timer);
+      if (rc) return rc;
+      S.refreshes++;
+    }
+    for (;;) {
+      const EvalCtl c = next_ctl(S);
+      int rc = GPL_OK;
+      if (j->graph_exec && !j->timer.enabled) {
+        *j->d.ctl_h = c;
+        GPL_CUDA(cudaGraphLaunch(j->graph_exec, j->stream));
+        j->timer.count((int)j->graph_kernels);
+      } else {
+        rc = put_ctl(j, c);
+        if (!rc) rc = launch_eval(j, false, c.area_cur);
+      }
+      if (rc) return rc;
+      GPL_CUDA(host_wait(j->stream, j->sync_ev));
+      const EvalResult r = *j->d.result_h;
+      IterEntry e;
+      bool logged = false;
+      const int a = after_eval(S, r, &e, &logged);
+      if (logged) record_iteration(j, e, S.iter, log);
+      if (a != kRetry) break;
+    }
+  }
+  return GPL_OK;
+}
+
+// NesterovPlace::doNesterovPlace (src/nesterovPlace.cpp:275-472), resumable:
+// the device loop when the job has one (no kernel timing), else the host loop.
+int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
+  NesterovState& S = j->S;
+  if (S.diverge_code == GPL_ERR_DIVERGED_INIT) { S.finished = 1; return S.diverge_code; }
+  if (!S.finished && S.iter < S.max_iter) {
+    int rc = build_loop_graph(j);
+    if (rc) return rc;
+    const bool device = j->loop_exec && !j->timer.enabled;
+    rc = device ? run_device_chunk(j, max_iters, log) : run_host_loop(j, max_iters, log);
+    if (rc) return rc;
+    if (S.finished && !S.diverge_code && j->m.p.verbose_level > 0) {
+      printf("[NesterovSolve] Finished with Overflow: %g\n", S.sum_overflow);
+      fflush(stdout);
+    }
+  }
+  if (S.iter >= S.max_iter) S.finished = 1;
+  switch (S.diverge_code) {
+    case GPL_ERR_DIVERGED_BACKTRACK: set_error("RePlAce divergence detected. Please decrease init_density_penalty value"); break;
+    case GPL_ERR_DIVERGED_NAN: set_error("RePlAce divergence detected: NaN or Inf in the gradient sums"); break;
+    case GPL_ERR_DIVERGED_PHI: set_error("RePlAce divergence detected. Please decrease max_phi_cof value"); break;
+    default: break;
+  }
   if (j->d.poisson_path == 2) {
     int flag = 0;
     int rc = poisson_gemm_error(j->d.pg, j->stream, &flag);
@@ -876,7 +956,7 @@ int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
       return GPL_ERR_CUDA;
     }
   }
-  return j->diverge_code;
+  return S.diverge_code;
 }
 
 void fill_info(gpl_job* j, gpl_job_info* info) {
@@ -908,6 +988,18 @@ int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
   gpl_job* j = new gpl_job();
   int rc = build_placer_base(j->m, nl, p);
   if (rc) { delete j; return rc; }
+  if (p->max_back_track < 1 || p->nesterov_place_max_iter < 0) {
+    delete j;
+    set_error("max_back_track must be at least 1 and nesterov_place_max_iter not negative");
+    return GPL_ERR_INVALID_ARG;
+  }
+  NesterovState& S = j->S;
+  S.cur_a = 1.0f;
+  S.min_sum_overflow = 1e30f;
+  S.hpwl_with_min = 1e30f;
+  S.max_phi_coef = p->max_phi_coef;
+  S.i_prev = 0; S.i_cur = 1; S.i_next = 2; S.c_cur = 0; S.c_next = 1;
+  S.last_slot = -1;
   j->device = p->device;
   rc = check_device(j->device);
   if (rc) { delete j; return rc; }
@@ -948,7 +1040,7 @@ int job_device_bytes(gpl_job* j, int64_t* bytes, bool centred) {
   // upper bounds: every gcell big, one WA block per net, the larger partial grid
   const size_t stride = std::max<size_t>((size_t)sm * 8, (size_t)c.cnt_y);
   const size_t arena = arena_bytes(ng, m.n_pins, m.n_nets, n_gpins, ng, nb, c.cnt_x, c.cnt_y, stride,
-                                   (size_t)m.n_nets + kWaBuckets);
+                                   (size_t)m.n_nets + kWaBuckets, (size_t)std::max(1, m.p.nesterov_place_max_iter));
   const size_t ip = m.p.initial_place_max_iter > 0 ? initial_place_bytes(m, sm) : 0;
   const size_t pg = (m.p.poisson_path != 1 && poisson_gemm_eligible(c.cnt_x, c.cnt_y))
                         ? (size_t)poisson_gemm_bytes(c.cnt_x, c.cnt_y) : 0;
@@ -994,6 +1086,7 @@ void gpl_params_default(gpl_params* p) {
   p->use_graph = 1;
   p->ip_solver = 0;
   p->poisson_path = 0;
+  p->device_loop = 0;
 }
 
 gpl_status gpl_create(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
@@ -1028,6 +1121,7 @@ void gpl_destroy(gpl_job* j) {
   if (j->stream) cudaStreamSynchronize(j->stream);
   j->timer.release();
   if (j->graph_exec) cudaGraphExecDestroy(j->graph_exec);
+  if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
   if (j->d.pg) poisson_gemm_free(j->d.pg, j->pool, j->stream);
   if (j->arena) dev_free(j->arena, j->pool, j->stream);
   if (j->own_pinned && j->pinned) cudaFreeHost(j->pinned);
@@ -1056,15 +1150,15 @@ gpl_status gpl_nesterov_run(gpl_job* j, int32_t max_iters, gpl_nesterov_stats* s
   cudaSetDevice(j->device);
   int rc = nesterov_run(j, max_iters, log);
   if (st) {
-    st->iterations = j->iter;
-    st->evaluations = j->evals;
-    st->finished = j->finished ? 1 : 0;
-    st->status = j->diverge_code;
-    st->overflow = j->sum_overflow;
-    st->step_length = j->step_length;
-    st->density_penalty = j->density_penalty;
-    st->wire_length_coef = j->wl_coef_x;
-    st->hpwl = j->prev_hpwl;
+    st->iterations = j->S.iter;
+    st->evaluations = j->S.evals;
+    st->finished = j->S.finished ? 1 : 0;
+    st->status = j->S.diverge_code;
+    st->overflow = j->S.sum_overflow;
+    st->step_length = j->S.step_length;
+    st->density_penalty = j->S.density_penalty;
+    st->wire_length_coef = j->S.wl_coef_x;
+    st->hpwl = j->S.prev_hpwl;
   }
   return (gpl_status)rc;
 }
@@ -1073,10 +1167,10 @@ gpl_status gpl_get_inst_locations(gpl_job* j, int32_t* lx, int32_t* ly) {
   if (!j || !lx || !ly) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
   const HostModel& m = j->m;
   for (int i = 0; i < m.n_insts; i++) { lx[i] = m.ilx[i]; ly[i] = m.ily[i]; }
-  if (j->np_ready && j->last_slot >= 0) {
+  if (j->np_ready && j->S.last_slot >= 0) {
     // NesterovPlace::updateDb: lx = dCx - dDx/2 at the last evaluated centres
     std::vector<float2> c(m.n_g);
-    GPL_CUDA(cudaMemcpyAsync(c.data(), j->d.slp[j->last_slot], m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+    GPL_CUDA(cudaMemcpyAsync(c.data(), j->d.slp[j->S.last_slot], m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
     GPL_CUDA(cudaStreamSynchronize(j->stream));
     for (int k = 0; k < m.n_place; k++) {
       const int i = m.place_insts[k];
@@ -1091,7 +1185,7 @@ gpl_status gpl_get_inst_locations(gpl_job* j, int32_t* lx, int32_t* ly) {
 gpl_status gpl_get_gcell_coords(gpl_job* j, float* xy) {
   if (!j || !xy) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
   if (!j->np_ready) { set_error("Nesterov not initialised"); return GPL_ERR_BAD_STATE; }
-  GPL_CUDA(cudaMemcpyAsync(xy, j->d.slp[j->i_cur], (size_t)j->m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
+  GPL_CUDA(cudaMemcpyAsync(xy, j->d.slp[j->S.i_cur], (size_t)j->m.n_g * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
   GPL_CUDA(cudaStreamSynchronize(j->stream));
   return GPL_OK;
 }
@@ -1123,12 +1217,12 @@ gpl_status gpl_eval(gpl_job* j, const float* xy, float cx, float cy, float* wl_g
   if (density_grad) GPL_CUDA(cudaMemcpyAsync(density_grad, d.d_out, ng * sizeof(float2), cudaMemcpyDeviceToHost, j->stream));
   GPL_CUDA(cudaStreamSynchronize(j->stream));
   if (st) {
-    st->overflow_area_f64 = j->last.overflow;
-    st->overflow_area = (int64_t)j->last.overflow;
-    st->hpwl = j->last.hpwl;
-    st->sum_phi = j->last.sum_phi;
-    st->wire_length_grad_sum = j->last.wl_sum;
-    st->density_grad_sum = j->last.d_sum;
+    st->overflow_area_f64 = j->S.last.overflow;
+    st->overflow_area = (int64_t)j->S.last.overflow;
+    st->hpwl = j->S.last.hpwl;
+    st->sum_phi = j->S.last.sum_phi;
+    st->wire_length_grad_sum = j->S.last.wl_sum;
+    st->density_grad_sum = j->S.last.d_sum;
   }
   return GPL_OK;
 }
@@ -1140,8 +1234,8 @@ gpl_status gpl_get_bins(gpl_job* j, int64_t* inst, int64_t* fill, int64_t* np, f
   DeviceModel& d = j->d;
   const size_t nb = (size_t)d.cnt_x * d.cnt_y;
   cudaStream_t s = j->stream;
-  if (inst) GPL_CUDA(cudaMemcpyAsync(inst, d.area[j->last_area], nb * 8, cudaMemcpyDeviceToHost, s));
-  if (fill) GPL_CUDA(cudaMemcpyAsync(fill, d.area[j->last_area] + nb, nb * 8, cudaMemcpyDeviceToHost, s));
+  if (inst) GPL_CUDA(cudaMemcpyAsync(inst, d.area[j->S.last_area], nb * 8, cudaMemcpyDeviceToHost, s));
+  if (fill) GPL_CUDA(cudaMemcpyAsync(fill, d.area[j->S.last_area] + nb, nb * 8, cudaMemcpyDeviceToHost, s));
   if (np) GPL_CUDA(cudaMemcpyAsync(np, d.nonplace, nb * 8, cudaMemcpyDeviceToHost, s));
   if (dens) GPL_CUDA(cudaMemcpyAsync(dens, d.density, nb * 4, cudaMemcpyDeviceToHost, s));
   if (phi) GPL_CUDA(cudaMemcpyAsync(phi, d.phi, nb * 4, cudaMemcpyDeviceToHost, s));

@@ -50,11 +50,13 @@ def test_diverge01_reports_code_3(gpu_lib):
 
 
 def test_run_is_deterministic_and_resumable(gpu_lib):
+    """Chunked runs, on the host loop and on the device loop, log the same
+    iterations as one run to the stop rule."""
     from replace_gb300 import Placer
     nl, opts = case("simple01")
     logs = []
-    for chunks in ((0,), (7, 13, 0)):
-        p = Placer(nl, **params_of(opts))
+    for chunks, dl in (((0,), 0), ((7, 13, 0), 0), ((7, 13, 0), 1)):
+        p = Placer(nl, **params_of(opts), device_loop=dl)
         p.initial_place()
         p.nesterov_init()
         ov, hp = [], []
@@ -63,17 +65,22 @@ def test_run_is_deterministic_and_resumable(gpu_lib):
             ov += list(lg["overflow"]); hp += list(lg["hpwl"])
         logs.append((np.array(ov), np.array(hp), st.hpwl))
         p.close()
-    assert np.array_equal(logs[0][0], logs[1][0]) and np.array_equal(logs[0][1], logs[1][1])
+    for other in logs[1:]:
+        assert np.array_equal(logs[0][0], other[0]) and np.array_equal(logs[0][1], other[1])
+        assert logs[0][2] == other[2]
 
 
-def test_graph_replay_matches_direct_launches(gpu_lib):
+@pytest.mark.parametrize("variant", [dict(use_graph=0), dict(device_loop=1)])
+def test_graph_replay_matches_direct_launches(gpu_lib, variant):
     """An evaluation replayed from the captured CUDA graph and one launched
-    kernel by kernel run the same kernels on the same control record."""
+    kernel by kernel run the same kernels on the same control record; the
+    loop driven from the device (conditional graph node and a control
+    kernel) runs the same control arithmetic as the host loop."""
     from replace_gb300 import Placer
     nl, opts = case("syn10k_b128")
     out = []
-    for g in (1, 0):
-        p = Placer(nl, **params_of(opts), use_graph=g)
+    for kw in (dict(use_graph=1), variant):
+        p = Placer(nl, **params_of(opts), **kw)
         p.initial_place()
         p.nesterov_init()
         rc, st, lg = p.nesterov_run(60, log_capacity=100)
