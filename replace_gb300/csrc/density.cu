@@ -467,6 +467,16 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
       if (i < n) tot[slot] += __ldcg(A.part + (size_t)slot * A.stride + i);
     }
   }
+  // the WA kernel's HPWL accumulators: one per lane of the first warp,
+  // summed by shuffles and cleared for the next evaluation
+  static_assert(kHpwlLanes == 32, "one HPWL accumulator per lane");
+  long long hpwl = 0;
+  if (threadIdx.x < 32) {
+    hpwl = __ldcg(A.hpwl_total + threadIdx.x * kHpwlStride);
+    A.hpwl_total[threadIdx.x * kHpwlStride] = 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) hpwl += __shfl_xor_sync(0xffffffffu, hpwl, o);
+  }
   block_reduce_n<kPartSlots>(tot, A.part_total, 1, sh, 0);   // thread 0 writes part_total[k]
   if (threadIdx.x == 0) {
     for (int slot = 0; slot < kPartSlots; slot++) tot[slot] = A.part_total[slot];
@@ -478,8 +488,7 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
     r.grad_dist = tot[kPartGradDist];
     r.sum_phi = tot[kPartPhi];
     r.nan_flag = tot[kPartNan];
-    r.hpwl = __ldcg(A.hpwl_total);
-    *A.hpwl_total = 0;                      // ready for the next evaluation's WA kernel
+    r.hpwl = hpwl;
     // getStepLength / getDistance (src/nesterovPlace.cpp:555-571, 598-607)
     const float cd = (float)sqrt(r.coord_dist / (2.0 * A.n_g));
     const float gd = (float)sqrt(r.grad_dist / (2.0 * A.n_g));

@@ -154,18 +154,4 @@ __device__ __forceinline__ long long block_sum_ordered_ll(const long long* p, in
   return r;
 }
 
-__device__ __forceinline__ void block_reduce_ll(long long v, long long* out, long long* sh) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) sh[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
-    v = lane < nw ? sh[lane] : 0ll;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) *out = v;
-  }
-  __syncthreads();
-}
-
 }  // namespace gpl

@@ -132,8 +132,7 @@ struct DeviceModel {
   // reduction partials
   double* part = nullptr;          // [kPartSlots * part_stride]
   int part_stride = 0;
-  long long* part_i = nullptr;     // int64 partials (HPWL)
-  long long* hpwl_total = nullptr; // HPWL accumulator (WA blocks add, the gcell kernel reads and clears)
+  long long* hpwl_total = nullptr; // HPWL accumulators (WA warps add, the gcell kernel sums and clears)
   double* part_total = nullptr;    // [kPartSlots] final sums
   unsigned* counters = nullptr;    // [2] last-block counters (gcell kernel, WA kernel)
   int sm_count = 0;
@@ -154,6 +153,11 @@ struct DeviceModel {
 };
 
 constexpr int kFftMax = 4096;
+
+// HPWL accumulators: kHpwlLanes int64 counters kHpwlStride apart (one
+// 32-byte sector each), so the WA warps' atomics spread over them.
+constexpr int kHpwlLanes = 32;
+constexpr int kHpwlStride = 4;
 
 enum PartSlot {
   kPartOverflow = 0, kPartWl, kPartD, kPartCoordDist, kPartGradDist, kPartNan,

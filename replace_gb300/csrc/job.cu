@@ -177,7 +177,7 @@ struct Carver {
 
 // Bytes of a job's arena (the carving in ensure_nb follows the same order).
 size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size_t n_big, size_t nb,
-                   int cnt_x, int cnt_y, size_t part_stride, size_t nnb, size_t log_cap) {
+                   int cnt_x, int cnt_y, size_t part_stride, size_t log_cap) {
   const size_t ps = (size_t)kPartSlots * part_stride;
   int tw, th, tx, ty;
   tile_grid(cnt_x, cnt_y, &tw, &th, &tx, &ty);
@@ -196,7 +196,7 @@ size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size
   S.add(ng, 8); S.add(ng, 8);                 // coordi
   S.add(ng, 8); S.add(ng, 8);                 // hook outputs: wl / density gradients
   S.add(1, sizeof(EvalCtl));
-  S.add(ps, 8); S.add(nnb, 8); S.add(1, sizeof(EvalResult)); S.add(1, 8); S.add(4, 4);
+  S.add(ps, 8); S.add(1, sizeof(EvalResult)); S.add(kHpwlLanes * kHpwlStride, 8); S.add(4, 4);
   S.add(kPartSlots, 8);
   S.add(1, sizeof(NesterovState)); S.add(log_cap, sizeof(IterEntry));   // device loop
   return S.bytes;
@@ -368,12 +368,11 @@ int ensure_nb(gpl_job* j) {
   const size_t ng = m.n_g;
   GPL_CUDA(cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, j->device));
   d.part_stride = std::max(std::max(cell_grid(d), poisson_blocks_a(m.cnt_x, m.cnt_y)), 1);
-  const size_t nnb = std::max(net_blocks(d), 1);
   const size_t ps = (size_t)kPartSlots * d.part_stride;
 
   const size_t log_cap = (size_t)std::max(1, m.p.nesterov_place_max_iter);
   const size_t bytes = arena_bytes(ng, m.n_pins, m.n_nets, m.g_pins.size(), st.big.size(), nb, m.cnt_x,
-                                   m.cnt_y, d.part_stride, nnb, log_cap);
+                                   m.cnt_y, d.part_stride, log_cap);
   cudaError_t e = dev_alloc((void**)&j->arena, bytes, j->pool, j->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -409,9 +408,9 @@ int ensure_nb(gpl_job* j) {
   d.coordi[0] = C.take<float2>(ng); d.coordi[1] = C.take<float2>(ng);
   d.wl_out = C.take<float2>(ng); d.d_out = C.take<float2>(ng);
   d.ctl = C.take<EvalCtl>(1);
-  d.part = C.take<double>(ps); d.part_i = C.take<long long>(nnb);
+  d.part = C.take<double>(ps);
   d.result = C.take<EvalResult>(1);
-  d.hpwl_total = C.take<long long>(1);
+  d.hpwl_total = C.take<long long>(kHpwlLanes * kHpwlStride);
   d.counters = C.take<unsigned>(4);
   d.part_total = C.take<double>(kPartSlots);
   j->d_state = C.take<NesterovState>(1);
@@ -441,7 +440,7 @@ int ensure_nb(gpl_job* j) {
   GPL_CUDA(cudaMemsetAsync(d.part, 0, ps * 8, s));
   GPL_CUDA(cudaMemsetAsync(d.phi, 0, nb * 4, s));
   GPL_CUDA(cudaMemsetAsync(d.counters, 0, 4 * sizeof(unsigned), s));
-  GPL_CUDA(cudaMemsetAsync(d.hpwl_total, 0, sizeof(long long), s));
+  GPL_CUDA(cudaMemsetAsync(d.hpwl_total, 0, sizeof(long long) * kHpwlLanes * kHpwlStride, s));
   d.result_h = &j->pinned->result;
   d.ctl_h = &j->pinned->ctl;
   memset(d.ctl_h, 0, sizeof(EvalCtl));
@@ -1037,10 +1036,10 @@ int job_device_bytes(gpl_job* j, int64_t* bytes, bool centred) {
   for (int i : m.place_insts) n_gpins += m.inst_pin_start[i + 1] - m.inst_pin_start[i];
   const size_t ng = m.place_insts.size() + (size_t)c.n_fill;
   const size_t nb = (size_t)c.cnt_x * c.cnt_y;
-  // upper bounds: every gcell big, one WA block per net, the larger partial grid
+  // upper bounds: every gcell big, the larger partial grid
   const size_t stride = std::max<size_t>((size_t)sm * 8, (size_t)c.cnt_y);
   const size_t arena = arena_bytes(ng, m.n_pins, m.n_nets, n_gpins, ng, nb, c.cnt_x, c.cnt_y, stride,
-                                   (size_t)m.n_nets + kWaBuckets, (size_t)std::max(1, m.p.nesterov_place_max_iter));
+                                   (size_t)std::max(1, m.p.nesterov_place_max_iter));
   const size_t ip = m.p.initial_place_max_iter > 0 ? initial_place_bytes(m, sm) : 0;
   const size_t pg = (m.p.poisson_path != 1 && poisson_gemm_eligible(c.cnt_x, c.cnt_y))
                         ? (size_t)poisson_gemm_bytes(c.cnt_x, c.cnt_y) : 0;

@@ -40,8 +40,7 @@ struct WaArgs {
   const EvalCtl* ctl;
   float bar;                    // minWireLengthForceBar
   float2* pin_grad;             // device pin order
-  long long* part_i;            // HPWL partial per block
-  long long* hpwl_total;        // accumulated by every block
+  long long* hpwl_total;        // kHpwlLanes spread accumulators (stride kHpwlStride)
 };
 
 // This evaluation's coordinates and wire-length coefficients (1/gamma), read
@@ -293,7 +292,6 @@ constexpr int kWaSplit = 6;
 
 template <bool kLarge>
 __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A) {
-  __shared__ long long sh[32];
   WaEval V;
   {
     const EvalCtl* C = A.ctl;
@@ -321,11 +319,16 @@ __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A)
     if (bucket == 6) hp = wa_warp<4>(A, V, 6, lb);
     else hp = wa_huge(A, V, 7, lb);
   }
-  // HPWL is an integer sum: one 64-bit atomic per block gives the exact,
-  // order-independent total (the gcell kernel reads and clears it)
-  block_reduce_ll(hp, &A.part_i[gb], sh);
-  if (threadIdx.x == 0) atomicAdd(reinterpret_cast<unsigned long long*>(A.hpwl_total),
-                                  (unsigned long long)A.part_i[gb]);
+  // HPWL is an integer sum, exact in any order: each warp adds its nets'
+  // total with one 64-bit atomic, spread over kHpwlLanes accumulators (no
+  // block barrier; the gcell kernel sums and clears them)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) hp += __shfl_xor_sync(0xffffffffu, hp, o);
+  if ((threadIdx.x & 31) == 0 && hp != 0) {
+    const int lane_slot = (gb * (kBlock / 32) + (threadIdx.x >> 5)) % kHpwlLanes;
+    atomicAdd(reinterpret_cast<unsigned long long*>(A.hpwl_total + lane_slot * kHpwlStride),
+              (unsigned long long)hp);
+  }
 }
 
 }  // namespace
@@ -347,7 +350,6 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.ctl = d.ctl;
   A.bar = a.min_wl_force_bar;
   A.pin_grad = d.pin_grad;
-  A.part_i = d.part_i;
   A.hpwl_total = d.hpwl_total;
   const int small = d.wa_block_start[kWaSplit];
   const int large = d.wa_block_start[kWaBuckets] - small;
