@@ -153,7 +153,9 @@ typedef struct gpl_job_info {
   int32_t poisson_path;      /* the form the job runs: 1 FFT, 2 tensor-core GEMMs */
   float poisson_fft_us;      /* the timings auto mode compared (0 if not timed) */
   float poisson_gemm_us;
-  int32_t pad;
+  int32_t scatter_tile;      /* the scatter's tile side in bins, chosen by timing (16, 32 or 64) */
+  int32_t scatter_chunk;     /* gcells per scatter block, chosen with the tile */
+  float scatter_us;          /* the chosen shape's scatter time */
 } gpl_job_info;
 
 /* One physics evaluation (the work of NesterovBase for one coordinate set). */

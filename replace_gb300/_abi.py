@@ -81,7 +81,7 @@ class JobInfo(C.Structure):
         ("macro_insts_area", C.c_int64), ("non_place_insts_area", C.c_int64),
         ("device_bytes", C.c_int64),
         ("poisson_path", C.c_int32), ("poisson_fft_us", C.c_float), ("poisson_gemm_us", C.c_float),
-        ("pad", C.c_int32),
+        ("scatter_tile", C.c_int32), ("scatter_chunk", C.c_int32), ("scatter_us", C.c_float),
     ]
 
 

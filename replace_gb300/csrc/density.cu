@@ -55,8 +55,9 @@ __device__ __forceinline__ float2 predict_one(const ScatterArgs& A, const EvalCt
 // ------------------------------------------------------------ tile order
 // The scatter visits gcells tile by tile: a tile is tile_w x tile_h bins, and
 // the gcells whose centres lie in it (at the last ordering) are consecutive
-// in `order`.  A block takes a chunk of at most kScatterChunk gcells of one
-// tile and accumulates their bin areas in a shared-memory window over the
+// in `order`.  A block takes a chunk of at most d.chunk gcells of one tile
+// (the tile side and chunk size are tuned per job, see nesterov_init) and
+// accumulates their bin areas in a shared-memory window over the
 // tile and a margin; the window's non-zero bins then go to the global areas
 // with one 64-bit atomic each.  Bins outside the window (cells that moved
 // away, large cells) go to the global areas directly.  The int64 sums do not
@@ -71,6 +72,7 @@ struct OrderArgs {
   const float2* slp;            // the coordinates to order by, or (slp == nullptr)
   const float2* slp_all[4];     // slot ctl->i_src of these (the device loop)
   const EvalCtl* ctl;
+  int chunk;                    // gcells per chunk (at most)
   int32_t* tile_count;
   int32_t* tile_start;
   int32_t* order;
@@ -100,7 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_order_count(OrderArgs O) {
 
 // One block: exclusive scan of the tile counts into tile_start, fill cursors
 // (tile_count := tile_start), and the chunk table (tiles cut into chunks of
-// at most kScatterChunk gcells).
+// at most O.chunk gcells).
 constexpr int kOrderScanT = 1024;
 __global__ void __launch_bounds__(kOrderScanT) k_order_scan(OrderArgs O) {
   __shared__ int32_t sc[kOrderScanT], sk[kOrderScanT];
@@ -111,7 +113,7 @@ __global__ void __launch_bounds__(kOrderScanT) k_order_scan(OrderArgs O) {
   for (int t = lo; t < hi; t++) {
     const int c = O.tile_count[t];
     cells += c;
-    chunks += (c + kScatterChunk - 1) / kScatterChunk;
+    chunks += (c + O.chunk - 1) / O.chunk;
   }
   sc[threadIdx.x] = cells;
   sk[threadIdx.x] = chunks;
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(kOrderScanT) k_order_scan(OrderArgs O) {
     const int c = O.tile_count[t];
     O.tile_start[t] = at;
     O.tile_count[t] = at;
-    for (int f = 0; f < c; f += kScatterChunk) O.chunks[ck++] = make_int4(t, at + f, at + min(f + kScatterChunk, c), 0);
+    for (int f = 0; f < c; f += O.chunk) O.chunks[ck++] = make_int4(t, at + f, at + min(f + O.chunk, c), 0);
     at += c;
   }
   if (threadIdx.x == kOrderScanT - 1) {
@@ -198,7 +200,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_scatter(ScatterArgs A, TileArgs T
         const int u = a - ox, w = cc - oy;
         if (u >= 0 && u < wx && w >= 0 && w < wy && v < (1ull << 32)) {
           // v < 2^32 split into 16-bit halves added to two 32-bit words: a
-          // chunk has at most kScatterChunk (< 2^16) gcells, one addition
+          // chunk has fewer than 2^16 gcells (set_scatter_shape), one addition
           // each per bin, so neither word can wrap; the adds return nothing
           const int i = half * wn + w * wx + u;
           atomicAdd(&win[i], (unsigned)(v & 0xffffu));
@@ -535,9 +537,8 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   TileArgs T;
   T.tile_w = d.tile_w; T.tile_h = d.tile_h; T.tiles_x = d.tiles_x;
   T.order = d.order; T.chunks = d.chunks; T.n_chunks = d.n_chunks;
-  const size_t smem = (size_t)4 * (d.tile_w + 2 * kTileMargin) * (d.tile_h + 2 * kTileMargin) * 4;
   t.begin(kKScatter);
-  k_scatter<<<d.max_chunks, kBlock, smem, s>>>(A, T);
+  k_scatter<<<d.max_chunks, kBlock, scatter_smem(d), s>>>(A, T);
   if (d.n_big) k_scatter_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
   t.end(kKScatter);
   t.count(d.n_big ? 2 : 1);
@@ -545,16 +546,42 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   return GPL_OK;
 }
 
-void tile_grid(int cnt_x, int cnt_y, int* tw, int* th, int* tx, int* ty) {
-  *tw = std::min(32, cnt_x);
-  *th = std::min(32, cnt_y);
+void tile_grid(int cnt_x, int cnt_y, int side, int* tw, int* th, int* tx, int* ty) {
+  *tw = std::min(side, cnt_x);
+  *th = std::min(side, cnt_y);
   *tx = (cnt_x + *tw - 1) / *tw;
   *ty = (cnt_y + *th - 1) / *th;
 }
 
-// every tile's chunks: one per kScatterChunk gcells, plus one per tile for
-// the partial last chunks
-int scatter_max_chunks(int n_g, int tiles) { return tiles + (n_g + kScatterChunk - 1) / kScatterChunk; }
+// every tile's chunks: one per `chunk` gcells, plus one per tile for the
+// partial last chunks
+int scatter_max_chunks(int n_g, int tiles, int chunk) { return tiles + (n_g + chunk - 1) / chunk; }
+
+bool set_scatter_shape(DeviceModel& d, int side, int chunk) {
+  int tw, th, tx, ty;
+  tile_grid(d.cnt_x, d.cnt_y, side, &tw, &th, &tx, &ty);
+  const int mc = scatter_max_chunks(d.n_g, tx * ty, chunk);
+  if (tx * ty > d.tile_cap || mc > d.chunk_cap || chunk <= 0 || chunk >= 65536) return false;
+  d.tile_w = tw; d.tile_h = th; d.tiles_x = tx; d.tiles_y = ty;
+  d.chunk = chunk;
+  d.max_chunks = mc;
+  return true;
+}
+
+// the window: two 32-bit words (16-bit split) per bin of the tile and its margin
+size_t scatter_smem(const DeviceModel& d) {
+  return (size_t)4 * (d.tile_w + 2 * kTileMargin) * (d.tile_h + 2 * kTileMargin) * 4;
+}
+
+int scatter_prepare_device() {
+  static int done = 0;   // per process (one device in use)
+  if (done) return GPL_OK;
+  const int side = kTileSides[sizeof(kTileSides) / sizeof(kTileSides[0]) - 1];
+  const int smem = 4 * (side + 2 * kTileMargin) * (side + 2 * kTileMargin) * 4;
+  GPL_CUDA(cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  done = 1;
+  return GPL_OK;
+}
 
 int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t) {
   OrderArgs O;
@@ -565,6 +592,7 @@ int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t) {
   O.slp = slot >= 0 ? d.slp[slot] : nullptr;
   for (int k = 0; k < 4; k++) O.slp_all[k] = d.slp[k];
   O.ctl = d.ctl;
+  O.chunk = d.chunk;
   O.tile_count = d.tile_count; O.tile_start = d.tile_start; O.order = d.order;
   O.chunks = d.chunks; O.n_chunks = d.n_chunks;
   t.begin(kKOther);

@@ -139,6 +139,8 @@ struct DeviceModel {
   // gcells ordered by bin tile for the scatter (refreshed every few
   // evaluations; any order gives the same int64 areas)
   int tile_w = 32, tile_h = 32, tiles_x = 1, tiles_y = 1, max_chunks = 1;
+  int chunk = 2048;                // gcells per scatter chunk (at most)
+  int tile_cap = 1, chunk_cap = 1; // capacity of the tile and chunk tables
   int32_t* order = nullptr;        // [n_g] gcell indices, tile by tile
   int32_t* tile_count = nullptr;   // [tiles] counts, then fill cursors
   int32_t* tile_start = nullptr;   // [tiles + 1]
@@ -316,10 +318,23 @@ int launch_loop_head(NesterovState* S, EvalCtl* ctl, cudaGraphConditionalHandle 
 int launch_loop_step(NesterovState* S, EvalCtl* ctl, const EvalResult* res, IterEntry* log, int log_cap,
                      cudaGraphConditionalHandle h_loop, cudaGraphConditionalHandle h_order, cudaStream_t s);
 // Tile grid of a bin grid, and the chunk-table bound, for sizing.
-constexpr int kScatterChunk = 2048;
-static_assert(kScatterChunk < 65536, "the scatter's 16-bit split window sums need < 2^16 gcells per chunk");
-void tile_grid(int cnt_x, int cnt_y, int* tw, int* th, int* tx, int* ty);
-int scatter_max_chunks(int n_g, int tiles);
+// Scatter shapes: tile side in bins and gcells per chunk.  The autotuner
+// (nesterov_init) times these on the job's first coordinates and keeps the
+// fastest; any shape gives the same int64 areas.
+constexpr int kScatterChunk = 2048;               // the default chunk
+constexpr int kTileSides[] = {16, 32, 64};
+constexpr int kScatterChunks[] = {1024, 2048};
+constexpr int kTileSideMin = 16, kScatterChunkMin = 1024;
+static_assert(kScatterChunk < 65536 && kScatterChunks[1] < 65536,
+              "the scatter's 16-bit split window sums need < 2^16 gcells per chunk");
+void tile_grid(int cnt_x, int cnt_y, int side, int* tw, int* th, int* tx, int* ty);
+int scatter_max_chunks(int n_g, int tiles, int chunk);
+// Sets the scatter shape (within the tables' capacity); false if it does not fit.
+bool set_scatter_shape(DeviceModel& d, int side, int chunk);
+// dynamic shared memory of the scatter kernel for the current shape, and the
+// kernel's limit raised to the largest shape (outside any stream capture)
+size_t scatter_smem(const DeviceModel& d);
+int scatter_prepare_device();
 int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t);
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t);
 // the Poisson passes of a job evaluation (area set chosen by EvalCtl)

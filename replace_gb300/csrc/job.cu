@@ -122,6 +122,7 @@ struct gpl_job {
   int log_cap = 0;
   long long order_kernels = 0;
   float poisson_fft_us = 0.0f, poisson_gemm_us = 0.0f;   // auto mode's timings
+  float scatter_us = 0.0f;                                // the chosen scatter shape's time
   bool poisson_chosen = false;
   // WA runs beside the Poisson passes on a second stream (fork after the
   // scatter, join before the gcell kernel)
@@ -179,12 +180,13 @@ struct Carver {
 size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size_t n_big, size_t nb,
                    int cnt_x, int cnt_y, size_t part_stride, size_t log_cap) {
   const size_t ps = (size_t)kPartSlots * part_stride;
+  // tile and chunk tables sized for the smallest scatter shape
   int tw, th, tx, ty;
-  tile_grid(cnt_x, cnt_y, &tw, &th, &tx, &ty);
+  tile_grid(cnt_x, cnt_y, kTileSideMin, &tw, &th, &tx, &ty);
   const size_t tiles = (size_t)tx * ty;
   Sizer S;
   S.add(ng, 4); S.add(tiles, 4); S.add(tiles + 1, 4);
-  S.add(scatter_max_chunks((int)ng, (int)tiles), 16); S.add(1, 4);
+  S.add(scatter_max_chunks((int)ng, (int)tiles, kScatterChunkMin), 16); S.add(1, 4);
   S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
   S.add(n_big, 4); S.add(ng, 4); S.add(n_big, 8);
   S.add(n_pins, 16); S.add(n_nets + 1, 4);
@@ -382,12 +384,17 @@ int ensure_nb(gpl_job* j) {
   }
   d.bytes = (int64_t)bytes;
   Carver C{j->arena};
-  tile_grid(m.cnt_x, m.cnt_y, &d.tile_w, &d.tile_h, &d.tiles_x, &d.tiles_y);
-  d.max_chunks = scatter_max_chunks((int)ng, d.tiles_x * d.tiles_y);
+  {
+    int tw, th, tx, ty;
+    tile_grid(m.cnt_x, m.cnt_y, kTileSideMin, &tw, &th, &tx, &ty);
+    d.tile_cap = tx * ty;
+    d.chunk_cap = scatter_max_chunks((int)ng, d.tile_cap, kScatterChunkMin);
+  }
+  set_scatter_shape(d, 32, kScatterChunk);        // until the autotuner picks
   d.order = C.take<int32_t>(ng);
-  d.tile_count = C.take<int32_t>((size_t)d.tiles_x * d.tiles_y);
-  d.tile_start = C.take<int32_t>((size_t)d.tiles_x * d.tiles_y + 1);
-  d.chunks = C.take<int4>(d.max_chunks);
+  d.tile_count = C.take<int32_t>((size_t)d.tile_cap);
+  d.tile_start = C.take<int32_t>((size_t)d.tile_cap + 1);
+  d.chunks = C.take<int4>(d.chunk_cap);
   d.n_chunks = C.take<int32_t>(1);
   d.g_half = C.take<int2>(ng); d.g_scale = C.take<float>(ng); d.g_kind = C.take<uint8_t>(ng);
   d.g_precond = C.take<float2>(ng); d.g_pin_start = C.take<int32_t>(ng + 1);
@@ -674,21 +681,81 @@ EvalCtl ctl_of(gpl_job* j, int i_eval, int i_ref, bool write_sum) {
 
 bool diverged(const gpl_job* j) { return diverged_result(j->S.last); }
 
+// The scatter's shape (tile side, gcells per chunk): every candidate is
+// timed on the job's first coordinates (slot `slot`) and the fastest kept.  The trial scatters only add into
+// area set 0, which is cleared afterwards; the areas do not depend on the
+// shape.
+int choose_scatter_shape(gpl_job* j, int slot) {
+  DeviceModel& d = j->d;
+  int rc = scatter_prepare_device();
+  if (rc) return rc;
+  // The trials run the predictor as the loop does (its loads and stores are
+  // part of the scatter's cost) with step 0 and coefficient 0, so the
+  // predicted coordinates equal slot `slot`'s; they go to the hook's slot 3
+  // and to coordi[c_next], both unread before they are next written.
+  const size_t ng = (size_t)d.n_g;
+  GPL_CUDA(cudaMemsetAsync(d.sum[slot], 0, ng * sizeof(float2), j->stream));
+  EvalCtl c;
+  memset(&c, 0, sizeof(c));
+  c.predict = 1;
+  c.i_src = slot;
+  c.i_eval = 3;
+  c.i_ref = -1;
+  c.c_cur = j->S.c_cur;
+  c.c_next = j->S.c_next;
+  rc = put_ctl(j, c);
+  if (rc) return rc;
+  Timer quiet;
+  cudaEvent_t a = nullptr, b = nullptr;
+  GPL_CUDA(cudaEventCreate(&a));
+  GPL_CUDA(cudaEventCreate(&b));
+  constexpr int kReps = 3;
+  float best = 1e30f;
+  int best_side = 32, best_chunk = kScatterChunk;
+  int seen[16][3];
+  int n_seen = 0;
+  for (int side : kTileSides) {
+    for (int chunk : kScatterChunks) {
+      if (!set_scatter_shape(d, side, chunk)) continue;
+      bool dup = false;
+      for (int k = 0; k < n_seen; k++) dup |= seen[k][0] == d.tile_w && seen[k][1] == d.tile_h && seen[k][2] == chunk;
+      if (dup || n_seen >= 16) continue;
+      seen[n_seen][0] = d.tile_w; seen[n_seen][1] = d.tile_h; seen[n_seen][2] = chunk;
+      n_seen++;
+      rc = launch_tile_order(d, slot, j->stream, quiet);
+      if (!rc) rc = launch_scatter(d, base_args(j), j->stream, quiet);    // warm-up
+      if (rc) break;
+      cudaEventRecord(a, j->stream);
+      for (int r = 0; r < kReps && !rc; r++) rc = launch_scatter(d, base_args(j), j->stream, quiet);
+      cudaEventRecord(b, j->stream);
+      if (rc) break;
+      float ms = 0.0f;
+      if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        rc = GPL_ERR_CUDA;
+        set_error("scatter autotuner: event timing failed");
+        break;
+      }
+      if (ms < best) { best = ms; best_side = side; best_chunk = chunk; }
+    }
+    if (rc) break;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  set_scatter_shape(d, best_side, best_chunk);
+  j->scatter_us = 1000.0f * best / kReps;
+  const size_t nb = (size_t)d.cnt_x * d.cnt_y;
+  GPL_CUDA(cudaMemsetAsync(d.area[0], 0, 2 * nb * 8, j->stream));
+  GPL_CUDA(cudaMemsetAsync(d.area[1], 0, 2 * nb * 8, j->stream));
+  return GPL_OK;
+}
+
 // NesterovPlace::init (src/nesterovPlace.cpp:64-175)
 int nesterov_init(gpl_job* j) {
   const bool tell = j->m.p.verbose_level >= 2;
   const double t0 = wall_ms();
   int rc = ensure_nb(j);
   if (rc) return rc;
-  const double t1 = wall_ms();
-  rc = choose_poisson_path(j);
-  if (rc) return rc;
-  const double t2 = wall_ms();
-  rc = build_graph(j);
-  if (rc) return rc;
-  if (tell)
-    printf("[NesterovInit] base and device model %.2f ms, Poisson form %.2f ms, graph %.2f ms\n", t1 - t0,
-           t2 - t1, wall_ms() - t2);
   HostModel& m = j->m;
   DeviceModel& d = j->d;
   NesterovState& S = j->S;
@@ -716,6 +783,19 @@ int nesterov_init(gpl_job* j) {
   if (rc) return rc;
   GPL_CUDA(cudaMemcpyAsync(d.slp[j->S.i_prev], d.slp[j->S.i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
   GPL_CUDA(cudaMemcpyAsync(d.coordi[j->S.c_cur], d.slp[j->S.i_cur], ng * sizeof(float2), cudaMemcpyDeviceToDevice, j->stream));
+  const double t1 = wall_ms();
+  // autotuned shapes: the scatter's tile and chunk, then the Poisson form
+  // (both before the evaluation graph is captured)
+  rc = choose_scatter_shape(j, j->S.i_cur);
+  if (rc) return rc;
+  rc = choose_poisson_path(j);
+  if (rc) return rc;
+  const double t2 = wall_ms();
+  rc = build_graph(j);
+  if (rc) return rc;
+  if (tell)
+    printf("[NesterovInit] base, device model and centres %.2f ms, autotuning %.2f ms (scatter tile %dx%d, "
+           "chunk %d), graph %.2f ms\n", t1 - t0, t2 - t1, d.tile_w, d.tile_h, d.chunk, wall_ms() - t2);
   j->S.density_penalty = 0.0f;
   j->S.max_phi_coef = m.p.max_phi_coef;
   j->S.wl_coef_x = j->S.wl_coef_y = 0.0f;
@@ -974,6 +1054,9 @@ void fill_info(gpl_job* j, gpl_job_info* info) {
   info->poisson_path = j->d.poisson_path;
   info->poisson_fft_us = j->poisson_fft_us;
   info->poisson_gemm_us = j->poisson_gemm_us;
+  info->scatter_tile = j->d.tile_w;
+  info->scatter_chunk = j->d.chunk;
+  info->scatter_us = j->scatter_us;
 }
 
 }  // namespace

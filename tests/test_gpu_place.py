@@ -138,3 +138,30 @@ def test_poisson_form_autotuned_per_grid(gpu_lib):
     q.nesterov_init()
     assert q.info.poisson_path == 1 and q.info.poisson_gemm_us == 0
     q.close()
+
+
+def test_scatter_shape_autotuned_and_results_independent_of_it(gpu_lib):
+    """nesterov_init times the scatter's tile / chunk shapes and keeps the
+    fastest; the int64 bin areas (and everything after them) do not depend
+    on the shape: the same coordinates evaluated by a job on the default
+    shape give identical bins and gradients."""
+    from replace_gb300 import Placer
+    nl, opts = case("syn10k_b128")
+    p = Placer(nl, **params_of(opts))
+    p.initial_place()
+    p.nesterov_init()
+    info = p.info
+    assert info.scatter_tile in (16, 32, 64) and info.scatter_chunk in (1024, 2048)
+    assert info.scatter_us > 0
+    xy = p.gcell_coords()
+    _, dg1, st1 = p.eval(xy, 2e-4)
+    b1 = p.bins(info.bin_cnt_x, info.bin_cnt_y)
+    q = Placer(nl, **params_of(opts))            # gpl_eval only: the default shape
+    _, dg2, st2 = q.eval(xy, 2e-4)
+    b2 = q.bins(info.bin_cnt_x, info.bin_cnt_y)
+    for k in ("inst_area", "filler_area", "density", "phi", "ex", "ey"):
+        assert np.array_equal(b1[k], b2[k]), k
+    assert np.array_equal(dg1, dg2)
+    assert st1.overflow_area == st2.overflow_area and st1.hpwl == st2.hpwl
+    p.close()
+    q.close()
