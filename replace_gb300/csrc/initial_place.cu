@@ -1313,8 +1313,13 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   double t_round = wall();
   float err = 0.0f;
   int rounds = 0, iters[2] = {0, 0}, coop_rounds = 0;
-  for (int round = 1; round <= prm.initial_place_max_iter && !rc; round++) {
-    timer.begin(kKOther);
+  // The round's assembly (11 kernels) and a chunk of 8 solver iterations of
+  // the phase form (48 kernels) have fixed arguments for the whole job, so
+  // each is captured once as a CUDA graph and replayed (one launch instead
+  // of tens: small jobs are bound by launches).  Without graphs (use_graph 0,
+  // kernel timing, or a failed capture) the same kernels are launched one
+  // by one.
+  auto assembly = [&]() {
     k_ip_pos<<<blocks_for(m.n_pins), kB, 0, s>>>(D);
     k_ip_bound<<<blocks_for(m.n_nets), kB, 0, s>>>(D);
     k_ip_count<<<dim3(scan_blocks, 2), kB, 0, s>>>(D, P);
@@ -1326,6 +1331,37 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     k_ip_rowsum<<<g2, kB, 0, s>>>(D);
     k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
     k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 1, P.max_iter);
+  };
+  auto phase_chunk = [&]() {
+    for (int k = 0; k < 8; k++) {
+      k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 0, P.max_iter);
+      k_bi_p<<<gs, kB, 0, s>>>(D);
+      k_bi_v<<<gs, kB, stage_bytes(kB), s>>>(D);
+      k_bi_s<<<gs, kB, 0, s>>>(D);
+      k_bi_t<<<gs, kB, stage_bytes(kB), s>>>(D);
+      k_bi_xr<<<gs, kB, 0, s>>>(D, P.max_iter);
+    }
+  };
+  auto capture = [&](auto&& body) -> cudaGraphExec_t {
+    if (!prm.use_graph || timer.enabled) return nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    body();
+    if (cudaStreamEndCapture(s, &g) != cudaSuccess || !g || cudaGraphInstantiate(&e, g, 0) != cudaSuccess) e = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return e;
+  };
+  cudaGraphExec_t assembly_exec = capture(assembly);
+  cudaGraphExec_t chunk_exec = (!cluster && !coop) ? capture(phase_chunk) : nullptr;
+  for (int round = 1; round <= prm.initial_place_max_iter && !rc; round++) {
+    timer.begin(kKOther);
+    if (assembly_exec) {
+      if (cudaGraphLaunch(assembly_exec, s) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+    } else {
+      assembly();
+    }
     timer.end(kKOther);
     timer.count(11);
     bool solved = false;
@@ -1382,13 +1418,10 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     // BiCGSTAB phase by phase: chunks of iterations, then poll the done flags
     for (int it = 0; !solved && it <= 2 * P.max_iter + 2; it += 8) {
       timer.begin(kKOther);
-      for (int k = 0; k < 8; k++) {
-        k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 0, P.max_iter);
-        k_bi_p<<<gs, kB, 0, s>>>(D);
-        k_bi_v<<<gs, kB, stage_bytes(kB), s>>>(D);
-        k_bi_s<<<gs, kB, 0, s>>>(D);
-        k_bi_t<<<gs, kB, stage_bytes(kB), s>>>(D);
-        k_bi_xr<<<gs, kB, 0, s>>>(D, P.max_iter);
+      if (chunk_exec) {
+        if (cudaGraphLaunch(chunk_exec, s) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+      } else {
+        phase_chunk();
       }
       timer.end(kKOther);
       timer.count(48);
@@ -1424,6 +1457,8 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
             cudaSuccess ||
         host_wait(s, sync_ev) != cudaSuccess) rc = GPL_ERR_CUDA;
   }
+  if (assembly_exec) cudaGraphExecDestroy(assembly_exec);
+  if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
   dev_free(D.mem, pool, s);
   if (rc) { set_error("initial place: CUDA error"); return rc; }
   if (fill_overflow) { set_error("initial place: B2B entries exceeded their bound"); return GPL_ERR_CUDA; }
