@@ -148,6 +148,59 @@ __device__ __forceinline__ void group_sum8(float (&S)[8]) {
     S[k] = __shfl_sync(full, V, base + ((k & 4) ? o1 : 0) + ((k & 2) ? o2 : 0) + ((k & 1) ? o3 : 0));
 }
 
+// The exponentials of both pins of a two-pin net, equal to pin_exps of each
+// pin: in every direction one pin is the extreme (exponent exactly 0, and
+// fast_exp(0) = 1 exactly), so only the other pin's exponential is computed,
+// one fast_exp per direction instead of two.
+__device__ __forceinline__ void pair_exps(int2 p0, int2 p1, int lx, int ux, int ly, int uy, float cx, float cy,
+                                          float bar, PinExp& E0, PinExp& E1) {
+  const float a0[4] = {__fmul_rn((float)(lx - p0.x), cx), __fmul_rn((float)(p0.x - ux), cx),
+                       __fmul_rn((float)(ly - p0.y), cy), __fmul_rn((float)(p0.y - uy), cy)};
+  const float a1[4] = {__fmul_rn((float)(lx - p1.x), cx), __fmul_rn((float)(p1.x - ux), cx),
+                       __fmul_rn((float)(ly - p1.y), cy), __fmul_rn((float)(p1.y - uy), cy)};
+  E0.flags = E1.flags = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    // the smaller exponent is the non-extreme pin's (or 0 for a tie)
+    const float am = fminf(a0[k], a1[k]);
+    const float v = am > bar ? fast_exp(am) : 0.0f;
+    E0.e[k] = 0.0f;
+    E1.e[k] = 0.0f;
+    if (a0[k] > bar) { E0.e[k] = a0[k] == am ? v : 1.0f; E0.flags |= 1u << k; }
+    if (a1[k] > bar) { E1.e[k] = a1[k] == am ? v : 1.0f; E1.flags |= 1u << k; }
+  }
+}
+
+// Nets of one or two pins (the most common kind): one thread per net, both
+// pins in registers; the same values as a two-lane group (the group's sums
+// are S0 + S1 in either lane, and float addition commutes).
+__device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval& V, int local_block) {
+  const int k = A.bucket_start[0] + local_block * kBlock + threadIdx.x;
+  if (k >= A.bucket_start[1]) return 0ll;
+  const int s = __ldg(&A.net_start[k]), e = __ldg(&A.net_start[k + 1]);
+  const int2 p0 = pin_pos(V, __ldg(&A.pins[s]));
+  if (e - s == 1) {
+    const PinExp E = pin_exps(p0, p0.x, p0.x, p0.y, p0.y, V.cx, V.cy, A.bar);
+    float S[8];
+    sums_of(p0, E, S);
+    A.pin_grad[s] = pin_gradient(p0, E, S, V.cx, V.cy);
+    return 0ll;
+  }
+  const int2 p1 = pin_pos(V, __ldg(&A.pins[s + 1]));
+  const int lx = min(p0.x, p1.x), ux = max(p0.x, p1.x), ly = min(p0.y, p1.y), uy = max(p0.y, p1.y);
+  PinExp E0, E1;
+  pair_exps(p0, p1, lx, ux, ly, uy, V.cx, V.cy, A.bar, E0, E1);
+  float S[8], T[8];
+  sums_of(p0, E0, S);
+  sums_of(p1, E1, T);
+#pragma unroll
+  for (int t = 0; t < 8; t++) S[t] += T[t];
+  float2* g = A.pin_grad + s;
+  g[0] = pin_gradient(p0, E0, S, V.cx, V.cy);
+  g[1] = pin_gradient(p1, E1, S, V.cx, V.cy);
+  return (long long)((ux - lx) + (uy - ly));
+}
+
 // One net per G-lane group, one pin per lane.
 template <int G>
 __device__ __forceinline__ long long wa_group(const WaArgs& A, const WaEval& V, int bucket,
@@ -308,7 +361,7 @@ __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A)
   long long hp = 0;
   if constexpr (!kLarge) {
     switch (bucket) {
-      case 0: hp = wa_group<2>(A, V, 0, lb); break;
+      case 0: hp = wa_pair(A, V, lb); break;
       case 1: hp = wa_group<4>(A, V, 1, lb); break;
       case 2: hp = wa_group<8>(A, V, 2, lb); break;
       case 3: hp = wa_group<16>(A, V, 3, lb); break;
@@ -333,8 +386,8 @@ __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A)
 
 }  // namespace
 
-// buckets 0-4: lane groups of 2 << bucket; 5-7: a warp per net
-int wa_nets_per_block(int bucket) { return bucket < 5 ? kBlock / (2 << bucket) : kBlock / 32; }
+// bucket 0: a thread per net; 1-4: lane groups of 2 << bucket; 5-7: a warp per net
+int wa_nets_per_block(int bucket) { return bucket == 0 ? kBlock : bucket < 5 ? kBlock / (2 << bucket) : kBlock / 32; }
 
 int net_blocks(const DeviceModel& d) { return d.wa_block_start[kWaBuckets]; }
 
