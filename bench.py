@@ -115,7 +115,7 @@ def algorithmic_bytes(kind, ng, npins, nn, nb):
 # roofline object when the dominant kernel is one of these.
 NCU_TRAFFIC = {
     "1m_cells_1024bins": {
-        "wa_wirelength": 104.6e6, "gcell_gradient": 131.1e6, "density_scatter": 64.7e6,
+        "wa_wirelength": 101.6e6, "gcell_gradient": 131.0e6, "density_scatter": 64.7e6,
         "poisson_rows_dct": 25.2e6, "poisson_cols_solve": 4.3e6, "poisson_rows_inverse": 8.4e6,
     },
 }
