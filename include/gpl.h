@@ -133,6 +133,10 @@ typedef struct gpl_params {
                                               512 bins per axis, for precision), 1 = shared-memory
                                               FFT, 2 = tensor-core GEMMs (bf16 three-term split;
                                               grids with both counts multiples of 128) */
+  int32_t scatter_tile;                    /* scatter tile side in bins (16, 32 or 64); 0 = chosen
+                                              by timing at gpl_nesterov_init */
+  int32_t scatter_chunk;                   /* gcells per scatter block (1024 or 2048); 0 = chosen
+                                              by timing (with the tile) */
   int32_t device_loop;                     /* 0 = the host drives the Nesterov loop, one
                                               evaluation graph at a time (default); 1 = the loop
                                               runs on the device (a CUDA graph with a conditional

@@ -67,6 +67,7 @@ class Params(C.Structure):
         ("use_graph", C.c_int32),
         ("ip_solver", C.c_int32),
         ("poisson_path", C.c_int32),
+        ("scatter_tile", C.c_int32), ("scatter_chunk", C.c_int32),
         ("device_loop", C.c_int32),
     ]
 
@@ -152,7 +153,7 @@ def default_params(**overrides) -> Params:
         target_overflow=0.1, min_phi_coef=0.95, max_phi_coef=1.05,
         min_preconditioner=1.0, initial_prev_coordi_update_coef=100.0,
         reference_hpwl=446000000.0, verbose_level=0, device=0, stream=None, use_graph=1,
-        ip_solver=0, poisson_path=0, device_loop=0,
+        ip_solver=0, poisson_path=0, scatter_tile=0, scatter_chunk=0, device_loop=0,
     )
     for k, v in overrides.items():
         setattr(p, k, v)

@@ -714,8 +714,10 @@ int choose_scatter_shape(gpl_job* j, int slot) {
   int best_side = 32, best_chunk = kScatterChunk;
   int seen[16][3];
   int n_seen = 0;
+  const int want_side = j->m.p.scatter_tile, want_chunk = j->m.p.scatter_chunk;
   for (int side : kTileSides) {
     for (int chunk : kScatterChunks) {
+      if ((want_side && side != want_side) || (want_chunk && chunk != want_chunk)) continue;
       if (!set_scatter_shape(d, side, chunk)) continue;
       bool dup = false;
       for (int k = 0; k < n_seen; k++) dup |= seen[k][0] == d.tile_w && seen[k][1] == d.tile_h && seen[k][2] == chunk;
@@ -743,7 +745,7 @@ int choose_scatter_shape(gpl_job* j, int slot) {
   cudaEventDestroy(b);
   if (rc) return rc;
   set_scatter_shape(d, best_side, best_chunk);
-  j->scatter_us = 1000.0f * best / kReps;
+  j->scatter_us = best < 1e29f ? 1000.0f * best / kReps : 0.0f;
   const size_t nb = (size_t)d.cnt_x * d.cnt_y;
   GPL_CUDA(cudaMemsetAsync(d.area[0], 0, 2 * nb * 8, j->stream));
   GPL_CUDA(cudaMemsetAsync(d.area[1], 0, 2 * nb * 8, j->stream));
@@ -1070,6 +1072,12 @@ int job_new(const gpl_netlist_desc* nl, const gpl_params* p, gpl_job** out) {
   gpl_job* j = new gpl_job();
   int rc = build_placer_base(j->m, nl, p);
   if (rc) { delete j; return rc; }
+  if ((p->scatter_tile && p->scatter_tile != 16 && p->scatter_tile != 32 && p->scatter_tile != 64) ||
+      (p->scatter_chunk && p->scatter_chunk != 1024 && p->scatter_chunk != 2048)) {
+    delete j;
+    set_error("scatter_tile must be 0, 16, 32 or 64 and scatter_chunk 0, 1024 or 2048");
+    return GPL_ERR_INVALID_ARG;
+  }
   if (p->max_back_track < 1 || p->nesterov_place_max_iter < 0) {
     delete j;
     set_error("max_back_track must be at least 1 and nesterov_place_max_iter not negative");
@@ -1168,6 +1176,8 @@ void gpl_params_default(gpl_params* p) {
   p->use_graph = 1;
   p->ip_solver = 0;
   p->poisson_path = 0;
+  p->scatter_tile = 0;
+  p->scatter_chunk = 0;
   p->device_loop = 0;
 }
 

@@ -63,6 +63,18 @@ def test_invalid_netlists_are_rejected_before_any_device_work():
     assert rc == _abi.GPL_ERR_UTIL
 
 
+def test_scatter_shape_parameters_are_checked():
+    from replace_gb300 import load
+    lib = load()
+    nl = N.generate(200, 210, n_io=5, seed=1)
+    h = _abi.DescHolder(nl)
+    for kw in (dict(scatter_tile=48), dict(scatter_chunk=3000)):
+        job = C.c_void_p()
+        rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params(**kw)), C.byref(job))
+        assert rc == _abi.GPL_ERR_INVALID_ARG
+        assert b"scatter" in lib.gpl_last_error()
+
+
 def test_instance_pin_lists_must_cover_each_pin_once():
     """inst_pins (the instance pin order) must list every pin of every
     instance exactly once: a repeated or a missing pin is rejected."""

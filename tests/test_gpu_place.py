@@ -159,9 +159,16 @@ def test_scatter_shape_autotuned_and_results_independent_of_it(gpu_lib):
     q = Placer(nl, **params_of(opts))            # gpl_eval only: the default shape
     _, dg2, st2 = q.eval(xy, 2e-4)
     b2 = q.bins(info.bin_cnt_x, info.bin_cnt_y)
-    for k in ("inst_area", "filler_area", "density", "phi", "ex", "ey"):
-        assert np.array_equal(b1[k], b2[k]), k
-    assert np.array_equal(dg1, dg2)
-    assert st1.overflow_area == st2.overflow_area and st1.hpwl == st2.hpwl
-    p.close()
-    q.close()
+    r = Placer(nl, **params_of(opts), scatter_tile=64, scatter_chunk=2048)   # a forced shape
+    r.initial_place()
+    r.nesterov_init()
+    assert r.info.scatter_tile == 64 and r.info.scatter_chunk == 2048
+    _, dg3, st3 = r.eval(xy, 2e-4)
+    b3 = r.bins(info.bin_cnt_x, info.bin_cnt_y)
+    for bo, dgo, sto in ((b2, dg2, st2), (b3, dg3, st3)):
+        for k in ("inst_area", "filler_area", "density", "phi", "ex", "ey"):
+            assert np.array_equal(b1[k], bo[k]), k
+        assert np.array_equal(dg1, dgo)
+        assert st1.overflow_area == sto.overflow_area and st1.hpwl == sto.hpwl
+    for x in (p, q, r):
+        x.close()
