@@ -453,7 +453,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world,
             "steps": iters_done, "warmup": args.warmup, "ms_per_step": ms / max(iters_done, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded generator, 1M cells)",
+            "data": "synthetic (seeded generator, %d movable cells)" % int((nl.inst_kind == 0).sum()),
             "config": {"workload": args.workload, "cells": int((nl.inst_kind == 0).sum()),
                        "nets": nl.n_nets, "io_pins": int((nl.pin_inst < 0).sum()),
                        "bins": f"{info.bin_cnt_x}x{info.bin_cnt_y}", "gcells": info.n_gcells,

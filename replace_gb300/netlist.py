@@ -480,6 +480,9 @@ WORKLOADS = {
     # profiles are captured on (working set above L2, a few hundred MB)
     "400k_cells_1024bins": dict(n_cells=400_000, n_nets=420_000, n_io=1_000,
                                 n_macros=0, util=0.60, target_density=0.75, bins=1024),
+    # scale-out check beyond the headline size: 4x the cells on 4x the bins
+    "4m_cells_2048bins": dict(n_cells=4_000_000, n_nets=4_200_000, n_io=4_000,
+                              n_macros=0, util=0.60, target_density=0.75, bins=2048),
 }
 
 
