@@ -238,6 +238,18 @@ gpl_status gpl_nesterov_init(struct gpl_job* job, gpl_job_info* info);
 gpl_status gpl_nesterov_run(struct gpl_job* job, int32_t max_iters,
                             gpl_nesterov_stats* stats, gpl_iter_log* log);
 
+/* Per-net weights: the hook of GNet::setCustomWeight / GNet::netWeight
+ * (src/nesterovBase.h:210-212, src/nesterovBase.cpp:264-266).  The reference
+ * stores the weights but does not apply them yet; here each pin's WA gradient
+ * (getWireLengthGradientPinWA, src/nesterovBase.cpp:1383-1440) is multiplied
+ * by its net's weight before the per-gcell sum (the form timing-driven
+ * placers use).  HPWL, the wire-length preconditioner and the initial place
+ * stay unweighted.  weights is [n_nets] in the netlist's net order, each
+ * finite and >= 0; NULL sets every weight back to 1 (no weighting).  May be
+ * called at any time after gpl_create, also between gpl_nesterov_run calls:
+ * every later evaluation uses the new weights. */
+gpl_status gpl_set_net_weights(struct gpl_job* job, const float* weights, int64_t n_nets);
+
 /* Final locations, NesterovPlace::updateDb (src/nesterovPlace.cpp:585-595):
  * lx = dCx - dDx/2, ly = dCy - dDy/2 for movable instances; other instances
  * keep their input location.  Arrays are [n_insts]. */

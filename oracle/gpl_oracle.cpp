@@ -612,10 +612,17 @@ struct Oracle {
       for (int q = netStart[n]; q < netStart[n + 1]; q++) pinNet[q] = n;
   }
 
+  // Per-net weights (GNet::customWeight, src/nesterovBase.h:210-212; stored
+  // but not applied by the reference): empty = every weight 1, otherwise
+  // each pin gradient is scaled by its net's weight before the gcell sum.
+  vector<float> netW;
+
   FP wlGrad(int g, float cx_, float cy_) const {
     FP s;
     for (int t = gPinStart[g]; t < gPinStart[g + 1]; t++) {
-      FP v = pinGrad(gPins[t], pinNet[gPins[t]], cx_, cy_);
+      const int n = pinNet[gPins[t]];
+      FP v = pinGrad(gPins[t], n, cx_, cy_);
+      if (!netW.empty()) { v.x *= netW[n]; v.y *= netW[n]; }
       s.x += v.x; s.y += v.y;
     }
     return s;
@@ -1049,6 +1056,14 @@ void* orc_create(const gpl_netlist_desc* d, const gpl_params* p, int* status) {
 }
 
 void orc_destroy(void* h) { delete (Oracle*)h; }
+
+int orc_set_net_weights(void* h, const float* w, int64_t n) {
+  Oracle* o = (Oracle*)h;
+  if (!w) { o->netW.clear(); return 0; }
+  if (n != o->nNets) return 1;
+  o->netW.assign(w, w + n);
+  return 0;
+}
 
 int orc_initial_place(void* h, gpl_ip_stats* st) { return ((Oracle*)h)->initialPlace(st); }
 

@@ -45,6 +45,7 @@ def lib():
         L.orc_create.restype = vp
         L.orc_create.argtypes = [C.POINTER(_abi.NetlistDesc), C.POINTER(_abi.Params), C.POINTER(C.c_int)]
         L.orc_destroy.argtypes = [vp]
+        L.orc_set_net_weights.argtypes = [vp, vp, C.c_int64]
         L.orc_initial_place.argtypes = [vp, C.POINTER(_abi.IpStats)]
         L.orc_nesterov_base.argtypes = [vp, C.POINTER(_abi.JobInfo)]
         L.orc_nesterov_init.argtypes = [vp, C.POINTER(_abi.JobInfo)]
@@ -82,6 +83,15 @@ class Oracle:
         if getattr(self, "h", None):
             lib().orc_destroy(self.h)
             self.h = None
+
+    def set_net_weights(self, weights=None):
+        """Per-net weights in net order (None: every weight 1)."""
+        if weights is None:
+            rc = lib().orc_set_net_weights(self.h, None, 0)
+        else:
+            self._w = np.ascontiguousarray(weights, dtype=np.float32)
+            rc = lib().orc_set_net_weights(self.h, _p(self._w), len(self._w))
+        assert rc == 0, rc
 
     def initial_place(self):
         s = _abi.IpStats()

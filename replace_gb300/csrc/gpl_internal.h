@@ -100,6 +100,8 @@ struct DeviceModel {
   int wa_bucket_start[kWaBuckets + 1] = {0};    // first net of each bucket
   int wa_block_start[kWaBuckets + 1] = {0};     // first block of each bucket in the WA launch
   float2* pin_grad = nullptr;      // WA gradient per device pin
+  float* net_w = nullptr;          // per-net weight, bucket order
+  bool net_weighted = false;       // launch the weighted WA variant
   // bin grid
   int cnt_x = 0, cnt_y = 0, size_x = 0, size_y = 0;
   int core_lx, core_ly, core_ux, core_uy;

@@ -94,6 +94,7 @@ struct DevStage {
   std::vector<float> wx, wy;
   int wa_bucket_start[kWaBuckets + 1] = {0};
   int wa_block_start[kWaBuckets + 1] = {0};
+  std::vector<int32_t> net_rank;       // device (bucket-order) index of each net
 };
 
 struct gpl_job {
@@ -134,6 +135,10 @@ struct gpl_job {
   int prep_rc = 0;
   std::string prep_err;
   bool static_done = false;
+  // per-net weights in the netlist's net order (empty: every weight 1) and
+  // the device index of each net, for uploads after the device model exists
+  std::vector<float> net_w;
+  std::vector<int32_t> net_rank;
 };
 
 namespace {
@@ -190,7 +195,7 @@ size_t arena_bytes(size_t ng, size_t n_pins, size_t n_nets, size_t n_gpins, size
   S.add(ng, sizeof(int2)); S.add(ng, 4); S.add(ng, 1); S.add(ng, 8); S.add(ng + 1, 4);
   S.add(n_big, 4); S.add(ng, 4); S.add(n_big, 8);
   S.add(n_pins, 16); S.add(n_nets + 1, 4);
-  S.add(n_pins, 8); S.add(n_gpins, 4);
+  S.add(n_pins, 8); S.add(n_nets, 4); S.add(n_gpins, 4);
   S.add(2 * nb, 8); S.add(2 * nb, 8); S.add(nb, 8);
   S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 4); S.add(nb, 8); S.add(nb, 4);
   S.add(cnt_x, 4); S.add(cnt_y, 4); S.add(cnt_x, 8); S.add(cnt_y, 8); S.add(kFftMax / 2, 8);
@@ -269,7 +274,8 @@ int stage_device_model(const HostModel& m, DevStage& st) {
   pins.resize(m.n_pins);
   dnet_start.assign(m.n_nets + 1, 0);
   {
-    std::vector<int32_t> rank(m.n_nets);
+    std::vector<int32_t>& rank = st.net_rank;
+    rank.assign(m.n_nets, 0);
     int w = 0;
     for (int k = 0; k < m.n_nets; k++) {
       const int n = net_order[k];
@@ -340,6 +346,38 @@ int finish_static_prep(gpl_job* j) {
   return GPL_OK;
 }
 
+int build_graph(gpl_job* j);
+
+// Uploads the job's net weights in device net order (stream-ordered after
+// earlier evaluations) and selects the WA kernel variant; when that changes,
+// the captured graphs are rebuilt (evaluation) or dropped until the next run
+// (device loop).
+int apply_net_weights(gpl_job* j) {
+  DeviceModel& d = j->d;
+  const bool on = !j->net_w.empty();
+  if (on) {
+    std::vector<float> w(j->net_w.size());
+    for (size_t n = 0; n < w.size(); n++) w[j->net_rank[n]] = j->net_w[n];
+    int rc = upload(d.net_w, w.data(), w.size() * sizeof(float), j->stream);
+    if (rc) return rc;
+    GPL_CUDA(cudaStreamSynchronize(j->stream));
+  }
+  if (on == d.net_weighted) return GPL_OK;
+  d.net_weighted = on;
+  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  if (j->loop_exec) {
+    cudaGraphExecDestroy(j->loop_exec);
+    j->loop_exec = nullptr;
+    j->loop_tried = false;
+  }
+  if (j->graph_exec) {
+    cudaGraphExecDestroy(j->graph_exec);
+    j->graph_exec = nullptr;
+    return build_graph(j);
+  }
+  return GPL_OK;
+}
+
 // NesterovBase, then the device model (one arena).
 int ensure_nb(gpl_job* j) {
   if (j->nb_ready) return GPL_OK;
@@ -403,6 +441,7 @@ int ensure_nb(gpl_job* j) {
   d.pins = C.take<int4>(m.n_pins);
   d.net_start = C.take<int32_t>(m.n_nets + 1);
   d.pin_grad = C.take<float2>(m.n_pins);
+  d.net_w = C.take<float>(m.n_nets);
   d.g_pins = C.take<int32_t>(m.g_pins.size());
   d.area[0] = C.take<unsigned long long>(2 * nb); d.area[1] = C.take<unsigned long long>(2 * nb);
   d.nonplace = C.take<int64_t>(nb);
@@ -452,9 +491,10 @@ int ensure_nb(gpl_job* j) {
   d.ctl_h = &j->pinned->ctl;
   memset(d.ctl_h, 0, sizeof(EvalCtl));
   GPL_CUDA(cudaStreamSynchronize(s));
+  j->net_rank.swap(j->stage->net_rank);
   j->stage.reset();     // the host copies are no longer needed
   j->nb_ready = true;
-  return GPL_OK;
+  return apply_net_weights(j);
 }
 
 EvalArgs base_args(gpl_job* j) {
@@ -1225,6 +1265,24 @@ void gpl_destroy(gpl_job* j) {
   if (j->ev_join) cudaEventDestroy(j->ev_join);
   if (j->own_stream && j->stream) cudaStreamDestroy(j->stream);
   delete j;
+}
+
+gpl_status gpl_set_net_weights(gpl_job* j, const float* w, int64_t n_nets) {
+  if (!j) { set_error("null job"); return GPL_ERR_INVALID_ARG; }
+  if (w) {
+    if (n_nets != j->m.n_nets) { set_error("net weights: n_nets differs from the netlist's"); return GPL_ERR_INVALID_ARG; }
+    for (int64_t n = 0; n < n_nets; n++)
+      if (!(w[n] >= 0.0f) || !std::isfinite(w[n])) {
+        set_error("net weights must be finite and >= 0 (net " + std::to_string(n) + ")");
+        return GPL_ERR_INVALID_ARG;
+      }
+    j->net_w.assign(w, w + n_nets);
+  } else {
+    j->net_w.clear();
+  }
+  if (!j->nb_ready) return GPL_OK;       // uploaded with the device model
+  cudaSetDevice(j->device);
+  return (gpl_status)apply_net_weights(j);
 }
 
 gpl_status gpl_nesterov_init(gpl_job* j, gpl_job_info* info) {

@@ -19,6 +19,11 @@
 // of 8 per step) and then broadcast.  Nets of more than 128 pins take a warp
 // each and loop over their pins.  One launch covers all buckets (the block
 // index selects the bucket), so warps never mix net sizes.
+//
+// Optional per-net weights (GNet::customWeight, src/nesterovBase.h:210-212)
+// scale each pin gradient as it is written.  They are a compile-time variant
+// of the kernel: the unweighted one keeps its register count (48 -> 40 per
+// thread, six blocks of 256 threads per SM instead of five).
 #include <climits>
 
 #include <cuda_runtime.h>
@@ -40,20 +45,33 @@ struct WaArgs {
   const EvalCtl* ctl;
   float bar;                    // minWireLengthForceBar
   float2* pin_grad;             // device pin order
+  const float* net_w;           // per-net weights (bucket order), weighted variant only
   long long* hpwl_total;        // kHpwlLanes spread accumulators (stride kHpwlStride)
 };
 
 // This evaluation's coordinates and wire-length coefficients (1/gamma), read
 // from the control record; kept apart from the (constant) kernel parameters.
+template <bool kW>
 struct WaEval {
   const float2* slp;
+  const float* w;               // per-net weights (kW only)
   float cx, cy;
 };
+
+// Net k's weight times a pin gradient (the weighted sum that timing-driven
+// placers form per gcell: weight x getWireLengthGradientPinWA).
+template <bool kW>
+__device__ __forceinline__ float2 weighed(const WaEval<kW>& V, int k, float2 g) {
+  if constexpr (!kW) return g;
+  const float w = __ldg(&V.w[k]);
+  return make_float2(__fmul_rn(g.x, w), __fmul_rn(g.y, w));
+}
 
 // Pin centre: gcell pins follow the truncated density centre
 // (GPin::updateDensityLocation, src/nesterovBase.cpp:411-415); other pins
 // keep their fixed position.
-__device__ __forceinline__ int2 pin_pos(const WaEval& V, const int4& r) {
+template <bool kW>
+__device__ __forceinline__ int2 pin_pos(const WaEval<kW>& V, const int4& r) {
   if (r.x < 0) return make_int2(r.y, r.z);
   const float2 c = __ldg(&V.slp[r.x]);
   return make_int2(__float2int_rz(c.x) + r.y, __float2int_rz(c.y) + r.z);
@@ -174,7 +192,8 @@ __device__ __forceinline__ void pair_exps(int2 p0, int2 p1, int lx, int ux, int 
 // Nets of one or two pins (the most common kind): one thread per net, both
 // pins in registers; the same values as a two-lane group (the group's sums
 // are S0 + S1 in either lane, and float addition commutes).
-__device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval& V, int local_block) {
+template <bool kW>
+__device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval<kW>& V, int local_block) {
   const int k = A.bucket_start[0] + local_block * kBlock + threadIdx.x;
   if (k >= A.bucket_start[1]) return 0ll;
   const int s = __ldg(&A.net_start[k]), e = __ldg(&A.net_start[k + 1]);
@@ -183,7 +202,7 @@ __device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval& V, i
     const PinExp E = pin_exps(p0, p0.x, p0.x, p0.y, p0.y, V.cx, V.cy, A.bar);
     float S[8];
     sums_of(p0, E, S);
-    A.pin_grad[s] = pin_gradient(p0, E, S, V.cx, V.cy);
+    A.pin_grad[s] = weighed(V, k, pin_gradient(p0, E, S, V.cx, V.cy));
     return 0ll;
   }
   const int2 p1 = pin_pos(V, __ldg(&A.pins[s + 1]));
@@ -196,14 +215,14 @@ __device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval& V, i
 #pragma unroll
   for (int t = 0; t < 8; t++) S[t] += T[t];
   float2* g = A.pin_grad + s;
-  g[0] = pin_gradient(p0, E0, S, V.cx, V.cy);
-  g[1] = pin_gradient(p1, E1, S, V.cx, V.cy);
+  g[0] = weighed(V, k, pin_gradient(p0, E0, S, V.cx, V.cy));
+  g[1] = weighed(V, k, pin_gradient(p1, E1, S, V.cx, V.cy));
   return (long long)((ux - lx) + (uy - ly));
 }
 
 // One net per G-lane group, one pin per lane.
-template <int G>
-__device__ __forceinline__ long long wa_group(const WaArgs& A, const WaEval& V, int bucket,
+template <int G, bool kW>
+__device__ __forceinline__ long long wa_group(const WaArgs& A, const WaEval<kW>& V, int bucket,
                                               int local_block) {
   const int per_block = kBlock / G;
   const int grp = threadIdx.x / G, li = threadIdx.x % G;
@@ -255,13 +274,13 @@ __device__ __forceinline__ long long wa_group(const WaArgs& A, const WaEval& V, 
 #pragma unroll
       for (int t = 0; t < 8; t++) S[t] += __shfl_xor_sync(0xffffffffu, S[t], o);
   }
-  if (valid) A.pin_grad[q] = pin_gradient(p, E, S, V.cx, V.cy);
+  if (valid) A.pin_grad[q] = weighed(V, k, pin_gradient(p, E, S, V.cx, V.cy));
   return (net_ok && li == 0) ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
 // One warp per net of up to 32 P pins, P pins per lane kept in registers.
-template <int P>
-__device__ __forceinline__ long long wa_warp(const WaArgs& A, const WaEval& V, int bucket,
+template <int P, bool kW>
+__device__ __forceinline__ long long wa_warp(const WaArgs& A, const WaEval<kW>& V, int bucket,
                                              int local_block) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -297,12 +316,13 @@ __device__ __forceinline__ long long wa_warp(const WaArgs& A, const WaEval& V, i
   group_sum8<32>(S);
 #pragma unroll
   for (int j = 0; j < P; j++)
-    if (ok[j]) A.pin_grad[s + lane + 32 * j] = pin_gradient(p[j], E[j], S, V.cx, V.cy);
+    if (ok[j]) A.pin_grad[s + lane + 32 * j] = weighed(V, k, pin_gradient(p[j], E[j], S, V.cx, V.cy));
   return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
 // One warp per net of more than 128 pins; lanes stride over the pins.
-__device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval& V, int bucket,
+template <bool kW>
+__device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval<kW>& V, int bucket,
                                              int local_block) {
   const int lane = threadIdx.x & 31;
   const int k = A.bucket_start[bucket] + local_block * (kBlock / 32) + (threadIdx.x >> 5);
@@ -333,7 +353,7 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval& V, i
     const int4 r = __ldg(&A.pins[q]);
     const int2 p = pin_pos(V, r);
     const PinExp E = pin_exps(p, lx, ux, ly, uy, V.cx, V.cy, A.bar);
-    A.pin_grad[q] = pin_gradient(p, E, S, V.cx, V.cy);
+    A.pin_grad[q] = weighed(V, k, pin_gradient(p, E, S, V.cx, V.cy));
   }
   return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
@@ -343,15 +363,16 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval& V, i
 // not lower the occupancy of the common case.
 constexpr int kWaSplit = 6;
 
-template <bool kLarge>
+template <bool kLarge, bool kW>
 __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A) {
-  WaEval V;
+  WaEval<kW> V;
   {
     const EvalCtl* C = A.ctl;
     const int i = C->i_eval;
     V.slp = i == 0 ? A.slp_all[0] : i == 1 ? A.slp_all[1] : i == 2 ? A.slp_all[2] : A.slp_all[3];
     V.cx = C->wl_coef_x;
     V.cy = C->wl_coef_y;
+    V.w = A.net_w;
   }
   const int gb = (int)blockIdx.x + (kLarge ? A.block_start[kWaSplit] : 0);
   int bucket = kLarge ? kWaSplit : 0;
@@ -362,14 +383,14 @@ __global__ void __launch_bounds__(kBlock) k_wa(const __grid_constant__ WaArgs A)
   if constexpr (!kLarge) {
     switch (bucket) {
       case 0: hp = wa_pair(A, V, lb); break;
-      case 1: hp = wa_group<4>(A, V, 1, lb); break;
-      case 2: hp = wa_group<8>(A, V, 2, lb); break;
-      case 3: hp = wa_group<16>(A, V, 3, lb); break;
-      case 4: hp = wa_group<32>(A, V, 4, lb); break;
-      default: hp = wa_warp<2>(A, V, 5, lb); break;
+      case 1: hp = wa_group<4, kW>(A, V, 1, lb); break;
+      case 2: hp = wa_group<8, kW>(A, V, 2, lb); break;
+      case 3: hp = wa_group<16, kW>(A, V, 3, lb); break;
+      case 4: hp = wa_group<32, kW>(A, V, 4, lb); break;
+      default: hp = wa_warp<2, kW>(A, V, 5, lb); break;
     }
   } else {
-    if (bucket == 6) hp = wa_warp<4>(A, V, 6, lb);
+    if (bucket == 6) hp = wa_warp<4, kW>(A, V, 6, lb);
     else hp = wa_huge(A, V, 7, lb);
   }
   // HPWL is an integer sum, exact in any order: each warp adds its nets'
@@ -403,12 +424,18 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.ctl = d.ctl;
   A.bar = a.min_wl_force_bar;
   A.pin_grad = d.pin_grad;
+  A.net_w = d.net_w;
   A.hpwl_total = d.hpwl_total;
   const int small = d.wa_block_start[kWaSplit];
   const int large = d.wa_block_start[kWaBuckets] - small;
   t.begin(kKWa);
-  if (small) k_wa<false><<<small, kBlock, 0, s>>>(A);
-  if (large) k_wa<true><<<large, kBlock, 0, s>>>(A);
+  if (d.net_weighted) {
+    if (small) k_wa<false, true><<<small, kBlock, 0, s>>>(A);
+    if (large) k_wa<true, true><<<large, kBlock, 0, s>>>(A);
+  } else {
+    if (small) k_wa<false, false><<<small, kBlock, 0, s>>>(A);
+    if (large) k_wa<true, false><<<large, kBlock, 0, s>>>(A);
+  }
   t.end(kKWa);
   t.count((small ? 1 : 0) + (large ? 1 : 0));
   GPL_CUDA(cudaGetLastError());

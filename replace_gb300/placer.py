@@ -55,6 +55,16 @@ class Placer:
     def __exit__(self, *a):
         self.close()
 
+    def set_net_weights(self, weights=None):
+        """Per-net weights in net order (GNet::setCustomWeight for every net,
+        src/nesterovBase.cpp:264-266); None sets every weight back to 1.
+        Allowed between nesterov_run calls."""
+        if weights is None:
+            check(self.lib.gpl_set_net_weights(self.h, None, 0))
+            return
+        self._net_w = np.ascontiguousarray(weights, dtype=np.float32)
+        check(self.lib.gpl_set_net_weights(self.h, _p(self._net_w), len(self._net_w)))
+
     # -- stages ---------------------------------------------------------------
     def initial_place(self):
         st = _abi.IpStats()
@@ -184,6 +194,7 @@ class Replace:
         self.incrementalPlaceMode_ = False
         self.verbose_ = 0
         self.device_ = 0
+        self.netWeights_ = None
 
     # setDb(odb::dbDatabase*) counterpart
     def setNetlist(self, netlist):
@@ -208,6 +219,19 @@ class Replace:
     def setIncrementalPlaceMode(self, m): self.incrementalPlaceMode_ = bool(m)
     def setVerboseLevel(self, v): self.verbose_ = int(v)
 
+    def setNetWeights(self, w):
+        """GNet::setCustomWeight for every net (net order); None = all 1.
+        Applies to the current job at once and to jobs made later."""
+        self.netWeights_ = None if w is None else np.asarray(w, dtype=np.float32)
+        if self._placer is not None:
+            self._placer.set_net_weights(self.netWeights_)
+
+    def _new_placer(self):
+        p = Placer(self._netlist, self.params())
+        if self.netWeights_ is not None:
+            p.set_net_weights(self.netWeights_)
+        return p
+
     def params(self) -> _abi.Params:
         return _abi.default_params(
             initial_place_max_iter=self.initialPlaceMaxIter_,
@@ -231,7 +255,7 @@ class Replace:
         reference builds a new PlacerBase here), then the initial place."""
         if self._netlist is None:
             raise GplError(_abi.GPL_ERR_BAD_STATE, "setNetlist first")
-        self._placer = Placer(self._netlist, self.params())
+        self._placer = self._new_placer()
         self.ip_stats = self._placer.initial_place()
         return self.ip_stats
 
@@ -240,7 +264,7 @@ class Replace:
         if self._placer is None:
             if self._netlist is None:
                 raise GplError(_abi.GPL_ERR_BAD_STATE, "setNetlist first")
-            self._placer = Placer(self._netlist, self.params())
+            self._placer = self._new_placer()
         self._placer.nesterov_init()
         rc, st, lg = self._placer.nesterov_run(0, log_capacity=log_capacity)
         self.np_stats = st

@@ -172,3 +172,62 @@ def test_scatter_shape_autotuned_and_results_independent_of_it(gpu_lib):
         assert st1.overflow_area == sto.overflow_area and st1.hpwl == sto.hpwl
     for x in (p, q, r):
         x.close()
+
+
+@pytest.mark.parametrize("name", ["simple02", "syn_macro"])
+def test_place_with_net_weights_matches_oracle(gpu_lib, oracle_mod, name):
+    """A whole weighted run (weights set before the initial place, also when
+    they change between chunks) against the oracle's run with the same
+    weights: same first logged iteration, overflow at target, final HPWL
+    within 0.5 %."""
+    from replace_gb300 import Placer
+    nl, opts = case(name)
+    n = nl.n_nets
+    rng = np.random.default_rng(11)
+    w1 = rng.lognormal(0.0, 0.5, n).astype(np.float32)
+    w2 = np.where(rng.random(n) < 0.2, 4.0, 1.0).astype(np.float32)
+    runs = []
+    for mk in ("gpu", "oracle"):
+        p = Placer(nl, **params_of(opts)) if mk == "gpu" else oracle_mod.Oracle(nl, **params_of(opts))
+        p.set_net_weights(w1)
+        p.initial_place()
+        p.nesterov_init()
+        _, _, lg1 = p.nesterov_run(40, log_capacity=4000)
+        p.set_net_weights(w2)
+        rc, st, lg2 = p.nesterov_run(0, log_capacity=4000)
+        runs.append((rc, st.finished, st.overflow, st.hpwl, st.iterations, lg1))
+    g, o = runs
+    assert g[0] == 0 and o[0] == 0 and g[1] and o[1]
+    assert abs(g[5]["overflow"][0] - o[5]["overflow"][0]) <= 1e-3
+    assert abs(int(g[5]["hpwl"][0]) - int(o[5]["hpwl"][0])) <= 1e-3 * int(o[5]["hpwl"][0])
+    assert g[2] <= 0.1 and o[2] <= 0.1
+    assert abs(g[3] - o[3]) <= 0.005 * o[3]
+    assert abs(g[4] - o[4]) <= max(15, 0.15 * o[4])
+
+
+@pytest.mark.parametrize("device_loop", [0, 1])
+def test_net_weights_switched_on_and_off_between_chunks(gpu_lib, oracle_mod, device_loop):
+    """Weights switched on after the evaluation graphs exist, then off again:
+    the graphs are rebuilt for the other WA variant and the run follows the
+    oracle's run with the same schedule."""
+    from replace_gb300 import Placer
+    nl, opts = case("syn_macro")
+    w = np.random.default_rng(5).lognormal(0.0, 0.7, nl.n_nets).astype(np.float32)
+    runs = []
+    for mk in ("gpu", "oracle"):
+        p = (Placer(nl, **params_of(opts), device_loop=device_loop) if mk == "gpu"
+             else oracle_mod.Oracle(nl, **params_of(opts)))
+        p.initial_place()
+        p.nesterov_init()
+        p.nesterov_run(30)
+        p.set_net_weights(w)
+        _, _, lg = p.nesterov_run(30, log_capacity=100)
+        p.set_net_weights(None)
+        rc, st, _ = p.nesterov_run(0)
+        runs.append((rc, st.finished, st.overflow, st.hpwl, lg))
+    g, o = runs
+    assert g[0] == 0 and o[0] == 0 and g[1] and o[1]
+    # the first weighted iteration follows 30 unweighted ones: FP32 transform
+    # rounding has had 30 iterations to move the two runs apart
+    assert abs(int(g[4]["hpwl"][0]) - int(o[4]["hpwl"][0])) <= 5e-3 * int(o[4]["hpwl"][0])
+    assert g[2] <= 0.1 and abs(g[3] - o[3]) <= 0.005 * o[3]

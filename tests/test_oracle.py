@@ -122,3 +122,34 @@ def test_initial_place_matches_reference_log(oracle_mod, name):
         h = nl.bbox_hpwl(lx, ly)
         assert abs(h - int(ref["hpwl"][k])) <= 1e-4 * int(ref["hpwl"][k]), (k, h)
         assert st.last_error < 1e-6
+
+
+def test_net_weights_scale_pin_gradients(oracle_mod):
+    """Per-net weights (GNet::customWeight): weight 1 everywhere is the
+    unweighted gradient bit for bit, weight 2 doubles it exactly, and two
+    complementary 0/1 weightings add up to the unweighted gradient; HPWL and
+    the density gradient do not change."""
+    nl, opts = case("simple02")
+    ref = golden("eval_simple02.npz")
+    o = oracle_mod.Oracle(nl, **params_of(opts))
+    o.initial_place()
+    assert o.nesterov_base() == 0
+    wlc = float(ref["fscalars"][1])
+    wl0, dg0, st0, _ = o.eval(ref["coords"], wlc)
+    n = nl.n_nets
+    o.set_net_weights(np.ones(n, np.float32))
+    wl1, dg1, st1, _ = o.eval(ref["coords"], wlc)
+    assert np.array_equal(wl1, wl0) and np.array_equal(dg1, dg0) and st1.hpwl == st0.hpwl
+    o.set_net_weights(np.full(n, 2.0, np.float32))
+    wl2, _, _, _ = o.eval(ref["coords"], wlc)
+    assert np.array_equal(wl2, 2.0 * wl0)
+    sel = np.random.default_rng(4).random(n) < 0.3
+    o.set_net_weights(sel.astype(np.float32))
+    wa, _, _, _ = o.eval(ref["coords"], wlc)
+    o.set_net_weights((~sel).astype(np.float32))
+    wb, dgb, stb, _ = o.eval(ref["coords"], wlc)
+    assert rel_l2(wa + wb, wl0) < 1e-6
+    assert np.array_equal(dgb, dg0) and stb.hpwl == st0.hpwl
+    o.set_net_weights(None)
+    wl3, _, _, _ = o.eval(ref["coords"], wlc)
+    assert np.array_equal(wl3, wl0)
