@@ -457,6 +457,390 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp form for 1024 x 1024 grids.  One warp transforms one packed pair (two
+// rows or two columns as real and imaginary parts) end to end, so the passes
+// need no block barriers; the 1024-point FFT keeps 32 elements per lane in
+// registers (four-step: 32-point DFTs along n2 in each lane, the twiddle
+// W^(n1 k2), one transpose through padded shared memory, 32-point DFTs along
+// n1) instead of five shared-memory radix-4 passes.  The density of each bin
+// comes from a separate grid-wide kernel, whose high occupancy suits the
+// DRAM-bound int64 reads better than a warp per row pair.
+
+constexpr int kWN = 1024;           // sequence length of the warp form
+constexpr int kWBuf = 2 * 32 * 33;  // floats per warp buffer: 1024 float2, or the padded transpose
+
+// exp(-2 pi i n1 k2 / 1024) at [k2 * 32 + n1]: one coalesced row per k2.
+__device__ __align__(16) float2 g_tw1024[kWN];
+
+__host__ __device__ constexpr int brev5(int r) {
+  return ((r & 1) << 4) | ((r & 2) << 2) | (r & 4) | ((r & 8) >> 2) | ((r & 16) >> 4);
+}
+
+// cos and sin of 2 pi m / 32, m = 0..8 (the other octants by symmetry).
+__host__ __device__ constexpr float cos32_oct(int m) {
+  return m == 0 ? 1.0f : m == 1 ? 0.980785280403230449f : m == 2 ? 0.923879532511286756f
+       : m == 3 ? 0.831469612302545237f : m == 4 ? 0.707106781186547524f
+       : m == 5 ? 0.555570233019602225f : m == 6 ? 0.382683432365089772f
+       : m == 7 ? 0.195090322016128268f : 0.0f;
+}
+__host__ __device__ constexpr float cos32(int m) {   // 0 <= m < 16
+  return m <= 8 ? cos32_oct(m) : -cos32_oct(16 - m);
+}
+__host__ __device__ constexpr float sin32(int m) {   // 0 <= m < 16
+  return m <= 8 ? cos32_oct(8 - m) : cos32_oct(m - 8);
+}
+
+// In-register 32-point DFT, radix-2 decimation in frequency: natural input
+// order, register r ends with output brev5(r).  Twiddles exp(kSign 2 pi i m /
+// 32) are compile-time constants after unrolling.
+template <int kSign>
+__device__ __forceinline__ void dft32(float (&re)[32], float (&im)[32]) {
+#pragma unroll
+  for (int len = 32; len >= 2; len >>= 1) {
+    const int half = len >> 1;
+#pragma unroll
+    for (int start = 0; start < 32; start += len) {
+#pragma unroll
+      for (int j = 0; j < half; j++) {
+        const int a = start + j, b = a + half;
+        const float ar = re[a], ai = im[a], br = re[b], bi = im[b];
+        re[a] = ar + br;
+        im[a] = ai + bi;
+        const float dr = ar - br, di = ai - bi;
+        const int m = j * (32 / len);
+        if (m == 0) {
+          re[b] = dr; im[b] = di;
+        } else if (m == 8) {        // exp(kSign i pi / 2) = kSign i
+          re[b] = kSign > 0 ? -di : di;
+          im[b] = kSign > 0 ? dr : -dr;
+        } else {
+          const float c = cos32(m), sn = kSign > 0 ? sin32(m) : -sin32(m);
+          re[b] = dr * c - di * sn;
+          im[b] = dr * sn + di * c;
+        }
+      }
+    }
+  }
+}
+
+// Asynchronous global -> shared copies (cp.async, sm_80+): a warp issues
+// all of its inputs and tables at once and waits once, so each pass pays one
+// memory latency instead of one per dependent load batch.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Copies n floats (n a multiple of 4 * 32, both pointers 16-byte aligned)
+// with the calling warp's 16-byte cp.async.
+__device__ __forceinline__ void warp_copy_async(float* dst, const float* src, int n) {
+  const int l = threadIdx.x & 31;
+  for (int t = 4 * l; t < n; t += 128) cp_async16(dst + t, src + t);
+}
+
+// 1024-point FFT of buf (natural order in and out, [kWBuf] floats, float2
+// view) by the calling warp; kSign -1 forward, +1 unnormalised inverse.
+// tws: the g_tw1024 table in shared memory.
+template <int kSign>
+__device__ __forceinline__ void warp_fft1024(float2* buf, const float2* tws) {
+  const int l = threadIdx.x & 31;
+  float re[32], im[32];
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    const float2 v = buf[l + 32 * j];
+    re[j] = v.x; im[j] = v.y;
+  }
+  dft32<kSign>(re, im);
+#pragma unroll
+  for (int r = 1; r < 32; r++) {
+    float2 w = tws[brev5(r) * 32 + l];
+    if (kSign > 0) w.y = -w.y;
+    const float xr = re[r], xi = im[r];
+    re[r] = xr * w.x - xi * w.y;
+    im[r] = xr * w.y + xi * w.x;
+  }
+  __syncwarp();
+  float* tr = reinterpret_cast<float*>(buf);
+  float* ti = tr + 32 * 33;
+#pragma unroll
+  for (int r = 0; r < 32; r++) {
+    tr[l * 33 + brev5(r)] = re[r];
+    ti[l * 33 + brev5(r)] = im[r];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int n1 = 0; n1 < 32; n1++) {
+    re[n1] = tr[n1 * 33 + l];
+    im[n1] = ti[n1 * 33 + l];
+  }
+  __syncwarp();
+  dft32<kSign>(re, im);
+#pragma unroll
+  for (int r = 0; r < 32; r++) buf[l + 32 * brev5(r)] = make_float2(re[r], im[r]);
+  __syncwarp();
+}
+
+// Density of every bin from the int64 areas, FP64 overflow partials (one per
+// block) and the other area set cleared: pass A's first half.
+__global__ void __launch_bounds__(256) k_poisson_dens(PassAArgs A) {
+  __shared__ double red[32];
+  const int nb = A.nx * A.ny;
+  const int cur = A.ctl->area_cur;
+  const unsigned long long* __restrict__ ar = cur == 0 ? A.area_pair[0] : A.area_pair[1];
+  unsigned long long* __restrict__ ac = cur == 0 ? A.area_pair[1] : A.area_pair[0];
+  const int64_t* __restrict__ np = A.nonplace;
+  float* __restrict__ dens = A.density;
+  float ovf = 0.0f;
+#pragma unroll 4
+  for (int b = blockIdx.x * 256 + threadIdx.x; b < nb; b += gridDim.x * 256) {
+    const int j = b / A.nx, i = b - j * A.nx;
+    const int blx = A.core_lx + i * A.size_x, bux = min(blx + A.size_x, A.core_ux);
+    const int bly = A.core_ly + j * A.size_y, buy = min(bly + A.size_y, A.core_uy);
+    const long long bin_area = (long long)(bux - blx) * (long long)(buy - bly);
+    const float cap = __fmul_rn(ll_to_float(bin_area), A.td);
+    const float fi = ll_to_float((long long)ar[b]);
+    const float ff = ll_to_float((long long)ar[nb + b]);
+    const float fn = ll_to_float(np[b]);
+    // BinGrid::updateBinsGCellDensityArea (src/nesterovBase.cpp:804-818)
+    dens[b] = __fdiv_rn(__fadd_rn(__fadd_rn(fi, ff), fn), cap);
+    ovf += fmaxf(0.0f, __fsub_rn(__fadd_rn(fi, fn), cap));
+    ac[b] = 0ull;
+    ac[nb + b] = 0ull;
+  }
+  if (A.part_overflow) block_reduce_add((double)ovf, &A.part_overflow[blockIdx.x], red);
+}
+
+// Pass A, warp form: DCT-II along x of row pair r (density rows 2r, 2r+1).
+// Shared memory: FFT buffer, w4 and twiddle tables.
+__global__ void __launch_bounds__(32) k_poisson_rows_w(PassAArgs A) {
+  extern __shared__ float2 smem[];
+  float2* buf = smem;
+  float2* w4s = smem + kWBuf / 2;
+  float2* tws = w4s + kWN;
+  const int l = threadIdx.x;
+  const int r = blockIdx.x;
+  const float* d0 = (A.density_in ? A.density_in : A.density) + (size_t)(2 * r) * kWN;
+  const float* d1 = d0 + kWN;
+  // Makhoul order: v[m] = x[2m], v[n-1-m] = x[2m+1]
+#pragma unroll 8
+  for (int j = 0; j < 32; j++) {
+    const int i = l + 32 * j;
+    float* dst = reinterpret_cast<float*>(&buf[makhoul_pos(i, kWN)]);
+    cp_async4(dst, d0 + i);
+    cp_async4(dst + 1, d1 + i);
+  }
+  warp_copy_async(reinterpret_cast<float*>(w4s), reinterpret_cast<const float*>(A.w4), 2 * kWN);
+  warp_copy_async(reinterpret_cast<float*>(tws), reinterpret_cast<const float*>(g_tw1024), 2 * kWN);
+  cp_async_wait_all();
+  __syncwarp();
+  warp_fft1024<-1>(buf, tws);
+  float* s0 = A.spec + (size_t)(2 * r) * kWN;
+  float* s1 = s0 + kWN;
+#pragma unroll 8
+  for (int j = 0; j < 32; j++) {
+    const int k = l + 32 * j;
+    const float2 c = dct2_post(buf[k], buf[(kWN - k) & (kWN - 1)], w4s[k]);
+    s0[k] = c.x;
+    s1[k] = c.y;
+  }
+}
+
+// Pass B, warp form: four warps per block, eight adjacent columns (32-byte
+// row segments); warp q transforms column pair (u_base + 2q, +1).
+constexpr int kWColsWarps = 4;
+
+__global__ void __launch_bounds__(32 * kWColsWarps) k_poisson_cols_w(PassBArgs B) {
+  extern __shared__ float2 smem[];
+  const int q = threadIdx.x >> 5, l = threadIdx.x & 31;
+  constexpr int kBufF2 = kWBuf / 2;
+  float2* buf = smem + (size_t)q * kBufF2;                              // FFT buffer of warp q
+  float2* spc = smem + (size_t)kWColsWarps * kBufF2 + (size_t)q * kWN;  // its spectrum
+  float2* w4s = smem + (size_t)kWColsWarps * (kBufF2 + kWN);           // [n] w4 (y)
+  float2* tws = w4s + kWN;                                              // [n] twiddles
+  float* wys = reinterpret_cast<float*>(tws + kWN);                     // [n] wy
+  const int u_base = blockIdx.x * 2 * kWColsWarps;
+  const int nx = B.nx;
+  // inputs: 8-byte copies of column pairs into each warp's buffer (Makhoul
+  // order), and the block's tables
+  for (int idx = threadIdx.x; idx < kWN * kWColsWarps; idx += 32 * kWColsWarps) {
+    const int v = idx >> 2, c = idx & 3;           // row v, pair c
+    cp_async8(smem + (size_t)c * kBufF2 + makhoul_pos(v, kWN), B.spec + (size_t)v * nx + u_base + 2 * c);
+  }
+  for (int t = 4 * threadIdx.x; t < 2 * kWN; t += 4 * 32 * kWColsWarps) {
+    cp_async16(reinterpret_cast<float*>(w4s) + t, reinterpret_cast<const float*>(B.w4) + t);
+    cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(g_tw1024) + t);
+  }
+  for (int t = 4 * threadIdx.x; t < kWN; t += 4 * 32 * kWColsWarps) cp_async16(wys + t, B.wy + t);
+  const float wx0 = __ldg(&B.wx[u_base + 2 * q]), wx1 = __ldg(&B.wx[u_base + 2 * q + 1]);
+  cp_async_wait_all();
+  __syncthreads();
+  warp_fft1024<-1>(buf, tws);
+  // DCT-II along y, then the spectral solve (src/fft.cpp:117-166)
+#pragma unroll 4
+  for (int j = 0; j < 32; j++) {
+    const int v = l + 32 * j;
+    const float2 a = dct2_post(buf[v], buf[(kWN - v) & (kWN - 1)], w4s[v]);
+    const float wyv = wys[v];
+    float out[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int u = u_base + 2 * q + h;
+      float d = h ? a.y : a.x;
+      if (u == 0) d *= 0.5f;
+      if (v == 0) d *= 0.5f;
+      d *= B.scale;
+      float ph = 0.0f;
+      if (u != 0 || v != 0) {
+        const float wxu = h ? wx1 : wx0;
+        ph = __fdiv_rn(d, __fadd_rn(__fmul_rn(wxu, wxu), __fmul_rn(wyv, wyv)));
+      }
+      out[h] = ph;
+    }
+    spc[v] = make_float2(out[0], out[1]);
+  }
+  __syncwarp();
+  // P1 = IDCT_y(phi^) of both columns (one complex inverse FFT)
+#pragma unroll 4
+  for (int j = 0; j < 32; j++) {
+    const int k = l + 32 * j;
+    const float2 w4 = w4s[k];
+    const float2 ak = spc[k], ank = k ? spc[kWN - k] : make_float2(0.f, 0.f);
+    const float2 c0 = dct3_pre(ak.x, ank.x, w4, k);
+    const float2 c1 = dct3_pre(ak.y, ank.y, w4, k);
+    buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
+  }
+  __syncwarp();
+  warp_fft1024<1>(buf, tws);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < kWN * 2; idx += 32 * kWColsWarps) {
+    const int v = idx >> 1, h = idx & 1;
+    const int m = makhoul_pos(v, kWN);
+    const float2* b0 = smem + (size_t)(2 * h) * kBufF2;
+    const float2* b1 = b0 + kBufF2;
+    const float2 x0 = b0[m], x1 = b1[m];
+    *reinterpret_cast<float4*>(B.p1 + (size_t)v * nx + u_base + 4 * h) = make_float4(x0.x, x0.y, x1.x, x1.y);
+  }
+  __syncthreads();
+  // P2 = IDST_y(wy * phi^): DCT-III of b[k] = wy[n-k] phi^[n-k] (b[0] = 0)
+#pragma unroll 4
+  for (int j = 0; j < 32; j++) {
+    const int k = l + 32 * j;
+    const float2 w4 = w4s[k];
+    float2 bk = make_float2(0.f, 0.f), bnk = make_float2(0.f, 0.f);
+    if (k) {
+      const float w = wys[kWN - k];
+      const float2 a = spc[kWN - k];
+      bk = make_float2(__fmul_rn(a.x, w), __fmul_rn(a.y, w));
+      const float w2 = wys[k];
+      const float2 b = spc[k];
+      bnk = make_float2(__fmul_rn(b.x, w2), __fmul_rn(b.y, w2));
+    }
+    const float2 c0 = dct3_pre(bk.x, bnk.x, w4, k);
+    const float2 c1 = dct3_pre(bk.y, bnk.y, w4, k);
+    buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
+  }
+  __syncwarp();
+  warp_fft1024<1>(buf, tws);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < kWN * 2; idx += 32 * kWColsWarps) {
+    const int v = idx >> 1, h = idx & 1;
+    const int m = makhoul_pos(v, kWN);
+    const float2* b0 = smem + (size_t)(2 * h) * kBufF2;
+    const float2* b1 = b0 + kBufF2;
+    const float2 x0 = b0[m], x1 = b1[m];
+    const float sg = (v & 1) ? -1.0f : 1.0f;
+    *reinterpret_cast<float4*>(B.p2 + (size_t)v * nx + u_base + 4 * h) =
+        make_float4(sg * x0.x, sg * x0.y, sg * x1.x, sg * x1.y);
+  }
+}
+
+// Pass C, warp form: row pair r of P1 and P2 -> phi, Ex, Ey.  Shared memory:
+// FFT buffer, the four input rows, w4, wx and the twiddles.
+__global__ void __launch_bounds__(32) k_poisson_field_w(PassCArgs C) {
+  extern __shared__ float2 smem[];
+  float2* buf = smem;
+  float* rows = reinterpret_cast<float*>(smem + kWBuf / 2);   // [4][n]: p1 row0, p1 row1, p2 row0, p2 row1
+  float2* w4s = reinterpret_cast<float2*>(rows + 4 * kWN);
+  float2* tws = w4s + kWN;
+  float* wxs = reinterpret_cast<float*>(tws + kWN);
+  const int l = threadIdx.x;
+  const int r = blockIdx.x;
+  const size_t b0 = (size_t)(2 * r) * kWN;
+  warp_copy_async(rows, C.p1 + b0, 2 * kWN);
+  warp_copy_async(rows + 2 * kWN, C.p2 + b0, 2 * kWN);
+  warp_copy_async(reinterpret_cast<float*>(w4s), reinterpret_cast<const float*>(C.w4), 2 * kWN);
+  warp_copy_async(reinterpret_cast<float*>(tws), reinterpret_cast<const float*>(g_tw1024), 2 * kWN);
+  warp_copy_async(wxs, C.wx, kWN);
+  cp_async_wait_all();
+  __syncwarp();
+  // three transforms: 0 = phi (IDCT P1), 1 = Ex (IDST wx*P1), 2 = Ey (IDCT P2)
+  for (int tr = (C.phi ? 0 : 1); tr < 3; tr++) {
+    const float* a0 = rows + (tr == 2 ? 2 : 0) * kWN;
+    const float* a1 = a0 + kWN;
+#pragma unroll 4
+    for (int j = 0; j < 32; j++) {
+      const int k = l + 32 * j;
+      float x0k, x0nk, x1k, x1nk;
+      if (tr != 1) {
+        x0k = a0[k]; x1k = a1[k];
+        x0nk = k ? a0[kWN - k] : 0.f; x1nk = k ? a1[kWN - k] : 0.f;
+      } else if (k) {
+        // b[k] = wx[n-k] a[n-k] for k >= 1, b[0] = 0
+        const float wa = wxs[kWN - k], wb = wxs[k];
+        x0k = __fmul_rn(a0[kWN - k], wa); x1k = __fmul_rn(a1[kWN - k], wa);
+        x0nk = __fmul_rn(a0[k], wb); x1nk = __fmul_rn(a1[k], wb);
+      } else {
+        x0k = x1k = x0nk = x1nk = 0.f;
+      }
+      const float2 w4 = w4s[k];
+      const float2 c0 = dct3_pre(x0k, x0nk, w4, k);
+      const float2 c1 = dct3_pre(x1k, x1nk, w4, k);
+      buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
+    }
+    __syncwarp();
+    warp_fft1024<1>(buf, tws);
+#pragma unroll 4
+    for (int j = 0; j < 32; j++) {
+      const int m = l + 32 * j;
+      const float2 w = buf[makhoul_pos(m, kWN)];
+      float v0 = w.x, v1 = w.y;
+      if (tr == 1 && (m & 1)) { v0 = -v0; v1 = -v1; }
+      if (tr == 0) {
+        C.phi[b0 + m] = v0; C.phi[b0 + kWN + m] = v1;
+      } else if (C.field) {
+        // Ex waits in the P1 rows (no longer read) and goes out with Ey
+        float* ex = rows;
+        if (tr == 1) {
+          ex[m] = v0; ex[kWN + m] = v1;
+        } else {
+          C.field[b0 + m] = make_float2(ex[m], v0);
+          C.field[b0 + kWN + m] = make_float2(ex[kWN + m], v1);
+        }
+      } else {
+        float* dst = tr == 1 ? C.fx : C.fy;
+        dst[b0 + m] = v0; dst[b0 + kWN + m] = v1;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+constexpr size_t kSmemRowsW = (size_t)kWBuf * 4 + 2 * kWN * 8;
+constexpr size_t kSmemColsW = (size_t)kWColsWarps * (kWBuf * 4 + kWN * 8) + 2 * kWN * 8 + kWN * 4;
+constexpr size_t kSmemFieldW = (size_t)kWBuf * 4 + 4 * kWN * 4 + 2 * kWN * 8 + kWN * 4;
+
+bool warp_form(int nx, int ny) { return nx == kWN && ny == kWN; }
+
 int ilog2(int v) { int l = 0; while ((1 << l) < v) l++; return l; }
 
 }  // namespace
@@ -491,6 +875,18 @@ int poisson_prepare_device() {
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_a, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_b, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_cols_w, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kSmemColsW));
+  {
+    // the warp form's twiddles, [k2 * 32 + n1] = exp(-2 pi i n1 k2 / 1024)
+    std::vector<float2> t(kWN);
+    for (int k2 = 0; k2 < 32; k2++)
+      for (int n1 = 0; n1 < 32; n1++) {
+        const double a = -2.0 * M_PI * (double)(n1 * k2) / (double)kWN;
+        t[k2 * 32 + n1] = make_float2((float)cos(a), (float)sin(a));
+      }
+    GPL_CUDA(cudaMemcpyToSymbol(g_tw1024, t.data(), kWN * sizeof(float2)));
+  }
   done[dev] = true;
   return GPL_OK;
 }
@@ -514,6 +910,30 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
   A.ctl = ctl; A.nonplace = nonplace;
   A.density_in = density_in; A.density = density; A.spec = spec;
   A.part_overflow = part_overflow; A.tw = g.tw; A.w4 = g.w4x;
+  if (warp_form(nx, ny)) {
+    const bool areas = area_pair && ctl;
+    if (t) t->begin(kKPoissonA);
+    if (areas) k_poisson_dens<<<poisson_blocks_a(nx, ny), 256, 0, s>>>(A);
+    k_poisson_rows_w<<<ny / 2, 32, kSmemRowsW, s>>>(A);
+    if (t) t->end(kKPoissonA);
+    PassBArgs B;
+    B.nx = nx; B.ny = ny; B.logn = ilog2(ny); B.col_pairs = kWColsWarps;
+    B.spec = spec; B.p1 = p1; B.p2 = p2; B.wx = g.wx; B.wy = g.wy; B.tw = g.tw; B.w4 = g.w4y;
+    B.scale = 4.0f / (float)nx / (float)ny;
+    if (t) t->begin(kKPoissonB);
+    k_poisson_cols_w<<<nx / (2 * kWColsWarps), 32 * kWColsWarps, kSmemColsW, s>>>(B);
+    if (t) t->end(kKPoissonB);
+    PassCArgs C;
+    C.nx = nx; C.ny = ny; C.logn = ilog2(nx); C.pairs_per_block = 1;
+    C.p1 = p1; C.p2 = p2; C.field = field; C.fx = fx; C.fy = fy; C.phi = phi;
+    C.wx = g.wx; C.tw = g.tw; C.w4 = g.w4x;
+    if (t) t->begin(kKPoissonC);
+    k_poisson_field_w<<<ny / 2, 32, kSmemFieldW, s>>>(C);
+    if (t) t->end(kKPoissonC);
+    if (t) t->count(areas ? 4 : 3);
+    GPL_CUDA(cudaGetLastError());
+    return GPL_OK;
+  }
   if (t) t->begin(kKPoissonA);
   k_poisson_a<<<poisson_blocks_a(nx, ny), 256, smem_a(nx, ny), s>>>(A);
   if (t) t->end(kKPoissonA);

@@ -107,6 +107,39 @@ def test_poisson_solve_matches_fp64(gpu_lib, oracle_mod, nx, ny):
     assert rel_l2(fy.cpu().numpy(), y64) < 1e-5
 
 
+def test_eval_parity_1024_grid(gpu_lib, oracle_mod):
+    """A 1024 x 1024 bin grid (the warp-per-row-pair FFT form of the Poisson
+    passes, with the density from its own grid-wide kernel): bin areas and
+    density bit-exact, overflow, potential, field and gradients against the
+    FP64 oracle."""
+    from replace_gb300 import Placer, netlist as N
+    nl = N.generate(30_000, 31_500, n_io=300, seed=5)
+    kw = dict(target_density=0.7, bin_grid_cnt_x=1024, bin_grid_cnt_y=1024, initial_place_max_iter=0)
+    p = Placer(nl, **kw)
+    p.initial_place()
+    o = oracle_mod.Oracle(nl, **kw)
+    o.initial_place()
+    o.nesterov_base()
+    n = o.info.n_gcells
+    rng = np.random.default_rng(3)
+    c = nl.core
+    xy = np.empty(2 * n, np.float32)
+    xy[0::2] = rng.uniform(c[0], c[2], n)
+    xy[1::2] = rng.uniform(c[1], c[3], n)
+    wl, dg, st = p.eval(xy, 0.01)
+    owl, odg, ost, _ = o.eval(xy, 0.01)
+    b = p.bins(1024, 1024)
+    ob = o.bins()
+    for k in ("inst_area", "filler_area", "nonplace_area", "density"):
+        assert np.array_equal(b[k], ob[k]), k
+    assert st.hpwl == ost.hpwl
+    assert abs(st.overflow_area_f64 - ost.overflow_area_f64) <= 1e-6 * max(ost.overflow_area_f64, 1.0)
+    for k in ("phi", "ex", "ey"):
+        assert rel_l2(b[k], ob[k]) < 1e-5, (k, rel_l2(b[k], ob[k]))
+    assert rel_l2(dg, odg) < TOL and rel_l2(wl, owl) < TOL
+    p.close()
+
+
 def test_eval_parity_tensor_core_poisson(gpu_lib, oracle_mod):
     """The Poisson solve as tensor-core GEMMs (bf16 three-term split): bin
     areas, density and HPWL are untouched and bit-exact; potential, field and
