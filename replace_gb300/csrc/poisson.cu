@@ -655,143 +655,159 @@ __global__ void __launch_bounds__(32) k_poisson_rows_w(PassAArgs A) {
   }
 }
 
-// Pass B, warp form: four warps per block, eight adjacent columns (32-byte
-// row segments); warp q transforms column pair (u_base + 2q, +1).
-constexpr int kWColsWarps = 4;
+// Pass B, warp form: four column pairs per block (eight adjacent columns,
+// 32-byte row segments) and two warps per pair: warp (q, 0) takes the
+// forward transform and the spectral solve of pair q, then the two inverse
+// transforms (P1 and P2) run side by side on warps (q, 0) and (q, 1).
+constexpr int kWColsPairs = 4;
+constexpr int kWColsThreads = 64 * kWColsPairs;
 
-__global__ void __launch_bounds__(32 * kWColsWarps) k_poisson_cols_w(PassBArgs B) {
+__global__ void __launch_bounds__(kWColsThreads) k_poisson_cols_w(PassBArgs B) {
   extern __shared__ float2 smem[];
-  const int q = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int q = w >> 1, role = w & 1;
   constexpr int kBufF2 = kWBuf / 2;
-  float2* buf = smem + (size_t)q * kBufF2;                              // FFT buffer of warp q
-  float2* spc = smem + (size_t)kWColsWarps * kBufF2 + (size_t)q * kWN;  // its spectrum
-  float2* w4s = smem + (size_t)kWColsWarps * (kBufF2 + kWN);           // [n] w4 (y)
-  float2* tws = w4s + kWN;                                              // [n] twiddles
-  float* wys = reinterpret_cast<float*>(tws + kWN);                     // [n] wy
-  const int u_base = blockIdx.x * 2 * kWColsWarps;
+  // [pair][role] FFT buffers, [pair] spectra, then the tables
+  float2* buf = smem + (size_t)w * kBufF2;
+  float2* spc = smem + (size_t)2 * kWColsPairs * kBufF2 + (size_t)q * kWN;
+  float2* w4s = smem + (size_t)kWColsPairs * (2 * kBufF2 + kWN);   // [n] w4 (y)
+  float2* tws = w4s + kWN;                                          // [n] twiddles
+  float* wys = reinterpret_cast<float*>(tws + kWN);                 // [n] wy
+  const int u_base = blockIdx.x * 2 * kWColsPairs;
   const int nx = B.nx;
-  // inputs: 8-byte copies of column pairs into each warp's buffer (Makhoul
-  // order), and the block's tables
-  for (int idx = threadIdx.x; idx < kWN * kWColsWarps; idx += 32 * kWColsWarps) {
-    const int v = idx >> 2, c = idx & 3;           // row v, pair c
-    cp_async8(smem + (size_t)c * kBufF2 + makhoul_pos(v, kWN), B.spec + (size_t)v * nx + u_base + 2 * c);
+  // inputs: 8-byte copies of column pairs into the pairs' role-0 buffers
+  // (Makhoul order), and the block's tables
+  for (int idx = threadIdx.x; idx < kWN * kWColsPairs; idx += kWColsThreads) {
+    const int v = idx / kWColsPairs, c = idx % kWColsPairs;       // row v, pair c
+    cp_async8(smem + (size_t)(2 * c) * kBufF2 + makhoul_pos(v, kWN), B.spec + (size_t)v * nx + u_base + 2 * c);
   }
-  for (int t = 4 * threadIdx.x; t < 2 * kWN; t += 4 * 32 * kWColsWarps) {
+  for (int t = 4 * threadIdx.x; t < 2 * kWN; t += 4 * kWColsThreads) {
     cp_async16(reinterpret_cast<float*>(w4s) + t, reinterpret_cast<const float*>(B.w4) + t);
     cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(g_tw1024) + t);
   }
-  for (int t = 4 * threadIdx.x; t < kWN; t += 4 * 32 * kWColsWarps) cp_async16(wys + t, B.wy + t);
+  for (int t = 4 * threadIdx.x; t < kWN; t += 4 * kWColsThreads) cp_async16(wys + t, B.wy + t);
   const float wx0 = __ldg(&B.wx[u_base + 2 * q]), wx1 = __ldg(&B.wx[u_base + 2 * q + 1]);
   cp_async_wait_all();
   __syncthreads();
-  warp_fft1024<-1>(buf, tws);
-  // DCT-II along y, then the spectral solve (src/fft.cpp:117-166)
+  if (role == 0) {
+    warp_fft1024<-1>(buf, tws);
+    // DCT-II along y, then the spectral solve (src/fft.cpp:117-166)
 #pragma unroll 4
-  for (int j = 0; j < 32; j++) {
-    const int v = l + 32 * j;
-    const float2 a = dct2_post(buf[v], buf[(kWN - v) & (kWN - 1)], w4s[v]);
-    const float wyv = wys[v];
-    float out[2];
+    for (int j = 0; j < 32; j++) {
+      const int v = l + 32 * j;
+      const float2 a = dct2_post(buf[v], buf[(kWN - v) & (kWN - 1)], w4s[v]);
+      const float wyv = wys[v];
+      float out[2];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int u = u_base + 2 * q + h;
-      float d = h ? a.y : a.x;
-      if (u == 0) d *= 0.5f;
-      if (v == 0) d *= 0.5f;
-      d *= B.scale;
-      float ph = 0.0f;
-      if (u != 0 || v != 0) {
-        const float wxu = h ? wx1 : wx0;
-        ph = __fdiv_rn(d, __fadd_rn(__fmul_rn(wxu, wxu), __fmul_rn(wyv, wyv)));
+      for (int h = 0; h < 2; h++) {
+        const int u = u_base + 2 * q + h;
+        float d = h ? a.y : a.x;
+        if (u == 0) d *= 0.5f;
+        if (v == 0) d *= 0.5f;
+        d *= B.scale;
+        float ph = 0.0f;
+        if (u != 0 || v != 0) {
+          const float wxu = h ? wx1 : wx0;
+          ph = __fdiv_rn(d, __fadd_rn(__fmul_rn(wxu, wxu), __fmul_rn(wyv, wyv)));
+        }
+        out[h] = ph;
       }
-      out[h] = ph;
+      spc[v] = make_float2(out[0], out[1]);
     }
-    spc[v] = make_float2(out[0], out[1]);
   }
-  __syncwarp();
-  // P1 = IDCT_y(phi^) of both columns (one complex inverse FFT)
+  __syncthreads();
+  if (role == 0) {
+    // P1 = IDCT_y(phi^) of both columns (one complex inverse FFT)
 #pragma unroll 4
-  for (int j = 0; j < 32; j++) {
-    const int k = l + 32 * j;
-    const float2 w4 = w4s[k];
-    const float2 ak = spc[k], ank = k ? spc[kWN - k] : make_float2(0.f, 0.f);
-    const float2 c0 = dct3_pre(ak.x, ank.x, w4, k);
-    const float2 c1 = dct3_pre(ak.y, ank.y, w4, k);
-    buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
+    for (int j = 0; j < 32; j++) {
+      const int k = l + 32 * j;
+      const float2 w4 = w4s[k];
+      const float2 ak = spc[k], ank = k ? spc[kWN - k] : make_float2(0.f, 0.f);
+      const float2 c0 = dct3_pre(ak.x, ank.x, w4, k);
+      const float2 c1 = dct3_pre(ak.y, ank.y, w4, k);
+      buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
+    }
+  } else {
+    // P2 = IDST_y(wy * phi^): DCT-III of b[k] = wy[n-k] phi^[n-k] (b[0] = 0)
+#pragma unroll 4
+    for (int j = 0; j < 32; j++) {
+      const int k = l + 32 * j;
+      const float2 w4 = w4s[k];
+      float2 bk = make_float2(0.f, 0.f), bnk = make_float2(0.f, 0.f);
+      if (k) {
+        const float wa = wys[kWN - k];
+        const float2 a = spc[kWN - k];
+        bk = make_float2(__fmul_rn(a.x, wa), __fmul_rn(a.y, wa));
+        const float wb = wys[k];
+        const float2 b = spc[k];
+        bnk = make_float2(__fmul_rn(b.x, wb), __fmul_rn(b.y, wb));
+      }
+      const float2 c0 = dct3_pre(bk.x, bnk.x, w4, k);
+      const float2 c1 = dct3_pre(bk.y, bnk.y, w4, k);
+      buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
+    }
   }
   __syncwarp();
   warp_fft1024<1>(buf, tws);
   __syncthreads();
-  for (int idx = threadIdx.x; idx < kWN * 2; idx += 32 * kWColsWarps) {
-    const int v = idx >> 1, h = idx & 1;
+  // stores: P1 from the role-0 buffers, P2 (signs alternating in v) from
+  // the role-1 buffers; a thread writes half a row segment as a float4
+  for (int idx = threadIdx.x; idx < kWN * 4; idx += kWColsThreads) {
+    const int v = idx >> 2, h = idx & 1, out = (idx >> 1) & 1;
     const int m = makhoul_pos(v, kWN);
-    const float2* b0 = smem + (size_t)(2 * h) * kBufF2;
-    const float2* b1 = b0 + kBufF2;
+    const float2* b0 = smem + (size_t)(2 * (2 * h) + out) * kBufF2;   // pair 2h, role out
+    const float2* b1 = b0 + 2 * kBufF2;                               // pair 2h + 1
     const float2 x0 = b0[m], x1 = b1[m];
-    *reinterpret_cast<float4*>(B.p1 + (size_t)v * nx + u_base + 4 * h) = make_float4(x0.x, x0.y, x1.x, x1.y);
-  }
-  __syncthreads();
-  // P2 = IDST_y(wy * phi^): DCT-III of b[k] = wy[n-k] phi^[n-k] (b[0] = 0)
-#pragma unroll 4
-  for (int j = 0; j < 32; j++) {
-    const int k = l + 32 * j;
-    const float2 w4 = w4s[k];
-    float2 bk = make_float2(0.f, 0.f), bnk = make_float2(0.f, 0.f);
-    if (k) {
-      const float w = wys[kWN - k];
-      const float2 a = spc[kWN - k];
-      bk = make_float2(__fmul_rn(a.x, w), __fmul_rn(a.y, w));
-      const float w2 = wys[k];
-      const float2 b = spc[k];
-      bnk = make_float2(__fmul_rn(b.x, w2), __fmul_rn(b.y, w2));
-    }
-    const float2 c0 = dct3_pre(bk.x, bnk.x, w4, k);
-    const float2 c1 = dct3_pre(bk.y, bnk.y, w4, k);
-    buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
-  }
-  __syncwarp();
-  warp_fft1024<1>(buf, tws);
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < kWN * 2; idx += 32 * kWColsWarps) {
-    const int v = idx >> 1, h = idx & 1;
-    const int m = makhoul_pos(v, kWN);
-    const float2* b0 = smem + (size_t)(2 * h) * kBufF2;
-    const float2* b1 = b0 + kBufF2;
-    const float2 x0 = b0[m], x1 = b1[m];
-    const float sg = (v & 1) ? -1.0f : 1.0f;
-    *reinterpret_cast<float4*>(B.p2 + (size_t)v * nx + u_base + 4 * h) =
+    const float sg = (out && (v & 1)) ? -1.0f : 1.0f;
+    float* dst = out ? B.p2 : B.p1;
+    *reinterpret_cast<float4*>(dst + (size_t)v * nx + u_base + 4 * h) =
         make_float4(sg * x0.x, sg * x0.y, sg * x1.x, sg * x1.y);
   }
 }
 
-// Pass C, warp form: row pair r of P1 and P2 -> phi, Ex, Ey.  Shared memory:
-// FFT buffer, the four input rows, w4, wx and the twiddles.
-__global__ void __launch_bounds__(32) k_poisson_field_w(PassCArgs C) {
+// Pass C, warp form: two row pairs per block and one warp per transform of
+// a pair (Ex = IDST_x(wx * P1), Ey = IDCT_x(P2), phi = IDCT_x(P1)); the
+// block writes the field (Ex, Ey per bin) once all transforms are done.
+constexpr int kWFieldPairs = 2;
+constexpr int kWFieldThreads = 96 * kWFieldPairs;
+
+__global__ void __launch_bounds__(kWFieldThreads) k_poisson_field_w(PassCArgs C) {
   extern __shared__ float2 smem[];
-  float2* buf = smem;
-  float* rows = reinterpret_cast<float*>(smem + kWBuf / 2);   // [4][n]: p1 row0, p1 row1, p2 row0, p2 row1
-  float2* w4s = reinterpret_cast<float2*>(rows + 4 * kWN);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int p = w / 3, role = w % 3;            // role 0 Ex, 1 Ey, 2 phi
+  constexpr int kBufF2 = kWBuf / 2;
+  float2* buf = smem + (size_t)w * kBufF2;
+  float* rows_all = reinterpret_cast<float*>(smem + (size_t)3 * kWFieldPairs * kBufF2);  // [pair][4][n]
+  float2* w4s = reinterpret_cast<float2*>(rows_all + (size_t)kWFieldPairs * 4 * kWN);
   float2* tws = w4s + kWN;
   float* wxs = reinterpret_cast<float*>(tws + kWN);
-  const int l = threadIdx.x;
-  const int r = blockIdx.x;
-  const size_t b0 = (size_t)(2 * r) * kWN;
-  warp_copy_async(rows, C.p1 + b0, 2 * kWN);
-  warp_copy_async(rows + 2 * kWN, C.p2 + b0, 2 * kWN);
-  warp_copy_async(reinterpret_cast<float*>(w4s), reinterpret_cast<const float*>(C.w4), 2 * kWN);
-  warp_copy_async(reinterpret_cast<float*>(tws), reinterpret_cast<const float*>(g_tw1024), 2 * kWN);
-  warp_copy_async(wxs, C.wx, kWN);
+  const int r0 = blockIdx.x * kWFieldPairs;
+  // inputs: P1 and P2 rows of both pairs (contiguous per array), tables
+  {
+    const size_t base = (size_t)(2 * r0) * kWN;
+    const int n = 2 * kWN * kWFieldPairs;       // floats per array
+    for (int t = 4 * threadIdx.x; t < n; t += 4 * kWFieldThreads) {
+      const int pp = t / (2 * kWN), o = t - pp * 2 * kWN;
+      cp_async16(rows_all + (size_t)pp * 4 * kWN + o, C.p1 + base + t);
+      cp_async16(rows_all + (size_t)pp * 4 * kWN + 2 * kWN + o, C.p2 + base + t);
+    }
+    for (int t = 4 * threadIdx.x; t < 2 * kWN; t += 4 * kWFieldThreads) {
+      cp_async16(reinterpret_cast<float*>(w4s) + t, reinterpret_cast<const float*>(C.w4) + t);
+      cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(g_tw1024) + t);
+    }
+    for (int t = 4 * threadIdx.x; t < kWN; t += 4 * kWFieldThreads) cp_async16(wxs + t, C.wx + t);
+  }
   cp_async_wait_all();
-  __syncwarp();
-  // three transforms: 0 = phi (IDCT P1), 1 = Ex (IDST wx*P1), 2 = Ey (IDCT P2)
-  for (int tr = (C.phi ? 0 : 1); tr < 3; tr++) {
-    const float* a0 = rows + (tr == 2 ? 2 : 0) * kWN;
+  __syncthreads();
+  const float* rows = rows_all + (size_t)p * 4 * kWN;
+  if (role != 2 || C.phi) {
+    const float* a0 = rows + (role == 1 ? 2 : 0) * kWN;
     const float* a1 = a0 + kWN;
 #pragma unroll 4
     for (int j = 0; j < 32; j++) {
       const int k = l + 32 * j;
       float x0k, x0nk, x1k, x1nk;
-      if (tr != 1) {
+      if (role != 0) {
         x0k = a0[k]; x1k = a1[k];
         x0nk = k ? a0[kWN - k] : 0.f; x1nk = k ? a1[kWN - k] : 0.f;
       } else if (k) {
@@ -809,35 +825,35 @@ __global__ void __launch_bounds__(32) k_poisson_field_w(PassCArgs C) {
     }
     __syncwarp();
     warp_fft1024<1>(buf, tws);
-#pragma unroll 4
-    for (int j = 0; j < 32; j++) {
-      const int m = l + 32 * j;
-      const float2 w = buf[makhoul_pos(m, kWN)];
-      float v0 = w.x, v1 = w.y;
-      if (tr == 1 && (m & 1)) { v0 = -v0; v1 = -v1; }
-      if (tr == 0) {
-        C.phi[b0 + m] = v0; C.phi[b0 + kWN + m] = v1;
-      } else if (C.field) {
-        // Ex waits in the P1 rows (no longer read) and goes out with Ey
-        float* ex = rows;
-        if (tr == 1) {
-          ex[m] = v0; ex[kWN + m] = v1;
-        } else {
-          C.field[b0 + m] = make_float2(ex[m], v0);
-          C.field[b0 + kWN + m] = make_float2(ex[kWN + m], v1);
-        }
-      } else {
-        float* dst = tr == 1 ? C.fx : C.fy;
-        dst[b0 + m] = v0; dst[b0 + kWN + m] = v1;
-      }
+  }
+  __syncthreads();
+  // outputs, bin m of rows 2r and 2r + 1 of both pairs (IDST signs alternate)
+  for (int idx = threadIdx.x; idx < kWFieldPairs * kWN; idx += kWFieldThreads) {
+    const int pp = idx / kWN, m = idx - pp * kWN;
+    const size_t b0 = (size_t)(2 * (r0 + pp)) * kWN;
+    const int mp = makhoul_pos(m, kWN);
+    const float2* bp = smem + (size_t)(3 * pp) * kBufF2;
+    float2 ex = bp[mp];
+    const float2 ey = bp[kBufF2 + mp];
+    if (m & 1) { ex.x = -ex.x; ex.y = -ex.y; }
+    if (C.field) {
+      C.field[b0 + m] = make_float2(ex.x, ey.x);
+      C.field[b0 + kWN + m] = make_float2(ex.y, ey.y);
+    } else {
+      C.fx[b0 + m] = ex.x; C.fx[b0 + kWN + m] = ex.y;
+      C.fy[b0 + m] = ey.x; C.fy[b0 + kWN + m] = ey.y;
     }
-    __syncwarp();
+    if (C.phi) {
+      const float2 ph = bp[2 * kBufF2 + mp];
+      C.phi[b0 + m] = ph.x; C.phi[b0 + kWN + m] = ph.y;
+    }
   }
 }
 
 constexpr size_t kSmemRowsW = (size_t)kWBuf * 4 + 2 * kWN * 8;
-constexpr size_t kSmemColsW = (size_t)kWColsWarps * (kWBuf * 4 + kWN * 8) + 2 * kWN * 8 + kWN * 4;
-constexpr size_t kSmemFieldW = (size_t)kWBuf * 4 + 4 * kWN * 4 + 2 * kWN * 8 + kWN * 4;
+constexpr size_t kSmemColsW = (size_t)kWColsPairs * (2 * kWBuf * 4 + kWN * 8) + 2 * kWN * 8 + kWN * 4;
+constexpr size_t kSmemFieldW =
+    (size_t)kWFieldPairs * (3 * kWBuf * 4 + 4 * kWN * 4) + 2 * kWN * 8 + kWN * 4;
 
 bool warp_form(int nx, int ny) { return nx == kWN && ny == kWN; }
 
@@ -860,7 +876,13 @@ size_t smem_a(int nx, int ny) { return ((size_t)2 * pairs_a(nx, ny) * nx + nx / 
 size_t smem_b(int nx, int ny) { return ((size_t)3 * pairs_b(nx, ny) * ny + ny / 2) * sizeof(float2); }
 size_t smem_c(int nx, int ny) { return ((size_t)4 * pairs_c(nx, ny) * nx + nx / 2) * sizeof(float2); }
 
-int poisson_blocks_a(int nx, int ny) { int r = pairs_a(nx, ny); return (ny / 2 + r - 1) / r; }
+// Blocks of the density pass (one FP64 overflow partial each): the warp
+// form's grid-wide density kernel takes four bins per thread.
+int poisson_blocks_a(int nx, int ny) {
+  if (warp_form(nx, ny)) return nx * ny / 1024;
+  int r = pairs_a(nx, ny);
+  return (ny / 2 + r - 1) / r;
+}
 
 // The dynamic shared-memory limit is a per-device function attribute.
 int poisson_prepare_device() {
@@ -877,6 +899,8 @@ int poisson_prepare_device() {
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_cols_w, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)kSmemColsW));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_field_w, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kSmemFieldW));
   {
     // the warp form's twiddles, [k2 * 32 + n1] = exp(-2 pi i n1 k2 / 1024)
     std::vector<float2> t(kWN);
@@ -917,18 +941,18 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
     k_poisson_rows_w<<<ny / 2, 32, kSmemRowsW, s>>>(A);
     if (t) t->end(kKPoissonA);
     PassBArgs B;
-    B.nx = nx; B.ny = ny; B.logn = ilog2(ny); B.col_pairs = kWColsWarps;
+    B.nx = nx; B.ny = ny; B.logn = ilog2(ny); B.col_pairs = kWColsPairs;
     B.spec = spec; B.p1 = p1; B.p2 = p2; B.wx = g.wx; B.wy = g.wy; B.tw = g.tw; B.w4 = g.w4y;
     B.scale = 4.0f / (float)nx / (float)ny;
     if (t) t->begin(kKPoissonB);
-    k_poisson_cols_w<<<nx / (2 * kWColsWarps), 32 * kWColsWarps, kSmemColsW, s>>>(B);
+    k_poisson_cols_w<<<nx / (2 * kWColsPairs), kWColsThreads, kSmemColsW, s>>>(B);
     if (t) t->end(kKPoissonB);
     PassCArgs C;
     C.nx = nx; C.ny = ny; C.logn = ilog2(nx); C.pairs_per_block = 1;
     C.p1 = p1; C.p2 = p2; C.field = field; C.fx = fx; C.fy = fy; C.phi = phi;
     C.wx = g.wx; C.tw = g.tw; C.w4 = g.w4x;
     if (t) t->begin(kKPoissonC);
-    k_poisson_field_w<<<ny / 2, 32, kSmemFieldW, s>>>(C);
+    k_poisson_field_w<<<ny / 2 / kWFieldPairs, kWFieldThreads, kSmemFieldW, s>>>(C);
     if (t) t->end(kKPoissonC);
     if (t) t->count(areas ? 4 : 3);
     GPL_CUDA(cudaGetLastError());
