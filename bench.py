@@ -400,9 +400,11 @@ def main():
     dom_ms, dom_launches = kt[dom]
     bytes_per = algorithmic_bytes(dom, info.n_gcells, nl.n_pins, nl.n_nets,
                                   info.bin_cnt_x * info.bin_cnt_y)
-    achieved = bytes_per * dom_launches / (dom_ms / 1000.0) / 1e9
+    # (a job that reached its stop rule inside the timed region runs no
+    # further iterations here: no kernel times, no roofline)
+    achieved = bytes_per * dom_launches / (dom_ms / 1000.0) / 1e9 if dom_ms > 0 else None
     total_ms = sum(v[0] for v in kt.values())
-    kernel_share = {k: round(v[0] / total_ms, 4) for k, v in kt.items() if v[1]}
+    kernel_share = {k: round(v[0] / total_ms, 4) for k, v in kt.items() if v[1] and total_ms > 0}
     kernel_ms = {k: round(v[0] / v[1], 4) for k, v in kt.items() if v[1]}
     precision = None
     if not args.no_precision and world == 1:
@@ -468,7 +470,8 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": e2e_line,
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+            "roofline": None if achieved is None else {
+                         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": f"of {peak_kind}",
                          "traffic": NCU_TRAFFIC.get(args.workload, {}).get(dom),
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
