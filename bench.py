@@ -116,7 +116,7 @@ def algorithmic_bytes(kind, ng, npins, nn, nb):
 NCU_TRAFFIC = {
     "1m_cells_1024bins": {
         "wa_wirelength": 101.6e6, "gcell_gradient": 131.0e6, "density_scatter": 64.7e6,
-        "poisson_rows_dct": 25.2e6, "poisson_cols_solve": 4.3e6, "poisson_rows_inverse": 8.4e6,
+        "poisson_rows_dct": 29.4e6, "poisson_cols_solve": 4.3e6, "poisson_rows_inverse": 8.5e6,
     },
 }
 
