@@ -462,8 +462,10 @@ def main():
                        "pins": nl.n_pins, "target_density": td,
                        "evals_per_iter": round((st.evaluations) / max(st.iterations, 1), 3),
                        "poisson_form": {1: "shared-memory FFT", 2: "tensor-core GEMM"}.get(info.poisson_path),
-                       "poisson_fft_us": round(info.poisson_fft_us, 1),
-                       "poisson_gemm_us": round(info.poisson_gemm_us, 1),
+                       # the autotuner's timings (None: not timed; auto mode
+                       # skips the GEMM form above 512 bins per axis)
+                       "poisson_fft_us": round(info.poisson_fft_us, 1) or None,
+                       "poisson_gemm_us": round(info.poisson_gemm_us, 1) or None,
                        "start": f"after initial place ({ip_stats.iterations} B2B rounds) and "
                                 f"{args.warmup} warm-up Nesterov iterations",
                        "l2": "inputs larger than L2 (job working set %.0f MB)" % (info.device_bytes / 1e6),

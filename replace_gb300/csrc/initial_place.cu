@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "device_common.cuh"
@@ -1192,29 +1193,49 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   D.n_pins = m.n_pins;
   D.n_nets = m.n_nets;
   const int nP = D.n_mov;
+  // The per-pin host arrays (tens of MB at a million cells, mostly fresh
+  // pages) are filled by a few threads over disjoint ranges.
+  const int n_thr = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
+  const auto parallel_ranges = [n_thr](int n, auto&& body) {
+    if (n_thr <= 1 || n < (1 << 16)) { body(0, n); return; }
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_thr; t++) {
+      const int a = (int)((long long)n * t / n_thr), b = (int)((long long)n * (t + 1) / n_thr);
+      th.emplace_back([&body, a, b]() { body(a, b); });
+    }
+    for (auto& x : th) x.join();
+  };
   std::vector<int32_t> ext(m.n_insts, -1);
   for (int k = 0; k < nP; k++) ext[m.place_insts[k]] = k;
   std::vector<int32_t> pin_net(m.n_pins), pin_mov(m.n_pins);
   std::vector<int2> pin_off(m.n_pins), pin_fix(m.n_pins);
-  for (int n = 0; n < m.n_nets; n++)
-    for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++) pin_net[q] = n;
-  for (int q = 0; q < m.n_pins; q++) {
-    const int i = m.pin_inst[q];
-    pin_mov[q] = i >= 0 ? ext[i] : -1;
-    pin_off[q] = make_int2(m.pin_ox[q], m.pin_oy[q]);
-    pin_fix[q] = make_int2(m.pin_x[q], m.pin_y[q]);
-  }
-  std::vector<int32_t> mps(nP + 1, 0), mp;
+  std::vector<int32_t> mps(nP + 1, 0);
   for (int k = 0; k < nP; k++) {
     const int i = m.place_insts[k];
-    for (int t = m.inst_pin_start[i]; t < m.inst_pin_start[i + 1]; t++) mp.push_back(m.inst_pins[t]);
-    mps[k + 1] = (int)mp.size();
+    mps[k + 1] = mps[k] + (m.inst_pin_start[i + 1] - m.inst_pin_start[i]);
   }
+  std::vector<int32_t> mp(mps[nP]);
   std::vector<int2> ctr(nP);
-  for (int k = 0; k < nP; k++) {
-    const int i = m.place_insts[k];
-    ctr[k] = make_int2((m.ilx[i] + m.iux[i]) / 2, (m.ily[i] + m.iuy[i]) / 2);
-  }
+  parallel_ranges(m.n_nets, [&](int a, int b) {
+    for (int n = a; n < b; n++)
+      for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++) pin_net[q] = n;
+  });
+  parallel_ranges(m.n_pins, [&](int a, int b) {
+    for (int q = a; q < b; q++) {
+      const int i = m.pin_inst[q];
+      pin_mov[q] = i >= 0 ? ext[i] : -1;
+      pin_off[q] = make_int2(m.pin_ox[q], m.pin_oy[q]);
+      pin_fix[q] = make_int2(m.pin_x[q], m.pin_y[q]);
+    }
+  });
+  parallel_ranges(nP, [&](int a, int b) {
+    for (int k = a; k < b; k++) {
+      const int i = m.place_insts[k];
+      int w = mps[k];
+      for (int t = m.inst_pin_start[i]; t < m.inst_pin_start[i + 1]; t++) mp[w++] = m.inst_pins[t];
+      ctr[k] = make_int2((m.ilx[i] + m.iux[i]) / 2, (m.ily[i] + m.iuy[i]) / 2);
+    }
+  });
   // The cooperative solve needs its whole grid (both axes) resident at once.
   int dev = 0, coop_attr = 0, per_sm = 0;
   cudaGetDevice(&dev);
@@ -1241,6 +1262,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   D.parts = grid;
   D.n_mp = (int)mp.size();
   const int scan_blocks = blocks_for(D.n_mp);
+  const double t_host = wall();
   cudaError_t e = dev_alloc((void**)&D.mem, z.bytes, pool, s);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -1296,6 +1318,11 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   up(D.mov_pins, mp.data(), mp.size() * 4);
   up(D.ctr, ctr.data(), nP * 8);
   if (!rc && cudaMemsetAsync(D.counters, 0, 16 * 4, s) != cudaSuccess) rc = GPL_ERR_CUDA;
+  if (prm.verbose_level >= 2) {
+    cudaStreamSynchronize(s);
+    printf("[InitialPlace] host arrays %.2f ms, device scratch %.1f MB + uploads %.2f ms\n", t_host - t_start,
+           z.bytes / 1e6, wall() - t_host);
+  }
   BiState* st_h = static_cast<BiState*>(pinned);
   if (rc) {
     set_error("initial place: upload failed");

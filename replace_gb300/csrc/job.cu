@@ -603,6 +603,13 @@ int choose_poisson_path(gpl_job* j) {
     }
     return GPL_OK;
   }
+  // The split's error grows with the transform length: measured against the
+  // FP64 oracle, the density gradient is 2.8e-5 off at 128^2 and 1.4e-4 at
+  // 1024^2 (field 7e-6 and 2e-5).  Auto mode considers the GEMM form only up
+  // to 512 bins per axis, where it stays inside the 1e-4 bar (and sets up
+  // nothing for larger grids).
+  const bool precise_enough = d.cnt_x <= 512 && d.cnt_y <= 512;
+  if (want == 0 && !precise_enough) return GPL_OK;
   int rc = poisson_gemm_setup(d, &d.pg, j->pool, j->stream);
   if (rc) {
     if (want == 2) return rc;
@@ -623,12 +630,7 @@ int choose_poisson_path(gpl_job* j) {
   j->poisson_gemm_us = time_poisson(j, 5);
   int flag = 0;
   poisson_gemm_error(d.pg, j->stream, &flag);
-  // The split's error grows with the transform length: measured against the
-  // FP64 oracle, the density gradient is 2.8e-5 off at 128^2 and 1.4e-4 at
-  // 1024^2 (field 7e-6 and 2e-5).  Auto mode keeps the GEMM form only up to
-  // 512 bins per axis, where it stays inside the 1e-4 bar.
-  const bool precise_enough = d.cnt_x <= 512 && d.cnt_y <= 512;
-  if (flag || !precise_enough || !(j->poisson_gemm_us > 0.0f) || j->poisson_gemm_us >= j->poisson_fft_us) {
+  if (flag || !(j->poisson_gemm_us > 0.0f) || j->poisson_gemm_us >= j->poisson_fft_us) {
     d.poisson_path = 1;
     poisson_gemm_free(d.pg, j->pool, j->stream);
     d.pg = nullptr;

@@ -140,6 +140,20 @@ def test_poisson_form_autotuned_per_grid(gpu_lib):
     q.close()
 
 
+def test_poisson_auto_mode_sets_up_no_gemm_above_512_bins(gpu_lib):
+    """Above 512 bins per axis the bf16-split GEMM form misses the 1e-4 bar,
+    so auto mode neither builds nor times it there."""
+    from replace_gb300 import Placer, netlist as N
+    nl = N.generate(30_000, 31_500, n_io=300, seed=5)
+    p = Placer(nl, target_density=0.7, bin_grid_cnt_x=1024, bin_grid_cnt_y=1024, initial_place_max_iter=0)
+    p.initial_place()
+    p.nesterov_init()
+    assert p.info.poisson_path == 1 and p.info.poisson_gemm_us == 0
+    rc, st, _ = p.nesterov_run(5)
+    assert rc == 0 and st.iterations == 5
+    p.close()
+
+
 def test_scatter_shape_autotuned_and_results_independent_of_it(gpu_lib):
     """nesterov_init times the scatter's tile / chunk shapes and keeps the
     fastest; the int64 bin areas (and everything after them) do not depend
