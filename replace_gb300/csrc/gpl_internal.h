@@ -3,8 +3,10 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gpl.h"
@@ -73,6 +75,21 @@ void place_gcells(HostModel& m);
 int build_nesterov_base(HostModel& m);
 // InitialPlace::placeInstsCenter + Instance::setCenterLocation
 void host_place_center(HostModel& m);
+
+// Runs body(a, b) over [0, n) split into disjoint ranges on a few host
+// threads (one range below 65,536 items): the per-pin host passes of a job
+// setup touch tens of MB of fresh pages at a million cells.
+template <class F>
+void parallel_ranges(int n, F&& body) {
+  const int n_thr = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
+  if (n_thr <= 1 || n < (1 << 16)) { body(0, n); return; }
+  std::vector<std::thread> th;
+  for (int t = 0; t < n_thr; t++) {
+    const int a = (int)((long long)n * t / n_thr), b = (int)((long long)n * (t + 1) / n_thr);
+    th.emplace_back([&body, a, b]() { body(a, b); });
+  }
+  for (auto& x : th) x.join();
+}
 void host_set_inst_center(HostModel& m, int inst, int x, int y);
 
 // WA net buckets by degree: 2, 4, 8, 16, 32 (lane groups), 64, 128 (a warp,

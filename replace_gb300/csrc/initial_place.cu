@@ -30,7 +30,6 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
-#include <thread>
 #include <vector>
 
 #include "device_common.cuh"
@@ -1193,18 +1192,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   D.n_pins = m.n_pins;
   D.n_nets = m.n_nets;
   const int nP = D.n_mov;
-  // The per-pin host arrays (tens of MB at a million cells, mostly fresh
-  // pages) are filled by a few threads over disjoint ranges.
-  const int n_thr = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
-  const auto parallel_ranges = [n_thr](int n, auto&& body) {
-    if (n_thr <= 1 || n < (1 << 16)) { body(0, n); return; }
-    std::vector<std::thread> th;
-    for (int t = 0; t < n_thr; t++) {
-      const int a = (int)((long long)n * t / n_thr), b = (int)((long long)n * (t + 1) / n_thr);
-      th.emplace_back([&body, a, b]() { body(a, b); });
-    }
-    for (auto& x : th) x.join();
-  };
+  // the per-pin host arrays are filled by a few threads (parallel_ranges)
   std::vector<int32_t> ext(m.n_insts, -1);
   for (int k = 0; k < nP; k++) ext[m.place_insts[k]] = k;
   std::vector<int32_t> pin_net(m.n_pins), pin_mov(m.n_pins);

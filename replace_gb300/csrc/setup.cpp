@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstring>
 #include <random>
 
 #include "gpl_internal.h"
@@ -40,12 +41,22 @@ int build_placer_base(HostModel& m, const gpl_netlist_desc* d, const gpl_params*
   m.iux.assign(d->inst_ux, d->inst_ux + m.n_insts);
   m.iuy.assign(d->inst_uy, d->inst_uy + m.n_insts);
   m.ikind.assign(d->inst_kind, d->inst_kind + m.n_insts);
-  m.pin_inst.assign(d->pin_inst, d->pin_inst + m.n_pins);
-  m.pin_ox.assign(d->pin_ox, d->pin_ox + m.n_pins);
-  m.pin_oy.assign(d->pin_oy, d->pin_oy + m.n_pins);
-  m.pin_x.assign(d->pin_x, d->pin_x + m.n_pins);
-  m.pin_y.assign(d->pin_y, d->pin_y + m.n_pins);
   m.net_start.assign(d->net_start, d->net_start + m.n_nets + 1);
+  // the per-pin copies and checks in parallel ranges
+  m.pin_inst.resize(m.n_pins); m.pin_ox.resize(m.n_pins); m.pin_oy.resize(m.n_pins);
+  m.pin_x.resize(m.n_pins); m.pin_y.resize(m.n_pins);
+  int bad_pin = 0;
+  parallel_ranges(m.n_pins, [&](int a, int b) {
+    const size_t w = (size_t)(b - a) * sizeof(int32_t);
+    memcpy(m.pin_inst.data() + a, d->pin_inst + a, w);
+    memcpy(m.pin_ox.data() + a, d->pin_ox + a, w);
+    memcpy(m.pin_oy.data() + a, d->pin_oy + a, w);
+    memcpy(m.pin_x.data() + a, d->pin_x + a, w);
+    memcpy(m.pin_y.data() + a, d->pin_y + a, w);
+    bool bad = false;
+    for (int q = a; q < b; q++) bad |= m.pin_inst[q] < -1 || m.pin_inst[q] >= m.n_insts;
+    if (bad) __atomic_store_n(&bad_pin, 1, __ATOMIC_RELAXED);
+  });
   if (m.net_start[0] != 0 || m.net_start[m.n_nets] != m.n_pins) {
     set_error("net_start must run from 0 to n_pins");
     return GPL_ERR_INVALID_ARG;
@@ -59,28 +70,40 @@ int build_placer_base(HostModel& m, const gpl_netlist_desc* d, const gpl_params*
       return GPL_ERR_INVALID_ARG;
     }
   }
-  for (int q = 0; q < m.n_pins; q++) {
-    if (m.pin_inst[q] < -1 || m.pin_inst[q] >= m.n_insts) { set_error("pin_inst out of range"); return GPL_ERR_INVALID_ARG; }
-  }
+  if (bad_pin) { set_error("pin_inst out of range"); return GPL_ERR_INVALID_ARG; }
   if (d->inst_pin_start && d->inst_pins) {
     m.inst_pin_start.assign(d->inst_pin_start, d->inst_pin_start + m.n_insts + 1);
     int np = m.inst_pin_start[m.n_insts];
     if (np < 0 || np > m.n_pins) { set_error("inst_pin_start out of range"); return GPL_ERR_INVALID_ARG; }
     m.inst_pins.assign(d->inst_pins, d->inst_pins + np);
-    // every instance pin listed exactly once, under its own instance
-    std::vector<uint64_t> seen(((size_t)m.n_pins + 63) / 64, 0);
-    for (int i = 0; i < m.n_insts; i++) {
+    for (int i = 0; i < m.n_insts; i++)
       if (m.inst_pin_start[i + 1] < m.inst_pin_start[i]) { set_error("inst_pin_start not monotone"); return GPL_ERR_INVALID_ARG; }
-      for (int k = m.inst_pin_start[i]; k < m.inst_pin_start[i + 1]; k++) {
-        int q = m.inst_pins[k];
-        if (q < 0 || q >= m.n_pins || m.pin_inst[q] != i) { set_error("inst_pins inconsistent with pin_inst"); return GPL_ERR_INVALID_ARG; }
-        const uint64_t bit = 1ull << (q & 63);
-        if (seen[q >> 6] & bit) { set_error("inst_pins lists a pin twice"); return GPL_ERR_INVALID_ARG; }
-        seen[q >> 6] |= bit;
+    if (m.inst_pin_start[0] < 0) { set_error("inst_pin_start out of range"); return GPL_ERR_INVALID_ARG; }
+    // every instance pin listed exactly once, under its own instance (the
+    // seen bitmap is shared by the ranges: atomic bit sets)
+    std::vector<uint64_t> seen(((size_t)m.n_pins + 63) / 64, 0);
+    int bad_owner = 0, twice = 0;
+    long long inst_owned = 0;
+    parallel_ranges(m.n_insts, [&](int a, int b) {
+      bool bo = false, tw = false;
+      for (int i = a; i < b && !bo; i++) {
+        for (int k = m.inst_pin_start[i]; k < m.inst_pin_start[i + 1]; k++) {
+          const int q = m.inst_pins[k];
+          if (q < 0 || q >= m.n_pins || m.pin_inst[q] != i) { bo = true; break; }
+          const uint64_t bit = 1ull << (q & 63);
+          if (__atomic_fetch_or(&seen[q >> 6], bit, __ATOMIC_RELAXED) & bit) tw = true;
+        }
       }
-    }
-    int64_t inst_owned = 0;
-    for (int q = 0; q < m.n_pins; q++) inst_owned += m.pin_inst[q] >= 0;
+      if (bo) __atomic_store_n(&bad_owner, 1, __ATOMIC_RELAXED);
+      if (tw) __atomic_store_n(&twice, 1, __ATOMIC_RELAXED);
+    });
+    if (bad_owner) { set_error("inst_pins inconsistent with pin_inst"); return GPL_ERR_INVALID_ARG; }
+    if (twice) { set_error("inst_pins lists a pin twice"); return GPL_ERR_INVALID_ARG; }
+    parallel_ranges(m.n_pins, [&](int a, int b) {
+      long long c = 0;
+      for (int q = a; q < b; q++) c += m.pin_inst[q] >= 0;
+      __atomic_fetch_add(&inst_owned, c, __ATOMIC_RELAXED);
+    });
     if (inst_owned != np) { set_error("inst_pins must list every pin of every instance"); return GPL_ERR_INVALID_ARG; }
   } else {
     m.inst_pin_start.assign(m.n_insts + 1, 0);
