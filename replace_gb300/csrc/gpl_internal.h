@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -75,6 +76,19 @@ void place_gcells(HostModel& m);
 int build_nesterov_base(HostModel& m);
 // InitialPlace::placeInstsCenter + Instance::setCenterLocation
 void host_place_center(HostModel& m);
+
+// A heap array left uninitialised, so that its pages are first touched by
+// the (parallel) pass that fills it.
+template <class T>
+struct RawArray {
+  std::unique_ptr<T[]> p;
+  size_t n;
+  explicit RawArray(size_t count) : p(new T[count > 0 ? count : 1]), n(count) {}
+  T* data() { return p.get(); }
+  size_t size() const { return n; }
+  T& operator[](size_t i) { return p[i]; }
+  const T& operator[](size_t i) const { return p[i]; }
+};
 
 // Runs body(a, b) over [0, n) split into disjoint ranges on a few host
 // threads (one range below 65,536 items): the per-pin host passes of a job

@@ -1195,15 +1195,15 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   // the per-pin host arrays are filled by a few threads (parallel_ranges)
   std::vector<int32_t> ext(m.n_insts, -1);
   for (int k = 0; k < nP; k++) ext[m.place_insts[k]] = k;
-  std::vector<int32_t> pin_net(m.n_pins), pin_mov(m.n_pins);
-  std::vector<int2> pin_off(m.n_pins), pin_fix(m.n_pins);
+  RawArray<int32_t> pin_net(m.n_pins), pin_mov(m.n_pins);
+  RawArray<int2> pin_off(m.n_pins), pin_fix(m.n_pins);
   std::vector<int32_t> mps(nP + 1, 0);
   for (int k = 0; k < nP; k++) {
     const int i = m.place_insts[k];
     mps[k + 1] = mps[k] + (m.inst_pin_start[i + 1] - m.inst_pin_start[i]);
   }
-  std::vector<int32_t> mp(mps[nP]);
-  std::vector<int2> ctr(nP);
+  RawArray<int32_t> mp(mps[nP]);
+  RawArray<int2> ctr(nP);
   parallel_ranges(m.n_nets, [&](int a, int b) {
     for (int n = a; n < b; n++)
       for (int q = m.net_start[n]; q < m.net_start[n + 1]; q++) pin_net[q] = n;
