@@ -99,20 +99,38 @@ __device__ __forceinline__ PinExp pin_exps(int2 p, int lx, int ux, int ly, int u
   return r;
 }
 
-// getWireLengthGradientPinWA for one pin given its net's eight sums S:
-// S[0..3] = (sum e, sum x e) for min x and max x, S[4..7] the same for y.
-__device__ __forceinline__ float2 pin_gradient(int2 p, const PinExp& E, const float* S, float cx,
-                                               float cy) {
+// getWireLengthGradientPinWA (src/nesterovBase.cpp:1383-1440) regrouped per
+// net.  With the net's sums S[0..3] = (sum e, sum x e) for min x and max x
+// (S[4..7] the same for y), the min-x term (s e (1 - c x) + c e S1) / s^2 is
+// e (A + B x) with A = 1/s + c S1 / s^2 and B = -c/s (max x: A = 1/s -
+// c S1 / s^2, B = c/s), so a pin costs one multiply-add and one multiply per
+// direction once the net's A and B are known.  The sums of exponentials are
+// in [1, degree] (the extreme pin contributes exp(0) = 1, every term is at
+// most 1), so the fast reciprocal (2 ulp) is safe; a direction whose
+// exponent fell below the force bar has e = 0 and contributes 0.
+struct NetCoef {
+  float a[4], b[4];
+};
+
+__device__ __forceinline__ NetCoef net_coef(const float* S, float cx, float cy) {
+  NetCoef K;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float c = k < 2 ? cx : cy;
+    const float inv = __fdividef(1.0f, S[2 * k]);
+    const float m = c * S[2 * k + 1] * inv * inv;
+    const bool lo = (k & 1) == 0;          // min side
+    K.a[k] = lo ? inv + m : inv - m;
+    K.b[k] = lo ? -c * inv : c * inv;
+  }
+  return K;
+}
+
+__device__ __forceinline__ float2 pin_gradient(int2 p, const PinExp& E, const NetCoef& K) {
   const float x = (float)p.x, y = (float)p.y;
-  float g[4] = {0.f, 0.f, 0.f, 0.f};
-  // The sums of exponentials are in [1, degree]: the net's extreme pin
-  // contributes exp(0) = 1 and every term is at most 1, so s*s lies in
-  // [1, degree^2] and the fast division (2 ulp) is exact enough and safe.
-  if (E.flags & 1u) { const float s = S[0]; g[0] = __fdividef(s * (E.e[0] * (1.0f - cx * x)) + cx * E.e[0] * S[1], s * s); }
-  if (E.flags & 2u) { const float s = S[2]; g[1] = __fdividef(s * (E.e[1] * (1.0f + cx * x)) - cx * E.e[1] * S[3], s * s); }
-  if (E.flags & 4u) { const float s = S[4]; g[2] = __fdividef(s * (E.e[2] * (1.0f - cy * y)) + cy * E.e[2] * S[5], s * s); }
-  if (E.flags & 8u) { const float s = S[6]; g[3] = __fdividef(s * (E.e[3] * (1.0f + cy * y)) - cy * E.e[3] * S[7], s * s); }
-  return make_float2(g[0] - g[1], g[2] - g[3]);
+  const float g0 = E.e[0] * (K.a[0] + K.b[0] * x), g1 = E.e[1] * (K.a[1] + K.b[1] * x);
+  const float g2 = E.e[2] * (K.a[2] + K.b[2] * y), g3 = E.e[3] * (K.a[3] + K.b[3] * y);
+  return make_float2(g0 - g1, g2 - g3);
 }
 
 __device__ __forceinline__ void sums_of(int2 p, const PinExp& E, float* S) {
@@ -202,7 +220,7 @@ __device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval<kW>& 
     const PinExp E = pin_exps(p0, p0.x, p0.x, p0.y, p0.y, V.cx, V.cy, A.bar);
     float S[8];
     sums_of(p0, E, S);
-    A.pin_grad[s] = weighed(V, k, pin_gradient(p0, E, S, V.cx, V.cy));
+    A.pin_grad[s] = weighed(V, k, pin_gradient(p0, E, net_coef(S, V.cx, V.cy)));
     return 0ll;
   }
   const int2 p1 = pin_pos(V, __ldg(&A.pins[s + 1]));
@@ -215,8 +233,9 @@ __device__ __forceinline__ long long wa_pair(const WaArgs& A, const WaEval<kW>& 
 #pragma unroll
   for (int t = 0; t < 8; t++) S[t] += T[t];
   float2* g = A.pin_grad + s;
-  g[0] = weighed(V, k, pin_gradient(p0, E0, S, V.cx, V.cy));
-  g[1] = weighed(V, k, pin_gradient(p1, E1, S, V.cx, V.cy));
+  const NetCoef K = net_coef(S, V.cx, V.cy);
+  g[0] = weighed(V, k, pin_gradient(p0, E0, K));
+  g[1] = weighed(V, k, pin_gradient(p1, E1, K));
   return (long long)((ux - lx) + (uy - ly));
 }
 
@@ -274,7 +293,7 @@ __device__ __forceinline__ long long wa_group(const WaArgs& A, const WaEval<kW>&
 #pragma unroll
       for (int t = 0; t < 8; t++) S[t] += __shfl_xor_sync(0xffffffffu, S[t], o);
   }
-  if (valid) A.pin_grad[q] = weighed(V, k, pin_gradient(p, E, S, V.cx, V.cy));
+  if (valid) A.pin_grad[q] = weighed(V, k, pin_gradient(p, E, net_coef(S, V.cx, V.cy)));
   return (net_ok && li == 0) ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
@@ -314,9 +333,10 @@ __device__ __forceinline__ long long wa_warp(const WaArgs& A, const WaEval<kW>& 
     }
   }
   group_sum8<32>(S);
+  const NetCoef K = net_coef(S, V.cx, V.cy);
 #pragma unroll
   for (int j = 0; j < P; j++)
-    if (ok[j]) A.pin_grad[s + lane + 32 * j] = weighed(V, k, pin_gradient(p[j], E[j], S, V.cx, V.cy));
+    if (ok[j]) A.pin_grad[s + lane + 32 * j] = weighed(V, k, pin_gradient(p[j], E[j], K));
   return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
 
@@ -349,11 +369,12 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval<kW>& 
 #pragma unroll
   for (int j = 0; j < 8; j++)
     for (int o = 16; o > 0; o >>= 1) S[j] += __shfl_xor_sync(0xffffffffu, S[j], o);
+  const NetCoef K = net_coef(S, V.cx, V.cy);
   for (int q = s + lane; q < e; q += 32) {
     const int4 r = __ldg(&A.pins[q]);
     const int2 p = pin_pos(V, r);
     const PinExp E = pin_exps(p, lx, ux, ly, uy, V.cx, V.cy, A.bar);
-    A.pin_grad[q] = weighed(V, k, pin_gradient(p, E, S, V.cx, V.cy));
+    A.pin_grad[q] = weighed(V, k, pin_gradient(p, E, K));
   }
   return lane == 0 ? (long long)((ux - lx) + (uy - ly)) : 0ll;
 }
