@@ -458,23 +458,42 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
 }
 
 // ---------------------------------------------------------------------------
-// Warp form for 1024 x 1024 grids.  One warp transforms one packed pair (two
-// rows or two columns as real and imaginary parts) end to end, so the passes
-// need no block barriers; the 1024-point FFT keeps 32 elements per lane in
-// registers (four-step: 32-point DFTs along n2 in each lane, the twiddle
-// W^(n1 k2), one transpose through padded shared memory, 32-point DFTs along
-// n1) instead of five shared-memory radix-4 passes.  The density of each bin
-// comes from a separate grid-wide kernel, whose high occupancy suits the
-// DRAM-bound int64 reads better than a warp per row pair.
+// Warp form for 1024 x 1024 and 512 x 512 grids.  One warp runs one N-point
+// FFT of a packed pair (two rows or two columns as real and imaginary parts)
+// with N/32 elements per lane in registers, four-step: DFTs along n2 inside
+// each lane, the twiddle W^(n1 k2), one transpose through padded shared
+// memory, then 32-point DFTs along n1 (for N = 512 each of those is split
+// over a lane pair: two 16-point DFTs and one radix-2 step by shuffle).  This
+// replaces five shared-memory radix-4 passes with block barriers.
+// Independent transforms of a pair run on separate warps (the column pass's
+// two inverse transforms, the field pass's three), inputs and tables arrive
+// by cp.async so that a warp waits for memory once, and the density comes
+// from its own grid-wide kernel first (fusing it into the row pass was
+// measured slower: its long blocks overlap worse with the WA kernel).
 
-constexpr int kWN = 1024;           // sequence length of the warp form
-constexpr int kWBuf = 2 * 32 * 33;  // floats per warp buffer: 1024 float2, or the padded transpose
+template <int N>
+struct WarpFft {
+  static_assert(N == 1024 || N == 512, "warp form sizes");
+  static constexpr int kE = N / 32;                     // elements per lane
+  static constexpr int kStride = kE + 1;                // padded transpose row
+  static constexpr int kBuf = 2 * N > 2 * 32 * kStride ? 2 * N : 2 * 32 * kStride;   // floats per warp buffer
+};
 
-// exp(-2 pi i n1 k2 / 1024) at [k2 * 32 + n1]: one coalesced row per k2.
-__device__ __align__(16) float2 g_tw1024[kWN];
+// exp(-2 pi i n1 k2 / N) at [k2 * 32 + n1], k2 < N/32: one coalesced row per k2.
+__device__ __align__(16) float2 g_tw1024[1024];
+__device__ __align__(16) float2 g_tw512[512];
 
-__host__ __device__ constexpr int brev5(int r) {
-  return ((r & 1) << 4) | ((r & 2) << 2) | (r & 4) | ((r & 8) >> 2) | ((r & 16) >> 4);
+template <int N>
+__device__ __forceinline__ const float2* tw_table() {
+  if constexpr (N == 1024) return g_tw1024;
+  else return g_tw512;
+}
+
+template <int kBits>
+__host__ __device__ constexpr int brev(int r) {
+  int o = 0;
+  for (int b = 0; b < kBits; b++) o |= ((r >> b) & 1) << (kBits - 1 - b);
+  return o;
 }
 
 // cos and sin of 2 pi m / 32, m = 0..8 (the other octants by symmetry).
@@ -491,34 +510,41 @@ __host__ __device__ constexpr float sin32(int m) {   // 0 <= m < 16
   return m <= 8 ? cos32_oct(8 - m) : cos32_oct(m - 8);
 }
 
-// In-register 32-point DFT, radix-2 decimation in frequency: natural input
-// order, register r ends with output brev5(r).  Twiddles exp(kSign 2 pi i m /
-// 32) are compile-time constants after unrolling.
+// (re, im) times exp(kSign 2 pi i m / 32), m < 16 a compile-time constant.
 template <int kSign>
-__device__ __forceinline__ void dft32(float (&re)[32], float (&im)[32]) {
+__device__ __forceinline__ void rot32(float& re, float& im, int m) {
+  if (m == 0) return;
+  const float r = re, i = im;
+  if (m == 8) {                     // exp(kSign i pi / 2) = kSign i
+    re = kSign > 0 ? -i : i;
+    im = kSign > 0 ? r : -r;
+    return;
+  }
+  const float c = cos32(m), sn = kSign > 0 ? sin32(m) : -sin32(m);
+  re = r * c - i * sn;
+  im = r * sn + i * c;
+}
+
+// In-register M-point DFT (M = 16 or 32), radix-2 decimation in frequency:
+// natural input order, register r ends with output brev(r).  Twiddles
+// exp(kSign 2 pi i j / len) = exp(kSign 2 pi i (j 32/len) / 32) are
+// compile-time constants after unrolling.
+template <int M, int kSign>
+__device__ __forceinline__ void dft_reg(float (&re)[M], float (&im)[M]) {
 #pragma unroll
-  for (int len = 32; len >= 2; len >>= 1) {
+  for (int len = M; len >= 2; len >>= 1) {
     const int half = len >> 1;
 #pragma unroll
-    for (int start = 0; start < 32; start += len) {
+    for (int start = 0; start < M; start += len) {
 #pragma unroll
       for (int j = 0; j < half; j++) {
         const int a = start + j, b = a + half;
         const float ar = re[a], ai = im[a], br = re[b], bi = im[b];
         re[a] = ar + br;
         im[a] = ai + bi;
-        const float dr = ar - br, di = ai - bi;
-        const int m = j * (32 / len);
-        if (m == 0) {
-          re[b] = dr; im[b] = di;
-        } else if (m == 8) {        // exp(kSign i pi / 2) = kSign i
-          re[b] = kSign > 0 ? -di : di;
-          im[b] = kSign > 0 ? dr : -dr;
-        } else {
-          const float c = cos32(m), sn = kSign > 0 ? sin32(m) : -sin32(m);
-          re[b] = dr * c - di * sn;
-          im[b] = dr * sn + di * c;
-        }
+        re[b] = ar - br;
+        im[b] = ai - bi;
+        rot32<kSign>(re[b], im[b], j * (32 / len));
       }
     }
   }
@@ -548,22 +574,35 @@ __device__ __forceinline__ void warp_copy_async(float* dst, const float* src, in
   for (int t = 4 * l; t < n; t += 128) cp_async16(dst + t, src + t);
 }
 
-// 1024-point FFT of buf (natural order in and out, [kWBuf] floats, float2
-// view) by the calling warp; kSign -1 forward, +1 unnormalised inverse.
-// tws: the g_tw1024 table in shared memory.
-template <int kSign>
-__device__ __forceinline__ void warp_fft1024(float2* buf, const float2* tws) {
+// N-point FFT of buf (natural order in and out, [WarpFft<N>::kBuf] floats,
+// float2 view) by the calling warp; kSign -1 forward, +1 unnormalised
+// inverse.  tws: the tw_table<N>() table in shared memory.
+template <int N, int kSign>
+__device__ __forceinline__ void warp_fft(float2* buf, const float2* tws) {
+  constexpr int E = WarpFft<N>::kE, S = WarpFft<N>::kStride;
+  constexpr int kBitsE = E == 32 ? 5 : 4;
   const int l = threadIdx.x & 31;
   float re[32], im[32];
+  // stage 1: lane n1 = l holds x[n1 + 32 n2], n2 < E; DFT along n2
 #pragma unroll
-  for (int j = 0; j < 32; j++) {
+  for (int j = 0; j < E; j++) {
     const float2 v = buf[l + 32 * j];
     re[j] = v.x; im[j] = v.y;
   }
-  dft32<kSign>(re, im);
+  if constexpr (E == 32) {
+    dft_reg<32, kSign>(re, im);
+  } else {
+    float r16[16], i16[16];
 #pragma unroll
-  for (int r = 1; r < 32; r++) {
-    float2 w = tws[brev5(r) * 32 + l];
+    for (int j = 0; j < 16; j++) { r16[j] = re[j]; i16[j] = im[j]; }
+    dft_reg<16, kSign>(r16, i16);
+#pragma unroll
+    for (int j = 0; j < 16; j++) { re[j] = r16[j]; im[j] = i16[j]; }
+  }
+  // twiddle W_N^(n1 k2), register r holding k2 = brev(r)
+#pragma unroll
+  for (int r = 1; r < E; r++) {
+    float2 w = tws[brev<kBitsE>(r) * 32 + l];
     if (kSign > 0) w.y = -w.y;
     const float xr = re[r], xi = im[r];
     re[r] = xr * w.x - xi * w.y;
@@ -571,22 +610,50 @@ __device__ __forceinline__ void warp_fft1024(float2* buf, const float2* tws) {
   }
   __syncwarp();
   float* tr = reinterpret_cast<float*>(buf);
-  float* ti = tr + 32 * 33;
+  float* ti = tr + 32 * S;
 #pragma unroll
-  for (int r = 0; r < 32; r++) {
-    tr[l * 33 + brev5(r)] = re[r];
-    ti[l * 33 + brev5(r)] = im[r];
+  for (int r = 0; r < E; r++) {
+    tr[l * S + brev<kBitsE>(r)] = re[r];
+    ti[l * S + brev<kBitsE>(r)] = im[r];
   }
   __syncwarp();
+  if constexpr (E == 32) {
+    // stage 2: lane k2 = l takes n1 = 0..31, a 32-point DFT, X[k2 + 32 k1]
 #pragma unroll
-  for (int n1 = 0; n1 < 32; n1++) {
-    re[n1] = tr[n1 * 33 + l];
-    im[n1] = ti[n1 * 33 + l];
+    for (int n1 = 0; n1 < 32; n1++) {
+      re[n1] = tr[n1 * S + l];
+      im[n1] = ti[n1 * S + l];
+    }
+    __syncwarp();
+    dft_reg<32, kSign>(re, im);
+#pragma unroll
+    for (int r = 0; r < 32; r++) buf[l + 32 * brev<5>(r)] = make_float2(re[r], im[r]);
+  } else {
+    // stage 2 for E = 16: lane pair (2 k2, 2 k2 + 1) takes the even and odd
+    // n1 of column k2, one 16-point DFT each, then X[k] = E[k] + W^k O[k]
+    // (even lane) and X[k + 16] = E[k] - W^k O[k] (odd lane), W = W_32
+    const int k2 = l >> 1, odd = l & 1;
+    float r16[16], i16[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+      r16[i] = tr[(2 * i + odd) * S + k2];
+      i16[i] = ti[(2 * i + odd) * S + k2];
+    }
+    __syncwarp();
+    dft_reg<16, kSign>(r16, i16);
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+      const int k = brev<4>(r);
+      const float pr = __shfl_xor_sync(0xffffffffu, r16[r], 1);
+      const float pi = __shfl_xor_sync(0xffffffffu, i16[r], 1);
+      // W^k O: O is the partner's value on the even lane, the own on the odd
+      float orr = odd ? r16[r] : pr, oi = odd ? i16[r] : pi;
+      rot32<kSign>(orr, oi, k);
+      const float er = odd ? pr : r16[r], ei = odd ? pi : i16[r];
+      const float xr = odd ? er - orr : er + orr, xi = odd ? ei - oi : ei + oi;
+      buf[k2 + 16 * (k + 16 * odd)] = make_float2(xr, xi);
+    }
   }
-  __syncwarp();
-  dft32<kSign>(re, im);
-#pragma unroll
-  for (int r = 0; r < 32; r++) buf[l + 32 * brev5(r)] = make_float2(re[r], im[r]);
   __syncwarp();
 }
 
@@ -622,80 +689,87 @@ __global__ void __launch_bounds__(256) k_poisson_dens(PassAArgs A) {
 
 // Pass A, warp form: DCT-II along x of row pair r (density rows 2r, 2r+1).
 // Shared memory: FFT buffer, w4 and twiddle tables.
+template <int N>
 __global__ void __launch_bounds__(32) k_poisson_rows_w(PassAArgs A) {
   extern __shared__ float2 smem[];
   float2* buf = smem;
-  float2* w4s = smem + kWBuf / 2;
-  float2* tws = w4s + kWN;
+  float2* w4s = smem + WarpFft<N>::kBuf / 2;
+  float2* tws = w4s + N;
   const int l = threadIdx.x;
   const int r = blockIdx.x;
-  const float* d0 = (A.density_in ? A.density_in : A.density) + (size_t)(2 * r) * kWN;
-  const float* d1 = d0 + kWN;
+  const float* d0 = (A.density_in ? A.density_in : A.density) + (size_t)(2 * r) * N;
+  const float* d1 = d0 + N;
   // Makhoul order: v[m] = x[2m], v[n-1-m] = x[2m+1]
 #pragma unroll 8
-  for (int j = 0; j < 32; j++) {
+  for (int j = 0; j < N / 32; j++) {
     const int i = l + 32 * j;
-    float* dst = reinterpret_cast<float*>(&buf[makhoul_pos(i, kWN)]);
+    float* dst = reinterpret_cast<float*>(&buf[makhoul_pos(i, N)]);
     cp_async4(dst, d0 + i);
     cp_async4(dst + 1, d1 + i);
   }
-  warp_copy_async(reinterpret_cast<float*>(w4s), reinterpret_cast<const float*>(A.w4), 2 * kWN);
-  warp_copy_async(reinterpret_cast<float*>(tws), reinterpret_cast<const float*>(g_tw1024), 2 * kWN);
+  warp_copy_async(reinterpret_cast<float*>(w4s), reinterpret_cast<const float*>(A.w4), 2 * N);
+  warp_copy_async(reinterpret_cast<float*>(tws), reinterpret_cast<const float*>(tw_table<N>()), 2 * N);
   cp_async_wait_all();
   __syncwarp();
-  warp_fft1024<-1>(buf, tws);
-  float* s0 = A.spec + (size_t)(2 * r) * kWN;
-  float* s1 = s0 + kWN;
+  warp_fft<N, -1>(buf, tws);
+  float* s0 = A.spec + (size_t)(2 * r) * N;
+  float* s1 = s0 + N;
 #pragma unroll 8
-  for (int j = 0; j < 32; j++) {
+  for (int j = 0; j < N / 32; j++) {
     const int k = l + 32 * j;
-    const float2 c = dct2_post(buf[k], buf[(kWN - k) & (kWN - 1)], w4s[k]);
+    const float2 c = dct2_post(buf[k], buf[(N - k) & (N - 1)], w4s[k]);
     s0[k] = c.x;
     s1[k] = c.y;
   }
 }
 
-// Pass B, warp form: four column pairs per block (eight adjacent columns,
-// 32-byte row segments) and two warps per pair: warp (q, 0) takes the
+// Pass B, warp form: kP column pairs per block (2 kP adjacent columns; 32-byte
+// row segments at kP = 4) and two warps per pair: warp (q, 0) takes the
 // forward transform and the spectral solve of pair q, then the two inverse
 // transforms (P1 and P2) run side by side on warps (q, 0) and (q, 1).
-constexpr int kWColsPairs = 4;
-constexpr int kWColsThreads = 64 * kWColsPairs;
+template <int N>
+struct ColsShape {
+  static constexpr int kP = N == 1024 ? 4 : 2;          // column pairs per block
+  static constexpr int kThreads = 64 * kP;
+  static constexpr int kH = kP / 2;                     // float4 segments per row
+};
 
-__global__ void __launch_bounds__(kWColsThreads) k_poisson_cols_w(PassBArgs B) {
+template <int N>
+__global__ void __launch_bounds__(ColsShape<N>::kThreads) k_poisson_cols_w(PassBArgs B) {
   extern __shared__ float2 smem[];
+  constexpr int kP = ColsShape<N>::kP, kT = ColsShape<N>::kThreads, kH = ColsShape<N>::kH;
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const int q = w >> 1, role = w & 1;
-  constexpr int kBufF2 = kWBuf / 2;
+  constexpr int kBufF2 = WarpFft<N>::kBuf / 2;
   // [pair][role] FFT buffers, [pair] spectra, then the tables
   float2* buf = smem + (size_t)w * kBufF2;
-  float2* spc = smem + (size_t)2 * kWColsPairs * kBufF2 + (size_t)q * kWN;
-  float2* w4s = smem + (size_t)kWColsPairs * (2 * kBufF2 + kWN);   // [n] w4 (y)
-  float2* tws = w4s + kWN;                                          // [n] twiddles
-  float* wys = reinterpret_cast<float*>(tws + kWN);                 // [n] wy
-  const int u_base = blockIdx.x * 2 * kWColsPairs;
+  float2* spc = smem + (size_t)2 * kP * kBufF2 + (size_t)q * N;
+  float2* w4s = smem + (size_t)kP * (2 * kBufF2 + N);    // [n] w4 (y)
+  float2* tws = w4s + N;                                 // [n] twiddles
+  float* wys = reinterpret_cast<float*>(tws + N);        // [n] wy
+  const int u_base = blockIdx.x * 2 * kP;
   const int nx = B.nx;
   // inputs: 8-byte copies of column pairs into the pairs' role-0 buffers
   // (Makhoul order), and the block's tables
-  for (int idx = threadIdx.x; idx < kWN * kWColsPairs; idx += kWColsThreads) {
-    const int v = idx / kWColsPairs, c = idx % kWColsPairs;       // row v, pair c
-    cp_async8(smem + (size_t)(2 * c) * kBufF2 + makhoul_pos(v, kWN), B.spec + (size_t)v * nx + u_base + 2 * c);
+  for (int idx = threadIdx.x; idx < N * kP; idx += kT) {
+    const int v = idx / kP, c = idx % kP;       // row v, pair c
+    cp_async8(smem + (size_t)(2 * c) * kBufF2 + makhoul_pos(v, N), B.spec + (size_t)v * nx + u_base + 2 * c);
   }
-  for (int t = 4 * threadIdx.x; t < 2 * kWN; t += 4 * kWColsThreads) {
+  for (int t = 4 * threadIdx.x; t < 2 * N; t += 4 * kT) {
     cp_async16(reinterpret_cast<float*>(w4s) + t, reinterpret_cast<const float*>(B.w4) + t);
-    cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(g_tw1024) + t);
+    cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(tw_table<N>()) + t);
   }
-  for (int t = 4 * threadIdx.x; t < kWN; t += 4 * kWColsThreads) cp_async16(wys + t, B.wy + t);
+  for (int t = 4 * threadIdx.x; t < N; t += 4 * kT) cp_async16(wys + t, B.wy + t);
   const float wx0 = __ldg(&B.wx[u_base + 2 * q]), wx1 = __ldg(&B.wx[u_base + 2 * q + 1]);
   cp_async_wait_all();
   __syncthreads();
   if (role == 0) {
-    warp_fft1024<-1>(buf, tws);
+    warp_fft<N, -1>(buf, tws);
     // DCT-II along y, then the spectral solve (src/fft.cpp:117-166)
 #pragma unroll 4
-    for (int j = 0; j < 32; j++) {
+    for (int j = 0; j < N / 32; j++) {
       const int v = l + 32 * j;
-      const float2 a = dct2_post(buf[v], buf[(kWN - v) & (kWN - 1)], w4s[v]);
+      const float2 a = dct2_post(buf[v], buf[(N - v) & (N - 1)], w4s[v]);
       const float wyv = wys[v];
       float out[2];
 #pragma unroll
@@ -719,10 +793,10 @@ __global__ void __launch_bounds__(kWColsThreads) k_poisson_cols_w(PassBArgs B) {
   if (role == 0) {
     // P1 = IDCT_y(phi^) of both columns (one complex inverse FFT)
 #pragma unroll 4
-    for (int j = 0; j < 32; j++) {
+    for (int j = 0; j < N / 32; j++) {
       const int k = l + 32 * j;
       const float2 w4 = w4s[k];
-      const float2 ak = spc[k], ank = k ? spc[kWN - k] : make_float2(0.f, 0.f);
+      const float2 ak = spc[k], ank = k ? spc[N - k] : make_float2(0.f, 0.f);
       const float2 c0 = dct3_pre(ak.x, ank.x, w4, k);
       const float2 c1 = dct3_pre(ak.y, ank.y, w4, k);
       buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
@@ -730,13 +804,13 @@ __global__ void __launch_bounds__(kWColsThreads) k_poisson_cols_w(PassBArgs B) {
   } else {
     // P2 = IDST_y(wy * phi^): DCT-III of b[k] = wy[n-k] phi^[n-k] (b[0] = 0)
 #pragma unroll 4
-    for (int j = 0; j < 32; j++) {
+    for (int j = 0; j < N / 32; j++) {
       const int k = l + 32 * j;
       const float2 w4 = w4s[k];
       float2 bk = make_float2(0.f, 0.f), bnk = make_float2(0.f, 0.f);
       if (k) {
-        const float wa = wys[kWN - k];
-        const float2 a = spc[kWN - k];
+        const float wa = wys[N - k];
+        const float2 a = spc[N - k];
         bk = make_float2(__fmul_rn(a.x, wa), __fmul_rn(a.y, wa));
         const float wb = wys[k];
         const float2 b = spc[k];
@@ -748,13 +822,13 @@ __global__ void __launch_bounds__(kWColsThreads) k_poisson_cols_w(PassBArgs B) {
     }
   }
   __syncwarp();
-  warp_fft1024<1>(buf, tws);
+  warp_fft<N, 1>(buf, tws);
   __syncthreads();
   // stores: P1 from the role-0 buffers, P2 (signs alternating in v) from
-  // the role-1 buffers; a thread writes half a row segment as a float4
-  for (int idx = threadIdx.x; idx < kWN * 4; idx += kWColsThreads) {
-    const int v = idx >> 2, h = idx & 1, out = (idx >> 1) & 1;
-    const int m = makhoul_pos(v, kWN);
+  // the role-1 buffers; a thread writes four columns (two pairs) as a float4
+  for (int idx = threadIdx.x; idx < N * kH * 2; idx += kT) {
+    const int h = idx % kH, out = (idx / kH) & 1, v = idx / (2 * kH);
+    const int m = makhoul_pos(v, N);
     const float2* b0 = smem + (size_t)(2 * (2 * h) + out) * kBufF2;   // pair 2h, role out
     const float2* b1 = b0 + 2 * kBufF2;                               // pair 2h + 1
     const float2 x0 = b0[m], x1 = b1[m];
@@ -771,49 +845,50 @@ __global__ void __launch_bounds__(kWColsThreads) k_poisson_cols_w(PassBArgs B) {
 constexpr int kWFieldPairs = 2;
 constexpr int kWFieldThreads = 96 * kWFieldPairs;
 
+template <int N>
 __global__ void __launch_bounds__(kWFieldThreads) k_poisson_field_w(PassCArgs C) {
   extern __shared__ float2 smem[];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const int p = w / 3, role = w % 3;            // role 0 Ex, 1 Ey, 2 phi
-  constexpr int kBufF2 = kWBuf / 2;
+  constexpr int kBufF2 = WarpFft<N>::kBuf / 2;
   float2* buf = smem + (size_t)w * kBufF2;
   float* rows_all = reinterpret_cast<float*>(smem + (size_t)3 * kWFieldPairs * kBufF2);  // [pair][4][n]
-  float2* w4s = reinterpret_cast<float2*>(rows_all + (size_t)kWFieldPairs * 4 * kWN);
-  float2* tws = w4s + kWN;
-  float* wxs = reinterpret_cast<float*>(tws + kWN);
+  float2* w4s = reinterpret_cast<float2*>(rows_all + (size_t)kWFieldPairs * 4 * N);
+  float2* tws = w4s + N;
+  float* wxs = reinterpret_cast<float*>(tws + N);
   const int r0 = blockIdx.x * kWFieldPairs;
   // inputs: P1 and P2 rows of both pairs (contiguous per array), tables
   {
-    const size_t base = (size_t)(2 * r0) * kWN;
-    const int n = 2 * kWN * kWFieldPairs;       // floats per array
+    const size_t base = (size_t)(2 * r0) * N;
+    const int n = 2 * N * kWFieldPairs;       // floats per array
     for (int t = 4 * threadIdx.x; t < n; t += 4 * kWFieldThreads) {
-      const int pp = t / (2 * kWN), o = t - pp * 2 * kWN;
-      cp_async16(rows_all + (size_t)pp * 4 * kWN + o, C.p1 + base + t);
-      cp_async16(rows_all + (size_t)pp * 4 * kWN + 2 * kWN + o, C.p2 + base + t);
+      const int pp = t / (2 * N), o = t - pp * 2 * N;
+      cp_async16(rows_all + (size_t)pp * 4 * N + o, C.p1 + base + t);
+      cp_async16(rows_all + (size_t)pp * 4 * N + 2 * N + o, C.p2 + base + t);
     }
-    for (int t = 4 * threadIdx.x; t < 2 * kWN; t += 4 * kWFieldThreads) {
+    for (int t = 4 * threadIdx.x; t < 2 * N; t += 4 * kWFieldThreads) {
       cp_async16(reinterpret_cast<float*>(w4s) + t, reinterpret_cast<const float*>(C.w4) + t);
-      cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(g_tw1024) + t);
+      cp_async16(reinterpret_cast<float*>(tws) + t, reinterpret_cast<const float*>(tw_table<N>()) + t);
     }
-    for (int t = 4 * threadIdx.x; t < kWN; t += 4 * kWFieldThreads) cp_async16(wxs + t, C.wx + t);
+    for (int t = 4 * threadIdx.x; t < N; t += 4 * kWFieldThreads) cp_async16(wxs + t, C.wx + t);
   }
   cp_async_wait_all();
   __syncthreads();
-  const float* rows = rows_all + (size_t)p * 4 * kWN;
+  const float* rows = rows_all + (size_t)p * 4 * N;
   if (role != 2 || C.phi) {
-    const float* a0 = rows + (role == 1 ? 2 : 0) * kWN;
-    const float* a1 = a0 + kWN;
+    const float* a0 = rows + (role == 1 ? 2 : 0) * N;
+    const float* a1 = a0 + N;
 #pragma unroll 4
-    for (int j = 0; j < 32; j++) {
+    for (int j = 0; j < N / 32; j++) {
       const int k = l + 32 * j;
       float x0k, x0nk, x1k, x1nk;
       if (role != 0) {
         x0k = a0[k]; x1k = a1[k];
-        x0nk = k ? a0[kWN - k] : 0.f; x1nk = k ? a1[kWN - k] : 0.f;
+        x0nk = k ? a0[N - k] : 0.f; x1nk = k ? a1[N - k] : 0.f;
       } else if (k) {
         // b[k] = wx[n-k] a[n-k] for k >= 1, b[0] = 0
-        const float wa = wxs[kWN - k], wb = wxs[k];
-        x0k = __fmul_rn(a0[kWN - k], wa); x1k = __fmul_rn(a1[kWN - k], wa);
+        const float wa = wxs[N - k], wb = wxs[k];
+        x0k = __fmul_rn(a0[N - k], wa); x1k = __fmul_rn(a1[N - k], wa);
         x0nk = __fmul_rn(a0[k], wb); x1nk = __fmul_rn(a1[k], wb);
       } else {
         x0k = x1k = x0nk = x1nk = 0.f;
@@ -824,38 +899,46 @@ __global__ void __launch_bounds__(kWFieldThreads) k_poisson_field_w(PassCArgs C)
       buf[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
     }
     __syncwarp();
-    warp_fft1024<1>(buf, tws);
+    warp_fft<N, 1>(buf, tws);
   }
   __syncthreads();
   // outputs, bin m of rows 2r and 2r + 1 of both pairs (IDST signs alternate)
-  for (int idx = threadIdx.x; idx < kWFieldPairs * kWN; idx += kWFieldThreads) {
-    const int pp = idx / kWN, m = idx - pp * kWN;
-    const size_t b0 = (size_t)(2 * (r0 + pp)) * kWN;
-    const int mp = makhoul_pos(m, kWN);
+  for (int idx = threadIdx.x; idx < kWFieldPairs * N; idx += kWFieldThreads) {
+    const int pp = idx / N, m = idx - pp * N;
+    const size_t b0 = (size_t)(2 * (r0 + pp)) * N;
+    const int mp = makhoul_pos(m, N);
     const float2* bp = smem + (size_t)(3 * pp) * kBufF2;
     float2 ex = bp[mp];
     const float2 ey = bp[kBufF2 + mp];
     if (m & 1) { ex.x = -ex.x; ex.y = -ex.y; }
     if (C.field) {
       C.field[b0 + m] = make_float2(ex.x, ey.x);
-      C.field[b0 + kWN + m] = make_float2(ex.y, ey.y);
+      C.field[b0 + N + m] = make_float2(ex.y, ey.y);
     } else {
-      C.fx[b0 + m] = ex.x; C.fx[b0 + kWN + m] = ex.y;
-      C.fy[b0 + m] = ey.x; C.fy[b0 + kWN + m] = ey.y;
+      C.fx[b0 + m] = ex.x; C.fx[b0 + N + m] = ex.y;
+      C.fy[b0 + m] = ey.x; C.fy[b0 + N + m] = ey.y;
     }
     if (C.phi) {
       const float2 ph = bp[2 * kBufF2 + mp];
-      C.phi[b0 + m] = ph.x; C.phi[b0 + kWN + m] = ph.y;
+      C.phi[b0 + m] = ph.x; C.phi[b0 + N + m] = ph.y;
     }
   }
 }
 
-constexpr size_t kSmemRowsW = (size_t)kWBuf * 4 + 2 * kWN * 8;
-constexpr size_t kSmemColsW = (size_t)kWColsPairs * (2 * kWBuf * 4 + kWN * 8) + 2 * kWN * 8 + kWN * 4;
-constexpr size_t kSmemFieldW =
-    (size_t)kWFieldPairs * (3 * kWBuf * 4 + 4 * kWN * 4) + 2 * kWN * 8 + kWN * 4;
+template <int N>
+constexpr size_t smem_rows_w() { return (size_t)WarpFft<N>::kBuf * 4 + 2 * N * 8; }
+template <int N>
+constexpr size_t smem_cols_w() {
+  return (size_t)ColsShape<N>::kP * (2 * WarpFft<N>::kBuf * 4 + N * 8) + 2 * N * 8 + N * 4;
+}
+template <int N>
+constexpr size_t smem_field_w() {
+  return (size_t)kWFieldPairs * (3 * WarpFft<N>::kBuf * 4 + 4 * N * 4) + 2 * N * 8 + N * 4;
+}
 
-bool warp_form(int nx, int ny) { return nx == kWN && ny == kWN; }
+// The sequence length of the warp form for this grid, or 0 (block form).
+int warp_form(int nx, int ny) { return nx == ny && (nx == 1024 || nx == 512) ? nx : 0; }
+
 
 int ilog2(int v) { int l = 0; while ((1 << l) < v) l++; return l; }
 
@@ -897,19 +980,24 @@ int poisson_prepare_device() {
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_a, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_b, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   GPL_CUDA(cudaFuncSetAttribute(k_poisson_c, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  GPL_CUDA(cudaFuncSetAttribute(k_poisson_cols_w, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kSmemColsW));
-  GPL_CUDA(cudaFuncSetAttribute(k_poisson_field_w, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kSmemFieldW));
-  {
-    // the warp form's twiddles, [k2 * 32 + n1] = exp(-2 pi i n1 k2 / 1024)
-    std::vector<float2> t(kWN);
-    for (int k2 = 0; k2 < 32; k2++)
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_cols_w<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_cols_w<1024>()));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_field_w<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_field_w<1024>()));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_cols_w<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_cols_w<512>()));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_field_w<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_field_w<512>()));
+  for (int n : {1024, 512}) {
+    // the warp form's twiddles, [k2 * 32 + n1] = exp(-2 pi i n1 k2 / n)
+    std::vector<float2> t(n);
+    for (int k2 = 0; k2 < n / 32; k2++)
       for (int n1 = 0; n1 < 32; n1++) {
-        const double a = -2.0 * M_PI * (double)(n1 * k2) / (double)kWN;
+        const double a = -2.0 * M_PI * (double)(n1 * k2) / (double)n;
         t[k2 * 32 + n1] = make_float2((float)cos(a), (float)sin(a));
       }
-    GPL_CUDA(cudaMemcpyToSymbol(g_tw1024, t.data(), kWN * sizeof(float2)));
+    if (n == 1024) GPL_CUDA(cudaMemcpyToSymbol(g_tw1024, t.data(), n * sizeof(float2)));
+    else GPL_CUDA(cudaMemcpyToSymbol(g_tw512, t.data(), n * sizeof(float2)));
   }
   done[dev] = true;
   return GPL_OK;
@@ -934,25 +1022,35 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
   A.ctl = ctl; A.nonplace = nonplace;
   A.density_in = density_in; A.density = density; A.spec = spec;
   A.part_overflow = part_overflow; A.tw = g.tw; A.w4 = g.w4x;
-  if (warp_form(nx, ny)) {
+  if (const int wn = warp_form(nx, ny)) {
     const bool areas = area_pair && ctl;
-    if (t) t->begin(kKPoissonA);
-    if (areas) k_poisson_dens<<<poisson_blocks_a(nx, ny), 256, 0, s>>>(A);
-    k_poisson_rows_w<<<ny / 2, 32, kSmemRowsW, s>>>(A);
-    if (t) t->end(kKPoissonA);
     PassBArgs B;
-    B.nx = nx; B.ny = ny; B.logn = ilog2(ny); B.col_pairs = kWColsPairs;
+    B.nx = nx; B.ny = ny; B.logn = ilog2(ny);
     B.spec = spec; B.p1 = p1; B.p2 = p2; B.wx = g.wx; B.wy = g.wy; B.tw = g.tw; B.w4 = g.w4y;
     B.scale = 4.0f / (float)nx / (float)ny;
-    if (t) t->begin(kKPoissonB);
-    k_poisson_cols_w<<<nx / (2 * kWColsPairs), kWColsThreads, kSmemColsW, s>>>(B);
-    if (t) t->end(kKPoissonB);
     PassCArgs C;
-    C.nx = nx; C.ny = ny; C.logn = ilog2(nx); C.pairs_per_block = 1;
+    C.nx = nx; C.ny = ny; C.logn = ilog2(nx); C.pairs_per_block = kWFieldPairs;
     C.p1 = p1; C.p2 = p2; C.field = field; C.fx = fx; C.fy = fy; C.phi = phi;
     C.wx = g.wx; C.tw = g.tw; C.w4 = g.w4x;
+    if (t) t->begin(kKPoissonA);
+    if (areas) k_poisson_dens<<<poisson_blocks_a(nx, ny), 256, 0, s>>>(A);
+    if (wn == 1024) k_poisson_rows_w<1024><<<ny / 2, 32, smem_rows_w<1024>(), s>>>(A);
+    else k_poisson_rows_w<512><<<ny / 2, 32, smem_rows_w<512>(), s>>>(A);
+    if (t) t->end(kKPoissonA);
+    if (t) t->begin(kKPoissonB);
+    if (wn == 1024) {
+      B.col_pairs = ColsShape<1024>::kP;
+      k_poisson_cols_w<1024><<<nx / (2 * ColsShape<1024>::kP), ColsShape<1024>::kThreads,
+                               smem_cols_w<1024>(), s>>>(B);
+    } else {
+      B.col_pairs = ColsShape<512>::kP;
+      k_poisson_cols_w<512><<<nx / (2 * ColsShape<512>::kP), ColsShape<512>::kThreads,
+                              smem_cols_w<512>(), s>>>(B);
+    }
+    if (t) t->end(kKPoissonB);
     if (t) t->begin(kKPoissonC);
-    k_poisson_field_w<<<ny / 2 / kWFieldPairs, kWFieldThreads, kSmemFieldW, s>>>(C);
+    if (wn == 1024) k_poisson_field_w<1024><<<ny / 2 / kWFieldPairs, kWFieldThreads, smem_field_w<1024>(), s>>>(C);
+    else k_poisson_field_w<512><<<ny / 2 / kWFieldPairs, kWFieldThreads, smem_field_w<512>(), s>>>(C);
     if (t) t->end(kKPoissonC);
     if (t) t->count(areas ? 4 : 3);
     GPL_CUDA(cudaGetLastError());

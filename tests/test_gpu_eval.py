@@ -88,7 +88,8 @@ def test_eval_all_cells_on_one_bin(gpu_lib, oracle_mod):
     assert st.hpwl == ost.hpwl
 
 
-@pytest.mark.parametrize("nx,ny", [(2, 2), (4, 8), (16, 16), (64, 32), (128, 128), (256, 512), (1024, 1024)])
+@pytest.mark.parametrize("nx,ny", [(2, 2), (4, 8), (16, 16), (64, 32), (128, 128), (256, 512), (512, 512),
+                                   (1024, 1024)])
 def test_poisson_solve_matches_fp64(gpu_lib, oracle_mod, nx, ny):
     """gpl_poisson_solve (FFT::doFFT semantics) vs the FP64 oracle."""
     import torch
@@ -107,14 +108,15 @@ def test_poisson_solve_matches_fp64(gpu_lib, oracle_mod, nx, ny):
     assert rel_l2(fy.cpu().numpy(), y64) < 1e-5
 
 
-def test_eval_parity_1024_grid(gpu_lib, oracle_mod):
-    """A 1024 x 1024 bin grid (the warp-per-row-pair FFT form of the Poisson
-    passes, with the density from its own grid-wide kernel): bin areas and
-    density bit-exact, overflow, potential, field and gradients against the
-    FP64 oracle."""
+@pytest.mark.parametrize("bins", [512, 1024])
+def test_eval_parity_warp_form_grids(gpu_lib, oracle_mod, bins):
+    """512 x 512 and 1024 x 1024 bin grids (the warp-per-pair FFT form of the
+    Poisson passes, with the density from its own grid-wide kernel): bin
+    areas and density bit-exact, overflow, potential, field and gradients
+    against the FP64 oracle."""
     from replace_gb300 import Placer, netlist as N
     nl = N.generate(30_000, 31_500, n_io=300, seed=5)
-    kw = dict(target_density=0.7, bin_grid_cnt_x=1024, bin_grid_cnt_y=1024, initial_place_max_iter=0)
+    kw = dict(target_density=0.7, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins, initial_place_max_iter=0)
     p = Placer(nl, **kw)
     p.initial_place()
     o = oracle_mod.Oracle(nl, **kw)
@@ -128,7 +130,7 @@ def test_eval_parity_1024_grid(gpu_lib, oracle_mod):
     xy[1::2] = rng.uniform(c[1], c[3], n)
     wl, dg, st = p.eval(xy, 0.01)
     owl, odg, ost, _ = o.eval(xy, 0.01)
-    b = p.bins(1024, 1024)
+    b = p.bins(bins, bins)
     ob = o.bins()
     for k in ("inst_area", "filler_area", "nonplace_area", "density"):
         assert np.array_equal(b[k], ob[k]), k
