@@ -368,6 +368,10 @@ gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out);
  * rejected here.  *ticket identifies the job in the calls below. */
 gpl_status gpl_server_submit(gpl_server* s, const gpl_netlist_desc* nl, const gpl_params* p,
                              int64_t* ticket);
+/* gpl_server_submit with per-net weights (as gpl_set_net_weights; weights
+ * [n_nets] are copied, NULL means unweighted). */
+gpl_status gpl_server_submit_weighted(gpl_server* s, const gpl_netlist_desc* nl, const gpl_params* p,
+                                      const float* weights, int64_t n_nets, int64_t* ticket);
 /* Up to capacity results of jobs that ended since the last poll, waiting up
  * to wait_ms for the first one; returns how many were written. */
 int32_t gpl_server_poll(gpl_server* s, gpl_server_result* out, int32_t capacity, int32_t wait_ms);

@@ -59,6 +59,8 @@ def load(build_if_missing: bool = True):
     L.gpl_kernel_launch_count.argtypes = [vp]
     L.gpl_server_params_default.argtypes = [C.POINTER(_abi.ServerParams)]
     L.gpl_server_create.argtypes = [C.POINTER(_abi.ServerParams), C.POINTER(vp)]
+    L.gpl_server_submit_weighted.argtypes = [vp, C.POINTER(_abi.NetlistDesc), C.POINTER(_abi.Params),
+                                             vp, C.c_int64, C.POINTER(C.c_int64)]
     L.gpl_server_submit.argtypes = [vp, C.POINTER(_abi.NetlistDesc), C.POINTER(_abi.Params),
                                     C.POINTER(C.c_int64)]
     L.gpl_server_poll.restype = C.c_int32
@@ -69,7 +71,8 @@ def load(build_if_missing: bool = True):
     L.gpl_server_counts.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_int32)]
     L.gpl_server_destroy.argtypes = [vp]
-    for name in ("gpl_server_create", "gpl_server_submit", "gpl_server_get_inst_locations",
+    for name in ("gpl_server_create", "gpl_server_submit", "gpl_server_submit_weighted",
+                 "gpl_server_get_inst_locations",
                  "gpl_server_release", "gpl_server_cancel"):
         getattr(L, name).restype = C.c_int
     for name in ("gpl_create", "gpl_initial_place", "gpl_nesterov_init", "gpl_nesterov_run",

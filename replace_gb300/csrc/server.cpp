@@ -203,11 +203,21 @@ gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out) {
 
 gpl_status gpl_server_submit(gpl_server* s, const gpl_netlist_desc* nl, const gpl_params* p,
                              int64_t* ticket) {
+  return gpl_server_submit_weighted(s, nl, p, nullptr, 0, ticket);
+}
+
+gpl_status gpl_server_submit_weighted(gpl_server* s, const gpl_netlist_desc* nl, const gpl_params* p,
+                                      const float* weights, int64_t n_nets, int64_t* ticket) {
   if (!s || !nl || !p || !ticket) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
   if (p->device != s->p.device) { set_error("job device differs from the server's"); return GPL_ERR_INVALID_ARG; }
   gpl_job* j = nullptr;
   int rc = job_new(nl, p, &j);
   if (rc) return (gpl_status)rc;
+  if (weights) {
+    // stored on the host now, uploaded with the job's device model
+    rc = gpl_set_net_weights(j, weights, n_nets);
+    if (rc) { gpl_destroy(j); return (gpl_status)rc; }
+  }
   int64_t bytes = 0;
   rc = job_device_bytes(j, &bytes, s->p.run_initial_place && !p->incremental_place_mode);
   if (rc) { gpl_destroy(j); return (gpl_status)rc; }

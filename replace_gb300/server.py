@@ -48,15 +48,21 @@ class PlacementServer:
         self.h = h
         self.pending = set()
 
-    def submit(self, netlist, params: _abi.Params | None = None, **overrides) -> int:
-        """Queue one placement job; returns its ticket.  The netlist is copied."""
+    def submit(self, netlist, params: _abi.Params | None = None, net_weights=None, **overrides) -> int:
+        """Queue one placement job; returns its ticket.  The netlist (and the
+        optional per-net weights, as Placer.set_net_weights) is copied."""
         prm = params if params is not None else _abi.default_params()
         for k, v in overrides.items():
             setattr(prm, k, v)
         prm.device = self.params.device
         holder = _abi.DescHolder(netlist)
         t = C.c_int64()
-        check(self.lib.gpl_server_submit(self.h, C.byref(holder.desc), C.byref(prm), C.byref(t)))
+        if net_weights is None:
+            check(self.lib.gpl_server_submit(self.h, C.byref(holder.desc), C.byref(prm), C.byref(t)))
+        else:
+            w = np.ascontiguousarray(net_weights, dtype=np.float32)
+            check(self.lib.gpl_server_submit_weighted(self.h, C.byref(holder.desc), C.byref(prm),
+                                                      w.ctypes.data_as(C.c_void_p), len(w), C.byref(t)))
         self.pending.add(int(t.value))
         return int(t.value)
 

@@ -104,3 +104,31 @@ def test_invalid_netlist_is_rejected_at_submit(gpu_lib):
             srv.submit(bad, target_density=td)
         assert ei.value.status == _abi.GPL_ERR_INVALID_ARG
         assert srv.counts() == {"queued": 0, "running": 0, "ended": 0}
+
+
+def test_weighted_jobs_match_alone(gpu_lib):
+    """Per-net weights submitted with a job (gpl_server_submit_weighted) give
+    the result of the same weighted job through the plain API; a weight
+    array of the wrong length is rejected at submit."""
+    from replace_gb300 import Placer, PlacementServer
+    from replace_gb300._lib import GplError
+    jobs = small_batch(n=3, seed=5)
+    ws = [np.random.default_rng(k).lognormal(0.0, 0.5, nl.n_nets).astype(np.float32)
+          for k, (nl, _) in enumerate(jobs)]
+    with PlacementServer(max_active=2) as srv:
+        tickets = [srv.submit(nl, target_density=td, net_weights=w) for (nl, td), w in zip(jobs, ws)]
+        res = {r["ticket"]: r for r in srv.wait_all(600)}
+        locs = {t: srv.locations(t, nl.n_insts) for t, (nl, _) in zip(tickets, jobs)}
+        with pytest.raises(GplError):
+            srv.submit(jobs[0][0], target_density=jobs[0][1], net_weights=ws[0][:-1])
+    for t, (nl, td), w in zip(tickets, jobs, ws):
+        p = Placer(nl, target_density=td)
+        p.set_net_weights(w)
+        p.initial_place()
+        p.nesterov_init()
+        rc, st, _ = p.nesterov_run(0)
+        lx, ly = p.inst_locations()
+        p.close()
+        r = res[t]
+        assert r["status"] == rc == 0 and r["iterations"] == st.iterations and r["hpwl"] == st.hpwl
+        assert np.array_equal(locs[t][0], lx) and np.array_equal(locs[t][1], ly)
