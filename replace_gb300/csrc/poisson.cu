@@ -17,6 +17,11 @@
 // or two columns packed as real and imaginary parts), using Makhoul's
 // even/odd reordering for the DCT-II and its inverse for the DCT-III; an
 // IDST is a DCT-III of the reversed input with alternating output signs.
+//
+// Two forms of the same passes: on 512 x 512 and 1024 x 1024 grids one warp
+// per packed pair runs a register FFT (the "warp form", with the density in
+// its own kernel before pass A); other grids use one packed pair per
+// 256-thread block and radix-4 Stockham passes in shared memory.
 #include <cuda_runtime.h>
 
 #include <cmath>
