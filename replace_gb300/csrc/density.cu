@@ -23,7 +23,7 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr int kBigBins = 64;
-constexpr int kCellBlocksPerSm = 5;   // the gcell kernel's residency (48 registers)        // cells covering more bins go to the big-cell kernels
+constexpr int kCellBlocksPerSm = 6;   // the gcell kernel's residency (40 registers, a few spilled)        // cells covering more bins go to the big-cell kernels
 
 struct ScatterArgs {
   BinGeom geo;
