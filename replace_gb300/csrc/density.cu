@@ -22,8 +22,8 @@ namespace gpl {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kBigBins = 64;
-constexpr int kCellBlocksPerSm = 6;   // the gcell kernel's residency (40 registers, a few spilled)        // cells covering more bins go to the big-cell kernels
+constexpr int kBigBins = 64;          // cells covering more bins go to the big-cell kernels
+constexpr int kCellBlocksPerSm = 6;   // the gcell kernel's residency (40 registers, a few spilled)
 
 struct ScatterArgs {
   BinGeom geo;
