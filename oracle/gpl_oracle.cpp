@@ -473,13 +473,18 @@ struct Oracle {
   }
 
   void binRange(int g, int& x0, int& x1, int& y0, int& y1) const {
-    // getDensityMinMaxIdxX/Y (src/nesterovBase.cpp:822-841), unclamped
+    // getDensityMinMaxIdxX/Y (src/nesterovBase.cpp:822-841).  The reference
+    // leaves the range unclamped and reads outside its bins for a cell that
+    // sticks out of the core (undefined behaviour); the range is clamped to
+    // the grid here, as the GPU does, which changes nothing for cells inside.
     x0 = (gdlx[g] - coreLx) / sizeX;
     x1 = fast_modulo(gdux[g] - coreLx, sizeX) == 0 ? (gdux[g] - coreLx) / sizeX
                                                   : (gdux[g] - coreLx) / sizeX + 1;
     y0 = (gdly[g] - coreLy) / sizeY;
     y1 = fast_modulo(gduy[g] - coreLy, sizeY) == 0 ? (gduy[g] - coreLy) / sizeY
                                                   : (gduy[g] - coreLy) / sizeY + 1;
+    x0 = std::max(x0, 0); y0 = std::max(y0, 0);
+    x1 = std::min(x1, cntX); y1 = std::min(y1, cntY);
   }
 
   float overlap(int b, int g) const {
