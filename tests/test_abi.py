@@ -138,3 +138,34 @@ def test_job_batch_and_stream_generators():
     assert np.all(np.diff(t) > 0)
     assert all(5_000 <= s["n_cells"] <= 500_000 for s in spec)
     assert 0 < sum(s["n_macros"] > 0 for s in spec) < 50
+
+
+def test_large_netlist_checks_run_in_parallel_ranges():
+    """Netlists of more than 65,536 pins are copied and checked by several
+    host threads: a bad pin, a pin listed twice and a missing pin are still
+    found wherever they are."""
+    from replace_gb300 import load
+    lib = load()
+    nl = N.generate(30_000, 31_500, n_io=100, seed=2)
+    assert nl.n_pins > (1 << 16)
+    bad = nl.copy()
+    bad.pin_inst = bad.pin_inst.copy()
+    bad.pin_inst[nl.n_pins - 7] = nl.n_insts + 5          # out of range, near the end
+    q = int(nl.inst_pin_start[20_000])
+    assert int(nl.inst_pin_start[20_001]) - q >= 2
+    dup = nl.copy()
+    dup.inst_pins = dup.inst_pins.copy()
+    dup.inst_pins[q + 1] = dup.inst_pins[q]
+    for net, msg in ((bad, b"pin_inst out of range"), (dup, b"twice")):
+        h = _abi.DescHolder(net)
+        job = C.c_void_p()
+        rc = lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job))
+        assert rc == _abi.GPL_ERR_INVALID_ARG
+        assert msg in lib.gpl_last_error()
+    # the valid netlist passes the checks (and stops at the missing device here)
+    import torch
+    if not torch.cuda.is_available():
+        h = _abi.DescHolder(nl)
+        job = C.c_void_p()
+        assert lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job)) == \
+            _abi.GPL_ERR_NO_DEVICE
