@@ -153,3 +153,29 @@ def test_net_weights_scale_pin_gradients(oracle_mod):
     o.set_net_weights(None)
     wl3, _, _, _ = o.eval(ref["coords"], wlc)
     assert np.array_equal(wl3, wl0)
+
+
+def test_cells_outside_the_core_are_clamped(oracle_mod):
+    """Cells that stick out of the core (the reference reads outside its bins
+    there) only touch in-core bins in the oracle, as on the GPU: with every
+    centre on the core's corner the area lands in the bins around that
+    corner, and repeated evaluations agree bit for bit."""
+    nl, opts = case("simple02")
+    o = oracle_mod.Oracle(nl, **params_of(opts))
+    o.initial_place()
+    assert o.nesterov_base() == 0
+    n = o.info.n_gcells
+    c = nl.core
+    xy = np.empty(2 * n, np.float32)
+    xy[0::2] = c[0]            # every centre on the core's lower-left corner
+    xy[1::2] = c[1]
+    _, _, st1, _ = o.eval(xy, 0.01)
+    b1 = o.bins()
+    _, _, st2, _ = o.eval(xy, 0.01)
+    b2 = o.bins()
+    assert np.array_equal(b1["inst_area"], b2["inst_area"])
+    assert np.array_equal(b1["filler_area"], b2["filler_area"])
+    # only the bins around the corner receive area
+    nx = o.info.bin_cnt_x
+    ia = b1["inst_area"].reshape(-1, nx) + b1["filler_area"].reshape(-1, nx)
+    assert ia.sum() > 0 and ia[-1, :].sum() == 0 and ia[:, -1].sum() == 0
