@@ -52,24 +52,31 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms from the
+    start of the warm-up to the end of the end-to-end job (the timed region
+    alone is often shorter than one sample period); `mark()` brackets the
+    timed region so the samples inside it are counted separately."""
 
     def __init__(self, gpu_index: int):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        self.t0 = time.time()
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        self.window = None
+        q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}",
-                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                       "--format=csv,noheader,nounits", "-lms", "50"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except FileNotFoundError:
             self.p = None
 
+    def mark(self, t0: float, t1: float):
+        self.window = (t0, t1)
+
     def stop(self):
         if self.p is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"],
+                    "samples": 0}
         self.p.terminate()
         try:
             self.p.wait(timeout=5)
@@ -77,23 +84,32 @@ class ClockSampler:
             self.p.kill()
         self.f.seek(0)
         rows = [l.strip().split(",") for l in self.f.read().splitlines() if l.strip()]
-        sm, smax, reasons = [], [], set()
+        os.unlink(self.f.name)
+        sm, smax, busy, inside, reasons = [], [], [], 0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
             r = [x.strip() for x in r]
             if len(r) < 9:
                 continue
             try:
-                sm.append(float(r[1])); smax.append(float(r[2]))
+                f_sm, f_max, util = float(r[1]), float(r[2]), float(r[4])
+                ts = time.mktime(time.strptime(r[0].split(".")[0], "%Y/%m/%d %H:%M:%S"))
             except ValueError:
                 continue
+            sm.append(f_sm); smax.append(f_max)
+            if util >= 50:
+                busy.append(f_sm)
+            if self.window and self.window[0] - 1 <= ts <= self.window[1] + 1:
+                inside += 1
             for n, v in zip(names, r[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
-        os.unlink(self.f.name)
-        return {"sm_mhz": statistics.median(sm) if sm else None,
+        return {"sm_mhz": statistics.median(busy) if busy else (statistics.median(sm) if sm else None),
                 "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_under_load": len(busy),
+                "samples_near_timed_region": inside,
+                "window": "from the warm-up to the end of the end-to-end job, every 50 ms; "
+                          "sm_mhz = median of the samples with GPU utilisation >= 50 %"}
 
 
 # Algorithmic bytes per launch group (each array touched once), for the
@@ -110,9 +126,11 @@ def algorithmic_bytes(kind, ng, npins, nn, nb):
     }.get(kind)
 
 
-# DRAM bytes per launch (read + write) measured with ncu on the 1M-cell
-# workload (profiles/traffic_1m_cells_1024bins.md): the `traffic` of the
-# roofline object when the dominant kernel is one of these.
+# DRAM bytes per launch (read + write) from one ncu capture of each kernel on
+# the 1M-cell workload (dram__bytes_read.sum + dram__bytes_write.sum),
+# refreshed when a kernel changes: the `traffic` of the roofline object when
+# the dominant kernel is one of these.  A static figure: bench.py does not
+# run under ncu.
 NCU_TRAFFIC = {
     "1m_cells_1024bins": {
         "wa_wirelength": 101.6e6, "gcell_gradient": 131.0e6, "density_scatter": 64.7e6,
@@ -138,19 +156,53 @@ def replica_value(world: int, iters_per_rank: int, ms: float) -> float:
     return world * iters_per_rank / (ms / 1000.0)
 
 
-def cpu_baseline_sample(nl, td, bins, iters=3):
-    """Oracle (single-threaded CPU restatement) on this host: setup, init,
-    then `iters` Nesterov iterations; returns steady-state iterations/s."""
+def host_cpu() -> dict:
+    """This host's CPU: model (lscpu) and the threads available to the process."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for l in out.splitlines():
+            if l.startswith("Model name:"):
+                model = l.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return {"nproc": os.cpu_count(), "cpu": model, "arch": platform.machine()}
+
+
+# The CPU sample of both CPU legs (cpu_baseline and the reference arm): the
+# same job, the same warm-up and the same timed iterations, so the two agree.
+CPU_WARMUP = 3
+CPU_STEPS = 5
+
+
+def cpu_baseline_sample(nl, td, bins, warmup=CPU_WARMUP, steps=CPU_STEPS):
+    """Oracle (single-threaded CPU restatement) on this host: setup and init
+    from the centred placement, `warmup` Nesterov iterations, then `steps`
+    timed iterations.  Returns (iterations/s, evaluations per iteration,
+    seconds of CPU work in all)."""
     from oracle import oracle as O
     t0 = time.perf_counter()
     o = O.Oracle(nl, target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
                  initial_place_max_iter=0)
     o.initial_place()
     o.nesterov_init()
+    _, s0, _ = o.nesterov_run(warmup)
     t1 = time.perf_counter()
-    o.nesterov_run(iters)
+    _, s1, _ = o.nesterov_run(steps)
     t2 = time.perf_counter()
-    return iters / (t2 - t1), t2 - t0
+    evals = (s1.evaluations - s0.evaluations) / max(steps, 1)
+    return steps / (t2 - t1), evals, t2 - t0
+
+
+def cpu_sample_text(steps, warmup, evals, seconds):
+    return (f"{steps} Nesterov iterations ({evals:.2f} evaluations each) of the same 1M-cell job "
+            f"after setup, init and {warmup} warm-up iterations, from the centred placement "
+            f"({seconds:.1f} s of single-threaded CPU work; the oracle restatement of the "
+            "reference's path, which has no threads: its initial place alone would take minutes "
+            "on one core, and the work of a Nesterov iteration does not depend on where the "
+            "cells are)")
 
 
 def serving_batch(n_jobs, slots, device):
@@ -279,6 +331,36 @@ def precision_form(nl, td, bins, device, stream, steps, warmup, fft_job):
     return out
 
 
+def reference_parity(nl, td, bins, device, workload):
+    """Final HPWL of the whole Nesterov loop against the reference's own
+    NesterovPlace run on the same netlist (tests/golden/scale_place_*.npz,
+    recorded from the reference build).  Both start without initial place
+    (every movable instance at the core centre): the reference's initial
+    place needs Eigen, which its build here does not have.  The GPU job runs
+    the FFT Poisson form."""
+    import numpy as np
+    from replace_gb300 import Placer
+    path = os.path.join(ROOT, "tests", "golden", f"scale_place_{workload}.npz")
+    if not os.path.exists(path):
+        return {"available": False, "reason": "no recorded reference run for this workload"}
+    ref = np.load(path)
+    p = Placer(nl, target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+               initial_place_max_iter=0, poisson_path=1, device=device)
+    p.initial_place()
+    p.nesterov_init()
+    rc, st, _ = p.nesterov_run(0)
+    p.close()
+    fh = int(ref["final_hpwl"])
+    return {"available": True, "start": "centred placement, no initial place",
+            "status": int(rc), "iterations": int(st.iterations), "final_overflow": float(st.overflow),
+            "final_hpwl": int(st.hpwl),
+            "reference_status": int(ref["rc"]), "reference_iterations": int(ref["iters"][-1]),
+            "reference_final_overflow": float(ref["final_overflow"]), "reference_final_hpwl": fh,
+            "hpwl_rel_diff": (int(st.hpwl) - fh) / fh if fh > 0 else None,
+            "within_0_5_percent": bool(fh > 0 and abs(int(st.hpwl) - fh) <= 0.005 * fh
+                                       and st.overflow <= 0.1)}
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -287,20 +369,12 @@ def run_reference(args):
     nl, td, bins = N.generate_workload(WORKLOAD, seed=1)
     from oracle import oracle as O
     O.build()
-    o = O.Oracle(nl, target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
-                 initial_place_max_iter=0)
-    o.initial_place()
-    o.nesterov_init()
     # Each CPU iteration of the 1M-cell job takes about a second: the arm
-    # times a bounded sample (at most 5 iterations after at most 3 warm-up
-    # iterations) so that the run ends within a few minutes.
-    warm = min(args.warmup, 3)
-    steps = max(1, min(args.steps, 5))
-    o.nesterov_run(warm)
-    t0 = time.perf_counter()
-    o.nesterov_run(steps)
-    dt = time.perf_counter() - t0
-    v = steps / dt
+    # times the same bounded sample as the cpu_baseline leg of the GPU arm.
+    warm = CPU_WARMUP
+    steps = CPU_STEPS
+    v, evals, secs = cpu_baseline_sample(nl, td, bins, warm, steps)
+    dt = steps / v
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1000 * dt / steps,
@@ -309,9 +383,10 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "cells": 1_000_000, "nets": 1_050_000, "bins": "1024x1024",
                    "target_density": td, "parallelism": "single-threaded CPU"},
         "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "port",
-                         "sample": f"{steps} Nesterov iterations after {warm} warm-up "
-                                   "iterations of the 1M-cell job (oracle restatement; the "
-                                   "reference's own build needs OpenDB/Eigen and is not on this host)"},
+                         "host": host_cpu(),
+                         "sample": cpu_sample_text(steps, warm, evals, secs) +
+                                   "; the reference's own build needs the reference sources, "
+                                   "OpenDB and Eigen, none of which is on this host"},
         "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -325,10 +400,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-iters", type=int, default=0,
                     help="Nesterov iteration cap of the end-to-end job (0 = run to the stop rule)")
-    ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the whole-loop comparison with the reference's recorded run")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--stream-jobs", type=int, default=40)
     ap.add_argument("--slots", type=int, default=16)
@@ -365,6 +441,7 @@ def main():
     ip_stats = p.initial_place()
     p.nesterov_init()
     info = p.info
+    clocks = ClockSampler(local_rank)
     p.nesterov_run(args.warmup)
 
     # timed region: K iterations, resident data, CUDA events on the job stream
@@ -374,17 +451,17 @@ def main():
             dist.barrier()
     barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local_rank)
     launches0 = p.kernel_launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    t_wall0 = time.time()
     e0.record(stream)
     rc, st, _ = p.nesterov_run(args.steps)
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.mark(t_wall0, time.time())
     barrier()
     ms = e0.elapsed_time(e1)
-    clk = clocks.stop()
     launches = p.kernel_launches() - launches0
     iters_done = st.iterations - args.warmup
     ms = max_over_ranks(ms, world, "cuda")
@@ -434,6 +511,10 @@ def main():
                             f"rule ({e2e_iters} iterations), location read-back",
                     "job_seconds": t1 - t0, "finished": bool(st2.finished),
                     "final_overflow": float(st2.overflow), "final_hpwl": int(st2.hpwl)}
+    clk = clocks.stop()
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = reference_parity(nl, td, bins, local_rank, args.workload)
 
     serving = None
     if world == 1 and not args.no_serving:
@@ -442,13 +523,9 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v_cpu, t_cpu = cpu_baseline_sample(nl, td, bins, args.cpu_iters)
-        cpu = {"value": v_cpu, "unit": "iters/s", "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_iters} Nesterov iterations of the same 1M-cell job after "
-                         f"setup and init ({t_cpu:.1f} s of single-threaded CPU work; the oracle "
-                         "restatement of the reference's path), from the centred placement: its "
-                         "initial place alone would take minutes on one core, and the work of a "
-                         "Nesterov iteration does not depend on where the cells are"}
+        v_cpu, ev_cpu, t_cpu = cpu_baseline_sample(nl, td, bins)
+        cpu = {"value": v_cpu, "unit": "iters/s", "cores": 1, "kind": "port", "host": host_cpu(),
+               "sample": cpu_sample_text(CPU_STEPS, CPU_WARMUP, ev_cpu, t_cpu)}
 
     if rank == 0:
         line = {
@@ -476,12 +553,14 @@ def main():
                          "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm, "peak_kind": f"of {peak_kind}",
                          "traffic": NCU_TRAFFIC.get(args.workload, {}).get(dom),
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
-                                           "(profiles/traffic_1m_cells_1024bins.md)",
+                         "traffic_kind": "static: dram__bytes_read.sum + dram__bytes_write.sum per "
+                                         "launch from one ncu capture of this kernel on this "
+                                         "workload, not measured in this run",
                          "algorithmic_bytes": bytes_per, "kernel_share": kernel_share,
                          "kernel_ms_per_launch": kernel_ms},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "final_hpwl_vs_reference": parity,
             "serving": serving,
             "precision_form": precision,
         }

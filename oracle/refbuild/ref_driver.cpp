@@ -17,6 +17,8 @@
 //                                      density centres with --init-coords):
 //                                      bin areas, density, phi, field, per-gcell
 //                                      WA and density gradients, HPWL.
+//                                      --coords <file> reads the centres
+//                                      instead (raw float32 x, y per gcell).
 //
 // Options: --density d  --bins n  --idp p (init density penalty)  --iwc c
 //          --minphi m --maxphi m --overflow o --maxiter n --incremental
@@ -33,6 +35,7 @@
 #include <vector>
 
 #include "opendb/db.h"
+#include "refnet_db.h"
 #include "placerBase.h"
 #include "nesterovBase.h"
 #include "nesterovPlace.h"
@@ -55,86 +58,8 @@ struct Opts {
   bool init_coords = false;
   float wlcoef = -1.0f;
   std::string out_pos;
+  std::string coords;
 };
-
-static odb::dbDatabase* read_net(const char* path) {
-  std::ifstream in(path);
-  if (!in) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
-  std::string tag;
-  auto db = new odb::dbDatabase();
-  db->tech = new odb::dbTech();
-  db->chip = new odb::dbChip();
-  auto blk = new odb::dbBlock();
-  db->chip->block = blk;
-  auto site = new odb::dbSite();
-  int nrows = 0, ninst = 0, nnet = 0;
-  in >> tag;  // REFNET
-  int ver; in >> ver;
-  in >> tag >> db->tech->dbu;                       // DBU
-  in >> tag >> site->w >> site->h;                  // SITE
-  in >> tag >> blk->bbox.xl >> blk->bbox.yl >> blk->bbox.xh >> blk->bbox.yh;  // DIE
-  in >> tag >> nrows;                               // ROWS
-  for (int i = 0; i < nrows; i++) {
-    auto r = new odb::dbRow();
-    in >> r->box.xl_ >> r->box.yl_ >> r->box.xh_ >> r->box.yh_;
-    r->site = site;
-    blk->rows.push_back(r);
-  }
-  in >> tag >> ninst;                               // INSTS
-  std::vector<std::vector<std::pair<int, odb::dbITerm*>>> inst_terms(ninst);
-  for (int i = 0; i < ninst; i++) {
-    auto inst = new odb::dbInst();
-    int st;
-    inst->master = new odb::dbMaster();
-    in >> inst->x >> inst->y >> inst->w >> inst->h >> inst->master->w >> inst->master->h >> st;
-    inst->status = st ? odb::dbPlacementStatus::FIRM : odb::dbPlacementStatus::NONE;
-    inst->bbox = odb::dbBox(inst->x, inst->y, inst->x + inst->w, inst->y + inst->h);
-    blk->insts.push_back(inst);
-  }
-  in >> tag >> nnet;                                // NETS
-  for (int n = 0; n < nnet; n++) {
-    auto net = new odb::dbNet();
-    int sig, ni, nb;
-    in >> sig >> ni >> nb;
-    net->sig = (odb::dbSigType::Value)sig;
-    for (int k = 0; k < ni; k++) {
-      int inst, key, has, xl, yl, xh, yh;
-      in >> inst >> key >> has >> xl >> yl >> xh >> yh;
-      auto it = new odb::dbITerm();
-      it->inst = blk->insts[inst];
-      it->mterm = new odb::dbMTerm();
-      if (has) {
-        auto mp = new odb::dbMPin();
-        mp->boxes.push_back(new odb::dbBox(xl, yl, xh, yh));
-        it->mterm->mpins.push_back(mp);
-      }
-      net->iterms.push_back(it);
-      inst_terms[inst].push_back({key, it});
-    }
-    for (int k = 0; k < nb; k++) {
-      int has, xl, yl, xh, yh;
-      in >> has >> xl >> yl >> xh >> yh;
-      auto bt = new odb::dbBTerm();
-      bt->name = "io" + std::to_string(n) + "_" + std::to_string(k);
-      if (has) {
-        auto bp = new odb::dbBPin();
-        bp->box = odb::dbBox(xl, yl, xh, yh);
-        bt->bpins.push_back(bp);
-      }
-      net->bterms.push_back(bt);
-    }
-    blk->nets.push_back(net);
-  }
-  // instance iterm order = master pin order (stable by key)
-  for (int i = 0; i < ninst; i++) {
-    auto& v = inst_terms[i];
-    std::stable_sort(v.begin(), v.end(),
-                     [](const std::pair<int, odb::dbITerm*>& a,
-                        const std::pair<int, odb::dbITerm*>& b) { return a.first < b.first; });
-    for (auto& p : v) blk->insts[i]->iterms.push_back(p.second);
-  }
-  return db;
-}
 
 static void parse_opts(int argc, char** argv, int start, Opts& o) {
   for (int i = start; i < argc; i++) {
@@ -154,6 +79,7 @@ static void parse_opts(int argc, char** argv, int start, Opts& o) {
     else if (a == "--init-coords") o.init_coords = true;
     else if (a == "--wlcoef") o.wlcoef = std::stof(nxt());
     else if (a == "--out-pos") o.out_pos = nxt();
+    else if (a == "--coords") o.coords = nxt();
     else { fprintf(stderr, "unknown option %s\n", a.c_str()); exit(2); }
   }
 }
@@ -218,6 +144,16 @@ int main(int argc, char** argv) {
     const auto& gcells = nb->gCells();
     const int ng = (int)gcells.size();
     std::vector<FloatPoint> coords(ng);
+    std::vector<float> given;
+    if (!o.coords.empty()) {
+      given.resize(2 * (size_t)ng);
+      FILE* cf = fopen(o.coords.c_str(), "rb");
+      if (!cf || fread(given.data(), sizeof(float), given.size(), cf) != given.size()) {
+        fprintf(stderr, "cannot read %d coordinate pairs from %s\n", ng, o.coords.c_str());
+        return 2;
+      }
+      fclose(cf);
+    }
     std::mt19937 rng(o.seed);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     std::vector<int32_t> ginfo;   // per gcell: lx ly ux uy dLx dLy dUx dUy kind
@@ -229,7 +165,9 @@ int main(int argc, char** argv) {
                                  g->dLx(), g->dLy(), g->dUx(), g->dUy(),
                                  g->isFiller() ? 2 : (g->isMacroInstance() ? 1 : 0)});
       gscale.push_back(g->densityScale());
-      if (o.init_coords) {
+      if (!given.empty()) {
+        coords[i] = FloatPoint(given[2 * i], given[2 * i + 1]);
+      } else if (o.init_coords) {
         coords[i] = FloatPoint(g->dCx(), g->dCy());
       } else {
         const Die& die = pb->die();

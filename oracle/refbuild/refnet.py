@@ -18,12 +18,19 @@ REF_DIR = os.path.join(os.path.dirname(HERE), "_ref")
 DRIVER = os.path.join(REF_DIR, "ref_driver")
 
 
+def default_ref_root() -> str:
+    """Where the reference tree is read from: $REPLACE_REFERENCE_ROOT, else
+    the build container's copy."""
+    return os.environ.get("REPLACE_REFERENCE_ROOT", "/root/reference")
+
+
 def available() -> bool:
     return os.path.exists(DRIVER)
 
 
-def build(ref_root: str = "/root/reference") -> bool:
+def build(ref_root: str | None = None) -> bool:
     """Compile the reference build if the reference sources are present."""
+    ref_root = ref_root or default_ref_root()
     if not os.path.isdir(os.path.join(ref_root, "src")):
         return available()
     r = subprocess.run(["make", "-s", "-C", HERE, f"REF={ref_root}", "-j8"],
@@ -118,13 +125,19 @@ def read_bin(path: str) -> dict:
     return out
 
 
-def run_eval(nl, **opts) -> dict:
-    """One reference NesterovBase evaluation; see ref_driver.cpp (eval)."""
+def run_eval(nl, coords=None, **opts) -> dict:
+    """One reference NesterovBase evaluation; see ref_driver.cpp (eval).
+    `coords` (float32, x y per gcell) replaces the driver's seeded centres."""
     with tempfile.TemporaryDirectory() as td:
         net = os.path.join(td, "net.txt")
         out = os.path.join(td, "out.bin")
         write_refnet(nl, net)
-        r = subprocess.run([DRIVER, "eval", net, out] + _opt_args(opts),
+        extra = []
+        if coords is not None:
+            cpath = os.path.join(td, "coords.bin")
+            np.ascontiguousarray(coords, np.float32).tofile(cpath)
+            extra = ["--coords", cpath]
+        r = subprocess.run([DRIVER, "eval", net, out] + _opt_args(opts) + extra,
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(r.stdout + r.stderr)

@@ -1,4 +1,4 @@
-"""Minimal LEF/DEF subset reader for placement netlists.
+"""Minimal LEF/DEF subset reader (and placement writer) for placement netlists.
 
 Reads what global placement needs from a LEF library and a DEF design:
 
@@ -14,6 +14,13 @@ rectangle transformed by the pin orientation and moved to the pin location
 (the box OpenDB returns from ``dbBPin::getBox``); component pin offsets use the
 master's pin geometry without the component orientation, as RePlAce does in
 ``Pin::updateCoordi(dbITerm*)`` (src/placerBase.cpp:330-376).
+
+Writing back: ``format_components`` prints a COMPONENTS section the way
+OpenDB's ``write_def`` does after ``global_placement`` (one line per
+component, ``- name master + PLACED ( x y ) N ;``), and ``write_placement``
+replaces the COMPONENTS section of an existing DEF with it, keeping every
+other byte of the file.  The locations are those NesterovPlace::updateDb
+writes into the database (src/nesterovPlace.cpp:585-595).
 """
 
 from __future__ import annotations
@@ -23,7 +30,8 @@ from dataclasses import dataclass, field
 
 __all__ = [
     "LefMacro", "LefLibrary", "DefComponent", "DefPin", "DefNet", "DefRow",
-    "DefDesign", "read_lef", "read_def", "transform_box",
+    "DefDesign", "read_lef", "read_def", "transform_box", "format_components",
+    "placed_components", "write_placement",
 ]
 
 
@@ -397,3 +405,49 @@ def _read_nets(toks, i, d, section):
         else:
             i += 1
     return i + 2
+
+
+_FIXED_STATUS = ("FIXED", "COVER", "LOCKED", "FIRM")
+
+
+def placed_components(components, lx, ly):
+    """Components after placement: movable ones (not FIXED / COVER / LOCKED /
+    FIRM) move to (lx[k], ly[k]) with status PLACED and keep their
+    orientation (N when they had none); fixed ones are unchanged.  lx, ly are
+    per component, in DEF order (the first len(components) instances of a
+    Netlist read from that DEF)."""
+    out = []
+    for k, c in enumerate(components):
+        if c.status in _FIXED_STATUS:
+            out.append(DefComponent(c.name, c.master, c.status, c.x, c.y, c.orient))
+        else:
+            out.append(DefComponent(c.name, c.master, "PLACED", int(lx[k]), int(ly[k]),
+                                    c.orient or "N"))
+    return out
+
+
+def format_components(components) -> str:
+    """A COMPONENTS section as OpenDB's write_def prints it."""
+    lines = [f"COMPONENTS {len(components)} ;"]
+    for c in components:
+        if c.status == "UNPLACED":
+            lines.append(f"    - {c.name} {c.master} ;")
+        else:
+            lines.append(f"    - {c.name} {c.master} + {c.status} ( {c.x} {c.y} ) {c.orient} ;")
+    lines.append("END COMPONENTS")
+    return "\n".join(lines) + "\n"
+
+
+def write_placement(def_in: str, def_out: str, lx, ly) -> None:
+    """Copy DEF `def_in` to `def_out` with its COMPONENTS section replaced by
+    the placed components (see placed_components)."""
+    with open(def_in) as f:
+        text = f.read()
+    m = re.search(r"^[ \t]*COMPONENTS\b.*?^[ \t]*END[ \t]+COMPONENTS[^\n]*\n?", text,
+                  re.MULTILINE | re.DOTALL)
+    if m is None:
+        raise ValueError(f"{def_in}: no COMPONENTS section")
+    d = read_def(def_in)
+    section = format_components(placed_components(d.components, lx, ly))
+    with open(def_out, "w") as f:
+        f.write(text[:m.start()] + section + text[m.end():])

@@ -4,6 +4,8 @@ Run where the reference tree is available (it is read, never modified):
 
     python tests/golden/make_golden.py [--ref /path/to/RePlAce]
 
+(default: $REPLACE_REFERENCE_ROOT, else the build container's copy)
+
 It builds the reference's unchanged placement sources with oracle/refbuild
 (outputs in oracle/_ref/, git-ignored), then records for each case:
 
@@ -18,6 +20,10 @@ It builds the reference's unchanged placement sources with oracle/refbuild
                        simple04): the rounds and Nesterov lines the
                        reference logged in test/<case>.ok (its initial place
                        needs Eigen, so it is not rebuilt here)
+* defok_<case>.npz     the COMPONENTS section of the reference's regression
+                       output test/<case>.defok (what its write_def produced
+                       after global_placement): per component its location,
+                       status and orientation, in DEF order
 """
 
 from __future__ import annotations
@@ -96,11 +102,32 @@ def parse_log(log):
             float(fin.group(1)) if fin else float("nan"), int(fh.group(1)) if fh else -1)
 
 
+STATUS_CODES = {"UNPLACED": 0, "PLACED": 1, "FIXED": 2, "COVER": 3}
+
+
+def save_defok(ref_root, name):
+    from replace_gb300 import lefdef
+    d = lefdef.read_def(os.path.join(ref_root, "test", name + ".defok"))
+    np.savez_compressed(os.path.join(HERE, f"defok_{name}.npz"),
+                        x=np.array([c.x for c in d.components], np.int32),
+                        y=np.array([c.y for c in d.components], np.int32),
+                        status=np.array([STATUS_CODES[c.status] for c in d.components], np.int8),
+                        orient=np.array([c.orient for c in d.components]),
+                        master=np.array([c.master for c in d.components]),
+                        name=np.array([c.name for c in d.components]))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    args = ap.parse_args()
     import refnet
+    ap.add_argument("--ref", default=refnet.default_ref_root())
+    ap.add_argument("--only-defok", action="store_true",
+                    help="write only the defok_<case>.npz fixtures")
+    args = ap.parse_args()
+    for name in LEFDEF_CASES:
+        save_defok(args.ref, name)
+    if args.only_defok:
+        return
     if not refnet.build(args.ref):
         raise SystemExit("reference build unavailable")
     t = os.path.join(args.ref, "test")

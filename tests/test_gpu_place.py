@@ -245,3 +245,46 @@ def test_net_weights_switched_on_and_off_between_chunks(gpu_lib, oracle_mod, dev
     # rounding has had 30 iterations to move the two runs apart
     assert abs(int(g[4]["hpwl"][0]) - int(o[4]["hpwl"][0])) <= 5e-3 * int(o[4]["hpwl"][0])
     assert g[2] <= 0.1 and abs(g[3] - o[3]) <= 0.005 * o[3]
+
+
+@pytest.mark.parametrize("name", ["syn_macro", "simple02"])
+def test_update_db_locations_match_oracle(gpu_lib, oracle_mod, name):
+    """NesterovPlace::updateDb (src/nesterovPlace.cpp:585-595): at identical
+    gcell centres the GPU job and the oracle give the same instance locations
+    (lx = dCx - dDx/2, ly = dCy - dDy/2 of the density rectangle), bit for
+    bit: (1) at seeded centres set through the gradient-check hook, (2) at
+    the GPU's own centres after 40 Nesterov iterations."""
+    from replace_gb300 import Placer
+    nl, opts = case(name)
+    kw = params_of(opts)
+    o = oracle_mod.Oracle(nl, **kw)
+    o.initial_place()
+    assert o.nesterov_init() == 0
+    n = o.info.n_gcells
+    c = nl.core
+    rng = np.random.default_rng(5)
+    xy = np.empty(2 * n, np.float32)
+    xy[0::2] = rng.uniform(c[0], c[2], n)
+    xy[1::2] = rng.uniform(c[1], c[3], n)
+    p = Placer(nl, **kw)
+    p.initial_place()
+    p.nesterov_init()
+    p.eval(xy, 1e-3)
+    o.eval(xy, 1e-3)
+    lx, ly = p.inst_locations()
+    olx, oly = o.inst_locations()
+    assert np.array_equal(lx, olx) and np.array_equal(ly, oly)
+    p.close()
+    q = Placer(nl, **kw)
+    q.initial_place()
+    q.nesterov_init()
+    rc, st, _ = q.nesterov_run(40)
+    assert rc == 0 and st.iterations == 40
+    lx, ly = q.inst_locations()
+    o.eval(q.gcell_coords().reshape(-1), 1e-3)
+    olx, oly = o.inst_locations()
+    assert np.array_equal(lx, olx) and np.array_equal(ly, oly)
+    # fixed and dummy instances keep their input locations
+    other = nl.inst_kind != 0
+    assert np.array_equal(lx[other], nl.inst_lx[other]) and np.array_equal(ly[other], nl.inst_ly[other])
+    q.close()

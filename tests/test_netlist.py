@@ -5,10 +5,11 @@ import os
 import numpy as np
 import pytest
 
+import refnet
 from conftest import GOLDEN, case
 from replace_gb300 import netlist as N
 
-REF_TEST = "/root/reference/test"
+REF_TEST = os.path.join(refnet.default_ref_root(), "test")
 
 
 def test_regression_designs_counts():

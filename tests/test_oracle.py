@@ -179,3 +179,35 @@ def test_cells_outside_the_core_are_clamped(oracle_mod):
     nx = o.info.bin_cnt_x
     ia = b1["inst_area"].reshape(-1, nx) + b1["filler_area"].reshape(-1, nx)
     assert ia.sum() > 0 and ia[-1, :].sum() == 0 and ia[:, -1].sum() == 0
+
+
+def test_eval_matches_reference_at_200k_cells(oracle_mod):
+    """The oracle against the reference build at the 200k-cell / 40-macro /
+    512-bin workload (digests in tests/golden/scale_eval_*.npz): bin areas,
+    density and HPWL bit for bit, WA gradients within the float tolerance,
+    field and density gradients within the FP64-vs-FP32 transform bar."""
+    import os
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import scale_cases as S
+    from replace_gb300 import netlist as N
+    name = "200k_cells_40macros_512bins"
+    ref = golden(f"scale_eval_{name}.npz")
+    nl, td, bins = N.generate_workload(name, seed=S.SCALE_WORKLOADS[name])
+    o = oracle_mod.Oracle(nl, target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
+                          initial_place_max_iter=0)
+    o.initial_place()
+    assert o.nesterov_base() == 0
+    n = o.info.n_gcells
+    assert n == int(ref["n_gcells"])
+    drect, _, _ = o.gcells()
+    xy = S.eval_coords(nl.core, drect)
+    owl, odg, ost, _ = o.eval(xy, float(ref["wl_coef"]))
+    dig = S.eval_digest(dict(o.bins(), wl_grad=owl, density_grad=odg), n, bins * bins)
+    for k in ("inst_area_sha", "filler_area_sha", "nonplace_area_sha", "density_sha"):
+        assert str(dig[k]) == str(ref[k]), k
+    assert ost.hpwl == int(ref["hpwl"])
+    assert rel_l2(dig["wl_grad_sample"], ref["wl_grad_sample"]) < 1e-5
+    for k in ("phi", "ex", "ey", "density_grad"):
+        assert rel_l2(dig[k + "_sample"], ref[k + "_sample"]) < 1e-4, k
