@@ -283,7 +283,9 @@ gpl_status gpl_get_gcells(struct gpl_job* job, int32_t* drect, float* scale, uin
 /* Electrostatic Poisson solve alone (FFT::doFFT, src/fft.cpp:112-177) on
  * device arrays: density, phi, field_x and field_y are device pointers of
  * [ny * nx] floats, row-major by y.  nx, ny: powers of two in [2, 4096].
- * Scratch memory is allocated on first use per device and cached.
+ * Scratch memory is allocated on first use per device and grid and cached
+ * for the device's current context (after cudaDeviceReset the entries of
+ * the old context are dropped, not freed, and new scratch is allocated).
  * stream: cudaStream_t (NULL = default stream). */
 gpl_status gpl_poisson_solve(int32_t nx, int32_t ny, int32_t bin_size_x,
                              int32_t bin_size_y, const float* density, float* phi,
@@ -298,8 +300,10 @@ gpl_status gpl_poisson_solve(int32_t nx, int32_t ny, int32_t bin_size_x,
  * library) and the call allocates nothing.  Limit: nx * ny <= 512 * 512
  * (larger grids return GPL_ERR_INVALID_ARG).  The first call on a device
  * looks up the array's device address; make that first call before any
- * stream capture.  All calls share the array, so calls that overlap on the
- * GPU race; order them (same stream, or events). */
+ * stream capture.  The address is kept per device context: the first call
+ * after a cudaDeviceReset looks it up again (also before any capture).  All
+ * calls share the array, so calls that overlap on the GPU race; order them
+ * (same stream, or events). */
 gpl_status gpl_poisson_solve_noalloc(int32_t nx, int32_t ny, int32_t bin_size_x,
                                      int32_t bin_size_y, const float* density, float* phi,
                                      float* field_x, float* field_y, void* stream);

@@ -411,6 +411,12 @@ int job_device_bytes(gpl_job* j, int64_t* bytes, bool centred);
 
 // twiddle / frequency tables (host computed, double precision)
 void make_twiddle(std::vector<float2>& tw);
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId through
+// the runtime's driver entry points; 0 when it cannot be read).  Caches of
+// device addresses are keyed on it: after cudaDeviceReset the device gets a
+// new primary context, whose memory and symbol addresses are new.
+unsigned long long current_context_id();
 void make_freq(int nx, int ny, int bsx, int bsy, std::vector<float>& wx, std::vector<float>& wy);
 
 }  // namespace gpl

@@ -22,8 +22,10 @@
 // per packed pair runs a register FFT (the "warp form", with the density in
 // its own kernel before pass A); other grids use one packed pair per
 // 256-thread block and radix-4 Stockham passes in shared memory.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <memory>
 #include <mutex>
@@ -1106,13 +1108,38 @@ void make_w4(int n, std::vector<float2>& w) {
 namespace {
 struct SolveCache {
   int device = -1, nx = 0, ny = 0, bsx = 0, bsy = 0;
+  unsigned long long ctx = 0;   // context the memory belongs to
   char* mem = nullptr;
   float *spec = nullptr, *p1 = nullptr, *p2 = nullptr, *wx = nullptr, *wy = nullptr;
   float2 *w4x = nullptr, *w4y = nullptr, *tw = nullptr;
 };
 std::mutex g_cache_mu;
 std::vector<std::unique_ptr<SolveCache>> g_cache;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
 }  // namespace
+
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_cur = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_cur || !get_id || get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 }  // namespace gpl
 
@@ -1129,15 +1156,22 @@ extern "C" gpl_status gpl_poisson_solve(int32_t nx, int32_t ny, int32_t bsx, int
   }
   int dev = 0;
   GPL_CUDA(cudaGetDevice(&dev));
+  GPL_CUDA(cudaSetDevice(dev));         // initialises the device's context if needed
+  const unsigned long long ctx = current_context_id();
   cudaStream_t s = (cudaStream_t)stream;
   SolveCache* c = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_cache_mu);
+    // entries of a context that no longer exists (cudaDeviceReset) hold
+    // memory that went with it: forget them without freeing
+    for (auto& e : g_cache)
+      if (e && e->device == dev && e->ctx != ctx) e.reset();
+    g_cache.erase(std::remove(g_cache.begin(), g_cache.end(), nullptr), g_cache.end());
     for (auto& e : g_cache)
       if (e->device == dev && e->nx == nx && e->ny == ny && e->bsx == bsx && e->bsy == bsy) c = e.get();
     if (!c) {
       SolveCache e;
-      e.device = dev; e.nx = nx; e.ny = ny; e.bsx = bsx; e.bsy = bsy;
+      e.device = dev; e.ctx = ctx; e.nx = nx; e.ny = ny; e.bsx = bsx; e.bsy = bsy;
       const size_t nb = (size_t)nx * ny;
       size_t bytes = 3 * nb * 4 + (nx + ny) * 4 + (nx + ny) * 8 + (kFftMax / 2) * 8 + 8 * 256;
       GPL_CUDA(cudaMalloc(&e.mem, bytes));

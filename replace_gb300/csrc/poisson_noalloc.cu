@@ -14,7 +14,9 @@
 // is only a stand-in symbol, not a device address), so the first call on each
 // device, with that device current, asks the runtime for the array's device
 // address (cudaGetSymbolAddress) and caches it.  That first call should come
-// before any stream capture.
+// before any stream capture.  The cached address belongs to the device's
+// context: after cudaDeviceReset the next call sees a new context and looks
+// the address up again (so that call, too, should precede any capture).
 //
 // Sharing: every call uses the same array and leaves its contents behind.
 // Nothing in it needs to start at zero: each call rewrites the tables and all
@@ -46,6 +48,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 std::mutex g_mu;
 void* g_addr[64] = {nullptr};
+unsigned long long g_ctx[64] = {0};    // context each cached address belongs to
 
 // Tables of FFT::init (src/fft.cpp:78-90) and of the transforms, written into
 // the scratch array for this call's grid.
@@ -99,10 +102,12 @@ extern "C" gpl_status gpl_poisson_solve_noalloc(int32_t nx, int32_t ny, int32_t 
   int dev = 0;
   GPL_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return GPL_ERR_INVALID_ARG; }
+  GPL_CUDA(cudaSetDevice(dev));         // initialises the device's context if needed
+  const unsigned long long ctx = current_context_id();
   unsigned char* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    if (!g_addr[dev] || g_ctx[dev] != ctx) {
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) {
@@ -111,6 +116,7 @@ extern "C" gpl_status gpl_poisson_solve_noalloc(int32_t nx, int32_t ny, int32_t 
         return GPL_ERR_CUDA;
       }
       g_addr[dev] = p;
+      g_ctx[dev] = ctx;
     }
     base = static_cast<unsigned char*>(g_addr[dev]);
   }

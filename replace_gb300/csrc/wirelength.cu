@@ -384,11 +384,13 @@ __device__ __forceinline__ long long wa_huge(const WaArgs& A, const WaEval<kW>& 
 // not lower the occupancy of the common case.
 constexpr int kWaSplit = 6;
 
-// The common-net variant is held to 32 registers (seven resident blocks of
-// 256 threads per SM instead of six: 71.1 -> 65.4 us at a million cells);
-// the large-net variant keeps its registers.
+// The unweighted common-net variant is held to 32 registers (seven resident
+// blocks of 256 threads per SM instead of six: 71.1 -> 65.4 us at a million
+// cells); at 32 registers the weighted one spills (4 bytes), so it keeps six
+// blocks per SM (40 registers, no spill); the large-net variants keep their
+// registers.
 template <bool kLarge, bool kW>
-__global__ void __launch_bounds__(kBlock, kLarge ? 1 : 7) k_wa(const __grid_constant__ WaArgs A) {
+__global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7)) k_wa(const __grid_constant__ WaArgs A) {
   WaEval<kW> V;
   {
     const EvalCtl* C = A.ctl;
