@@ -240,6 +240,26 @@ gpl_status gpl_nesterov_init(struct gpl_job* job, gpl_job_info* info);
 gpl_status gpl_nesterov_run(struct gpl_job* job, int32_t max_iters,
                             gpl_nesterov_stats* stats, gpl_iter_log* log);
 
+/* Batched form of gpl_nesterov_run: the Nesterov loops of n_jobs jobs run
+ * together (no counterpart in the reference, which places one design per
+ * process).  Every round, each running job's next evaluation -- its next
+ * back-tracking try or the first try of its next iteration -- joins one
+ * persistent launch per phase (scatter, WA, the three Poisson passes, the
+ * gcell gradients) driven by a table of work items (job, block of that job's
+ * own launch); each job's control then takes its result as gpl_nesterov_run
+ * would, and a job leaves the table when its loop ends.  The rounds replay
+ * one CUDA graph.  Every job's iterations, log and result are bit-identical
+ * to gpl_nesterov_run on that job alone.
+ * The jobs: distinct, on one device, after gpl_nesterov_init, on the FFT
+ * Poisson form with its shared-memory passes (poisson_path 1, a grid other
+ * than 512 x 512 or 1024 x 1024; others return GPL_ERR_INVALID_ARG).
+ * max_iters: further iterations per job (<= 0: to the stop rule).  stats and
+ * status are [n_jobs] (may be NULL): each job's progress and its
+ * gpl_nesterov_run status; *kernel_launches (may be NULL): kernels
+ * launched.  The call itself returns GPL_OK unless it could not run. */
+gpl_status gpl_batch_nesterov_run(struct gpl_job* const* jobs, int32_t n_jobs, int32_t max_iters,
+                                  gpl_nesterov_stats* stats, gpl_status* status, int64_t* kernel_launches);
+
 /* Per-net weights: the hook of GNet::setCustomWeight / GNet::netWeight
  * (src/nesterovBase.h:210-212, src/nesterovBase.cpp:264-266).  The reference
  * stores the weights but does not apply them yet; here each pin's WA gradient

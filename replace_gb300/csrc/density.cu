@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "device_common.cuh"
 
@@ -165,14 +166,15 @@ struct TileArgs {
 // Per (gcell, bin) the area is (int64)(float overlap * scale [* td for a
 // macro]), added into the inst or filler set.  The predictor runs here for
 // every gcell (big ones included; their bins are left to k_scatter_big).
-__global__ void __launch_bounds__(kBlock, 5) k_scatter(ScatterArgs A, TileArgs T) {
-  extern __shared__ unsigned win[];                // [2][wy][wx] low 16-bit sums, then high 16-bit sums
-  if ((int)blockIdx.x >= *T.n_chunks) return;      // block-uniform
+// The body of one block (chunk vb); `win` is the block's dynamic shared
+// window.  Shared by the per-job launch and the batched one.
+__device__ __forceinline__ void scatter_body(const ScatterArgs& A, const TileArgs& T, int vb, unsigned* win) {
+  if (vb >= *T.n_chunks) return;                   // block-uniform
   const EvalCtl C = *A.ctl;
   unsigned long long* area = pick2(A.area, C.area_cur);
   const BinGeom& G = A.geo;
   const int nb = G.cnt_x * G.cnt_y;
-  const int4 ch = T.chunks[blockIdx.x];
+  const int4 ch = T.chunks[vb];
   const int ox = (ch.x % T.tiles_x) * T.tile_w - kTileMargin;
   const int oy = (ch.x / T.tiles_x) * T.tile_h - kTileMargin;
   const int wx = T.tile_w + 2 * kTileMargin, wy = T.tile_h + 2 * kTileMargin, wn = wx * wy;
@@ -221,11 +223,16 @@ __global__ void __launch_bounds__(kBlock, 5) k_scatter(ScatterArgs A, TileArgs T
   }
 }
 
+__global__ void __launch_bounds__(kBlock, 5) k_scatter(ScatterArgs A, TileArgs T) {
+  extern __shared__ unsigned win[];                // [2][wy][wx] low 16-bit sums, then high 16-bit sums
+  scatter_body(A, T, (int)blockIdx.x, win);
+}
+
 // One block per big cell (macros): threads stride over its bins.
-__global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int32_t* big, int n_big) {
+__device__ __forceinline__ void scatter_big_body(const ScatterArgs& A, const int32_t* big, int vb) {
   const EvalCtl C = *A.ctl;
   unsigned long long* area = pick2(A.area, C.area_cur);
-  const int g = big[blockIdx.x];
+  const int g = big[vb];
   const BinGeom& G = A.geo;
   const int nb = G.cnt_x * G.cnt_y;
   const int2 h = A.half[g];
@@ -254,6 +261,10 @@ __global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int
     const long long v = (long long)trunc_u64(f);
     if (v) atomicAdd(&area[((k & 3) == 2 ? nb : 0) + cc * G.cnt_x + a], (unsigned long long)v);
   }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter_big(ScatterArgs A, const int32_t* big, int n_big) {
+  scatter_big_body(A, big, (int)blockIdx.x);
 }
 
 struct CellArgs {
@@ -285,9 +296,9 @@ struct CellArgs {
 };
 
 // Density gradient of one big cell, reduced over a block (fixed tree order).
-__global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t* big, int n_big) {
+__device__ __forceinline__ void dgrad_big_body(const CellArgs& A, const int32_t* big, int vb) {
   __shared__ float sx[kBlock], sy[kBlock];
-  const int g = big[blockIdx.x];
+  const int g = big[vb];
   const BinGeom& G = A.geo;
   const EvalCtl C = *A.ctl;
   int lx, ux, ly, uy, x0, x1, y0, y1;
@@ -309,14 +320,19 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t*
     if (threadIdx.x < s) { sx[threadIdx.x] += sx[threadIdx.x + s]; sy[threadIdx.x] += sy[threadIdx.x + s]; }
     __syncthreads();
   }
-  if (threadIdx.x == 0) A.d_big[blockIdx.x] = make_float2(sx[0], sy[0]);
+  if (threadIdx.x == 0) A.d_big[vb] = make_float2(sx[0], sy[0]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_dgrad_big(CellArgs A, const int32_t* big, int n_big) {
+  dgrad_big_body(A, big, (int)blockIdx.x);
 }
 
 // One gcell per thread, grid-stride over a grid sized to the SM count; the
 // block partial sums are reduced by the last block to finish (threadfence +
 // counter), in a fixed order, so there is no separate reduction launch and
 // the result is the same run to run.
-__global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
+// Block vb of a launch of vgrid blocks.
+__device__ __forceinline__ void cell_body(const CellArgs& A, int vb, int vgrid) {
   __shared__ double sh[32 * kPartSlots];
   __shared__ bool last;
   // per-thread sums in float over the thread's few gcells; FP64 from the
@@ -347,7 +363,7 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
   // warp-uniform grid-stride loop: the warps gather the pins of cells with
   // more than 32 pins (macros) together
 #pragma unroll 2
-  for (int base = blockIdx.x * kBlock + (threadIdx.x & ~31); base < A.n_g; base += gridDim.x * kBlock) {
+  for (int base = vb * kBlock + (threadIdx.x & ~31); base < A.n_g; base += vgrid * kBlock) {
     const int g = base + lane;
     const bool valid = g < A.n_g;
     int ps = 0, pe = 0;
@@ -445,13 +461,13 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
     if (threadIdx.x < 5) {
       double t = 0.0;
       for (int w8 = 0; w8 < nw; w8++) t += sh[threadIdx.x * 32 + w8];
-      A.part[(size_t)(kPartWl + threadIdx.x) * A.stride + blockIdx.x] = t;
+      A.part[(size_t)(kPartWl + threadIdx.x) * A.stride + vb] = t;
     }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     __threadfence();
-    last = atomicAdd(&A.counters[0], 1u) == gridDim.x - 1;
+    last = atomicAdd(&A.counters[0], 1u) == (unsigned)vgrid - 1;
   }
   __syncthreads();
   if (!last) return;
@@ -460,12 +476,12 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
   double tot[kPartSlots];
 #pragma unroll
   for (int slot = 0; slot < kPartSlots; slot++) tot[slot] = 0.0;
-  const int n_max = max(max((int)gridDim.x, A.n_ovf_blocks), A.n_phi_blocks);
+  const int n_max = max(max(vgrid, A.n_ovf_blocks), A.n_phi_blocks);
   for (int i = threadIdx.x; i < n_max; i += blockDim.x) {
 #pragma unroll
     for (int slot = 0; slot < kPartSlots; slot++) {
       const int n = slot == kPartOverflow ? A.n_ovf_blocks
-                                          : (slot == kPartPhi ? A.n_phi_blocks : (int)gridDim.x);
+                                          : (slot == kPartPhi ? A.n_phi_blocks : vgrid);
       if (i < n) tot[slot] += __ldcg(A.part + (size_t)slot * A.stride + i);
     }
   }
@@ -501,6 +517,10 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
   }
 }
 
+__global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell(CellArgs A) {
+  cell_body(A, (int)blockIdx.x, (int)gridDim.x);
+}
+
 // sum over bins of phi * (nonPlace + inst + filler) in FP64
 // (NesterovBase::updateDensityForceBin, src/nesterovBase.cpp:1494-1505)
 __global__ void __launch_bounds__(kBlock) k_sum_phi(const float* phi, const unsigned long long* area,
@@ -523,7 +543,8 @@ BinGeom geom(const DeviceModel& d) {
 
 int cell_blocks(const DeviceModel& d) { return (d.n_g + kBlock - 1) / kBlock; }
 
-int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+namespace {
+ScatterArgs scatter_args(const DeviceModel& d) {
   ScatterArgs A;
   A.geo = geom(d);
   A.n_g = d.n_g;
@@ -533,10 +554,47 @@ int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) 
   A.coordi[0] = d.coordi[0]; A.coordi[1] = d.coordi[1];
   A.area[0] = d.area[0]; A.area[1] = d.area[1];
   A.ctl = d.ctl;
-  (void)a;
+  return A;
+}
+
+TileArgs tile_args(const DeviceModel& d) {
   TileArgs T;
   T.tile_w = d.tile_w; T.tile_h = d.tile_h; T.tiles_x = d.tiles_x;
   T.order = d.order; T.chunks = d.chunks; T.n_chunks = d.n_chunks;
+  return T;
+}
+
+CellArgs cell_args(const DeviceModel& d, const EvalArgs& a, int n_phi_blocks) {
+  CellArgs A;
+  A.geo = geom(d);
+  A.n_g = d.n_g;
+  A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
+  for (int k = 0; k < 4; k++) { A.slp[k] = d.slp[k]; A.sum[k] = d.sum[k]; }
+  A.ctl = d.ctl;
+  A.field = d.field;
+  A.g_pin_start = d.g_pin_start;
+  A.g_pins = d.g_pins;
+  A.pin_grad = d.pin_grad;
+  A.precond = d.g_precond;
+  A.big_idx = d.g_big_idx; A.d_big = d.d_big;
+  A.min_precond = a.min_precond;
+  A.wl_out = d.wl_out; A.d_out = d.d_out;
+  A.part = d.part;
+  A.stride = d.part_stride;
+  A.n_ovf_blocks = poisson_blocks_a(d.cnt_x, d.cnt_y);
+  A.n_phi_blocks = n_phi_blocks;
+  A.counters = d.counters;
+  A.hpwl_total = d.hpwl_total;
+  A.part_total = d.part_total;
+  A.out = d.result;
+  return A;
+}
+}  // namespace
+
+int launch_scatter(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+  const ScatterArgs A = scatter_args(d);
+  const TileArgs T = tile_args(d);
+  (void)a;
   t.begin(kKScatter);
   k_scatter<<<d.max_chunks, kBlock, scatter_smem(d), s>>>(A, T);
   if (d.n_big) k_scatter_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
@@ -612,28 +670,7 @@ int launch_tile_order(DeviceModel& d, int slot, cudaStream_t s, Timer& t) {
 int cell_grid(const DeviceModel& d) { return std::max(1, std::min(cell_blocks(d), d.sm_count * kCellBlocksPerSm)); }
 
 int launch_cell(DeviceModel& d, const EvalArgs& a, int n_phi_blocks, cudaStream_t s, Timer& t) {
-  CellArgs A;
-  A.geo = geom(d);
-  A.n_g = d.n_g;
-  A.half = d.g_half; A.scale = d.g_scale; A.kind = d.g_kind;
-  for (int k = 0; k < 4; k++) { A.slp[k] = d.slp[k]; A.sum[k] = d.sum[k]; }
-  A.ctl = d.ctl;
-  A.field = d.field;
-  A.g_pin_start = d.g_pin_start;
-  A.g_pins = d.g_pins;
-  A.pin_grad = d.pin_grad;
-  A.precond = d.g_precond;
-  A.big_idx = d.g_big_idx; A.d_big = d.d_big;
-  A.min_precond = a.min_precond;
-  A.wl_out = d.wl_out; A.d_out = d.d_out;
-  A.part = d.part;
-  A.stride = d.part_stride;
-  A.n_ovf_blocks = poisson_blocks_a(d.cnt_x, d.cnt_y);
-  A.n_phi_blocks = n_phi_blocks;
-  A.counters = d.counters;
-  A.hpwl_total = d.hpwl_total;
-  A.part_total = d.part_total;
-  A.out = d.result;
+  const CellArgs A = cell_args(d, a, n_phi_blocks);
   t.begin(kKCell);
   if (d.n_big) k_dgrad_big<<<d.n_big, kBlock, 0, s>>>(A, d.big_cells, d.n_big);
   k_cell<<<cell_grid(d), kBlock, 0, s>>>(A);
@@ -679,6 +716,120 @@ int launch_sum_phi(DeviceModel& d, int area_set, cudaStream_t s, Timer& t, int* 
   t.count(1);
   GPL_CUDA(cudaGetLastError());
   *n_blocks = blocks;
+  return GPL_OK;
+}
+
+// ------------------------------------------------------------ batched form
+// Many jobs' evaluations in one launch per phase: a persistent grid whose
+// blocks take work items (instance, block of that instance's own launch,
+// that launch's grid) from a table and run the same block body as the
+// per-job kernels, on the instance's arguments (kept in device memory).  A
+// job's blocks therefore compute exactly what its own launch computes.
+namespace {
+
+struct ScatterBatchArgs {
+  ScatterArgs A;
+  TileArgs T;
+  const int32_t* big;
+};
+
+struct CellBatchArgs {
+  CellArgs A;
+  const int32_t* big;
+};
+
+__global__ void __launch_bounds__(kBlock, 5) k_scatter_batch(const ScatterBatchArgs* args, const int4* items,
+                                                             const int* count) {
+  extern __shared__ unsigned win[];
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    const ScatterBatchArgs& a = args[it.x];
+    scatter_body(a.A, a.T, it.y, win);
+    __syncthreads();                  // the window is the next item's
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scatter_big_batch(const ScatterBatchArgs* args, const int4* items,
+                                                              const int* count) {
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    scatter_big_body(args[it.x].A, args[it.x].big, it.y);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_dgrad_big_batch(const CellBatchArgs* args, const int4* items,
+                                                            const int* count) {
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    dgrad_big_body(args[it.x].A, args[it.x].big, it.y);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell_batch(const CellBatchArgs* args,
+                                                                         const int4* items, const int* count) {
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    cell_body(args[it.x].A, it.y, it.z);
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+size_t scatter_batch_args_bytes() { return (sizeof(ScatterBatchArgs) + 15) / 16 * 16; }
+size_t cell_batch_args_bytes() { return (sizeof(CellBatchArgs) + 15) / 16 * 16; }
+
+void write_scatter_batch_args(const DeviceModel& d, void* dst) {
+  ScatterBatchArgs x;
+  x.A = scatter_args(d);
+  x.T = tile_args(d);
+  x.big = d.big_cells;
+  memcpy(dst, &x, sizeof(x));
+}
+
+void write_cell_batch_args(const DeviceModel& d, const EvalArgs& a, void* dst) {
+  CellBatchArgs x;
+  x.A = cell_args(d, a, 0);
+  x.big = d.big_cells;
+  memcpy(dst, &x, sizeof(x));
+}
+
+int scatter_batch_prepare_device() {
+  static int done = 0;
+  if (done) return GPL_OK;
+  const int side = kTileSides[sizeof(kTileSides) / sizeof(kTileSides[0]) - 1];
+  const int smem = 4 * (side + 2 * kTileMargin) * (side + 2 * kTileMargin) * 4;
+  GPL_CUDA(cudaFuncSetAttribute(k_scatter_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  done = 1;
+  return GPL_OK;
+}
+
+int launch_density_batch(int phase, const void* args, const int4* items, const int* count, int grid,
+                         size_t smem, cudaStream_t s) {
+  switch (phase) {
+    case kBScatter:
+      k_scatter_batch<<<grid, kBlock, smem, s>>>(static_cast<const ScatterBatchArgs*>(args), items, count);
+      break;
+    case kBScatterBig:
+      k_scatter_big_batch<<<grid, kBlock, 0, s>>>(static_cast<const ScatterBatchArgs*>(args), items, count);
+      break;
+    case kBDgradBig:
+      k_dgrad_big_batch<<<grid, kBlock, 0, s>>>(static_cast<const CellBatchArgs*>(args), items, count);
+      break;
+    case kBCell:
+      k_cell_batch<<<grid, kBlock, 0, s>>>(static_cast<const CellBatchArgs*>(args), items, count);
+      break;
+    default:
+      set_error("launch_density_batch: unknown phase");
+      return GPL_ERR_INVALID_ARG;
+  }
+  GPL_CUDA(cudaGetLastError());
   return GPL_OK;
 }
 

@@ -412,6 +412,37 @@ int job_device_bytes(gpl_job* j, int64_t* bytes, bool centred);
 // twiddle / frequency tables (host computed, double precision)
 void make_twiddle(std::vector<float2>& tw);
 
+// ------------------------------------------------------------ batched form
+// Phases of one evaluation run for many jobs at once (batch.cu): each is one
+// persistent launch over a table of work items int4 (instance, block of the
+// instance's own launch, that launch's grid, 0).
+enum BatchPhase {
+  kBScatter = 0, kBScatterBig, kBWaSmall, kBWaLarge, kBWaSmallW, kBWaLargeW,
+  kBPoissonA, kBPoissonB, kBPoissonC, kBDgradBig, kBCell, kBPhases
+};
+size_t scatter_batch_args_bytes();
+size_t cell_batch_args_bytes();
+size_t wa_batch_args_bytes();
+// blocks of a job's small-net and large-net WA launches
+void wa_launch_blocks(const DeviceModel& d, int* small, int* large);
+size_t poisson_batch_args_bytes(int pass);     // pass 0, 1, 2 = A, B, C
+void write_scatter_batch_args(const DeviceModel& d, void* dst);
+void write_cell_batch_args(const DeviceModel& d, const EvalArgs& a, void* dst);
+void write_wa_batch_args(const DeviceModel& d, const EvalArgs& a, void* dst);
+// the block-form Poisson passes of a job's grid: arguments, grids and
+// dynamic shared memory of passes A, B, C; false for the warp form
+// (512 x 512 and 1024 x 1024 grids) and the tensor-core form
+bool write_poisson_batch_args(const DeviceModel& d, void* dst_a, void* dst_b, void* dst_c,
+                              int grid[3], size_t smem[3]);
+int scatter_batch_prepare_device();
+int poisson_batch_prepare_device();
+int launch_density_batch(int phase, const void* args, const int4* items, const int* count, int grid,
+                         size_t smem, cudaStream_t s);
+int launch_wa_batch(bool large, bool weighted, const void* args, const int4* items, const int* count, int grid,
+                    cudaStream_t s);
+int launch_poisson_batch(int pass, const void* args, const int4* items, const int* count, int grid,
+                         size_t smem, cudaStream_t s);
+
 // Unique id of the calling thread's current CUDA context (cuCtxGetId through
 // the runtime's driver entry points; 0 when it cannot be read).  Caches of
 // device addresses are keyed on it: after cudaDeviceReset the device gets a

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -1047,6 +1048,8 @@ int run_host_loop(gpl_job* j, int max_iters, gpl_iter_log* log) {
   return GPL_OK;
 }
 
+int end_of_run(gpl_job* j);
+
 // NesterovPlace::doNesterovPlace (src/nesterovPlace.cpp:275-472), resumable:
 // the device loop when the job has one (no kernel timing), else the host loop.
 int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
@@ -1063,6 +1066,13 @@ int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
       fflush(stdout);
     }
   }
+  return end_of_run(j);
+}
+
+// After a chunk of iterations: the stop on the iteration limit, the
+// divergence message, and the tensor-core form's time-out flag.
+int end_of_run(gpl_job* j) {
+  NesterovState& S = j->S;
   if (S.iter >= S.max_iter) S.finished = 1;
   switch (S.diverge_code) {
     case GPL_ERR_DIVERGED_BACKTRACK: set_error("RePlAce divergence detected. Please decrease init_density_penalty value"); break;
@@ -1080,6 +1090,331 @@ int nesterov_run(gpl_job* j, int max_iters, gpl_iter_log* log) {
     }
   }
   return S.diverge_code;
+}
+
+// ------------------------------------------------------------ batched form
+// The Nesterov loops of many jobs in lockstep: every round, each running
+// job's next evaluation (its next back-tracking try, or the first try of its
+// next iteration) goes into one launch per phase (batched kernels of
+// density.cu, wirelength.cu, poisson.cu) driven by a table of work items
+// (instance, block of the instance's own launch); then each job's control
+// (control.h) processes its result exactly as the host loop does.  A job's
+// blocks compute what its own launches compute, in the same blocks, so its
+// iterates, log and result are bit-identical to running it alone.  Jobs
+// leave the table when their loop ends; the round's launches are captured
+// once as a CUDA graph (persistent grids, tables in device memory).
+struct BatchRun {
+  int n = 0, device = 0;
+  cudaStream_t s = nullptr;
+  char* dev = nullptr;                 // argument tables, control and result records, items
+  char* host = nullptr;                // pinned: control and result records, items, counts
+  size_t dev_bytes = 0, host_bytes = 0;
+  char* args[6] = {nullptr};           // scatter, wa, poisson A, B, C, cell
+  size_t stride[6] = {0};
+  EvalCtl* ctl_d = nullptr;
+  EvalResult* res_d = nullptr;
+  int4* items_d = nullptr;
+  int* counts_d = nullptr;
+  EvalCtl* ctl_h = nullptr;
+  EvalResult* res_h = nullptr;
+  int4* items_h = nullptr;
+  int* counts_h = nullptr;
+  int item_off[kBPhases] = {0}, item_cap[kBPhases] = {0};
+  int grid[kBPhases] = {0};
+  size_t smem_scatter = 0, smem_p[3] = {0, 0, 0};
+  std::vector<std::array<int, kBPhases>> vgrid;
+  cudaGraphExec_t exec = nullptr;
+  long long launches_per_round = 0;
+  ~BatchRun() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (s) cudaStreamSynchronize(s);
+    if (dev) cudaFree(dev);
+    if (host) cudaFreeHost(host);
+    if (s) cudaStreamDestroy(s);
+  }
+};
+
+enum BatchTable { kTScatter = 0, kTWa, kTPa, kTPb, kTPc, kTCell };
+
+// Argument tables, persistent grids and item capacities of a batch.
+int batch_setup(BatchRun& B, const std::vector<gpl_job*>& jobs) {
+  const int n = (int)jobs.size();
+  B.n = n;
+  B.device = jobs[0]->device;
+  GPL_CUDA(cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking));
+  int rc = scatter_prepare_device();
+  if (!rc) rc = scatter_batch_prepare_device();
+  if (!rc) rc = poisson_prepare_device();
+  if (!rc) rc = poisson_batch_prepare_device();
+  if (rc) return rc;
+  B.stride[kTScatter] = scatter_batch_args_bytes();
+  B.stride[kTWa] = wa_batch_args_bytes();
+  B.stride[kTPa] = poisson_batch_args_bytes(0);
+  B.stride[kTPb] = poisson_batch_args_bytes(1);
+  B.stride[kTPc] = poisson_batch_args_bytes(2);
+  B.stride[kTCell] = cell_batch_args_bytes();
+  B.vgrid.assign(n, {});
+  for (int k = 0; k < n; k++) {
+    const DeviceModel& d = jobs[k]->d;
+    std::array<int, kBPhases>& v = B.vgrid[k];
+    v.fill(0);
+    v[kBScatter] = d.max_chunks;
+    v[kBScatterBig] = d.n_big;
+    v[kBDgradBig] = d.n_big;
+    v[kBCell] = cell_grid(d);
+    int small = 0, large = 0;
+    wa_launch_blocks(d, &small, &large);
+    v[d.net_weighted ? kBWaSmallW : kBWaSmall] = small;
+    v[d.net_weighted ? kBWaLargeW : kBWaLarge] = large;
+    B.smem_scatter = std::max(B.smem_scatter, scatter_smem(d));
+  }
+  // one device block: tables, records, items, counts (256-byte aligned parts)
+  size_t off = 0;
+  auto take = [&](size_t b) { const size_t o = off; off += (b + 255) / 256 * 256; return o; };
+  size_t o_args[6];
+  for (int t = 0; t < 6; t++) o_args[t] = take(B.stride[t] * n);
+  const size_t o_ctl = take(sizeof(EvalCtl) * n), o_res = take(sizeof(EvalResult) * n);
+  int total = 0;
+  for (int p = 0; p < kBPhases; p++) {
+    B.item_off[p] = total;
+    int cap = 0;
+    for (int k = 0; k < n; k++) cap += B.vgrid[k][p];
+    // Poisson items are known once the per-job grids are (below)
+    B.item_cap[p] = cap;
+    total += cap;
+  }
+  // Poisson passes: the grids of each job's block form
+  std::vector<char> pa(B.stride[kTPa] * n), pb(B.stride[kTPb] * n), pc(B.stride[kTPc] * n);
+  for (int k = 0; k < n; k++) {
+    int g3[3];
+    size_t sm3[3];
+    if (!write_poisson_batch_args(jobs[k]->d, pa.data() + k * B.stride[kTPa], pb.data() + k * B.stride[kTPb],
+                                  pc.data() + k * B.stride[kTPc], g3, sm3)) {
+      set_error("batched Nesterov loop: job " + std::to_string(k) +
+                " does not run the block-form FFT Poisson passes (its grid is 512 x 512 or 1024 x 1024, "
+                "or it runs the tensor-core form); run it alone");
+      return GPL_ERR_INVALID_ARG;
+    }
+    for (int q = 0; q < 3; q++) {
+      B.vgrid[k][kBPoissonA + q] = g3[q];
+      B.smem_p[q] = std::max(B.smem_p[q], sm3[q]);
+    }
+  }
+  total = 0;
+  for (int p = 0; p < kBPhases; p++) {
+    int cap = 0;
+    for (int k = 0; k < n; k++) cap += B.vgrid[k][p];
+    B.item_off[p] = total;
+    B.item_cap[p] = cap;
+    total += cap;
+  }
+  const size_t o_items = take(sizeof(int4) * std::max(total, 1)), o_counts = take(sizeof(int) * kBPhases);
+  B.dev_bytes = off;
+  GPL_CUDA(cudaMalloc(&B.dev, B.dev_bytes));
+  for (int t = 0; t < 6; t++) B.args[t] = B.dev + o_args[t];
+  B.ctl_d = reinterpret_cast<EvalCtl*>(B.dev + o_ctl);
+  B.res_d = reinterpret_cast<EvalResult*>(B.dev + o_res);
+  B.items_d = reinterpret_cast<int4*>(B.dev + o_items);
+  B.counts_d = reinterpret_cast<int*>(B.dev + o_counts);
+  // pinned: records, items, counts
+  size_t hoff = 0;
+  auto htake = [&](size_t b) { const size_t o = hoff; hoff += (b + 255) / 256 * 256; return o; };
+  const size_t h_ctl = htake(sizeof(EvalCtl) * n), h_res = htake(sizeof(EvalResult) * n);
+  const size_t h_items = htake(sizeof(int4) * std::max(total, 1)), h_counts = htake(sizeof(int) * kBPhases);
+  B.host_bytes = hoff;
+  GPL_CUDA(cudaMallocHost(&B.host, B.host_bytes));
+  memset(B.host, 0, B.host_bytes);
+  B.ctl_h = reinterpret_cast<EvalCtl*>(B.host + h_ctl);
+  B.res_h = reinterpret_cast<EvalResult*>(B.host + h_res);
+  B.items_h = reinterpret_cast<int4*>(B.host + h_items);
+  B.counts_h = reinterpret_cast<int*>(B.host + h_counts);
+  // the tables: each job's arguments with its control and result records
+  // redirected to the batch's slots
+  std::vector<char> ts(B.stride[kTScatter] * n), tw(B.stride[kTWa] * n), tc(B.stride[kTCell] * n);
+  for (int k = 0; k < n; k++) {
+    DeviceModel& d = jobs[k]->d;
+    EvalCtl* own_ctl = d.ctl;
+    EvalResult* own_res = d.result;
+    d.ctl = B.ctl_d + k;
+    d.result = B.res_d + k;
+    write_scatter_batch_args(d, ts.data() + k * B.stride[kTScatter]);
+    write_wa_batch_args(d, base_args(jobs[k]), tw.data() + k * B.stride[kTWa]);
+    write_cell_batch_args(d, base_args(jobs[k]), tc.data() + k * B.stride[kTCell]);
+    int g3[3];
+    size_t sm3[3];
+    write_poisson_batch_args(d, pa.data() + k * B.stride[kTPa], pb.data() + k * B.stride[kTPb],
+                             pc.data() + k * B.stride[kTPc], g3, sm3);
+    d.ctl = own_ctl;
+    d.result = own_res;
+  }
+  GPL_CUDA(cudaMemcpyAsync(B.args[kTScatter], ts.data(), ts.size(), cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.args[kTWa], tw.data(), tw.size(), cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.args[kTPa], pa.data(), pa.size(), cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.args[kTPb], pb.data(), pb.size(), cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.args[kTPc], pc.data(), pc.size(), cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.args[kTCell], tc.data(), tc.size(), cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaStreamSynchronize(B.s));
+  // persistent grids: about the per-job kernels' residency per SM
+  const int sms = std::max(1, jobs[0]->d.sm_count);
+  const int per_sm[kBPhases] = {4, 4, 7, 1, 6, 1, 4, 4, 4, 4, 6};
+  for (int p = 0; p < kBPhases; p++) B.grid[p] = std::min(B.item_cap[p], sms * per_sm[p]);
+  return GPL_OK;
+}
+
+// Work items of the running jobs (`on`): instance k's blocks of each phase.
+int batch_items(BatchRun& B, const std::vector<char>& on) {
+  for (int p = 0; p < kBPhases; p++) {
+    int c = 0;
+    int4* dst = B.items_h + B.item_off[p];
+    for (int k = 0; k < B.n; k++) {
+      if (!on[k]) continue;
+      const int vg = B.vgrid[k][p];
+      for (int vb = 0; vb < vg; vb++) dst[c++] = make_int4(k, vb, vg, 0);
+    }
+    B.counts_h[p] = c;
+  }
+  int total = 0;
+  for (int p = 0; p < kBPhases; p++) total += B.item_cap[p];
+  if (total) GPL_CUDA(cudaMemcpyAsync(B.items_d, B.items_h, sizeof(int4) * total, cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.counts_d, B.counts_h, sizeof(int) * kBPhases, cudaMemcpyHostToDevice, B.s));
+  return GPL_OK;
+}
+
+// One round: control records up, every phase, result records down.
+int batch_launch_round(BatchRun& B) {
+  long long nl = 0;
+  GPL_CUDA(cudaMemcpyAsync(B.ctl_d, B.ctl_h, sizeof(EvalCtl) * B.n, cudaMemcpyHostToDevice, B.s));
+  auto items = [&](int p) { return B.items_d + B.item_off[p]; };
+  auto count = [&](int p) { return B.counts_d + p; };
+  int rc = GPL_OK;
+  if (B.grid[kBScatter]) {
+    rc = launch_density_batch(kBScatter, B.args[kTScatter], items(kBScatter), count(kBScatter), B.grid[kBScatter],
+                              B.smem_scatter, B.s);
+    nl++;
+  }
+  if (!rc && B.grid[kBScatterBig]) {
+    rc = launch_density_batch(kBScatterBig, B.args[kTScatter], items(kBScatterBig), count(kBScatterBig),
+                              B.grid[kBScatterBig], 0, B.s);
+    nl++;
+  }
+  const int wa_phase[4] = {kBWaSmall, kBWaLarge, kBWaSmallW, kBWaLargeW};
+  for (int q = 0; q < 4 && !rc; q++) {
+    const int p = wa_phase[q];
+    if (!B.grid[p]) continue;
+    rc = launch_wa_batch(q & 1, q >= 2, B.args[kTWa], items(p), count(p), B.grid[p], B.s);
+    nl++;
+  }
+  for (int q = 0; q < 3 && !rc; q++) {
+    const int p = kBPoissonA + q;
+    if (!B.grid[p]) continue;
+    rc = launch_poisson_batch(q, B.args[kTPa + q], items(p), count(p), B.grid[p], B.smem_p[q], B.s);
+    nl++;
+  }
+  if (!rc && B.grid[kBDgradBig]) {
+    rc = launch_density_batch(kBDgradBig, B.args[kTCell], items(kBDgradBig), count(kBDgradBig), B.grid[kBDgradBig],
+                              0, B.s);
+    nl++;
+  }
+  if (!rc && B.grid[kBCell]) {
+    rc = launch_density_batch(kBCell, B.args[kTCell], items(kBCell), count(kBCell), B.grid[kBCell], 0, B.s);
+    nl++;
+  }
+  if (rc) return rc;
+  GPL_CUDA(cudaMemcpyAsync(B.res_h, B.res_d, sizeof(EvalResult) * B.n, cudaMemcpyDeviceToHost, B.s));
+  B.launches_per_round = nl;
+  return GPL_OK;
+}
+
+// The round as one CUDA graph (a failure leaves direct launches).
+void batch_capture(BatchRun& B) {
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(B.s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  const int rc = batch_launch_round(B);
+  const cudaError_t e = cudaStreamEndCapture(B.s, &g);
+  if (!rc && e == cudaSuccess && g) {
+    if (cudaGraphInstantiate(&B.exec, g, 0) != cudaSuccess) B.exec = nullptr;
+  }
+  if (g) cudaGraphDestroy(g);
+  cudaGetLastError();
+}
+
+int batch_run(const std::vector<gpl_job*>& jobs, int max_iters, gpl_iter_log* const* logs,
+              long long* launches) {
+  const int n = (int)jobs.size();
+  BatchRun B;
+  int rc = batch_setup(B, jobs);
+  if (rc) return rc;
+  // the jobs' own streams may still hold work (initialisation)
+  for (gpl_job* j : jobs) GPL_CUDA(cudaStreamSynchronize(j->stream));
+  std::vector<char> on(n, 0), start(n, 1);
+  std::vector<int> done(n, 0);
+  for (int k = 0; k < n; k++) {
+    const NesterovState& S = jobs[k]->S;
+    on[k] = !S.finished && S.iter < S.max_iter && S.diverge_code != GPL_ERR_DIVERGED_INIT;
+  }
+  rc = batch_items(B, on);
+  if (rc) return rc;
+  batch_capture(B);
+  long long nl = 0;
+  for (;;) {
+    int running = 0;
+    for (int k = 0; k < n; k++) running += on[k] ? 1 : 0;
+    if (!running) break;
+    for (int k = 0; k < n; k++) {
+      if (!on[k]) continue;
+      gpl_job* j = jobs[k];
+      NesterovState& S = j->S;
+      if (start[k]) {
+        start_iteration(S);
+        if (S.iter % kTileOrderEvery == 0) {
+          rc = launch_tile_order(j->d, S.i_cur, B.s, j->timer);
+          if (rc) return rc;
+          S.refreshes++;
+          nl += 3;
+        }
+        start[k] = 0;
+      }
+      B.ctl_h[k] = next_ctl(S);
+    }
+    if (B.exec) {
+      GPL_CUDA(cudaGraphLaunch(B.exec, B.s));
+    } else {
+      rc = batch_launch_round(B);
+      if (rc) return rc;
+    }
+    nl += B.launches_per_round;
+    GPL_CUDA(cudaStreamSynchronize(B.s));
+    bool changed = false;
+    for (int k = 0; k < n; k++) {
+      if (!on[k]) continue;
+      gpl_job* j = jobs[k];
+      NesterovState& S = j->S;
+      IterEntry e;
+      bool logged = false;
+      const int a = after_eval(S, B.res_h[k], &e, &logged);
+      if (logged) record_iteration(j, e, S.iter, logs ? logs[k] : nullptr);
+      if (a == kRetry) continue;
+      start[k] = 1;
+      done[k]++;
+      if (S.finished || S.iter >= S.max_iter || (max_iters > 0 && done[k] >= max_iters)) {
+        on[k] = 0;
+        changed = true;
+        if (S.finished && !S.diverge_code && j->m.p.verbose_level > 0) {
+          printf("[NesterovSolve] Finished with Overflow: %g\n", S.sum_overflow);
+          fflush(stdout);
+        }
+      }
+    }
+    if (changed) {
+      rc = batch_items(B, on);
+      if (rc) return rc;
+    }
+  }
+  if (launches) *launches = nl;
+  return GPL_OK;
 }
 
 void fill_info(gpl_job* j, gpl_job_info* info) {
@@ -1313,6 +1648,45 @@ gpl_status gpl_nesterov_run(gpl_job* j, int32_t max_iters, gpl_nesterov_stats* s
     st->hpwl = j->S.prev_hpwl;
   }
   return (gpl_status)rc;
+}
+
+gpl_status gpl_batch_nesterov_run(gpl_job* const* jobs, int32_t n_jobs, int32_t max_iters,
+                                  gpl_nesterov_stats* stats, gpl_status* status, int64_t* kernel_launches) {
+  if (!jobs || n_jobs <= 0) { set_error("gpl_batch_nesterov_run: no jobs"); return GPL_ERR_INVALID_ARG; }
+  std::vector<gpl_job*> v(jobs, jobs + n_jobs);
+  for (int k = 0; k < n_jobs; k++) {
+    if (!v[k]) { set_error("gpl_batch_nesterov_run: null job"); return GPL_ERR_INVALID_ARG; }
+    if (!v[k]->np_ready) { set_error("gpl_batch_nesterov_run: call gpl_nesterov_init first"); return GPL_ERR_BAD_STATE; }
+    if (v[k]->device != v[0]->device) {
+      set_error("gpl_batch_nesterov_run: the jobs must be on one device");
+      return GPL_ERR_INVALID_ARG;
+    }
+    for (int q = 0; q < k; q++)
+      if (v[q] == v[k]) { set_error("gpl_batch_nesterov_run: a job is listed twice"); return GPL_ERR_INVALID_ARG; }
+  }
+  cudaSetDevice(v[0]->device);
+  long long nl = 0;
+  int rc = batch_run(v, max_iters, nullptr, &nl);
+  if (kernel_launches) *kernel_launches = nl;
+  if (rc) return (gpl_status)rc;
+  for (int k = 0; k < n_jobs; k++) {
+    gpl_job* j = v[k];
+    const int st = j->S.diverge_code == GPL_ERR_DIVERGED_INIT ? j->S.diverge_code : end_of_run(j);
+    if (status) status[k] = (gpl_status)st;
+    if (stats) {
+      gpl_nesterov_stats& o = stats[k];
+      o.iterations = j->S.iter;
+      o.evaluations = j->S.evals;
+      o.finished = j->S.finished ? 1 : 0;
+      o.status = j->S.diverge_code;
+      o.overflow = j->S.sum_overflow;
+      o.step_length = j->S.step_length;
+      o.density_penalty = j->S.density_penalty;
+      o.wire_length_coef = j->S.wl_coef_x;
+      o.hpwl = j->S.prev_hpwl;
+    }
+  }
+  return GPL_OK;
 }
 
 gpl_status gpl_get_inst_locations(gpl_job* j, int32_t* lx, int32_t* ly) {

@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <memory>
 #include <mutex>
 #include <vector>
@@ -175,8 +176,9 @@ struct PassAArgs {
   const float2* w4;                  // exp(-i pi k / 2nx), k < nx
 };
 
-__global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
-  extern __shared__ float2 smem[];
+// Block vb of pass A (smem: the block's dynamic shared memory); shared by the
+// per-job launch and the batched one, as are the bodies of passes B and C.
+__device__ __forceinline__ void poisson_a_body(const PassAArgs& A, int vb, float2* smem) {
   __shared__ double red[32];
   const int n = A.nx;
   const int rp_n = A.pairs_per_block;
@@ -196,7 +198,7 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
   if (A.density_in) {
     for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
       const int rp = idx / n, i = idx - rp * n;
-      const int r = blockIdx.x * rp_n + rp;
+      const int r = vb * rp_n + rp;
       float d0 = 0.0f, d1 = 0.0f;
       if (r < A.ny / 2) {
         d0 = A.density_in[(2 * r) * n + i];
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
 #pragma unroll 4
     for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
       const int rp = idx / n, i = idx - rp * n;
-      const int r = blockIdx.x * rp_n + rp;
+      const int r = vb * rp_n + rp;
       float dd[2] = {0.0f, 0.0f};
       if (r < A.ny / 2) {
         const int blx = A.core_lx + i * A.size_x;
@@ -246,14 +248,19 @@ __global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
   float2* res = block_fft(buf0, buf1, n, A.logn, rp_n, -1, tws);
   for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
     const int rp = idx / n, k = idx - rp * n;
-    const int r = blockIdx.x * rp_n + rp;
+    const int r = vb * rp_n + rp;
     if (r >= A.ny / 2) continue;
     const float2* z = res + rp * n;
     float2 c = dct2_post(z[k], z[(n - k) & (n - 1)], __ldg(&A.w4[k]));
     A.spec[(2 * r) * n + k] = c.x;
     A.spec[(2 * r + 1) * n + k] = c.y;
   }
-  if (A.part_overflow) block_reduce_add((double)ovf_f, &A.part_overflow[blockIdx.x], red);
+  if (A.part_overflow) block_reduce_add((double)ovf_f, &A.part_overflow[vb], red);
+}
+
+__global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
+  extern __shared__ float2 smem[];
+  poisson_a_body(A, (int)blockIdx.x, smem);
 }
 
 struct PassBArgs {
@@ -268,8 +275,7 @@ struct PassBArgs {
   float scale;                       // 4 / (nx ny)
 };
 
-__global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
-  extern __shared__ float2 smem[];
+__device__ __forceinline__ void poisson_b_body(const PassBArgs& B, int vb, float2* smem) {
   const int n = B.ny;
   const int cp = B.col_pairs;
   float2* s0 = smem;                 // [cp][n] work
@@ -277,7 +283,7 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
   float2* s2 = smem + 2 * cp * n;    // [cp][n] spectrum: (phi^ col u0, phi^ col u1)
   float2* tws = smem + 3 * cp * n;   // [n/2] twiddles
   load_twiddles(tws, B.tw, n);
-  const int u_base = blockIdx.x * 2 * cp;
+  const int u_base = vb * 2 * cp;
   // load: column pair q holds columns u_base + 2q, +1
 #pragma unroll 4
   for (int idx = threadIdx.x; idx < 2 * cp * n; idx += blockDim.x) {
@@ -364,6 +370,11 @@ __global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
   }
 }
 
+__global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
+  extern __shared__ float2 smem[];
+  poisson_b_body(B, (int)blockIdx.x, smem);
+}
+
 struct PassCArgs {
   int nx, ny, logn, pairs_per_block;
   const float* p1;
@@ -401,8 +412,7 @@ __device__ __forceinline__ void build_dct3_pair(const float* a0, const float* a1
   dst[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
 }
 
-__global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
-  extern __shared__ float2 smem[];
+__device__ __forceinline__ void poisson_c_body(const PassCArgs& C, int vb, float2* smem) {
   const int n = C.nx;
   const int rp_n = C.pairs_per_block;
   float* rows = reinterpret_cast<float*>(smem);       // [rp][4][n]: p1 row0, p1 row1, p2 row0, p2 row1
@@ -414,7 +424,7 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
   for (int idx = threadIdx.x; idx < rp_n * 2 * n; idx += blockDim.x) {
     const int rp = idx / (2 * n), t = idx - rp * 2 * n;
     const int h = t / n, i = t - h * n;
-    const int r = blockIdx.x * rp_n + rp;
+    const int r = vb * rp_n + rp;
     float a = 0.f, b = 0.f;
     if (r < C.ny / 2) {
       a = C.p1[(2 * r + h) * n + i];
@@ -436,7 +446,7 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
     float2* res = block_fft(s0, s1, n, C.logn, rp_n, +1, tws);
     for (int idx = threadIdx.x; idx < rp_n * n; idx += blockDim.x) {
       const int rp = idx / n, m = idx - rp * n;
-      const int r = blockIdx.x * rp_n + rp;
+      const int r = vb * rp_n + rp;
       if (r >= C.ny / 2) continue;
       const float2 w = res[rp * n + makhoul_pos(m, n)];
       float v0 = w.x, v1 = w.y;
@@ -462,6 +472,11 @@ __global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
     __syncthreads();
     if (res != s0) { float2* t = s0; s0 = s1; s1 = t; }
   }
+}
+
+__global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
+  extern __shared__ float2 smem[];
+  poisson_c_body(C, (int)blockIdx.x, smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -1010,6 +1025,127 @@ int poisson_prepare_device() {
   return GPL_OK;
 }
 
+namespace {
+// Passes B and C of the block form, with the grids and dynamic shared memory
+// of passes A, B and C.
+void block_form_bc(const PoissonGrid& g, float* spec, float* p1, float* p2, float2* field, float* fx,
+                   float* fy, float* phi, PassBArgs& B, PassCArgs& C, int grid[3], size_t smem[3]) {
+  const int nx = g.nx, ny = g.ny;
+  B.nx = nx; B.ny = ny; B.logn = ilog2(ny); B.col_pairs = pairs_b(nx, ny);
+  B.spec = spec; B.p1 = p1; B.p2 = p2; B.wx = g.wx; B.wy = g.wy; B.tw = g.tw; B.w4 = g.w4y;
+  B.scale = 4.0f / (float)nx / (float)ny;
+  C.nx = nx; C.ny = ny; C.logn = ilog2(nx); C.pairs_per_block = pairs_c(nx, ny);
+  C.p1 = p1; C.p2 = p2; C.field = field; C.fx = fx; C.fy = fy; C.phi = phi;
+  C.wx = g.wx; C.tw = g.tw; C.w4 = g.w4x;
+  grid[0] = poisson_blocks_a(nx, ny);
+  grid[1] = nx / (2 * B.col_pairs);
+  grid[2] = (ny / 2 + C.pairs_per_block - 1) / C.pairs_per_block;
+  smem[0] = smem_a(nx, ny);
+  smem[1] = smem_b(nx, ny);
+  smem[2] = smem_c(nx, ny);
+}
+
+PassAArgs pass_a_args(const PoissonGrid& g, unsigned long long* const* area_pair, const EvalCtl* ctl,
+                      const int64_t* nonplace, float td, const float* density_in, float* density,
+                      double* part_overflow, float* spec) {
+  PassAArgs A;
+  A.nx = g.nx; A.ny = g.ny; A.logn = ilog2(g.nx); A.pairs_per_block = pairs_a(g.nx, g.ny);
+  A.core_lx = g.core_lx; A.core_ly = g.core_ly; A.core_ux = g.core_ux; A.core_uy = g.core_uy;
+  A.size_x = g.size_x; A.size_y = g.size_y; A.td = td;
+  A.area_pair[0] = area_pair ? area_pair[0] : nullptr;
+  A.area_pair[1] = area_pair ? area_pair[1] : nullptr;
+  A.ctl = ctl; A.nonplace = nonplace;
+  A.density_in = density_in; A.density = density; A.spec = spec;
+  A.part_overflow = part_overflow; A.tw = g.tw; A.w4 = g.w4x;
+  return A;
+}
+
+PoissonGrid job_grid(const DeviceModel& d) {
+  PoissonGrid g;
+  g.nx = d.cnt_x; g.ny = d.cnt_y; g.size_x = d.size_x; g.size_y = d.size_y;
+  g.core_lx = d.core_lx; g.core_ly = d.core_ly; g.core_ux = d.core_ux; g.core_uy = d.core_uy;
+  g.wx = d.wx; g.wy = d.wy; g.w4x = d.w4x; g.w4y = d.w4y; g.tw = d.twiddle;
+  return g;
+}
+
+// Batched form of the block passes: work items (instance, block); each
+// block runs the per-job kernel's body on its instance's arguments.
+__global__ void __launch_bounds__(256) k_poisson_a_batch(const PassAArgs* args, const int4* items, const int* count) {
+  extern __shared__ float2 smem[];
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    poisson_a_body(args[it.x], it.y, smem);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_poisson_b_batch(const PassBArgs* args, const int4* items, const int* count) {
+  extern __shared__ float2 smem[];
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    poisson_b_body(args[it.x], it.y, smem);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_poisson_c_batch(const PassCArgs* args, const int4* items, const int* count) {
+  extern __shared__ float2 smem[];
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    poisson_c_body(args[it.x], it.y, smem);
+    __syncthreads();
+  }
+}
+}  // namespace
+
+size_t poisson_batch_args_bytes(int pass) {
+  const size_t b = pass == 0 ? sizeof(PassAArgs) : pass == 1 ? sizeof(PassBArgs) : sizeof(PassCArgs);
+  return (b + 15) / 16 * 16;
+}
+
+bool write_poisson_batch_args(const DeviceModel& d, void* dst_a, void* dst_b, void* dst_c, int grid[3],
+                              size_t smem[3]) {
+  if (d.poisson_path != 1 || warp_form(d.cnt_x, d.cnt_y)) return false;
+  const PoissonGrid g = job_grid(d);
+  const PassAArgs A = pass_a_args(g, d.area, d.ctl, d.nonplace, d.target_density, nullptr, d.density,
+                                  d.part + (size_t)kPartOverflow * d.part_stride, d.spec);
+  PassBArgs B;
+  PassCArgs C;
+  block_form_bc(g, d.spec, d.p1, d.p2, d.field, nullptr, nullptr, nullptr, B, C, grid, smem);
+  memcpy(dst_a, &A, sizeof(A));
+  memcpy(dst_b, &B, sizeof(B));
+  memcpy(dst_c, &C, sizeof(C));
+  return true;
+}
+
+int poisson_batch_prepare_device() {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  GPL_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return GPL_ERR_INVALID_ARG; }
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev]) return GPL_OK;
+  const int big = 200 * 1024;
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_a_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_b_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  GPL_CUDA(cudaFuncSetAttribute(k_poisson_c_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  done[dev] = true;
+  return GPL_OK;
+}
+
+int launch_poisson_batch(int pass, const void* args, const int4* items, const int* count, int grid, size_t smem,
+                         cudaStream_t s) {
+  if (pass == 0) k_poisson_a_batch<<<grid, 256, smem, s>>>(static_cast<const PassAArgs*>(args), items, count);
+  else if (pass == 1) k_poisson_b_batch<<<grid, 256, smem, s>>>(static_cast<const PassBArgs*>(args), items, count);
+  else k_poisson_c_batch<<<grid, 256, smem, s>>>(static_cast<const PassCArgs*>(args), items, count);
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
 // The three passes on arbitrary device arrays.  Area mode (area != null):
 // the density comes from the int64 areas; otherwise from density_in.
 int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
@@ -1020,15 +1156,7 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
   int rc = poisson_prepare_device();
   if (rc) return rc;
   const int nx = g.nx, ny = g.ny;
-  PassAArgs A;
-  A.nx = nx; A.ny = ny; A.logn = ilog2(nx); A.pairs_per_block = pairs_a(nx, ny);
-  A.core_lx = g.core_lx; A.core_ly = g.core_ly; A.core_ux = g.core_ux; A.core_uy = g.core_uy;
-  A.size_x = g.size_x; A.size_y = g.size_y; A.td = td;
-  A.area_pair[0] = area_pair ? area_pair[0] : nullptr;
-  A.area_pair[1] = area_pair ? area_pair[1] : nullptr;
-  A.ctl = ctl; A.nonplace = nonplace;
-  A.density_in = density_in; A.density = density; A.spec = spec;
-  A.part_overflow = part_overflow; A.tw = g.tw; A.w4 = g.w4x;
+  const PassAArgs A = pass_a_args(g, area_pair, ctl, nonplace, td, density_in, density, part_overflow, spec);
   if (const int wn = warp_form(nx, ny)) {
     const bool areas = area_pair && ctl;
     PassBArgs B;
@@ -1063,22 +1191,19 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
     GPL_CUDA(cudaGetLastError());
     return GPL_OK;
   }
-  if (t) t->begin(kKPoissonA);
-  k_poisson_a<<<poisson_blocks_a(nx, ny), 256, smem_a(nx, ny), s>>>(A);
-  if (t) t->end(kKPoissonA);
   PassBArgs B;
-  B.nx = nx; B.ny = ny; B.logn = ilog2(ny); B.col_pairs = pairs_b(nx, ny);
-  B.spec = spec; B.p1 = p1; B.p2 = p2; B.wx = g.wx; B.wy = g.wy; B.tw = g.tw; B.w4 = g.w4y;
-  B.scale = 4.0f / (float)nx / (float)ny;
-  if (t) t->begin(kKPoissonB);
-  k_poisson_b<<<nx / (2 * B.col_pairs), 256, smem_b(nx, ny), s>>>(B);
-  if (t) t->end(kKPoissonB);
   PassCArgs C;
-  C.nx = nx; C.ny = ny; C.logn = ilog2(nx); C.pairs_per_block = pairs_c(nx, ny);
-  C.p1 = p1; C.p2 = p2; C.field = field; C.fx = fx; C.fy = fy; C.phi = phi;
-  C.wx = g.wx; C.tw = g.tw; C.w4 = g.w4x;
+  int grid[3];
+  size_t smem[3];
+  block_form_bc(g, spec, p1, p2, field, fx, fy, phi, B, C, grid, smem);
+  if (t) t->begin(kKPoissonA);
+  k_poisson_a<<<grid[0], 256, smem[0], s>>>(A);
+  if (t) t->end(kKPoissonA);
+  if (t) t->begin(kKPoissonB);
+  k_poisson_b<<<grid[1], 256, smem[1], s>>>(B);
+  if (t) t->end(kKPoissonB);
   if (t) t->begin(kKPoissonC);
-  k_poisson_c<<<(ny / 2 + C.pairs_per_block - 1) / C.pairs_per_block, 256, smem_c(nx, ny), s>>>(C);
+  k_poisson_c<<<grid[2], 256, smem[2], s>>>(C);
   if (t) t->end(kKPoissonC);
   if (t) t->count(3);
   GPL_CUDA(cudaGetLastError());
@@ -1087,10 +1212,7 @@ int poisson_passes(const PoissonGrid& g, unsigned long long* const* area_pair,
 
 int launch_poisson_job(DeviceModel& d, bool want_phi, cudaStream_t s, Timer& t) {
   if (d.poisson_path == 2 && d.pg) return launch_poisson_gemm(d, d.pg, want_phi, s, t);
-  PoissonGrid g;
-  g.nx = d.cnt_x; g.ny = d.cnt_y; g.size_x = d.size_x; g.size_y = d.size_y;
-  g.core_lx = d.core_lx; g.core_ly = d.core_ly; g.core_ux = d.core_ux; g.core_uy = d.core_uy;
-  g.wx = d.wx; g.wy = d.wy; g.w4x = d.w4x; g.w4y = d.w4y; g.tw = d.twiddle;
+  const PoissonGrid g = job_grid(d);
   return poisson_passes(g, d.area, d.ctl, d.nonplace, d.target_density, nullptr, d.density,
                         d.part + (size_t)kPartOverflow * d.part_stride, d.spec, d.p1, d.p2,
                         d.field, nullptr, nullptr, want_phi ? d.phi : nullptr, s, &t);

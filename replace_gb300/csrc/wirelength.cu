@@ -25,6 +25,7 @@
 // of the kernel: the unweighted one keeps its register count (48 -> 40 per
 // thread, six blocks of 256 threads per SM instead of five).
 #include <climits>
+#include <cstring>
 
 #include <cuda_runtime.h>
 
@@ -389,8 +390,10 @@ constexpr int kWaSplit = 6;
 // cells); at 32 registers the weighted one spills (4 bytes), so it keeps six
 // blocks per SM (40 registers, no spill); the large-net variants keep their
 // registers.
+// Block vb of the small-net (kLarge = false) or large-net launch; shared by
+// the per-job launch and the batched one.
 template <bool kLarge, bool kW>
-__global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7)) k_wa(const __grid_constant__ WaArgs A) {
+__device__ __forceinline__ void wa_body(const WaArgs& A, int vb) {
   WaEval<kW> V;
   {
     const EvalCtl* C = A.ctl;
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7)) k_wa(const 
     V.cy = C->wl_coef_y;
     V.w = A.net_w;
   }
-  const int gb = (int)blockIdx.x + (kLarge ? A.block_start[kWaSplit] : 0);
+  const int gb = vb + (kLarge ? A.block_start[kWaSplit] : 0);
   int bucket = kLarge ? kWaSplit : 0;
   const int last = kLarge ? kWaBuckets - 1 : kWaSplit - 1;
   while (bucket < last && gb >= A.block_start[bucket + 1]) bucket++;
@@ -431,6 +434,11 @@ __global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7)) k_wa(const 
   }
 }
 
+template <bool kLarge, bool kW>
+__global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7)) k_wa(const __grid_constant__ WaArgs A) {
+  wa_body<kLarge, kW>(A, (int)blockIdx.x);
+}
+
 }  // namespace
 
 // bucket 0: a thread per net; 1-4: lane groups of 2 << bucket; 5-7: a warp per net
@@ -438,7 +446,8 @@ int wa_nets_per_block(int bucket) { return bucket == 0 ? kBlock : bucket < 5 ? k
 
 int net_blocks(const DeviceModel& d) { return d.wa_block_start[kWaBuckets]; }
 
-int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+namespace {
+WaArgs wa_args(const DeviceModel& d, const EvalArgs& a) {
   WaArgs A;
   for (int b = 0; b <= kWaBuckets; b++) {
     A.bucket_start[b] = d.wa_bucket_start[b];
@@ -452,6 +461,50 @@ int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
   A.pin_grad = d.pin_grad;
   A.net_w = d.net_w;
   A.hpwl_total = d.hpwl_total;
+  return A;
+}
+
+// Batched form: work items (instance, block of the instance's small- or
+// large-net launch); the block body is the per-job kernel's.
+template <bool kLarge, bool kW>
+__global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7))
+    k_wa_batch(const WaArgs* args, const int4* items, const int* count) {
+  const int n = *count;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {
+    const int4 it = items[w];
+    wa_body<kLarge, kW>(args[it.x], it.y);
+  }
+}
+}  // namespace
+
+size_t wa_batch_args_bytes() { return (sizeof(WaArgs) + 15) / 16 * 16; }
+
+void wa_launch_blocks(const DeviceModel& d, int* small, int* large) {
+  *small = d.wa_block_start[kWaSplit];
+  *large = d.wa_block_start[kWaBuckets] - *small;
+}
+
+void write_wa_batch_args(const DeviceModel& d, const EvalArgs& a, void* dst) {
+  const WaArgs A = wa_args(d, a);
+  memcpy(dst, &A, sizeof(A));
+}
+
+int launch_wa_batch(bool large, bool weighted, const void* args, const int4* items, const int* count, int grid,
+                    cudaStream_t s) {
+  const WaArgs* A = static_cast<const WaArgs*>(args);
+  if (large) {
+    if (weighted) k_wa_batch<true, true><<<grid, kBlock, 0, s>>>(A, items, count);
+    else k_wa_batch<true, false><<<grid, kBlock, 0, s>>>(A, items, count);
+  } else {
+    if (weighted) k_wa_batch<false, true><<<grid, kBlock, 0, s>>>(A, items, count);
+    else k_wa_batch<false, false><<<grid, kBlock, 0, s>>>(A, items, count);
+  }
+  GPL_CUDA(cudaGetLastError());
+  return GPL_OK;
+}
+
+int launch_wa(DeviceModel& d, const EvalArgs& a, cudaStream_t s, Timer& t) {
+  const WaArgs A = wa_args(d, a);
   const int small = d.wa_block_start[kWaSplit];
   const int large = d.wa_block_start[kWaBuckets] - small;
   t.begin(kKWa);

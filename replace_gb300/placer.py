@@ -148,6 +148,21 @@ class Placer:
         return int(self.lib.gpl_kernel_launch_count(self.h))
 
 
+def batch_nesterov_run(placers, max_iters: int = 0):
+    """gpl_batch_nesterov_run: the Nesterov loops of several jobs (Placer
+    objects after nesterov_init, one device, FFT Poisson form) in one
+    batched launch per phase.  Returns ([NesterovStats], [status],
+    kernel_launches); every job's result equals nesterov_run on it alone."""
+    lib = load()
+    n = len(placers)
+    handles = (C.c_void_p * n)(*[p.h.value for p in placers])
+    stats = (_abi.NesterovStats * n)()
+    status = (C.c_int32 * n)()
+    launches = C.c_int64(0)
+    check(lib.gpl_batch_nesterov_run(handles, n, max_iters, stats, status, C.byref(launches)))
+    return list(stats), list(status), int(launches.value)
+
+
 def poisson_solve(density_dev_ptr: int, phi_dev_ptr: int, fx_dev_ptr: int, fy_dev_ptr: int,
                   nx: int, ny: int, bin_size_x: int, bin_size_y: int, stream: int = 0):
     """gpl_poisson_solve on device pointers (e.g. torch tensors' data_ptr())."""
