@@ -439,8 +439,10 @@ __device__ __forceinline__ void cell_body(const CellArgs& A, int vb, int vgrid) 
       // getDistance (src/nesterovPlace.cpp:598-607): float differences
       const float dx = c.x - r.x, dy = c.y - r.y;
       const float gx = s.x - q.x, gy = s.y - q.y;
-      acc[2] += dx * dx + dy * dy;
-      acc[3] += gx * gx + gy * gy;
+      // rounding spelled out: the per-job and the batched kernel inline
+      // this body, and must not fuse differently
+      acc[2] = __fadd_rn(acc[2], __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+      acc[3] = __fadd_rn(acc[3], __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
     }
     if (!isfinite(aw) || !isfinite(ad)) bad = 1;
   }
@@ -770,7 +772,9 @@ __global__ void __launch_bounds__(kBlock) k_dgrad_big_batch(const CellBatchArgs*
   }
 }
 
-__global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell_batch(const CellBatchArgs* args,
+// (fewer resident blocks than the per-job kernel: the work-item loop and the
+// arguments read from memory need the registers)
+__global__ void __launch_bounds__(kBlock, 4) k_cell_batch(const CellBatchArgs* args,
                                                                          const int4* items, const int* count) {
   const int n = *count;
   for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -782,8 +786,8 @@ __global__ void __launch_bounds__(kBlock, kCellBlocksPerSm) k_cell_batch(const C
 
 }  // namespace
 
-size_t scatter_batch_args_bytes() { return (sizeof(ScatterBatchArgs) + 15) / 16 * 16; }
-size_t cell_batch_args_bytes() { return (sizeof(CellBatchArgs) + 15) / 16 * 16; }
+size_t scatter_batch_args_bytes() { return sizeof(ScatterBatchArgs); }
+size_t cell_batch_args_bytes() { return sizeof(CellBatchArgs); }
 
 void write_scatter_batch_args(const DeviceModel& d, void* dst) {
   ScatterBatchArgs x;

@@ -420,6 +420,8 @@ enum BatchPhase {
   kBScatter = 0, kBScatterBig, kBWaSmall, kBWaLarge, kBWaSmallW, kBWaLargeW,
   kBPoissonA, kBPoissonB, kBPoissonC, kBDgradBig, kBCell, kBPhases
 };
+// element sizes of the argument tables (the batched kernels index them as
+// arrays of the per-job argument structures)
 size_t scatter_batch_args_bytes();
 size_t cell_batch_args_bytes();
 size_t wa_batch_args_bytes();

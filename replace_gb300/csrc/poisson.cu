@@ -178,7 +178,11 @@ struct PassAArgs {
 
 // Block vb of pass A (smem: the block's dynamic shared memory); shared by the
 // per-job launch and the batched one, as are the bodies of passes B and C.
-__device__ __forceinline__ void poisson_a_body(const PassAArgs& A, int vb, float2* smem) {
+// The pass bodies are compiled once (not inlined) and called by both
+// kernels: inlined into two kernels, the same float expressions can be
+// contracted into fused multiply-adds differently, and a job's result would
+// then depend on which kernel ran it.
+__device__ __noinline__ void poisson_a_body(const PassAArgs& A, int vb, float2* smem) {
   __shared__ double red[32];
   const int n = A.nx;
   const int rp_n = A.pairs_per_block;
@@ -258,7 +262,7 @@ __device__ __forceinline__ void poisson_a_body(const PassAArgs& A, int vb, float
   if (A.part_overflow) block_reduce_add((double)ovf_f, &A.part_overflow[vb], red);
 }
 
-__global__ void __launch_bounds__(256) k_poisson_a(PassAArgs A) {
+__global__ void __launch_bounds__(256) k_poisson_a(const __grid_constant__ PassAArgs A) {
   extern __shared__ float2 smem[];
   poisson_a_body(A, (int)blockIdx.x, smem);
 }
@@ -275,7 +279,7 @@ struct PassBArgs {
   float scale;                       // 4 / (nx ny)
 };
 
-__device__ __forceinline__ void poisson_b_body(const PassBArgs& B, int vb, float2* smem) {
+__device__ __noinline__ void poisson_b_body(const PassBArgs& B, int vb, float2* smem) {
   const int n = B.ny;
   const int cp = B.col_pairs;
   float2* s0 = smem;                 // [cp][n] work
@@ -370,7 +374,7 @@ __device__ __forceinline__ void poisson_b_body(const PassBArgs& B, int vb, float
   }
 }
 
-__global__ void __launch_bounds__(256) k_poisson_b(PassBArgs B) {
+__global__ void __launch_bounds__(256) k_poisson_b(const __grid_constant__ PassBArgs B) {
   extern __shared__ float2 smem[];
   poisson_b_body(B, (int)blockIdx.x, smem);
 }
@@ -412,7 +416,7 @@ __device__ __forceinline__ void build_dct3_pair(const float* a0, const float* a1
   dst[k] = make_float2(c0.x - c1.y, c0.y + c1.x);
 }
 
-__device__ __forceinline__ void poisson_c_body(const PassCArgs& C, int vb, float2* smem) {
+__device__ __noinline__ void poisson_c_body(const PassCArgs& C, int vb, float2* smem) {
   const int n = C.nx;
   const int rp_n = C.pairs_per_block;
   float* rows = reinterpret_cast<float*>(smem);       // [rp][4][n]: p1 row0, p1 row1, p2 row0, p2 row1
@@ -474,7 +478,7 @@ __device__ __forceinline__ void poisson_c_body(const PassCArgs& C, int vb, float
   }
 }
 
-__global__ void __launch_bounds__(256) k_poisson_c(PassCArgs C) {
+__global__ void __launch_bounds__(256) k_poisson_c(const __grid_constant__ PassCArgs C) {
   extern __shared__ float2 smem[];
   poisson_c_body(C, (int)blockIdx.x, smem);
 }
@@ -1102,8 +1106,8 @@ __global__ void __launch_bounds__(256) k_poisson_c_batch(const PassCArgs* args, 
 }  // namespace
 
 size_t poisson_batch_args_bytes(int pass) {
-  const size_t b = pass == 0 ? sizeof(PassAArgs) : pass == 1 ? sizeof(PassBArgs) : sizeof(PassCArgs);
-  return (b + 15) / 16 * 16;
+  // the element size of the device arrays the batched kernels index
+  return pass == 0 ? sizeof(PassAArgs) : pass == 1 ? sizeof(PassBArgs) : sizeof(PassCArgs);
 }
 
 bool write_poisson_batch_args(const DeviceModel& d, void* dst_a, void* dst_b, void* dst_c, int grid[3],

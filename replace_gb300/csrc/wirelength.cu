@@ -119,19 +119,25 @@ __device__ __forceinline__ NetCoef net_coef(const float* S, float cx, float cy) 
   for (int k = 0; k < 4; k++) {
     const float c = k < 2 ? cx : cy;
     const float inv = __fdividef(1.0f, S[2 * k]);
-    const float m = c * S[2 * k + 1] * inv * inv;
+    const float m = __fmul_rn(__fmul_rn(__fmul_rn(c, S[2 * k + 1]), inv), inv);
     const bool lo = (k & 1) == 0;          // min side
-    K.a[k] = lo ? inv + m : inv - m;
-    K.b[k] = lo ? -c * inv : c * inv;
+    K.a[k] = lo ? __fadd_rn(inv, m) : __fsub_rn(inv, m);
+    K.b[k] = lo ? __fmul_rn(-c, inv) : __fmul_rn(c, inv);
   }
   return K;
 }
 
+// (The arithmetic of this and net_coef is spelled out with rounding
+// intrinsics, so that every kernel that inlines it -- the per-job WA kernel
+// and the batched one -- computes the same values: left to the compiler, a
+// multiply and an add may be fused in one kernel and not in the other.)
 __device__ __forceinline__ float2 pin_gradient(int2 p, const PinExp& E, const NetCoef& K) {
   const float x = (float)p.x, y = (float)p.y;
-  const float g0 = E.e[0] * (K.a[0] + K.b[0] * x), g1 = E.e[1] * (K.a[1] + K.b[1] * x);
-  const float g2 = E.e[2] * (K.a[2] + K.b[2] * y), g3 = E.e[3] * (K.a[3] + K.b[3] * y);
-  return make_float2(g0 - g1, g2 - g3);
+  const float g0 = __fmul_rn(E.e[0], __fmaf_rn(K.b[0], x, K.a[0]));
+  const float g1 = __fmul_rn(E.e[1], __fmaf_rn(K.b[1], x, K.a[1]));
+  const float g2 = __fmul_rn(E.e[2], __fmaf_rn(K.b[2], y, K.a[2]));
+  const float g3 = __fmul_rn(E.e[3], __fmaf_rn(K.b[3], y, K.a[3]));
+  return make_float2(__fsub_rn(g0, g1), __fsub_rn(g2, g3));
 }
 
 __device__ __forceinline__ void sums_of(int2 p, const PinExp& E, float* S) {
@@ -467,7 +473,7 @@ WaArgs wa_args(const DeviceModel& d, const EvalArgs& a) {
 // Batched form: work items (instance, block of the instance's small- or
 // large-net launch); the block body is the per-job kernel's.
 template <bool kLarge, bool kW>
-__global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7))
+__global__ void __launch_bounds__(kBlock, kLarge ? 1 : 5)
     k_wa_batch(const WaArgs* args, const int4* items, const int* count) {
   const int n = *count;
   for (int w = blockIdx.x; w < n; w += gridDim.x) {
@@ -477,7 +483,7 @@ __global__ void __launch_bounds__(kBlock, kLarge ? 1 : (kW ? 6 : 7))
 }
 }  // namespace
 
-size_t wa_batch_args_bytes() { return (sizeof(WaArgs) + 15) / 16 * 16; }
+size_t wa_batch_args_bytes() { return sizeof(WaArgs); }
 
 void wa_launch_blocks(const DeviceModel& d, int* small, int* large) {
   *small = d.wa_block_start[kWaSplit];
