@@ -12,9 +12,11 @@ host arrays (netlist upload, init, iterations, location read-back).  The
 reference arm times the CPU restatement of the reference's path (the oracle)
 on this host.  Multi-GPU runs are independent replicas (no collectives).
 
-At one GPU the line also carries `serving`: the batched form (64 jobs of
-2k-50k cells submitted at once to the placement server, against the same
-jobs placed one at a time) and the serving form (the first --stream-jobs
+At one GPU the line also carries `serving`: the batch of config 4 (64 jobs
+of 2k-50k cells submitted at once to the placement server, against the same
+jobs placed one at a time), its batched form (the jobs' Nesterov loops in
+one persistent launch per phase, and the server in batched mode) and the
+serving form (the first --stream-jobs
 requests of a 500-job Poisson stream at 2 jobs/s, 5k-500k cells, against a
 one-job-at-a-time server): placements/h and p50/p99 job latency.
 """
@@ -239,6 +241,62 @@ def serving_batch(n_jobs, slots, device):
         "converged": int(sum(res[t]["status"] == 0 and res[t]["finished"] and res[t]["overflow"] <= 0.1
                              for t in ts)),
         "same_result_alone_and_in_mix": bool(same),
+    }
+
+
+def batched_form(n_jobs, slots, device):
+    """The batched form of config 4's jobs: (1) their Nesterov loops after
+    initial place and init, one at a time (gpl_nesterov_run per job) against
+    all together (gpl_batch_nesterov_run: one persistent launch per phase
+    over a work table of (job, block), rounds replayed as one CUDA graph);
+    (2) whole jobs through the placement server in batched mode (jobs join
+    the running batch after their initial place).  Results must be
+    bit-identical between the forms."""
+    import numpy as np
+    from replace_gb300 import Placer, PlacementServer, batch_nesterov_run, netlist as N
+    jobs = N.job_batch(n_jobs, seed=4)
+
+    def prepared():
+        ps = []
+        for nl, td in jobs:
+            p = Placer(nl, target_density=td, device=device, poisson_path=1)
+            p.initial_place()
+            p.nesterov_init()
+            ps.append(p)
+        return ps
+    ps = prepared()
+    t0 = time.perf_counter()
+    alone = [p.nesterov_run(0, allow_divergence=True)[1] for p in ps]
+    t_alone = time.perf_counter() - t0
+    loc_alone = [p.inst_locations() for p in ps]
+    for p in ps:
+        p.close()
+    ps = prepared()
+    t0 = time.perf_counter()
+    stats, status, launches = batch_nesterov_run(ps)
+    t_batch = time.perf_counter() - t0
+    loc_batch = [p.inst_locations() for p in ps]
+    for p in ps:
+        p.close()
+    same = all(a.hpwl == b.hpwl and a.iterations == b.iterations and np.array_equal(la[0], lb[0])
+               and np.array_equal(la[1], lb[1]) for a, b, la, lb in zip(alone, stats, loc_alone, loc_batch))
+    iters = sum(s.iterations for s in stats)
+    with PlacementServer(device=device, max_active=slots, batched=True) as srv:
+        t0 = time.perf_counter()
+        ts = [srv.submit(nl, target_density=td, poisson_path=1) for nl, td in jobs]
+        res = {r["ticket"]: r for r in srv.wait_all(1800)}
+        t_srv = time.perf_counter() - t0
+    lat = np.array([res[t]["latency_s"] for t in ts])
+    same_srv = all(res[t]["hpwl"] == a.hpwl for t, a in zip(ts, alone))
+    return {
+        "nesterov_phase": {"jobs": n_jobs, "iterations": iters, "one_at_a_time_s": t_alone,
+                           "batched_s": t_batch, "speedup": t_alone / t_batch,
+                           "batched_iters_per_s": iters / t_batch, "kernel_launches": launches,
+                           "same_result": bool(same)},
+        "server_batched": {"slots": slots, "placements_per_hour": n_jobs / t_srv * 3600.0,
+                           "makespan_s": t_srv, "p50_latency_s": float(np.percentile(lat, 50)),
+                           "p99_latency_s": float(np.percentile(lat, 99)),
+                           "same_result_as_one_at_a_time": bool(same_srv)},
     }
 
 
@@ -519,6 +577,7 @@ def main():
     serving = None
     if world == 1 and not args.no_serving:
         serving = {"batch": serving_batch(args.batch_jobs, args.slots, local_rank),
+                   "batched_form": batched_form(args.batch_jobs, args.slots, local_rank),
                    "stream": serving_stream(args.stream_jobs, args.slots, local_rank)}
 
     cpu = None

@@ -370,7 +370,14 @@ typedef struct gpl_server_params {
   int32_t chunk_iters;        /* Nesterov iterations between cancel checks (64) */
   int32_t run_initial_place;  /* 1 = gpl_initial_place before the Nesterov loop (1) */
   int32_t blocking_sync;      /* 1 = slot threads sleep while waiting for the GPU (1) */
-  int32_t pad;
+  int32_t batched;            /* 1 = admitted jobs run their Nesterov loops together as
+                                 one batch (gpl_batch_nesterov_run's kernels): a job joins
+                                 the running batch when its initialisation is done and
+                                 leaves it when its loop ends; jobs the batched kernels do
+                                 not cover (512 x 512 and 1024 x 1024 grids) run alone on
+                                 their slot.  Jobs with poisson_path 0 (auto) take the FFT
+                                 form (1) in this mode.  0 = every job runs its own loop
+                                 on its slot's stream (0) */
 } gpl_server_params;
 
 typedef struct gpl_server_result {

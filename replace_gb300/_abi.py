@@ -122,7 +122,7 @@ class ServerParams(C.Structure):
     _fields_ = [
         ("device", C.c_int32), ("max_active", C.c_int32), ("hbm_budget_bytes", C.c_int64),
         ("chunk_iters", C.c_int32), ("run_initial_place", C.c_int32),
-        ("blocking_sync", C.c_int32), ("pad", C.c_int32),
+        ("blocking_sync", C.c_int32), ("batched", C.c_int32),
     ]
 
 

@@ -445,6 +445,29 @@ int launch_wa_batch(bool large, bool weighted, const void* args, const int4* ite
 int launch_poisson_batch(int pass, const void* args, const int4* items, const int* count, int grid,
                          size_t smem, cudaStream_t s);
 
+// The host side of the batched form (job.cu): members join and leave
+// between rounds; a round runs every running member's next evaluation.
+struct BatchRun;
+struct BatchMember {
+  gpl_job* job = nullptr;
+  bool running = false;     // still iterating in this batch
+  bool start = true;        // its next evaluation starts an iteration
+  int done = 0;             // iterations in this batch
+  int limit = 0;            // iteration limit in this batch (0: to the stop rule)
+  gpl_iter_log* log = nullptr;
+};
+BatchRun* batch_create(int device, int capacity, int* rc);
+void batch_destroy(BatchRun* b);
+bool batch_eligible(const gpl_job* j);
+int batch_join(BatchRun* b, int slot, gpl_job* j, int max_iters, gpl_iter_log* log);
+void batch_leave(BatchRun* b, int slot);
+int batch_round(BatchRun* b, long long* launches);
+bool batch_running(const BatchRun* b, int slot);
+int batch_count_running(const BatchRun* b);
+void batch_stop_member(BatchRun* b, int slot);     // ends the member's loop here (cancel)
+// the member's gpl_nesterov_run status and stats once it stopped running
+int batch_member_status(gpl_job* j, gpl_nesterov_stats* stats);
+
 // Unique id of the calling thread's current CUDA context (cuCtxGetId through
 // the runtime's driver entry points; 0 when it cannot be read).  Caches of
 // device addresses are keyed on it: after cudaDeviceReset the device gets a

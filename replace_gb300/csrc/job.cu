@@ -1093,240 +1093,291 @@ int end_of_run(gpl_job* j) {
 }
 
 // ------------------------------------------------------------ batched form
-// The Nesterov loops of many jobs in lockstep: every round, each running
-// job's next evaluation (its next back-tracking try, or the first try of its
-// next iteration) goes into one launch per phase (batched kernels of
+// The Nesterov loops of many jobs in lockstep: every round, each member
+// job's next evaluation (its next back-tracking try, or the first try of
+// its next iteration) goes into one launch per phase (batched kernels of
 // density.cu, wirelength.cu, poisson.cu) driven by a table of work items
-// (instance, block of the instance's own launch); then each job's control
-// (control.h) processes its result exactly as the host loop does.  A job's
-// blocks compute what its own launches compute, in the same blocks, so its
-// iterates, log and result are bit-identical to running it alone.  Jobs
-// leave the table when their loop ends; the round's launches are captured
-// once as a CUDA graph (persistent grids, tables in device memory).
+// (member slot, block of the job's own launch, that launch's grid); then
+// each job's control (control.h) takes its result exactly as the host loop
+// does.  A job's blocks compute what its own launches compute, in the same
+// blocks, so its iterates, log and result are bit-identical to running it
+// alone.  Members join and leave between rounds; the round's launches are
+// one CUDA graph (persistent grids; argument tables and items in device
+// memory), captured again only when the launches themselves change.
+}  // namespace
+
+namespace gpl {
+
+enum BatchTable { kTScatter = 0, kTWa, kTPa, kTPb, kTPc, kTCell, kTables };
+
 struct BatchRun {
-  int n = 0, device = 0;
+  int cap = 0, device = 0, sms = 1;
   cudaStream_t s = nullptr;
-  char* dev = nullptr;                 // argument tables, control and result records, items
-  char* host = nullptr;                // pinned: control and result records, items, counts
-  size_t dev_bytes = 0, host_bytes = 0;
-  char* args[6] = {nullptr};           // scatter, wa, poisson A, B, C, cell
-  size_t stride[6] = {0};
+  char* dev = nullptr;                 // argument tables, control and result records, counts
+  char* host = nullptr;                // pinned: control and result records, counts
+  char* args[kTables] = {nullptr};
+  size_t stride[kTables] = {0};
   EvalCtl* ctl_d = nullptr;
   EvalResult* res_d = nullptr;
-  int4* items_d = nullptr;
   int* counts_d = nullptr;
   EvalCtl* ctl_h = nullptr;
   EvalResult* res_h = nullptr;
-  int4* items_h = nullptr;
   int* counts_h = nullptr;
-  int item_off[kBPhases] = {0}, item_cap[kBPhases] = {0};
-  int grid[kBPhases] = {0};
+  int4* items_d = nullptr;             // [items_cap], grown on demand
+  int4* items_h = nullptr;             // pinned mirror
+  int items_cap = 0;
+  int item_off[kBPhases] = {0};
+  bool phase_used[kBPhases] = {false};
   size_t smem_scatter = 0, smem_p[3] = {0, 0, 0};
   std::vector<std::array<int, kBPhases>> vgrid;
+  std::vector<BatchMember> members;    // by slot; job == nullptr: free
   cudaGraphExec_t exec = nullptr;
+  bool items_dirty = true, graph_dirty = true;
   long long launches_per_round = 0;
   ~BatchRun() {
     if (exec) cudaGraphExecDestroy(exec);
     if (s) cudaStreamSynchronize(s);
     if (dev) cudaFree(dev);
+    if (items_d) cudaFree(items_d);
     if (host) cudaFreeHost(host);
+    if (items_h) cudaFreeHost(items_h);
     if (s) cudaStreamDestroy(s);
   }
 };
 
-enum BatchTable { kTScatter = 0, kTWa, kTPa, kTPb, kTPc, kTCell };
-
-// Argument tables, persistent grids and item capacities of a batch.
-int batch_setup(BatchRun& B, const std::vector<gpl_job*>& jobs) {
-  const int n = (int)jobs.size();
-  B.n = n;
-  B.device = jobs[0]->device;
-  GPL_CUDA(cudaStreamCreateWithFlags(&B.s, cudaStreamNonBlocking));
+BatchRun* batch_create(int device, int capacity, int* rc_out) {
+  *rc_out = GPL_OK;
+  std::unique_ptr<BatchRun> B(new BatchRun());
+  B->cap = capacity;
+  B->device = device;
+  auto fail = [&](int rc) { *rc_out = rc; return nullptr; };
+  if (cudaSetDevice(device) != cudaSuccess) { set_error("batch: cudaSetDevice failed"); return fail(GPL_ERR_CUDA); }
+  cudaDeviceGetAttribute(&B->sms, cudaDevAttrMultiProcessorCount, device);
+  B->sms = std::max(1, B->sms);
+  if (cudaStreamCreateWithFlags(&B->s, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("batch: stream creation failed");
+    return fail(GPL_ERR_CUDA);
+  }
   int rc = scatter_prepare_device();
   if (!rc) rc = scatter_batch_prepare_device();
   if (!rc) rc = poisson_prepare_device();
   if (!rc) rc = poisson_batch_prepare_device();
-  if (rc) return rc;
-  B.stride[kTScatter] = scatter_batch_args_bytes();
-  B.stride[kTWa] = wa_batch_args_bytes();
-  B.stride[kTPa] = poisson_batch_args_bytes(0);
-  B.stride[kTPb] = poisson_batch_args_bytes(1);
-  B.stride[kTPc] = poisson_batch_args_bytes(2);
-  B.stride[kTCell] = cell_batch_args_bytes();
-  B.vgrid.assign(n, {});
-  for (int k = 0; k < n; k++) {
-    const DeviceModel& d = jobs[k]->d;
-    std::array<int, kBPhases>& v = B.vgrid[k];
-    v.fill(0);
-    v[kBScatter] = d.max_chunks;
-    v[kBScatterBig] = d.n_big;
-    v[kBDgradBig] = d.n_big;
-    v[kBCell] = cell_grid(d);
-    int small = 0, large = 0;
-    wa_launch_blocks(d, &small, &large);
-    v[d.net_weighted ? kBWaSmallW : kBWaSmall] = small;
-    v[d.net_weighted ? kBWaLargeW : kBWaLarge] = large;
-    B.smem_scatter = std::max(B.smem_scatter, scatter_smem(d));
-  }
-  // one device block: tables, records, items, counts (256-byte aligned parts)
+  if (rc) return fail(rc);
+  B->stride[kTScatter] = scatter_batch_args_bytes();
+  B->stride[kTWa] = wa_batch_args_bytes();
+  B->stride[kTPa] = poisson_batch_args_bytes(0);
+  B->stride[kTPb] = poisson_batch_args_bytes(1);
+  B->stride[kTPc] = poisson_batch_args_bytes(2);
+  B->stride[kTCell] = cell_batch_args_bytes();
   size_t off = 0;
   auto take = [&](size_t b) { const size_t o = off; off += (b + 255) / 256 * 256; return o; };
-  size_t o_args[6];
-  for (int t = 0; t < 6; t++) o_args[t] = take(B.stride[t] * n);
-  const size_t o_ctl = take(sizeof(EvalCtl) * n), o_res = take(sizeof(EvalResult) * n);
-  int total = 0;
-  for (int p = 0; p < kBPhases; p++) {
-    B.item_off[p] = total;
-    int cap = 0;
-    for (int k = 0; k < n; k++) cap += B.vgrid[k][p];
-    // Poisson items are known once the per-job grids are (below)
-    B.item_cap[p] = cap;
-    total += cap;
+  size_t o_args[kTables];
+  for (int t = 0; t < kTables; t++) o_args[t] = take(B->stride[t] * capacity);
+  const size_t o_ctl = take(sizeof(EvalCtl) * capacity), o_res = take(sizeof(EvalResult) * capacity);
+  const size_t o_counts = take(sizeof(int) * kBPhases);
+  if (cudaMalloc(&B->dev, off) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("batch: device tables");
+    return fail(GPL_ERR_OUT_OF_MEMORY);
   }
-  // Poisson passes: the grids of each job's block form
-  std::vector<char> pa(B.stride[kTPa] * n), pb(B.stride[kTPb] * n), pc(B.stride[kTPc] * n);
-  for (int k = 0; k < n; k++) {
-    int g3[3];
-    size_t sm3[3];
-    if (!write_poisson_batch_args(jobs[k]->d, pa.data() + k * B.stride[kTPa], pb.data() + k * B.stride[kTPb],
-                                  pc.data() + k * B.stride[kTPc], g3, sm3)) {
-      set_error("batched Nesterov loop: job " + std::to_string(k) +
-                " does not run the block-form FFT Poisson passes (its grid is 512 x 512 or 1024 x 1024, "
-                "or it runs the tensor-core form); run it alone");
-      return GPL_ERR_INVALID_ARG;
-    }
-    for (int q = 0; q < 3; q++) {
-      B.vgrid[k][kBPoissonA + q] = g3[q];
-      B.smem_p[q] = std::max(B.smem_p[q], sm3[q]);
-    }
-  }
-  total = 0;
-  for (int p = 0; p < kBPhases; p++) {
-    int cap = 0;
-    for (int k = 0; k < n; k++) cap += B.vgrid[k][p];
-    B.item_off[p] = total;
-    B.item_cap[p] = cap;
-    total += cap;
-  }
-  const size_t o_items = take(sizeof(int4) * std::max(total, 1)), o_counts = take(sizeof(int) * kBPhases);
-  B.dev_bytes = off;
-  GPL_CUDA(cudaMalloc(&B.dev, B.dev_bytes));
-  for (int t = 0; t < 6; t++) B.args[t] = B.dev + o_args[t];
-  B.ctl_d = reinterpret_cast<EvalCtl*>(B.dev + o_ctl);
-  B.res_d = reinterpret_cast<EvalResult*>(B.dev + o_res);
-  B.items_d = reinterpret_cast<int4*>(B.dev + o_items);
-  B.counts_d = reinterpret_cast<int*>(B.dev + o_counts);
-  // pinned: records, items, counts
+  for (int t = 0; t < kTables; t++) B->args[t] = B->dev + o_args[t];
+  B->ctl_d = reinterpret_cast<EvalCtl*>(B->dev + o_ctl);
+  B->res_d = reinterpret_cast<EvalResult*>(B->dev + o_res);
+  B->counts_d = reinterpret_cast<int*>(B->dev + o_counts);
   size_t hoff = 0;
   auto htake = [&](size_t b) { const size_t o = hoff; hoff += (b + 255) / 256 * 256; return o; };
-  const size_t h_ctl = htake(sizeof(EvalCtl) * n), h_res = htake(sizeof(EvalResult) * n);
-  const size_t h_items = htake(sizeof(int4) * std::max(total, 1)), h_counts = htake(sizeof(int) * kBPhases);
-  B.host_bytes = hoff;
-  GPL_CUDA(cudaMallocHost(&B.host, B.host_bytes));
-  memset(B.host, 0, B.host_bytes);
-  B.ctl_h = reinterpret_cast<EvalCtl*>(B.host + h_ctl);
-  B.res_h = reinterpret_cast<EvalResult*>(B.host + h_res);
-  B.items_h = reinterpret_cast<int4*>(B.host + h_items);
-  B.counts_h = reinterpret_cast<int*>(B.host + h_counts);
-  // the tables: each job's arguments with its control and result records
-  // redirected to the batch's slots
-  std::vector<char> ts(B.stride[kTScatter] * n), tw(B.stride[kTWa] * n), tc(B.stride[kTCell] * n);
-  for (int k = 0; k < n; k++) {
-    DeviceModel& d = jobs[k]->d;
-    EvalCtl* own_ctl = d.ctl;
-    EvalResult* own_res = d.result;
-    d.ctl = B.ctl_d + k;
-    d.result = B.res_d + k;
-    write_scatter_batch_args(d, ts.data() + k * B.stride[kTScatter]);
-    write_wa_batch_args(d, base_args(jobs[k]), tw.data() + k * B.stride[kTWa]);
-    write_cell_batch_args(d, base_args(jobs[k]), tc.data() + k * B.stride[kTCell]);
-    int g3[3];
-    size_t sm3[3];
-    write_poisson_batch_args(d, pa.data() + k * B.stride[kTPa], pb.data() + k * B.stride[kTPb],
-                             pc.data() + k * B.stride[kTPc], g3, sm3);
-    d.ctl = own_ctl;
-    d.result = own_res;
+  const size_t h_ctl = htake(sizeof(EvalCtl) * capacity), h_res = htake(sizeof(EvalResult) * capacity);
+  const size_t h_counts = htake(sizeof(int) * kBPhases);
+  if (cudaMallocHost(&B->host, hoff) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("batch: pinned records");
+    return fail(GPL_ERR_OUT_OF_MEMORY);
   }
-  GPL_CUDA(cudaMemcpyAsync(B.args[kTScatter], ts.data(), ts.size(), cudaMemcpyHostToDevice, B.s));
-  GPL_CUDA(cudaMemcpyAsync(B.args[kTWa], tw.data(), tw.size(), cudaMemcpyHostToDevice, B.s));
-  GPL_CUDA(cudaMemcpyAsync(B.args[kTPa], pa.data(), pa.size(), cudaMemcpyHostToDevice, B.s));
-  GPL_CUDA(cudaMemcpyAsync(B.args[kTPb], pb.data(), pb.size(), cudaMemcpyHostToDevice, B.s));
-  GPL_CUDA(cudaMemcpyAsync(B.args[kTPc], pc.data(), pc.size(), cudaMemcpyHostToDevice, B.s));
-  GPL_CUDA(cudaMemcpyAsync(B.args[kTCell], tc.data(), tc.size(), cudaMemcpyHostToDevice, B.s));
-  GPL_CUDA(cudaStreamSynchronize(B.s));
-  // persistent grids: about the per-job kernels' residency per SM
-  const int sms = std::max(1, jobs[0]->d.sm_count);
-  const int per_sm[kBPhases] = {4, 4, 7, 1, 6, 1, 4, 4, 4, 4, 6};
-  for (int p = 0; p < kBPhases; p++) B.grid[p] = std::min(B.item_cap[p], sms * per_sm[p]);
+  memset(B->host, 0, hoff);
+  B->ctl_h = reinterpret_cast<EvalCtl*>(B->host + h_ctl);
+  B->res_h = reinterpret_cast<EvalResult*>(B->host + h_res);
+  B->counts_h = reinterpret_cast<int*>(B->host + h_counts);
+  B->vgrid.assign(capacity, {});
+  for (auto& v : B->vgrid) v.fill(0);
+  B->members.assign(capacity, BatchMember());
+  return B.release();
+}
+
+void batch_destroy(BatchRun* B) { delete B; }
+
+// Whether the job can run in a batch: the FFT Poisson form with its
+// shared-memory passes (the batched kernels' form).
+bool batch_eligible(const gpl_job* j) {
+  return j->np_ready && j->d.poisson_path == 1 &&
+         !(j->d.cnt_x == j->d.cnt_y && (j->d.cnt_x == 512 || j->d.cnt_x == 1024));
+}
+
+// The job takes member slot `slot`: its argument tables (its control and
+// result records redirected to the batch's slots) and its blocks per phase.
+int batch_join(BatchRun* B, int slot, gpl_job* j, int max_iters, gpl_iter_log* log) {
+  if (slot < 0 || slot >= B->cap || B->members[slot].job) { set_error("batch: slot in use"); return GPL_ERR_BAD_STATE; }
+  if (!batch_eligible(j)) {
+    set_error("batched Nesterov loop: the job does not run the block-form FFT Poisson passes (its grid is "
+              "512 x 512 or 1024 x 1024, or it runs the tensor-core form); run it alone");
+    return GPL_ERR_INVALID_ARG;
+  }
+  if (j->device != B->device) { set_error("batch: the job is on another device"); return GPL_ERR_INVALID_ARG; }
+  DeviceModel& d = j->d;
+  std::vector<char> buf;
+  size_t total = 0;
+  for (int t = 0; t < kTables; t++) total += B->stride[t];
+  buf.assign(total, 0);
+  char* part[kTables];
+  size_t o = 0;
+  for (int t = 0; t < kTables; t++) { part[t] = buf.data() + o; o += B->stride[t]; }
+  EvalCtl* own_ctl = d.ctl;
+  EvalResult* own_res = d.result;
+  d.ctl = B->ctl_d + slot;
+  d.result = B->res_d + slot;
+  write_scatter_batch_args(d, part[kTScatter]);
+  write_wa_batch_args(d, base_args(j), part[kTWa]);
+  write_cell_batch_args(d, base_args(j), part[kTCell]);
+  int g3[3];
+  size_t sm3[3];
+  const bool ok = write_poisson_batch_args(d, part[kTPa], part[kTPb], part[kTPc], g3, sm3);
+  d.ctl = own_ctl;
+  d.result = own_res;
+  if (!ok) { set_error("batch: Poisson arguments"); return GPL_ERR_INVALID_ARG; }
+  // the job's own stream may still hold work (initialisation)
+  GPL_CUDA(cudaStreamSynchronize(j->stream));
+  for (int t = 0; t < kTables; t++)
+    GPL_CUDA(cudaMemcpyAsync(B->args[t] + (size_t)slot * B->stride[t], part[t], B->stride[t],
+                             cudaMemcpyHostToDevice, B->s));
+  GPL_CUDA(cudaStreamSynchronize(B->s));       // the staging buffer is local
+  std::array<int, kBPhases>& v = B->vgrid[slot];
+  v.fill(0);
+  v[kBScatter] = d.max_chunks;
+  v[kBScatterBig] = d.n_big;
+  v[kBDgradBig] = d.n_big;
+  v[kBCell] = cell_grid(d);
+  int small = 0, large = 0;
+  wa_launch_blocks(d, &small, &large);
+  v[d.net_weighted ? kBWaSmallW : kBWaSmall] = small;
+  v[d.net_weighted ? kBWaLargeW : kBWaLarge] = large;
+  for (int q = 0; q < 3; q++) v[kBPoissonA + q] = g3[q];
+  const size_t ss = scatter_smem(d);
+  if (ss > B->smem_scatter) { B->smem_scatter = ss; B->graph_dirty = true; }
+  for (int q = 0; q < 3; q++)
+    if (sm3[q] > B->smem_p[q]) { B->smem_p[q] = sm3[q]; B->graph_dirty = true; }
+  for (int p = 0; p < kBPhases; p++)
+    if (v[p] && !B->phase_used[p]) { B->phase_used[p] = true; B->graph_dirty = true; }
+  BatchMember& m = B->members[slot];
+  m = BatchMember();
+  m.job = j;
+  m.limit = max_iters;
+  m.log = log;
+  const NesterovState& S = j->S;
+  m.running = !S.finished && S.iter < S.max_iter && S.diverge_code != GPL_ERR_DIVERGED_INIT;
+  B->items_dirty = true;
   return GPL_OK;
 }
 
-// Work items of the running jobs (`on`): instance k's blocks of each phase.
-int batch_items(BatchRun& B, const std::vector<char>& on) {
+void batch_leave(BatchRun* B, int slot) {
+  if (slot < 0 || slot >= B->cap) return;
+  B->members[slot] = BatchMember();
+  B->vgrid[slot].fill(0);
+  B->items_dirty = true;
+}
+
+namespace {
+
+// Work items of the running members: slot k's blocks of each phase.
+int batch_items(BatchRun& B) {
+  int total = 0;
+  for (int p = 0; p < kBPhases; p++)
+    for (int k = 0; k < B.cap; k++)
+      if (B.members[k].job && B.members[k].running) total += B.vgrid[k][p];
+  if (total > B.items_cap) {
+    const int cap = std::max(total, 2 * B.items_cap);
+    if (B.items_d) cudaFree(B.items_d);
+    if (B.items_h) cudaFreeHost(B.items_h);
+    B.items_d = nullptr;
+    B.items_h = nullptr;
+    B.items_cap = 0;
+    GPL_CUDA(cudaMalloc(&B.items_d, sizeof(int4) * cap));
+    GPL_CUDA(cudaMallocHost(&B.items_h, sizeof(int4) * cap));
+    B.items_cap = cap;
+    B.graph_dirty = true;              // the launches read the new buffer
+  }
+  int at = 0;
   for (int p = 0; p < kBPhases; p++) {
+    B.item_off[p] = at;
     int c = 0;
-    int4* dst = B.items_h + B.item_off[p];
-    for (int k = 0; k < B.n; k++) {
-      if (!on[k]) continue;
+    for (int k = 0; k < B.cap; k++) {
+      const BatchMember& m = B.members[k];
+      if (!m.job || !m.running) continue;
       const int vg = B.vgrid[k][p];
-      for (int vb = 0; vb < vg; vb++) dst[c++] = make_int4(k, vb, vg, 0);
+      for (int vb = 0; vb < vg; vb++) B.items_h[at + c++] = make_int4(k, vb, vg, 0);
     }
     B.counts_h[p] = c;
+    at += c;
   }
-  int total = 0;
-  for (int p = 0; p < kBPhases; p++) total += B.item_cap[p];
-  if (total) GPL_CUDA(cudaMemcpyAsync(B.items_d, B.items_h, sizeof(int4) * total, cudaMemcpyHostToDevice, B.s));
+  if (at) GPL_CUDA(cudaMemcpyAsync(B.items_d, B.items_h, sizeof(int4) * at, cudaMemcpyHostToDevice, B.s));
   GPL_CUDA(cudaMemcpyAsync(B.counts_d, B.counts_h, sizeof(int) * kBPhases, cudaMemcpyHostToDevice, B.s));
+  // the item offsets are launch arguments: a new layout is a new graph
+  static_assert(kBPhases <= 16, "phase table");
+  B.graph_dirty = true;
+  B.items_dirty = false;
   return GPL_OK;
 }
 
-// One round: control records up, every phase, result records down.
+// One round's launches: control records up, every phase in use, result
+// records down.  Persistent grids of about the per-job kernels' residency.
 int batch_launch_round(BatchRun& B) {
+  static const int per_sm[kBPhases] = {4, 4, 5, 1, 5, 1, 4, 4, 4, 4, 4};
   long long nl = 0;
-  GPL_CUDA(cudaMemcpyAsync(B.ctl_d, B.ctl_h, sizeof(EvalCtl) * B.n, cudaMemcpyHostToDevice, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.ctl_d, B.ctl_h, sizeof(EvalCtl) * B.cap, cudaMemcpyHostToDevice, B.s));
   auto items = [&](int p) { return B.items_d + B.item_off[p]; };
   auto count = [&](int p) { return B.counts_d + p; };
+  auto grid = [&](int p) { return B.sms * per_sm[p]; };
   int rc = GPL_OK;
-  if (B.grid[kBScatter]) {
-    rc = launch_density_batch(kBScatter, B.args[kTScatter], items(kBScatter), count(kBScatter), B.grid[kBScatter],
+  if (B.phase_used[kBScatter]) {
+    rc = launch_density_batch(kBScatter, B.args[kTScatter], items(kBScatter), count(kBScatter), grid(kBScatter),
                               B.smem_scatter, B.s);
     nl++;
   }
-  if (!rc && B.grid[kBScatterBig]) {
+  if (!rc && B.phase_used[kBScatterBig]) {
     rc = launch_density_batch(kBScatterBig, B.args[kTScatter], items(kBScatterBig), count(kBScatterBig),
-                              B.grid[kBScatterBig], 0, B.s);
+                              grid(kBScatterBig), 0, B.s);
     nl++;
   }
   const int wa_phase[4] = {kBWaSmall, kBWaLarge, kBWaSmallW, kBWaLargeW};
   for (int q = 0; q < 4 && !rc; q++) {
     const int p = wa_phase[q];
-    if (!B.grid[p]) continue;
-    rc = launch_wa_batch(q & 1, q >= 2, B.args[kTWa], items(p), count(p), B.grid[p], B.s);
+    if (!B.phase_used[p]) continue;
+    rc = launch_wa_batch(q & 1, q >= 2, B.args[kTWa], items(p), count(p), grid(p), B.s);
     nl++;
   }
   for (int q = 0; q < 3 && !rc; q++) {
     const int p = kBPoissonA + q;
-    if (!B.grid[p]) continue;
-    rc = launch_poisson_batch(q, B.args[kTPa + q], items(p), count(p), B.grid[p], B.smem_p[q], B.s);
+    if (!B.phase_used[p]) continue;
+    rc = launch_poisson_batch(q, B.args[kTPa + q], items(p), count(p), grid(p), B.smem_p[q], B.s);
     nl++;
   }
-  if (!rc && B.grid[kBDgradBig]) {
-    rc = launch_density_batch(kBDgradBig, B.args[kTCell], items(kBDgradBig), count(kBDgradBig), B.grid[kBDgradBig],
+  if (!rc && B.phase_used[kBDgradBig]) {
+    rc = launch_density_batch(kBDgradBig, B.args[kTCell], items(kBDgradBig), count(kBDgradBig), grid(kBDgradBig),
                               0, B.s);
     nl++;
   }
-  if (!rc && B.grid[kBCell]) {
-    rc = launch_density_batch(kBCell, B.args[kTCell], items(kBCell), count(kBCell), B.grid[kBCell], 0, B.s);
+  if (!rc && B.phase_used[kBCell]) {
+    rc = launch_density_batch(kBCell, B.args[kTCell], items(kBCell), count(kBCell), grid(kBCell), 0, B.s);
     nl++;
   }
   if (rc) return rc;
-  GPL_CUDA(cudaMemcpyAsync(B.res_h, B.res_d, sizeof(EvalResult) * B.n, cudaMemcpyDeviceToHost, B.s));
+  GPL_CUDA(cudaMemcpyAsync(B.res_h, B.res_d, sizeof(EvalResult) * B.cap, cudaMemcpyDeviceToHost, B.s));
   B.launches_per_round = nl;
   return GPL_OK;
 }
 
 // The round as one CUDA graph (a failure leaves direct launches).
 void batch_capture(BatchRun& B) {
+  if (B.exec) { cudaGraphExecDestroy(B.exec); B.exec = nullptr; }
+  B.graph_dirty = false;
   cudaGraph_t g = nullptr;
   if (cudaStreamBeginCapture(B.s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
@@ -1341,81 +1392,107 @@ void batch_capture(BatchRun& B) {
   cudaGetLastError();
 }
 
-int batch_run(const std::vector<gpl_job*>& jobs, int max_iters, gpl_iter_log* const* logs,
-              long long* launches) {
-  const int n = (int)jobs.size();
-  BatchRun B;
-  int rc = batch_setup(B, jobs);
-  if (rc) return rc;
-  // the jobs' own streams may still hold work (initialisation)
-  for (gpl_job* j : jobs) GPL_CUDA(cudaStreamSynchronize(j->stream));
-  std::vector<char> on(n, 0), start(n, 1);
-  std::vector<int> done(n, 0);
-  for (int k = 0; k < n; k++) {
-    const NesterovState& S = jobs[k]->S;
-    on[k] = !S.finished && S.iter < S.max_iter && S.diverge_code != GPL_ERR_DIVERGED_INIT;
+}  // namespace
+
+// One round over the running members: each one's next evaluation, then its
+// control.  Members whose loop ended (stop rule, divergence, iteration limit
+// of this run) stop running; the caller sees m.running == false.
+int batch_round(BatchRun* Bp, long long* launches) {
+  BatchRun& B = *Bp;
+  int running = 0;
+  for (const BatchMember& m : B.members) running += (m.job && m.running) ? 1 : 0;
+  if (!running) return GPL_OK;
+  if (B.items_dirty) {
+    int rc = batch_items(B);
+    if (rc) return rc;
   }
-  rc = batch_items(B, on);
-  if (rc) return rc;
-  batch_capture(B);
+  if (B.graph_dirty) batch_capture(B);
   long long nl = 0;
-  for (;;) {
-    int running = 0;
-    for (int k = 0; k < n; k++) running += on[k] ? 1 : 0;
-    if (!running) break;
-    for (int k = 0; k < n; k++) {
-      if (!on[k]) continue;
-      gpl_job* j = jobs[k];
-      NesterovState& S = j->S;
-      if (start[k]) {
-        start_iteration(S);
-        if (S.iter % kTileOrderEvery == 0) {
-          rc = launch_tile_order(j->d, S.i_cur, B.s, j->timer);
-          if (rc) return rc;
-          S.refreshes++;
-          nl += 3;
-        }
-        start[k] = 0;
+  for (int k = 0; k < B.cap; k++) {
+    BatchMember& m = B.members[k];
+    if (!m.job || !m.running) continue;
+    NesterovState& S = m.job->S;
+    if (m.start) {
+      start_iteration(S);
+      if (S.iter % kTileOrderEvery == 0) {
+        int rc = launch_tile_order(m.job->d, S.i_cur, B.s, m.job->timer);
+        if (rc) return rc;
+        S.refreshes++;
+        nl += 3;
       }
-      B.ctl_h[k] = next_ctl(S);
+      m.start = false;
     }
-    if (B.exec) {
-      GPL_CUDA(cudaGraphLaunch(B.exec, B.s));
-    } else {
-      rc = batch_launch_round(B);
-      if (rc) return rc;
-    }
-    nl += B.launches_per_round;
-    GPL_CUDA(cudaStreamSynchronize(B.s));
-    bool changed = false;
-    for (int k = 0; k < n; k++) {
-      if (!on[k]) continue;
-      gpl_job* j = jobs[k];
-      NesterovState& S = j->S;
-      IterEntry e;
-      bool logged = false;
-      const int a = after_eval(S, B.res_h[k], &e, &logged);
-      if (logged) record_iteration(j, e, S.iter, logs ? logs[k] : nullptr);
-      if (a == kRetry) continue;
-      start[k] = 1;
-      done[k]++;
-      if (S.finished || S.iter >= S.max_iter || (max_iters > 0 && done[k] >= max_iters)) {
-        on[k] = 0;
-        changed = true;
-        if (S.finished && !S.diverge_code && j->m.p.verbose_level > 0) {
-          printf("[NesterovSolve] Finished with Overflow: %g\n", S.sum_overflow);
-          fflush(stdout);
-        }
+    B.ctl_h[k] = next_ctl(S);
+  }
+  if (B.exec) {
+    GPL_CUDA(cudaGraphLaunch(B.exec, B.s));
+  } else {
+    int rc = batch_launch_round(B);
+    if (rc) return rc;
+  }
+  nl += B.launches_per_round;
+  GPL_CUDA(cudaStreamSynchronize(B.s));
+  for (int k = 0; k < B.cap; k++) {
+    BatchMember& m = B.members[k];
+    if (!m.job || !m.running) continue;
+    gpl_job* j = m.job;
+    NesterovState& S = j->S;
+    IterEntry e;
+    bool logged = false;
+    const int a = after_eval(S, B.res_h[k], &e, &logged);
+    if (logged) record_iteration(j, e, S.iter, m.log);
+    if (a == kRetry) continue;
+    m.start = true;
+    m.done++;
+    if (S.finished || S.iter >= S.max_iter || (m.limit > 0 && m.done >= m.limit)) {
+      m.running = false;
+      B.items_dirty = true;
+      if (S.finished && !S.diverge_code && j->m.p.verbose_level > 0) {
+        printf("[NesterovSolve] Finished with Overflow: %g\n", S.sum_overflow);
+        fflush(stdout);
       }
-    }
-    if (changed) {
-      rc = batch_items(B, on);
-      if (rc) return rc;
     }
   }
-  if (launches) *launches = nl;
+  if (launches) *launches += nl;
   return GPL_OK;
 }
+
+bool batch_running(const BatchRun* B, int slot) {
+  return slot >= 0 && slot < B->cap && B->members[slot].job && B->members[slot].running;
+}
+
+int batch_count_running(const BatchRun* B) {
+  int n = 0;
+  for (const BatchMember& m : B->members) n += (m.job && m.running) ? 1 : 0;
+  return n;
+}
+
+void batch_stop_member(BatchRun* B, int slot) {
+  if (slot < 0 || slot >= B->cap || !B->members[slot].job) return;
+  B->members[slot].running = false;
+  B->items_dirty = true;
+}
+
+// A member's loop status after it stopped running (gpl_nesterov_run's).
+int batch_member_status(gpl_job* j, gpl_nesterov_stats* o) {
+  const int st = j->S.diverge_code == GPL_ERR_DIVERGED_INIT ? j->S.diverge_code : end_of_run(j);
+  if (o) {
+    o->iterations = j->S.iter;
+    o->evaluations = j->S.evals;
+    o->finished = j->S.finished ? 1 : 0;
+    o->status = j->S.diverge_code;
+    o->overflow = j->S.sum_overflow;
+    o->step_length = j->S.step_length;
+    o->density_penalty = j->S.density_penalty;
+    o->wire_length_coef = j->S.wl_coef_x;
+    o->hpwl = j->S.prev_hpwl;
+  }
+  return st;
+}
+
+}  // namespace gpl
+
+namespace {
 
 void fill_info(gpl_job* j, gpl_job_info* info) {
   if (!info) return;
@@ -1653,38 +1730,40 @@ gpl_status gpl_nesterov_run(gpl_job* j, int32_t max_iters, gpl_nesterov_stats* s
 gpl_status gpl_batch_nesterov_run(gpl_job* const* jobs, int32_t n_jobs, int32_t max_iters,
                                   gpl_nesterov_stats* stats, gpl_status* status, int64_t* kernel_launches) {
   if (!jobs || n_jobs <= 0) { set_error("gpl_batch_nesterov_run: no jobs"); return GPL_ERR_INVALID_ARG; }
-  std::vector<gpl_job*> v(jobs, jobs + n_jobs);
   for (int k = 0; k < n_jobs; k++) {
-    if (!v[k]) { set_error("gpl_batch_nesterov_run: null job"); return GPL_ERR_INVALID_ARG; }
-    if (!v[k]->np_ready) { set_error("gpl_batch_nesterov_run: call gpl_nesterov_init first"); return GPL_ERR_BAD_STATE; }
-    if (v[k]->device != v[0]->device) {
+    if (!jobs[k]) { set_error("gpl_batch_nesterov_run: null job"); return GPL_ERR_INVALID_ARG; }
+    if (!jobs[k]->np_ready) { set_error("gpl_batch_nesterov_run: call gpl_nesterov_init first"); return GPL_ERR_BAD_STATE; }
+    if (jobs[k]->device != jobs[0]->device) {
       set_error("gpl_batch_nesterov_run: the jobs must be on one device");
       return GPL_ERR_INVALID_ARG;
     }
     for (int q = 0; q < k; q++)
-      if (v[q] == v[k]) { set_error("gpl_batch_nesterov_run: a job is listed twice"); return GPL_ERR_INVALID_ARG; }
+      if (jobs[q] == jobs[k]) { set_error("gpl_batch_nesterov_run: a job is listed twice"); return GPL_ERR_INVALID_ARG; }
   }
-  cudaSetDevice(v[0]->device);
+  for (int k = 0; k < n_jobs; k++)
+    if (!batch_eligible(jobs[k])) {
+      set_error("gpl_batch_nesterov_run: job " + std::to_string(k) +
+                " does not run the block-form FFT Poisson passes (its grid is 512 x 512 or 1024 x 1024, or it "
+                "runs the tensor-core form); run it alone");
+      return GPL_ERR_INVALID_ARG;
+    }
+  int rc = GPL_OK;
+  std::unique_ptr<BatchRun, void (*)(BatchRun*)> B(batch_create(jobs[0]->device, n_jobs, &rc), batch_destroy);
+  if (!B) return (gpl_status)rc;
+  for (int k = 0; k < n_jobs && !rc; k++) rc = batch_join(B.get(), k, jobs[k], max_iters, nullptr);
   long long nl = 0;
-  int rc = batch_run(v, max_iters, nullptr, &nl);
+  for (;;) {
+    if (rc) break;
+    bool any = false;
+    for (const BatchMember& m : B->members) any |= m.job && m.running;
+    if (!any) break;
+    rc = batch_round(B.get(), &nl);
+  }
   if (kernel_launches) *kernel_launches = nl;
   if (rc) return (gpl_status)rc;
   for (int k = 0; k < n_jobs; k++) {
-    gpl_job* j = v[k];
-    const int st = j->S.diverge_code == GPL_ERR_DIVERGED_INIT ? j->S.diverge_code : end_of_run(j);
+    const int st = batch_member_status(jobs[k], stats ? &stats[k] : nullptr);
     if (status) status[k] = (gpl_status)st;
-    if (stats) {
-      gpl_nesterov_stats& o = stats[k];
-      o.iterations = j->S.iter;
-      o.evaluations = j->S.evals;
-      o.finished = j->S.finished ? 1 : 0;
-      o.status = j->S.diverge_code;
-      o.overflow = j->S.sum_overflow;
-      o.step_length = j->S.step_length;
-      o.density_penalty = j->S.density_penalty;
-      o.wire_length_coef = j->S.wl_coef_x;
-      o.hpwl = j->S.prev_hpwl;
-    }
   }
   return GPL_OK;
 }

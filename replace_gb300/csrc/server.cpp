@@ -10,6 +10,14 @@
 // ordinary job path (initial place, Nesterov init, Nesterov loop in chunks)
 // on its slot's stream; its evaluations replay the job's own CUDA graph, so
 // the kernels of all admitted jobs overlap on the device.
+//
+// Batched mode (gpl_server_params.batched): after its initial place and
+// Nesterov init on its slot, a job joins one running batch (the batched
+// form of the Nesterov loop, BatchRun in job.cu): a batch thread runs
+// rounds in which every member's next evaluation goes into one launch per
+// phase, admits new members between rounds and retires members whose loop
+// ended; the slot thread then finishes the job as before.  A member's
+// result is bit-identical to the same job run alone.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -38,6 +46,10 @@ struct Entry {
   gpl_job* job = nullptr;
   int64_t bytes = 0;
   std::atomic<bool> cancel{false};
+  // batched mode: set by the batch thread when the job's loop ended there
+  bool batch_done = false;
+  int batch_rc = 0;
+  bool batch_cancelled = false;
   gpl_server_result res{};
   std::vector<int32_t> lx, ly;
 };
@@ -66,6 +78,12 @@ struct gpl_server {
   std::deque<int64_t> unpolled;
   int64_t next_ticket = 1;
   bool stop = false;
+  // batched mode: the batch thread, its batch, and the jobs waiting to join
+  std::thread batcher;
+  BatchRun* batch = nullptr;
+  std::deque<std::pair<int, Entry*>> batch_in;
+  std::condition_variable cv_batch;   // a job joins, a slot thread ends, or stop
+  int workers_exited = 0;
   std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
 
   double now() const {
@@ -84,7 +102,25 @@ void run_job(gpl_server* s, int slot, Entry& e) {
   if (s->p.run_initial_place) rc = gpl_initial_place(j, &ip);
   if (!rc) rc = gpl_nesterov_init(j, nullptr);
   gpl_nesterov_stats st{};
-  while (!rc) {
+  if (!rc && s->batch && batch_eligible(j)) {
+    // the loop runs in the batch; this thread waits for its end
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->batch_in.emplace_back(slot, &e);
+      s->cv_batch.notify_all();
+      s->cv_done.wait(lk, [&] { return e.batch_done; });
+    }
+    if (e.batch_rc) {
+      rc = e.batch_rc;
+    } else if (e.batch_cancelled) {
+      rc = GPL_ERR_CANCELLED;
+      set_error("cancelled");
+      batch_member_status(j, &st);
+    } else {
+      rc = batch_member_status(j, &st);
+    }
+  }
+  while (!rc && !st.finished && !e.batch_done) {
     if (e.cancel.load()) {
       rc = GPL_ERR_CANCELLED;
       set_error("cancelled");
@@ -109,7 +145,70 @@ void run_job(gpl_server* s, int slot, Entry& e) {
   host_wait(s->streams[slot], s->sync_ev[slot]); // the memory is back in the pool
 }
 
+// Batched mode: runs rounds while members run; takes joining jobs between
+// rounds, retires members whose loop ended (or that were cancelled) and
+// wakes their slot threads.
+void batcher(gpl_server* s) {
+  cudaSetDevice(s->p.device);
+  std::vector<Entry*> member(s->p.max_active, nullptr);
+  for (;;) {
+    std::deque<std::pair<int, Entry*>> joining;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      // at stop, the batch serves until every slot thread has ended (a slot
+      // may still be initialising a job that will join)
+      const int n_slots = s->p.max_active;
+      s->cv_batch.wait(lk, [&] {
+        return (s->stop && s->workers_exited == n_slots) || !s->batch_in.empty() ||
+               batch_count_running(s->batch) > 0;
+      });
+      joining.swap(s->batch_in);
+      if (joining.empty() && batch_count_running(s->batch) == 0) return;   // stopped, slots ended
+    }
+    std::vector<Entry*> ended;
+    for (auto& jn : joining) {
+      const int rc = batch_join(s->batch, jn.first, jn.second->job, 0, nullptr);
+      if (rc) {
+        jn.second->batch_rc = rc;
+        ended.push_back(jn.second);
+      } else {
+        member[jn.first] = jn.second;
+      }
+    }
+    for (int k = 0; k < (int)member.size(); k++)
+      if (member[k] && member[k]->cancel.load() && batch_running(s->batch, k)) {
+        member[k]->batch_cancelled = true;
+        batch_stop_member(s->batch, k);
+      }
+    long long nl = 0;
+    int rc = batch_round(s->batch, &nl);
+    for (int k = 0; k < (int)member.size(); k++) {
+      if (!member[k]) continue;
+      if (rc) member[k]->batch_rc = rc;
+      if (rc || !batch_running(s->batch, k)) {
+        batch_leave(s->batch, k);
+        ended.push_back(member[k]);
+        member[k] = nullptr;
+      }
+    }
+    if (!ended.empty()) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (Entry* e : ended) e->batch_done = true;
+      s->cv_done.notify_all();
+    }
+  }
+}
+
+void worker_loop(gpl_server* s, int slot);
+
 void worker(gpl_server* s, int slot) {
+  worker_loop(s, slot);
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->workers_exited++;
+  s->cv_batch.notify_all();
+}
+
+void worker_loop(gpl_server* s, int slot) {
   cudaSetDevice(s->p.device);
   for (;;) {
     std::shared_ptr<Entry> e;
@@ -153,6 +252,7 @@ void gpl_server_params_default(gpl_server_params* p) {
   p->chunk_iters = 64;
   p->run_initial_place = 1;
   p->blocking_sync = 1;
+  p->batched = 0;
 }
 
 gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out) {
@@ -195,7 +295,13 @@ gpl_status gpl_server_create(const gpl_server_params* p, gpl_server** out) {
       GPL_CUDA(cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming));
     s->sync_ev.push_back(ev);
   }
+  if (p->batched) {
+    int rc = GPL_OK;
+    s->batch = batch_create(p->device, p->max_active, &rc);
+    if (!s->batch) return (gpl_status)rc;
+  }
   gpl_server* raw = s.release();
+  if (raw->batch) raw->batcher = std::thread(batcher, raw);
   for (int k = 0; k < p->max_active; k++) raw->workers.emplace_back(worker, raw, k);
   *out = raw;
   return GPL_OK;
@@ -210,8 +316,10 @@ gpl_status gpl_server_submit_weighted(gpl_server* s, const gpl_netlist_desc* nl,
                                       const float* weights, int64_t n_nets, int64_t* ticket) {
   if (!s || !nl || !p || !ticket) { set_error("null argument"); return GPL_ERR_INVALID_ARG; }
   if (p->device != s->p.device) { set_error("job device differs from the server's"); return GPL_ERR_INVALID_ARG; }
+  gpl_params prm = *p;
+  if (s->p.batched && prm.poisson_path == 0) prm.poisson_path = 1;   // the batched kernels' form
   gpl_job* j = nullptr;
-  int rc = job_new(nl, p, &j);
+  int rc = job_new(nl, &prm, &j);
   if (rc) return (gpl_status)rc;
   if (weights) {
     // stored on the host now, uploaded with the job's device model
@@ -219,7 +327,7 @@ gpl_status gpl_server_submit_weighted(gpl_server* s, const gpl_netlist_desc* nl,
     if (rc) { gpl_destroy(j); return (gpl_status)rc; }
   }
   int64_t bytes = 0;
-  rc = job_device_bytes(j, &bytes, s->p.run_initial_place && !p->incremental_place_mode);
+  rc = job_device_bytes(j, &bytes, s->p.run_initial_place && !prm.incremental_place_mode);
   if (rc) { gpl_destroy(j); return (gpl_status)rc; }
   bytes += kJobSlack;
   if (bytes > s->budget) {
@@ -333,7 +441,10 @@ void gpl_server_destroy(gpl_server* s) {
     for (auto& r : s->running) r.second->cancel = true;
   }
   s->cv_work.notify_all();
+  s->cv_batch.notify_all();
   for (auto& t : s->workers) t.join();
+  if (s->batcher.joinable()) s->batcher.join();
+  if (s->batch) batch_destroy(s->batch);
   for (auto& e : dropped) gpl_destroy(e->job);
   cudaSetDevice(s->p.device);
   for (auto st : s->streams) {

@@ -8,7 +8,9 @@ GPU (gpl_server_* in include/gpl.h).
 
 Jobs are admitted in submission order as slots and HBM free up; admitted
 jobs run concurrently on their own streams and retire when their Nesterov
-loop ends.  A job's result does not depend on the other jobs in the mix.
+loop ends.  With batched=True the admitted jobs' Nesterov loops run as one
+batch (one launch per phase for all of them; jobs join and leave between
+rounds).  A job's result does not depend on the other jobs in the mix.
 """
 
 from __future__ import annotations
@@ -35,13 +37,15 @@ def _result_dict(r: _abi.ServerResult) -> dict:
 
 class PlacementServer:
     def __init__(self, device: int = 0, max_active: int = 8, hbm_budget_bytes: int = 0,
-                 chunk_iters: int = 64, run_initial_place: bool = True, blocking_sync: bool = True):
+                 chunk_iters: int = 64, run_initial_place: bool = True, blocking_sync: bool = True,
+                 batched: bool = False):
         self.lib = load()
         p = _abi.ServerParams()
         self.lib.gpl_server_params_default(C.byref(p))
         p.device, p.max_active, p.hbm_budget_bytes = device, max_active, hbm_budget_bytes
         p.chunk_iters, p.run_initial_place = chunk_iters, 1 if run_initial_place else 0
         p.blocking_sync = 1 if blocking_sync else 0
+        p.batched = 1 if batched else 0
         self.params = p
         h = C.c_void_p()
         check(self.lib.gpl_server_create(C.byref(p), C.byref(h)))

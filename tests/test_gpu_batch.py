@@ -95,3 +95,33 @@ def test_batch_rejects_warp_form_grids(gpu_lib):
     assert e.value.status == _abi.GPL_ERR_INVALID_ARG
     ok.close()
     big.close()
+
+
+def test_batched_server_matches_alone_and_cancels(gpu_lib):
+    """The server's batched mode: jobs join the running batch after their
+    initialisation and leave it when their loop ends; every result equals
+    the job run alone.  A job cancelled while it runs in the batch ends
+    with the cancel code; the server shuts down with jobs still running."""
+    from replace_gb300 import PlacementServer
+    jobs = _jobs(n=10, seed=33, cells=(2_000, 20_000))
+    with PlacementServer(max_active=6, batched=True) as srv:
+        tickets = [srv.submit(nl, target_density=td, poisson_path=1) for nl, td in jobs]
+        res = {r["ticket"]: r for r in srv.wait_all(600)}
+        locs = {t: srv.locations(t, nl.n_insts) for t, (nl, _) in zip(tickets, jobs)}
+    spans = sorted((res[t]["admit_s"], res[t]["finish_s"]) for t in tickets)
+    assert any(spans[k + 1][0] < spans[k][1] for k in range(len(spans) - 1))
+    for t, (nl, td) in zip(tickets, jobs):
+        r = res[t]
+        rc, st, lx, ly = _alone(nl, td)
+        assert r["status"] == rc
+        assert r["iterations"] == st.iterations and r["hpwl"] == st.hpwl and r["finished"] == st.finished
+        assert np.array_equal(locs[t][0], lx) and np.array_equal(locs[t][1], ly)
+    big = N.generate(40_000, 42_000, n_io=100, seed=4)
+    with PlacementServer(max_active=3, batched=True) as srv:
+        t = srv.submit(big, target_density=0.7, poisson_path=1)
+        import time
+        time.sleep(1.0)
+        srv.cancel(t)
+        r = srv.wait_all(600)[0]
+        assert r["status"] in (0, 21)              # done before the cancel arrived, or cancelled
+        srv.submit(big, target_density=0.7, poisson_path=1)   # left running at shutdown
