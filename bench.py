@@ -16,9 +16,10 @@ At one GPU the line also carries `serving`: the batch of config 4 (64 jobs
 of 2k-50k cells submitted at once to the placement server, against the same
 jobs placed one at a time), its batched form (the jobs' Nesterov loops in
 one persistent launch per phase, and the server in batched mode) and the
-serving form (the first --stream-jobs
-requests of a 500-job Poisson stream at 2 jobs/s, 5k-500k cells, against a
-one-job-at-a-time server): placements/h and p50/p99 job latency.
+serving form (the first --stream-jobs requests of the 500-job Poisson stream
+at 2 jobs/s, 5k-500k cells, against a one-job-at-a-time server; and the
+first --saturating-jobs requests at 20 jobs/s, where arrivals outpace the
+GPU): placements/h and p50/p99 job latency.
 """
 
 from __future__ import annotations
@@ -300,28 +301,30 @@ def batched_form(n_jobs, slots, device):
     }
 
 
-def serving_stream(n_jobs, slots, device):
-    """The serving form on a bounded sample: the first n_jobs requests of the
-    500-job Poisson stream (2 jobs/s; 5k-500k cells; 10 % mixed-size),
-    submitted at their arrival times to a server with `slots` slots and to a
-    one-slot server (one job at a time, FIFO).  Latency = end of the job -
-    its arrival (host netlist conversion and submission included)."""
+def serving_stream(n_jobs, slots, device, rate_scale=1.0, arms=("server", "one_at_a_time")):
+    """The serving form: the first n_jobs requests of the 500-job Poisson
+    stream (2 jobs/s; 5k-500k cells; 10 % mixed-size), submitted at their
+    arrival times (divided by rate_scale: 10 means ten times as many jobs
+    per second) to a server with `slots` slots ("server"), the same server
+    in batched mode ("server_batched") and a one-slot server, one job at a
+    time, FIFO ("one_at_a_time").  Latency = end of the job - its arrival
+    (host netlist conversion and submission included)."""
     import numpy as np
     from replace_gb300 import PlacementServer, netlist as N
     spec = N.job_stream_spec(500, 2.0, seed=5)[:n_jobs]
     nets = [N.stream_job(s) for s in spec]
     base = spec[0]["arrival_s"]
 
-    def run(k):
-        with PlacementServer(device=device, max_active=k) as srv:
+    def run(k, batched):
+        with PlacementServer(device=device, max_active=k, batched=batched) as srv:
             t_create = time.perf_counter()
             arrive = {}
             for s, nl in zip(spec, nets):
-                due = t_create + (s["arrival_s"] - base)
+                due = t_create + (s["arrival_s"] - base) / rate_scale
                 while time.perf_counter() < due:
                     time.sleep(min(0.005, max(due - time.perf_counter(), 0)))
                 ta = time.perf_counter()
-                t = srv.submit(nl, target_density=s["td"])
+                t = srv.submit(nl, target_density=s["td"], poisson_path=1)
                 arrive[t] = ta - t_create
             res = srv.wait_all(3600)
         lat = np.array([r["finish_s"] - arrive[r["ticket"]] for r in res])
@@ -329,13 +332,23 @@ def serving_stream(n_jobs, slots, device):
         ok = sum(r["status"] == 0 and r["finished"] and r["overflow"] <= 0.1 for r in res)
         return {"slots": k, "placements_per_hour": len(res) / span * 3600.0, "span_s": span,
                 "p50_latency_s": float(np.percentile(lat, 50)),
-                "p99_latency_s": float(np.percentile(lat, 99)), "converged": int(ok)}
+                "p99_latency_s": float(np.percentile(lat, 99)), "converged": int(ok),
+                "hpwl": {int(r["ticket"]): int(r["hpwl"]) for r in res}}
 
-    srv = run(slots)
-    one = run(1)
-    return {"jobs": n_jobs, "of_stream": 500, "rate_per_s": 2.0,
-            "cells": "5k-500k log-uniform", "td": "0.60-0.90", "mixed_size_share": 0.10,
-            "server": srv, "one_at_a_time": one}
+    out = {"jobs": n_jobs, "of_stream": 500, "rate_per_s": 2.0 * rate_scale,
+           "arrival_span_s": (spec[-1]["arrival_s"] - base) / rate_scale,
+           "cells": "5k-500k log-uniform", "td": "0.60-0.90", "mixed_size_share": 0.10,
+           "poisson_form": "FFT (pinned, so that every arm computes the same placements)"}
+    runs = {}
+    for arm in arms:
+        runs[arm] = run(1, False) if arm == "one_at_a_time" else run(slots, arm == "server_batched")
+    hp = [r.pop("hpwl") for r in runs.values()]
+    out.update(runs)
+    out["same_results_in_every_arm"] = all(sorted(h.values()) == sorted(hp[0].values()) for h in hp)
+    if "server" in runs and "one_at_a_time" in runs:
+        out["server_vs_one_at_a_time_placements_per_hour"] = (runs["server"]["placements_per_hour"] /
+                                                              runs["one_at_a_time"]["placements_per_hour"])
+    return out
 
 
 def precision_form(nl, td, bins, device, stream, steps, warmup, fft_job):
@@ -464,7 +477,10 @@ def main():
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the whole-loop comparison with the reference's recorded run")
     ap.add_argument("--batch-jobs", type=int, default=64)
-    ap.add_argument("--stream-jobs", type=int, default=40)
+    ap.add_argument("--stream-jobs", type=int, default=40,
+                    help="requests of the 500-job stream replayed at 2 jobs/s (500: the whole stream)")
+    ap.add_argument("--saturating-jobs", type=int, default=120,
+                    help="requests of the stream replayed at 20 jobs/s, where the GPU is the limit")
     ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--workload", default=WORKLOAD,
                     help="named synthetic workload (replace_gb300.netlist.WORKLOADS)")
@@ -578,7 +594,10 @@ def main():
     if world == 1 and not args.no_serving:
         serving = {"batch": serving_batch(args.batch_jobs, args.slots, local_rank),
                    "batched_form": batched_form(args.batch_jobs, args.slots, local_rank),
-                   "stream": serving_stream(args.stream_jobs, args.slots, local_rank)}
+                   "stream": serving_stream(args.stream_jobs, args.slots, local_rank),
+                   "stream_saturating": serving_stream(args.saturating_jobs, args.slots, local_rank,
+                                                       rate_scale=10.0,
+                                                       arms=("server", "server_batched", "one_at_a_time"))}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -130,11 +130,12 @@ typedef struct gpl_params {
                                               cluster per axis (up to 65536 instances) */
   int32_t poisson_path;                    /* Poisson solve: 0 = auto (times both forms on the job's
                                               grid and keeps the faster; the GEMM form only up to
-                                              512 bins per axis, for precision: larger grids keep
-                                              the FFT form untimed), 1 = FFT (register FFTs per
-                                              warp on 512^2 and 1024^2 grids, shared-memory FFTs
-                                              otherwise), 2 = tensor-core GEMMs (bf16 three-term
-                                              split; grids with both counts multiples of 128) */
+                                              512 bins per axis, where it can be the faster: larger
+                                              grids keep the FFT form untimed), 1 = FFT (register
+                                              FFTs per warp on 512^2 and 1024^2 grids, shared-memory
+                                              FFTs otherwise), 2 = tensor-core GEMMs (each value
+                                              split into three bf16 terms, six products per GEMM;
+                                              grids with both counts multiples of 128) */
   int32_t scatter_tile;                    /* scatter tile side in bins (16, 32 or 64); 0 = chosen
                                               by timing at gpl_nesterov_init */
   int32_t scatter_chunk;                   /* gcells per scatter block (1024 or 2048); 0 = chosen

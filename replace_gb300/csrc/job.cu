@@ -604,13 +604,13 @@ int choose_poisson_path(gpl_job* j) {
     }
     return GPL_OK;
   }
-  // The split's error grows with the transform length: measured against the
-  // FP64 oracle, the density gradient is 2.8e-5 off at 128^2 and 1.4e-4 at
-  // 1024^2 (field 7e-6 and 2e-5).  Auto mode considers the GEMM form only up
-  // to 512 bins per axis, where it stays inside the 1e-4 bar (and sets up
-  // nothing for larger grids).
-  const bool precise_enough = d.cnt_x <= 512 && d.cnt_y <= 512;
-  if (want == 0 && !precise_enough) return GPL_OK;
+  // Auto mode considers the GEMM form only up to 512 bins per axis: above
+  // that it is measured slower than the register-FFT form (1024^2: 196 us
+  // against 59 us per solve), so larger grids set up nothing for it.  Its
+  // error against the FP64 oracle is within the bars at every size (field
+  // 7e-7 at 128^2, 2.6e-6 at 512^2, 5.3e-6 at 1024^2).
+  const bool worth_timing = d.cnt_x <= 512 && d.cnt_y <= 512;
+  if (want == 0 && !worth_timing) return GPL_OK;
   int rc = poisson_gemm_setup(d, &d.pg, j->pool, j->stream);
   if (rc) {
     if (want == 2) return rc;

@@ -2,12 +2,20 @@
 // src/fft.cpp:112-177) as dense transforms on the tensor cores: every 1-D
 // DCT-II / DCT-III / DST of the solve is a product with a constant n x n
 // matrix, computed by the tcgen05 GEMM (tc_gemm.cuh) in bf16 with a
-// three-term split: x = x_hi + x_lo (both bf16), and
-//   A * B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi,
-// one GEMM over K' = 3K with A stored as [hi | hi | lo] and B as
-// [hi | lo | hi] along K, accumulated in fp32.  The dropped lo * lo term
-// leaves an error near 2^-16 of each product (the FFT path is FP32-exact to
-// 1e-7).  Data layout, with rows listed first (D = A * B^T):
+// three-term split: x = x0 + x1 + x2 (bf16 each, 24 significant bits in
+// all: x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1), both
+// differences exact in fp32), and
+//   A * B ~ a0 b0 + a0 b1 + a0 b2 + a1 b0 + a1 b1 + a2 b0,
+// the six products of order <= 2, as one GEMM over K' = 6K with A stored as
+// [a2 | a1 | a1 | a0 | a0 | a0] and B as [b0 | b1 | b0 | b2 | b1 | b0] along
+// K, accumulated in fp32.  The dropped terms are near 2^-24 of each product.
+// The order matters: the tensor core's fp32 accumulation truncates, with an
+// error that grows with the accumulated length and the accumulator's size
+// (measured: 3e-7 relative at K = 256, 1.7e-6 at 1024, 2.3e-5 at 6144).
+// The small products go first, while the accumulator is small, and the
+// leading a0 b0 block last, so the result's error is about that of one
+// K-long product (a first layout with a0 b0 first gave 5e-5 on the field at
+// 1024 x 1024).  Data layout, with rows listed first (D = A * B^T):
 //   G1  T[j][u]   = rho[j][.]  . C2x[u][.]         density rows, DCT-II along x
 //   G2  S[u][v]   = T^T[u][.]  . C2y[v][.]         DCT-II along y -> spectrum^T;
 //                                                  the epilogue solves and
@@ -33,22 +41,44 @@ namespace {
 
 constexpr int kPgThreads = 256;
 
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn(x);
-  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+// Terms of the split along K (operand width kSplit * k for k values):
+// 6 = three bf16 terms per value and the six products of order <= 2;
+// 3 = two terms per value (hi, lo) and the products hi hi, hi lo, lo hi.
+#ifndef GPL_PG_SPLIT
+#define GPL_PG_SPLIT 6
+#endif
+constexpr int kSplit = GPL_PG_SPLIT;
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& t0, __nv_bfloat16& t1, __nv_bfloat16& t2) {
+  t0 = __float2bfloat16_rn(x);
+  const float r1 = __fsub_rn(x, __bfloat162float(t0));      // exact
+  t1 = __float2bfloat16_rn(r1);
+  t2 = __float2bfloat16_rn(__fsub_rn(r1, __bfloat162float(t1)));
 }
 
-// Row r of a split operand of width k: A pattern [hi | hi | lo], B pattern
-// [hi | lo | hi].
+// Column c of a split operand row of width k, smallest products first.
+// kSplit 6: A [t2 | t1 | t1 | t0 | t0 | t0], B [t0 | t1 | t0 | t2 | t1 | t0]
+// (products t2 t0, t1 t1, t1 t0, t0 t2, t0 t1, t0 t0).  kSplit 3: A
+// [t1 | t0 | t0], B [t0 | t1 | t0] (t1 t0, t0 t1, t0 t0).
 __device__ __forceinline__ void put_a(__nv_bfloat16* row, int k, int c, float x) {
-  __nv_bfloat16 hi, lo;
-  split_bf16(x, hi, lo);
-  row[c] = hi; row[k + c] = hi; row[2 * k + c] = lo;
+  __nv_bfloat16 t0, t1, t2;
+  split_bf16(x, t0, t1, t2);
+  if constexpr (kSplit == 6) {
+    row[c] = t2; row[k + c] = t1; row[2 * k + c] = t1;
+    row[3 * k + c] = t0; row[4 * k + c] = t0; row[5 * k + c] = t0;
+  } else {
+    row[c] = t1; row[k + c] = t0; row[2 * k + c] = t0;
+  }
 }
 __device__ __forceinline__ void put_b(__nv_bfloat16* row, int k, int c, float x) {
-  __nv_bfloat16 hi, lo;
-  split_bf16(x, hi, lo);
-  row[c] = hi; row[k + c] = lo; row[2 * k + c] = hi;
+  __nv_bfloat16 t0, t1, t2;
+  split_bf16(x, t0, t1, t2);
+  if constexpr (kSplit == 6) {
+    row[c] = t0; row[k + c] = t1; row[2 * k + c] = t0;
+    row[3 * k + c] = t2; row[4 * k + c] = t1; row[5 * k + c] = t0;
+  } else {
+    row[c] = t0; row[k + c] = t1; row[2 * k + c] = t0;
+  }
 }
 
 // Constant matrices, evaluated in double with exact argument reduction:
@@ -66,7 +96,7 @@ __global__ void k_pg_matrix(__nv_bfloat16* out, int rows, int n, int kind, int p
     double s, c;
     sincospi((double)num / (2.0 * n), &s, &c);
     double v = kind == 2 ? (k ? s * (double)w[k] : 0.0) : c;
-    __nv_bfloat16* row = out + (size_t)(row0 + m) * 3 * n;
+    __nv_bfloat16* row = out + (size_t)(row0 + m) * kSplit * n;
     if (pattern == 0) put_a(row, n, k, (float)v);
     else put_b(row, n, k, (float)v);
   }
@@ -81,7 +111,7 @@ struct PgArgs {
   const int64_t* nonplace;
   float* density;
   double* part_overflow;
-  __nv_bfloat16* rho_a;       // [ny][3 nx]
+  __nv_bfloat16* rho_a;       // [ny][kSplit nx]
 };
 
 // Density of every bin from the int64 areas (as pass A of the FFT path),
@@ -109,7 +139,12 @@ __global__ void __launch_bounds__(kPgThreads) k_pg_density(PgArgs A) {
     ac[b] = 0ull;
     ac[nb + b] = 0ull;
     A.density[b] = d;
-    put_a(A.rho_a + (size_t)j * 3 * A.nx, A.nx, i, d);
+    // The transforms take d - 1: a constant changes only the (0, 0)
+    // coefficient, which the solve sets to zero, and the density's mean is
+    // close to 1 (the fillers fill the free space to the target density), so
+    // the sums the tensor cores accumulate -- and their truncation error --
+    // shrink to the density's fluctuations.
+    put_a(A.rho_a + (size_t)j * kSplit * A.nx, A.nx, i, __fsub_rn(d, 1.0f));
   }
   double v = ovf;
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -132,7 +167,7 @@ struct EpiT {
   int ny;
   __device__ __forceinline__ void operator()(int j, int u0, const float (&v)[32]) const {
 #pragma unroll
-    for (int t = 0; t < 32; t++) put_a(out + (size_t)(u0 + t) * 3 * ny, ny, j, v[t]);
+    for (int t = 0; t < 32; t++) put_a(out + (size_t)(u0 + t) * kSplit * ny, ny, j, v[t]);
   }
 };
 
@@ -155,7 +190,7 @@ struct EpiS {
       const float wxu = __ldg(wx + u), wyv = __ldg(wy + vv);
       ph = __fdiv_rn(d, __fadd_rn(__fmul_rn(wxu, wxu), __fmul_rn(wyv, wyv)));
     }
-    put_b(out + (size_t)u * 3 * ny, ny, vv, ph);
+    put_b(out + (size_t)u * kSplit * ny, ny, vv, ph);
   }
 };
 
@@ -164,7 +199,7 @@ struct EpiP {
   static constexpr bool kRowMajor = true;
   __nv_bfloat16* out;
   int nx;
-  __device__ __forceinline__ void at(int y, int u, float v) const { put_a(out + (size_t)y * 3 * nx, nx, u, v); }
+  __device__ __forceinline__ void at(int y, int u, float v) const { put_a(out + (size_t)y * kSplit * nx, nx, u, v); }
 };
 
 // G5/G6/G7 epilogue: one component of the field (or phi) at [y][x].
@@ -204,10 +239,10 @@ void poisson_gemm_free(PoissonGemm* pg, cudaMemPool_t pool, cudaStream_t s) {
 }
 
 int64_t poisson_gemm_bytes(int nx, int ny) {
-  const size_t x3 = 3 * (size_t)nx, y3 = 3 * (size_t)ny;
+  const size_t xk = kSplit * (size_t)nx, yk = kSplit * (size_t)ny;
   size_t b = 0;
-  b += (size_t)nx * x3 + (size_t)ny * y3 + 2 * (size_t)ny * y3 + 2 * (size_t)nx * x3;   // constants
-  b += (size_t)ny * x3 + (size_t)nx * y3 + (size_t)nx * y3 + 2 * (size_t)ny * x3;       // data
+  b += (size_t)nx * xk + (size_t)ny * yk + 2 * (size_t)ny * yk + 2 * (size_t)nx * xk;   // constants
+  b += (size_t)ny * xk + (size_t)nx * yk + (size_t)nx * yk + 2 * (size_t)ny * xk;       // data
   return (int64_t)(b * 2 + 16 * 256);
 }
 
@@ -218,7 +253,7 @@ int poisson_gemm_setup(DeviceModel& d, PoissonGemm** out, cudaMemPool_t pool, cu
   if (!poisson_gemm_eligible(nx, ny)) { set_error("GEMM Poisson path: grid not eligible"); return GPL_ERR_INVALID_ARG; }
   std::unique_ptr<PoissonGemm> pg(new PoissonGemm());
   pg->nx = nx; pg->ny = ny;
-  const size_t x3 = 3 * (size_t)nx, y3 = 3 * (size_t)ny;
+  const size_t xk = kSplit * (size_t)nx, yk = kSplit * (size_t)ny;
   pg->bytes = (size_t)poisson_gemm_bytes(nx, ny);
   cudaError_t e = dev_alloc((void**)&pg->mem, pg->bytes, pool, s);
   if (e != cudaSuccess) { cudaGetLastError(); set_error("GEMM Poisson path: device allocation failed"); return GPL_ERR_OUT_OF_MEMORY; }
@@ -228,15 +263,15 @@ int poisson_gemm_setup(DeviceModel& d, PoissonGemm** out, cudaMemPool_t pool, cu
     cur += (elems * 2 + 255) / 256 * 256;
     return p;
   };
-  pg->c2x = take((size_t)nx * x3);
-  pg->c2y = take((size_t)ny * y3);
-  pg->a34 = take(2 * (size_t)ny * y3);
-  pg->swx = take((size_t)nx * x3);
-  pg->c3x = take((size_t)nx * x3);
-  pg->rho = take((size_t)ny * x3);
-  pg->txt = take((size_t)nx * y3);
-  pg->phit = take((size_t)nx * y3);
-  pg->p12 = take(2 * (size_t)ny * x3);
+  pg->c2x = take((size_t)nx * xk);
+  pg->c2y = take((size_t)ny * yk);
+  pg->a34 = take(2 * (size_t)ny * yk);
+  pg->swx = take((size_t)nx * xk);
+  pg->c3x = take((size_t)nx * xk);
+  pg->rho = take((size_t)ny * xk);
+  pg->txt = take((size_t)nx * yk);
+  pg->phit = take((size_t)nx * yk);
+  pg->p12 = take(2 * (size_t)ny * xk);
   pg->err = reinterpret_cast<int*>(cur);
   GPL_CUDA(cudaMemsetAsync(pg->err, 0, sizeof(int), s));
   const int grid = 4 * std::max(d.sm_count, 1);
@@ -247,12 +282,12 @@ int poisson_gemm_setup(DeviceModel& d, PoissonGemm** out, cudaMemPool_t pool, cu
   k_pg_matrix<<<grid, kPgThreads, 0, s>>>(pg->swx, nx, nx, 2, 1, d.wx, 0);
   k_pg_matrix<<<grid, kPgThreads, 0, s>>>(pg->c3x, nx, nx, 1, 1, nullptr, 0);
   GPL_CUDA(cudaGetLastError());
-  int rc = pg->g1.prepare(pg->rho, (int)x3, pg->c2x, (int)x3, ny, nx, (int)x3);
-  if (!rc) rc = pg->g2.prepare(pg->txt, (int)y3, pg->c2y, (int)y3, nx, ny, (int)y3);
-  if (!rc) rc = pg->g34.prepare(pg->a34, (int)y3, pg->phit, (int)y3, 2 * ny, nx, (int)y3);
-  if (!rc) rc = pg->g6.prepare(pg->p12, (int)x3, pg->swx, (int)x3, ny, nx, (int)x3);
-  if (!rc) rc = pg->g7.prepare(pg->p12 + (size_t)ny * x3, (int)x3, pg->c3x, (int)x3, ny, nx, (int)x3);
-  if (!rc) rc = pg->g5.prepare(pg->p12, (int)x3, pg->c3x, (int)x3, ny, nx, (int)x3);
+  int rc = pg->g1.prepare(pg->rho, (int)xk, pg->c2x, (int)xk, ny, nx, (int)xk);
+  if (!rc) rc = pg->g2.prepare(pg->txt, (int)yk, pg->c2y, (int)yk, nx, ny, (int)yk);
+  if (!rc) rc = pg->g34.prepare(pg->a34, (int)yk, pg->phit, (int)yk, 2 * ny, nx, (int)yk);
+  if (!rc) rc = pg->g6.prepare(pg->p12, (int)xk, pg->swx, (int)xk, ny, nx, (int)xk);
+  if (!rc) rc = pg->g7.prepare(pg->p12 + (size_t)ny * xk, (int)xk, pg->c3x, (int)xk, ny, nx, (int)xk);
+  if (!rc) rc = pg->g5.prepare(pg->p12, (int)xk, pg->c3x, (int)xk, ny, nx, (int)xk);
   if (rc) { dev_free(pg->mem, pool, s); pg->mem = nullptr; return rc; }
   *out = pg.release();
   return GPL_OK;
