@@ -246,42 +246,61 @@ def serving_batch(n_jobs, slots, device):
 
 
 def batched_form(n_jobs, slots, device):
-    """The batched form of config 4's jobs: (1) their Nesterov loops after
-    initial place and init, one at a time (gpl_nesterov_run per job) against
-    all together (gpl_batch_nesterov_run: one persistent launch per phase
-    over a work table of (job, block), rounds replayed as one CUDA graph);
-    (2) whole jobs through the placement server in batched mode (jobs join
-    the running batch after their initial place).  Results must be
-    bit-identical between the forms."""
+    """The batched form of config 4's jobs: (1) each job's whole flow
+    (initial place, Nesterov init, loop) one job at a time through the plain
+    job API, against the batched flow: all initial places together
+    (gpl_batch_initial_place: lockstep rounds, one launch per phase over a
+    work table of (job, block, axis)), each job's init, then all loops
+    together (gpl_batch_nesterov_run: one persistent launch per phase over a
+    work table of (job, block), rounds replayed as one CUDA graph); (2) whole
+    jobs through the placement server in batched mode (jobs join the running
+    batch after their initial place).  Results must be bit-identical between
+    the forms.  Netlist conversion (gpl_create) is outside the timings."""
     import numpy as np
-    from replace_gb300 import Placer, PlacementServer, batch_nesterov_run, netlist as N
+    from replace_gb300 import Placer, PlacementServer, batch_initial_place, batch_nesterov_run, netlist as N
     jobs = N.job_batch(n_jobs, seed=4)
 
-    def prepared():
-        ps = []
-        for nl, td in jobs:
-            p = Placer(nl, target_density=td, device=device, poisson_path=1)
-            p.initial_place()
-            p.nesterov_init()
-            ps.append(p)
-        return ps
-    ps = prepared()
-    t0 = time.perf_counter()
-    alone = [p.nesterov_run(0, allow_divergence=True)[1] for p in ps]
-    t_alone = time.perf_counter() - t0
+    def make():
+        return [Placer(nl, target_density=td, device=device, poisson_path=1) for nl, td in jobs]
+    ps = make()
+    t_ip = t_init = t_loop = 0.0
+    ip_alone, alone = [], []
+    for p in ps:
+        t0 = time.perf_counter()
+        ip_alone.append(p.initial_place())
+        t1 = time.perf_counter()
+        p.nesterov_init()
+        t2 = time.perf_counter()
+        alone.append(p.nesterov_run(0, allow_divergence=True)[1])
+        t3 = time.perf_counter()
+        t_ip += t1 - t0
+        t_init += t2 - t1
+        t_loop += t3 - t2
     loc_alone = [p.inst_locations() for p in ps]
     for p in ps:
         p.close()
-    ps = prepared()
+    ps = make()
     t0 = time.perf_counter()
+    ip_batch, _, ip_launches = batch_initial_place(ps)
+    t1 = time.perf_counter()
+    for p in ps:
+        p.nesterov_init()
+    t2 = time.perf_counter()
     stats, status, launches = batch_nesterov_run(ps)
-    t_batch = time.perf_counter() - t0
+    t3 = time.perf_counter()
+    b_ip, b_init, t_batch = t1 - t0, t2 - t1, t3 - t2
     loc_batch = [p.inst_locations() for p in ps]
     for p in ps:
         p.close()
-    same = all(a.hpwl == b.hpwl and a.iterations == b.iterations and np.array_equal(la[0], lb[0])
-               and np.array_equal(la[1], lb[1]) for a, b, la, lb in zip(alone, stats, loc_alone, loc_batch))
+    same_ip = all(a.iterations == b.iterations and a.last_error == b.last_error
+                  and a.solver_iters_x == b.solver_iters_x and a.solver_iters_y == b.solver_iters_y
+                  for a, b in zip(ip_alone, ip_batch))
+    same = same_ip and all(a.hpwl == b.hpwl and a.iterations == b.iterations and np.array_equal(la[0], lb[0])
+                           and np.array_equal(la[1], lb[1])
+                           for a, b, la, lb in zip(alone, stats, loc_alone, loc_batch))
     iters = sum(s.iterations for s in stats)
+    t_whole_alone = t_ip + t_init + t_loop
+    t_whole_batch = b_ip + b_init + t_batch
     with PlacementServer(device=device, max_active=slots, batched=True) as srv:
         t0 = time.perf_counter()
         ts = [srv.submit(nl, target_density=td, poisson_path=1) for nl, td in jobs]
@@ -290,8 +309,16 @@ def batched_form(n_jobs, slots, device):
     lat = np.array([res[t]["latency_s"] for t in ts])
     same_srv = all(res[t]["hpwl"] == a.hpwl for t, a in zip(ts, alone))
     return {
-        "nesterov_phase": {"jobs": n_jobs, "iterations": iters, "one_at_a_time_s": t_alone,
-                           "batched_s": t_batch, "speedup": t_alone / t_batch,
+        "whole_flow": {"jobs": n_jobs, "one_at_a_time_s": t_whole_alone, "batched_s": t_whole_batch,
+                       "speedup": t_whole_alone / t_whole_batch,
+                       "placements_per_hour": n_jobs / t_whole_batch * 3600.0,
+                       "same_result": bool(same)},
+        "initial_place_phase": {"rounds": int(sum(s.iterations for s in ip_batch)),
+                                "one_at_a_time_s": t_ip, "batched_s": b_ip, "speedup": t_ip / b_ip,
+                                "kernel_launches": ip_launches, "same_result": bool(same_ip)},
+        "init_phase": {"one_at_a_time_s": t_init, "batched_flow_s": b_init},
+        "nesterov_phase": {"jobs": n_jobs, "iterations": iters, "one_at_a_time_s": t_loop,
+                           "batched_s": t_batch, "speedup": t_loop / t_batch,
                            "batched_iters_per_s": iters / t_batch, "kernel_launches": launches,
                            "same_result": bool(same)},
         "server_batched": {"slots": slots, "placements_per_hour": n_jobs / t_srv * 3600.0,

@@ -230,6 +230,24 @@ void gpl_destroy(struct gpl_job* job);
  * incremental), then up to initial_place_max_iter B2B + BiCGSTAB rounds. */
 gpl_status gpl_initial_place(struct gpl_job* job, gpl_ip_stats* stats);
 
+/* Batched form of gpl_initial_place: the initial places of n_jobs jobs run
+ * together (no counterpart in the reference, which places one design per
+ * process).  Each job is centred (unless incremental) as gpl_initial_place
+ * does; then the B2B + BiCGSTAB rounds of all jobs run in lockstep: each
+ * assembly phase and each solver phase is one launch over a table of work
+ * items (job, block of that job's own launch, axis), a job leaves when its
+ * rounds end (error <= 1e-5 after at least 5 rounds, or
+ * initial_place_max_iter).  Every job's result -- instance locations,
+ * rounds, error, solver iterations -- is bit-identical to gpl_initial_place
+ * on that job alone with the kernel-per-phase solver (ip_solver 0 or 1; the
+ * batch always runs that form).  The jobs: distinct, on one device, before
+ * gpl_nesterov_init.  stats and status are [n_jobs] (may be NULL): each
+ * job's statistics and its gpl_initial_place status; *kernel_launches (may
+ * be NULL): kernels launched by the batch.  The call itself returns GPL_OK
+ * unless it could not run. */
+gpl_status gpl_batch_initial_place(struct gpl_job* const* jobs, int32_t n_jobs, gpl_ip_stats* stats,
+                                   gpl_status* status, int64_t* kernel_launches);
+
 /* NesterovBase(nbVars, pb, log) + NesterovPlace::init()
  * (src/replace.cpp:112-125, src/nesterovBase.cpp:917-1062,
  * src/nesterovPlace.cpp:64-175). */

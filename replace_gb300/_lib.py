@@ -48,6 +48,8 @@ def load(build_if_missing: bool = True):
     L.gpl_batch_nesterov_run.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32,
                                          C.POINTER(_abi.NesterovStats), C.POINTER(C.c_int32),
                                          C.POINTER(C.c_int64)]
+    L.gpl_batch_initial_place.argtypes = [C.POINTER(vp), C.c_int32, C.POINTER(_abi.IpStats),
+                                          C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     L.gpl_get_inst_locations.argtypes = [vp, vp, vp]
     L.gpl_get_gcell_coords.argtypes = [vp, vp]
     L.gpl_eval.argtypes = [vp, vp, C.c_float, C.c_float, vp, vp, C.POINTER(_abi.EvalStats)]
@@ -79,7 +81,7 @@ def load(build_if_missing: bool = True):
                  "gpl_server_release", "gpl_server_cancel"):
         getattr(L, name).restype = C.c_int
     for name in ("gpl_create", "gpl_initial_place", "gpl_nesterov_init", "gpl_nesterov_run",
-                 "gpl_batch_nesterov_run",
+                 "gpl_batch_nesterov_run", "gpl_batch_initial_place",
                  "gpl_set_net_weights",
                  "gpl_get_inst_locations", "gpl_get_gcell_coords", "gpl_eval", "gpl_get_bins",
                  "gpl_get_gcells", "gpl_poisson_solve"):

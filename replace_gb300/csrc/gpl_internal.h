@@ -397,6 +397,22 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
                       void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev);
 // device bytes run_initial_place allocates for this model
 size_t initial_place_bytes(const HostModel& m, int sm_count);
+// One job of the batched initial place: its host model, and the stream,
+// pinned block, pool and event its setup and read-back use (as
+// run_initial_place's); stats may be null; status is the job's result.
+struct IpBatchJob {
+  HostModel* m = nullptr;
+  cudaStream_t s = nullptr;
+  void* pinned = nullptr;
+  cudaMemPool_t pool = nullptr;
+  cudaEvent_t sync_ev = nullptr;
+  gpl_ip_stats* stats = nullptr;
+  int status = 0;
+};
+// The initial place of n jobs in lockstep rounds, one launch per phase over
+// all jobs (initial_place.cu); each job's result is bit-identical to
+// run_initial_place's kernel-per-phase form.  *launches: kernels launched.
+int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* launches);
 
 // A job's host model without a stream or staging (a server binds those when
 // it admits the job), and the binding: stream, pinned staging and pool stay

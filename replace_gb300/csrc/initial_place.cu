@@ -91,8 +91,8 @@ struct IpParams {
 };
 
 // ------------------------------------------------------------ assembly
-__global__ void k_ip_pos(IpDev D) {
-  const int q = blockIdx.x * kB + threadIdx.x;
+__device__ __forceinline__ void ip_pos_body(const IpDev& D, int vb) {
+  const int q = vb * kB + threadIdx.x;
   if (q >= D.n_pins) return;
   const int m = D.pin_mov[q];
   if (m >= 0) {
@@ -105,8 +105,8 @@ __global__ void k_ip_pos(IpDev D) {
 
 // updatePinInfo: the first pin (in net order) at a strict new minimum or
 // maximum keeps the flag, i.e. the first occurrence of the extreme value.
-__global__ void k_ip_bound(IpDev D) {
-  const int n = blockIdx.x * kB + threadIdx.x;
+__device__ __forceinline__ void ip_bound_body(const IpDev& D, int vb) {
+  const int n = vb * kB + threadIdx.x;
   if (n >= D.n_nets) return;
   int lx = INT_MAX, ly = INT_MAX, ux = INT_MIN, uy = INT_MIN;
   int4 b = make_int4(-1, -1, -1, -1);
@@ -174,10 +174,10 @@ constexpr int kLongList = 32;
 
 // Entries each slot contributes (movable partners); lanes take one slot each,
 // long partner lists are counted by the warp together.
-__global__ void k_ip_count(IpDev D, IpParams P) {
+__device__ __forceinline__ void ip_count_body(const IpDev& D, const IpParams& P, int vb, int vgrid, int axis) {
   const unsigned full = 0xffffffffu;
-  const int axis = blockIdx.y, lane = threadIdx.x & 31;
-  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < D.n_mp; w += gridDim.x * kB) {
+  const int lane = threadIdx.x & 31;
+  for (int w = vb * kB + (threadIdx.x & ~31); w < D.n_mp; w += vgrid * kB) {
     const int t = w + lane;
     int c = 0;
     bool lng = false;
@@ -207,10 +207,10 @@ __global__ void k_ip_count(IpDev D, IpParams P) {
 }
 
 // exclusive scan of cnt[axis] into rowptr[axis] (three kernels)
-__global__ void k_scan_blocks(const int32_t* in, int32_t* out, int32_t* part, int n) {
+__device__ __forceinline__ void scan_blocks_body(const int32_t* in, int32_t* out, int32_t* part, int n, int vb,
+                                                 int vgrid, int axis) {
   __shared__ int32_t sh[kB];
-  const int axis = blockIdx.y;
-  const int i = blockIdx.x * kB + threadIdx.x;
+  const int i = vb * kB + threadIdx.x;
   const int v = i < n ? in[axis * n + i] : 0;
   sh[threadIdx.x] = v;
   __syncthreads();
@@ -221,16 +221,15 @@ __global__ void k_scan_blocks(const int32_t* in, int32_t* out, int32_t* part, in
     __syncthreads();
   }
   if (i < n) out[axis * (n + 1) + i] = sh[threadIdx.x] - v;     // exclusive within the block
-  if (threadIdx.x == kB - 1) part[axis * gridDim.x + blockIdx.x] = sh[kB - 1];
+  if (threadIdx.x == kB - 1) part[axis * vgrid + vb] = sh[kB - 1];
 }
 
 // Exclusive scan of the block sums (one block of kScanT threads per axis:
 // contiguous chunks per thread, then a scan of the chunk sums); the total
 // goes to out[n].
 constexpr int kScanT = 1024;
-__global__ void __launch_bounds__(kScanT) k_scan_parts(int32_t* part, int nparts, int32_t* out, int n) {
+__device__ __forceinline__ void scan_parts_body(int32_t* part, int nparts, int32_t* out, int n, int axis) {
   __shared__ int32_t sh[kScanT];
-  const int axis = blockIdx.x;
   int32_t* pp = part + axis * nparts;
   const int chunk = (nparts + kScanT - 1) / kScanT;
   const int lo = min(threadIdx.x * chunk, nparts), hi = min(lo + chunk, nparts);
@@ -253,16 +252,15 @@ __global__ void __launch_bounds__(kScanT) k_scan_parts(int32_t* part, int nparts
   if (threadIdx.x == kScanT - 1) out[axis * (n + 1) + n] = sh[kScanT - 1];
 }
 
-__global__ void k_scan_add(int32_t* rowptr, const int32_t* part, int n) {
-  const int axis = blockIdx.y;
-  const int i = blockIdx.x * kB + threadIdx.x;
-  if (i < n) rowptr[axis * (n + 1) + i] += part[axis * gridDim.x + blockIdx.x];
+__device__ __forceinline__ void scan_add_body(int32_t* rowptr, const int32_t* part, int n, int vb, int vgrid,
+                                              int axis) {
+  const int i = vb * kB + threadIdx.x;
+  if (i < n) rowptr[axis * (n + 1) + i] += part[axis * vgrid + vb];
 }
 
 // Row pointers: a row starts at its instance's first slot.
-__global__ void k_ip_rowptr(IpDev D) {
-  const int i = blockIdx.x * kB + threadIdx.x;
-  const int axis = blockIdx.y;
+__device__ __forceinline__ void ip_rowptr_body(const IpDev& D, int vb, int axis) {
+  const int i = vb * kB + threadIdx.x;
   if (i > D.n_mov) return;
   const int t = i < D.n_mov ? D.mov_pin_start[i] : D.n_mp;
   D.rowptr[axis * (D.n_mov + 1) + i] = D.slot_off[axis * (D.n_mp + 1) + t];
@@ -278,12 +276,12 @@ __global__ void k_ip_rowptr(IpDev D) {
 // entry is dropped and the initial place reports an error.
 constexpr int kFillOverflow = 7;
 
-__global__ void k_ip_fill(IpDev D, IpParams P) {
+__device__ __forceinline__ void ip_fill_body(const IpDev& D, const IpParams& P, int vb, int vgrid, int axis) {
   const unsigned full = 0xffffffffu;
-  const int axis = blockIdx.y, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   int32_t* col = D.col + axis * D.nnz_cap;
   float* val = D.val + axis * D.nnz_cap;
-  for (int w = blockIdx.x * kB + (threadIdx.x & ~31); w < D.n_mp; w += gridDim.x * kB) {
+  for (int w = vb * kB + (threadIdx.x & ~31); w < D.n_mp; w += vgrid * kB) {
     const int t = w + lane;
     float diag = 0.0f, rhs = 0.0f;
     bool lng = false;
@@ -317,9 +315,9 @@ __global__ void k_ip_fill(IpDev D, IpParams P) {
               at++;
               const int2 cj = D.ctr[j];
               const int off_r = pr - (axis ? cj.y : cj.x);
-              rhs += -wgt * (float)(off_q - off_r);
+              rhs = __fmaf_rn(-wgt, (float)(off_q - off_r), rhs);
             } else {
-              rhs += wgt * (float)(pr - off_q);
+              rhs = __fmaf_rn(wgt, (float)(pr - off_q), rhs);
             }
           });
         }
@@ -348,9 +346,9 @@ __global__ void k_ip_fill(IpDev D, IpParams P) {
           if (j >= 0) {
             const int2 cj = D.ctr[j];
             const int off_r = pr - (axis ? cj.y : cj.x);
-            rh += -wgt * (float)(soff - off_r);
+            rh = __fmaf_rn(-wgt, (float)(soff - off_r), rh);
           } else {
-            rh += wgt * (float)(pr - soff);
+            rh = __fmaf_rn(wgt, (float)(pr - soff), rh);
           }
         }
         const unsigned mv = __ballot_sync(full, partner && j >= 0);
@@ -380,9 +378,8 @@ __global__ void k_ip_fill(IpDev D, IpParams P) {
 }
 
 // Diagonal and right-hand side of each row: its slots' parts in pin order.
-__global__ void k_ip_rowsum(IpDev D) {
-  const int i = blockIdx.x * kB + threadIdx.x;
-  const int axis = blockIdx.y;
+__device__ __forceinline__ void ip_rowsum_body(const IpDev& D, int vb, int axis) {
+  const int i = vb * kB + threadIdx.x;
   if (i >= D.n_mov) return;
   float diag = 0.0f, rhs = 0.0f;
   for (int t = D.mov_pin_start[i]; t < D.mov_pin_start[i + 1]; t++) {
@@ -392,6 +389,28 @@ __global__ void k_ip_rowsum(IpDev D) {
   D.diag[axis * D.n_mov + i] = diag;
   D.b[axis * D.n_mov + i] = rhs;
 }
+
+// The per-job launches of the assembly phases (blockIdx.y = axis); the
+// batched form runs the same bodies from a work table.
+__global__ void k_ip_pos(const __grid_constant__ IpDev D) { ip_pos_body(D, (int)blockIdx.x); }
+__global__ void k_ip_bound(const __grid_constant__ IpDev D) { ip_bound_body(D, (int)blockIdx.x); }
+__global__ void k_ip_count(const __grid_constant__ IpDev D, const __grid_constant__ IpParams P) {
+  ip_count_body(D, P, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_scan_blocks(const int32_t* in, int32_t* out, int32_t* part, int n) {
+  scan_blocks_body(in, out, part, n, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void __launch_bounds__(kScanT) k_scan_parts(int32_t* part, int nparts, int32_t* out, int n) {
+  scan_parts_body(part, nparts, out, n, (int)blockIdx.x);
+}
+__global__ void k_scan_add(int32_t* rowptr, const int32_t* part, int n) {
+  scan_add_body(rowptr, part, n, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_ip_rowptr(const __grid_constant__ IpDev D) { ip_rowptr_body(D, (int)blockIdx.x, (int)blockIdx.y); }
+__global__ void k_ip_fill(const __grid_constant__ IpDev D, const __grid_constant__ IpParams P) {
+  ip_fill_body(D, P, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_ip_rowsum(const __grid_constant__ IpDev D) { ip_rowsum_body(D, (int)blockIdx.x, (int)blockIdx.y); }
 
 // ------------------------------------------------------------ solver
 // Sparse products: each warp takes windows of 32 consecutive rows (row
@@ -432,6 +451,28 @@ struct RowFetch {
   float acc;       // diag * x_i (the row's first term)
   float aux;       // the caller's per-row operand (read with the row)
 };
+
+// Starts moving a window's matrix entries (col and val, rows w .. w + 31)
+// from DRAM into L2 while the warp works on the window before it: one bulk
+// L2 prefetch per array, issued by lane 0, the range widened to 16-byte
+// boundaries (it stays inside the arrays' 256-byte padding).
+__device__ __forceinline__ void prefetch_window(const int32_t* col, const float* val, const RowFetch& f,
+                                                bool valid) {
+  const unsigned full = 0xffffffffu;
+  const unsigned m = __ballot_sync(full, valid);
+  if (!m) return;
+  const int last = 31 - __clz(m);
+  const int base = __shfl_sync(full, f.s, 0);
+  const int end = __shfl_sync(full, f.e, last);
+  if ((threadIdx.x & 31) == 0 && end > base) {
+    const uintptr_t c0 = reinterpret_cast<uintptr_t>(col + base) & ~uintptr_t(15);
+    const uintptr_t c1 = (reinterpret_cast<uintptr_t>(col + end) + 15) & ~uintptr_t(15);
+    const uintptr_t v0 = reinterpret_cast<uintptr_t>(val + base) & ~uintptr_t(15);
+    const uintptr_t v1 = (reinterpret_cast<uintptr_t>(val + end) + 15) & ~uintptr_t(15);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(c0), "r"((unsigned)(c1 - c0)) : "memory");
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(v0), "r"((unsigned)(v1 - v0)) : "memory");
+  }
+}
 
 // One window: returns the lane's row product (valid lanes).
 template <bool kFromL2, int kBatch>
@@ -486,17 +527,17 @@ __device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, co
     const int ls = __shfl_sync(full, s, src), le = __shfl_sync(full, e, src);
     float part = 0.0f;
 #pragma unroll 4
-    for (int k = ls + lane; k < le; k += 32) part += val[k] * ld(col[k]);
+    for (int k = ls + lane; k < le; k += 32) part = __fmaf_rn(val[k], ld(col[k]), part);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(full, part, o);
-    if (lane == src) acc += part;
+    for (int o = 16; o > 0; o >>= 1) part = __fadd_rn(part, __shfl_xor_sync(full, part, o));
+    if (lane == src) acc = __fadd_rn(acc, part);
   }
   return acc;
 }
 
 // (A xv)_i for the warp's windows w0, w0 + step, ...; epi(i, value, aux[i])
 // for every row.  All 32 lanes call it together (w0 is warp-uniform).
-template <bool kFromL2 = false, int kBatch = 16, class Epi>
+template <bool kFromL2 = false, int kBatch = 16, bool kPrefetch = true, class Epi>
 __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float* xv, const float* aux,
                                           int w0, int step, float* stage, Epi epi) {
   const int n = D.n_mov;
@@ -511,18 +552,22 @@ __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float*
     if (i < n) {
       f.s = rp[i];
       f.e = rp[i + 1];
-      f.acc = dg[i] * (kFromL2 ? __ldcg(xv + i) : xv[i]);
+      f.acc = __fmul_rn(dg[i], kFromL2 ? __ldcg(xv + i) : xv[i]);
       f.aux = aux ? (kFromL2 ? __ldcg(aux + i) : aux[i]) : 0.0f;
     }
     return f;
   };
+  // row data two windows ahead, matrix entries one window ahead (in L2)
   RowFetch cur = fetch(w0);
+  RowFetch next = fetch(w0 + step);
   for (int w = w0; w < n; w += step) {
-    const RowFetch next = fetch(w + step);
+    if (kPrefetch) prefetch_window(col, val, next, w + step + lane < n);
+    const RowFetch next2 = fetch(w + 2 * step);
     const int i = w + lane;
     const float v = spmv_window<kFromL2, kBatch>(col, val, xv, cur, i < n, stage);
     if (i < n) epi(i, v, cur.aux);
     cur = next;
+    next = next2;
   }
 }
 
@@ -545,7 +590,7 @@ __device__ __forceinline__ void phase_p(float* p, const float* r, const float* v
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int k = i + u * step;
-      if (k < n) p[k] = rr[u] + beta * (pp[u] - w * vv[u]);
+      if (k < n) p[k] = __fmaf_rn(beta, __fmaf_rn(-w, vv[u], pp[u]), rr[u]);
     }
   }
 }
@@ -564,7 +609,7 @@ __device__ __forceinline__ void phase_s(float* s, const float* r, const float* v
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int k = i + u * step;
-      if (k < n) s[k] = rr[u] - alpha * vv[u];
+      if (k < n) s[k] = __fmaf_rn(-alpha, vv[u], rr[u]);
     }
   }
 }
@@ -585,11 +630,11 @@ __device__ __forceinline__ void phase_xr(float* x, float* r, const float* p, con
     for (int u = 0; u < U; u++) {
       const int k = i + u * step;
       if (k < n) {
-        x[k] = xx[u] + (alpha * pp[u] + w * ss[u]);
-        const float ri = ss[u] - w * tt[u];
+        x[k] = __fadd_rn(xx[u], __fmaf_rn(alpha, pp[u], __fmul_rn(w, ss[u])));
+        const float ri = __fmaf_rn(-w, tt[u], ss[u]);
         r[k] = ri;
-        acc[0] += ri * ri;
-        acc[1] += qq[u] * ri;
+        acc[0] = __fmaf_rn(ri, ri, acc[0]);
+        acc[1] = __fmaf_rn(qq[u], ri, acc[1]);
       }
     }
   }
@@ -604,25 +649,25 @@ __device__ __forceinline__ float* warp_stage() {
 // block partial sums of up to 2 products, then the last block of this axis
 // runs `fin` with the totals (fixed-order reduction)
 template <int N, class Fin>
-__device__ __forceinline__ void reduce_and_finish(IpDev& D, int kernel_id, const float (&vf)[N], Fin fin) {
+__device__ __forceinline__ void reduce_and_finish(const IpDev& D, int kernel_id, const float (&vf)[N], Fin fin,
+                                                  int vb, int vgrid, int axis) {
   __shared__ double sh[32 * N];
   __shared__ bool last;
-  const int axis = blockIdx.y;
   double* part = D.part + (size_t)(axis * 2) * D.parts;
   double v[N];
 #pragma unroll
   for (int k = 0; k < N; k++) v[k] = vf[k];      // the thread's rows in float, FP64 across threads
-  block_reduce_n<N>(v, part, D.parts, sh);
+  block_reduce_n<N>(v, part, D.parts, sh, vb);
   if (threadIdx.x == 0) {
     __threadfence();
-    last = atomicAdd(&D.counters[axis * 8 + kernel_id], 1u) == gridDim.x - 1;
+    last = atomicAdd(&D.counters[axis * 8 + kernel_id], 1u) == (unsigned)vgrid - 1;
   }
   __syncthreads();
   if (!last) return;
   double tot[N];
 #pragma unroll
   for (int k = 0; k < N; k++) tot[k] = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+  for (int b = threadIdx.x; b < vgrid; b += blockDim.x)
 #pragma unroll
     for (int k = 0; k < N; k++) tot[k] += __ldcg(part + (size_t)k * D.parts + b);
   __shared__ double tt[N];
@@ -646,9 +691,9 @@ __device__ __forceinline__ void loop_head(BiState& S, int max_iter) {
 }
 
 // r = b - A x (r0 = r when restarting), with |r|^2 and |b|^2
-__global__ void k_bi_residual(IpDev D, int init, int max_iter) {
+__device__ __forceinline__ void bi_residual_body(const IpDev& D, int init, int max_iter, int vb, int vgrid,
+                                                 int axis) {
   float* stage = warp_stage();
-  const int axis = blockIdx.y;
   BiState& S = D.st[axis];
   if (!init && (S.done || !S.need_restart)) return;
   const int n = D.n_mov;
@@ -657,13 +702,13 @@ __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
   float* r = D.r + axis * n;
   float* r0 = D.r0 + axis * n;
   float v[2] = {0.0f, 0.0f};
-  spmv_rows(D, axis, x, bb, blockIdx.x * kB + (threadIdx.x & ~31), gridDim.x * kB, stage,
+  spmv_rows(D, axis, x, bb, vb * kB + (threadIdx.x & ~31), vgrid * kB, stage,
             [&](int i, float ax, float bi) {
               const float ri = bi - ax;
               r[i] = ri;
               r0[i] = ri;
-              v[0] += ri * ri;
-              v[1] += bi * bi;
+              v[0] = __fmaf_rn(ri, ri, v[0]);
+              v[1] = __fmaf_rn(bi, bi, v[1]);
             });
   reduce_and_finish<2>(D, 0, v, [&](BiState& s, const double* t) {
     if (init) {
@@ -681,42 +726,46 @@ __global__ void k_bi_residual(IpDev D, int init, int max_iter) {
       if (s.restarts++ == 0) s.i = 0;
       s.need_restart = 0;
     }
-  });
+  }, vb, vgrid, axis);
 }
 
-__global__ void k_bi_p(IpDev D) {
-  const int axis = blockIdx.y;
+__device__ __forceinline__ void bi_p_body(const IpDev& D, int vb, int vgrid, int axis) {
   const BiState& S = D.st[axis];
   if (S.done) return;
-  const double beta = (S.rho / S.rho_old) * (S.alpha / S.w);
+  // beta once per block: FP64 division is slow on this part, and every
+  // thread would otherwise divide twice
+  __shared__ float sc[2];
+  if (threadIdx.x == 0) {
+    const double beta = (S.rho / S.rho_old) * (S.alpha / S.w);
+    sc[0] = (float)beta;                // Eigen's scalars are float
+    sc[1] = (float)S.w;
+  }
+  __syncthreads();
   const int n = D.n_mov;
   float* p = D.p + axis * n;
   const float* r = D.r + axis * n;
   const float* v = D.v + axis * n;
-  const float bf = (float)beta, wf = (float)S.w;   // Eigen's scalars are float
-  phase_p(p, r, v, bf, wf, blockIdx.x * kB + threadIdx.x, gridDim.x * kB, n);
+  phase_p(p, r, v, sc[0], sc[1], vb * kB + threadIdx.x, vgrid * kB, n);
 }
 
 // v = A p, alpha = rho / (r0 . v)
-__global__ void k_bi_v(IpDev D) {
+__device__ __forceinline__ void bi_v_body(const IpDev& D, int vb, int vgrid, int axis) {
   float* stage = warp_stage();
-  const int axis = blockIdx.y;
   if (D.st[axis].done) return;
   const int n = D.n_mov;
   const float* p = D.p + axis * n;
   float* v = D.v + axis * n;
   const float* r0 = D.r0 + axis * n;
   float acc[1] = {0.0f};
-  spmv_rows(D, axis, p, r0, blockIdx.x * kB + (threadIdx.x & ~31), gridDim.x * kB, stage,
+  spmv_rows(D, axis, p, r0, vb * kB + (threadIdx.x & ~31), vgrid * kB, stage,
             [&](int i, float vi, float r0i) {
               v[i] = vi;
-              acc[0] += r0i * vi;
+              acc[0] = __fmaf_rn(r0i, vi, acc[0]);
             });
-  reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; });
+  reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; }, vb, vgrid, axis);
 }
 
-__global__ void k_bi_s(IpDev D) {
-  const int axis = blockIdx.y;
+__device__ __forceinline__ void bi_s_body(const IpDev& D, int vb, int vgrid, int axis) {
   const BiState& S = D.st[axis];
   if (S.done) return;
   const int n = D.n_mov;
@@ -724,32 +773,30 @@ __global__ void k_bi_s(IpDev D) {
   const float* v = D.v + axis * n;
   float* s = D.s + axis * n;
   const float af = (float)S.alpha;
-  phase_s(s, r, v, af, blockIdx.x * kB + threadIdx.x, gridDim.x * kB, n);
+  phase_s(s, r, v, af, vb * kB + threadIdx.x, vgrid * kB, n);
 }
 
 // t = A s, omega = (t . s) / (t . t)
-__global__ void k_bi_t(IpDev D) {
+__device__ __forceinline__ void bi_t_body(const IpDev& D, int vb, int vgrid, int axis) {
   float* stage = warp_stage();
-  const int axis = blockIdx.y;
   if (D.st[axis].done) return;
   const int n = D.n_mov;
   const float* s = D.s + axis * n;
   float* t = D.t + axis * n;
   float acc[2] = {0.0f, 0.0f};
-  spmv_rows(D, axis, s, s, blockIdx.x * kB + (threadIdx.x & ~31), gridDim.x * kB, stage,
+  spmv_rows(D, axis, s, s, vb * kB + (threadIdx.x & ~31), vgrid * kB, stage,
             [&](int i, float ti, float si) {
               t[i] = ti;
-              acc[0] += ti * ti;
-              acc[1] += ti * si;
+              acc[0] = __fmaf_rn(ti, ti, acc[0]);
+              acc[1] = __fmaf_rn(ti, si, acc[1]);
             });
   reduce_and_finish<2>(D, 2, acc, [&](BiState& st, const double* tt) {
     st.w = tt[0] > 0.0 ? tt[1] / tt[0] : 0.0;
-  });
+  }, vb, vgrid, axis);
 }
 
 // x += alpha p + omega s; r = s - omega t; |r|^2 and r0 . r; next loop head
-__global__ void k_bi_xr(IpDev D, int max_iter) {
-  const int axis = blockIdx.y;
+__device__ __forceinline__ void bi_xr_body(const IpDev& D, int max_iter, int vb, int vgrid, int axis) {
   const BiState& S = D.st[axis];
   if (S.done) return;
   const int n = D.n_mov;
@@ -761,13 +808,33 @@ __global__ void k_bi_xr(IpDev D, int max_iter) {
   const float* r0 = D.r0 + axis * n;
   const float af = (float)S.alpha, wf = (float)S.w;
   float acc[2] = {0.0f, 0.0f};
-  phase_xr(x, r, p, s, t, r0, af, wf, blockIdx.x * kB + threadIdx.x, gridDim.x * kB, n, acc);
+  phase_xr(x, r, p, s, t, r0, af, wf, vb * kB + threadIdx.x, vgrid * kB, n, acc);
   reduce_and_finish<2>(D, 3, acc, [&](BiState& st, const double* tt) {
     st.rr = tt[0];
     st.dot_r0r = tt[1];
     st.i++;
     loop_head(st, max_iter);
-  });
+  }, vb, vgrid, axis);
+}
+
+// The per-job launches of the solver phases (blockIdx.y = axis).
+__global__ void k_bi_residual(const __grid_constant__ IpDev D, int init, int max_iter) {
+  bi_residual_body(D, init, max_iter, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_bi_p(const __grid_constant__ IpDev D) {
+  bi_p_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_bi_v(const __grid_constant__ IpDev D) {
+  bi_v_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_bi_s(const __grid_constant__ IpDev D) {
+  bi_s_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_bi_t(const __grid_constant__ IpDev D) {
+  bi_t_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+}
+__global__ void k_bi_xr(const __grid_constant__ IpDev D, int max_iter) {
+  bi_xr_body(D, max_iter, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
 
 // ---------------------------------------------------- cooperative solve
@@ -877,8 +944,8 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
           const float ri = bi - ax;
           r[i] = ri;
           r0[i] = ri;
-          acc[0] += ri * ri;
-          acc[1] += bi * bi;
+          acc[0] = __fmaf_rn(ri, ri, acc[0]);
+          acc[1] = __fmaf_rn(bi, bi, acc[1]);
         });
       block_partials<2>(acc, cpart(D, 3, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
@@ -908,7 +975,7 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
       if (live)
         spmv_rows<true, 4>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
           v[i] = vi;
-          acc[0] += r0i * vi;
+          acc[0] = __fmaf_rn(r0i, vi, acc[0]);
         });
       block_partials<1>(acc, cpart(D, 0, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
@@ -931,8 +998,8 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
       if (live)
         spmv_rows<true, 4>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
           t[i] = ti;
-          acc[0] += ti * ti;
-          acc[1] += ti * si;
+          acc[0] = __fmaf_rn(ti, ti, acc[0]);
+          acc[1] = __fmaf_rn(ti, si, acc[1]);
         });
       block_partials<2>(acc, cpart(D, 1, axis), D.parts, sh);
       if (!grid_barrier(D.bar)) return;
@@ -1030,12 +1097,12 @@ k_bi_cluster(IpDev D, int max_iter) {
     // restart: r = r0 = b - A x
     if (S.need_restart) {
       float acc[2] = {0.0f, 0.0f};
-      spmv_rows<true, 8>(D, axis, x, bb, w0, step, stage, [&](int i, float ax, float bi) {
+      spmv_rows<true, 8, false>(D, axis, x, bb, w0, step, stage, [&](int i, float ax, float bi) {
         const float ri = bi - ax;
         r[i] = ri;
         r0[i] = ri;
-        acc[0] += ri * ri;
-        acc[1] += bi * bi;
+        acc[0] = __fmaf_rn(ri, ri, acc[0]);
+        acc[1] = __fmaf_rn(bi, bi, acc[1]);
       });
       double tot[2];
       cluster_total<2>(cl, acc, slot[3], sh, tot_sh, tot);
@@ -1056,9 +1123,9 @@ k_bi_cluster(IpDev D, int max_iter) {
     // v = A p, alpha = rho / (r0 . v)
     {
       float acc[1] = {0.0f};
-      spmv_rows<true, 8>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
+      spmv_rows<true, 8, false>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
         v[i] = vi;
-        acc[0] += r0i * vi;
+        acc[0] = __fmaf_rn(r0i, vi, acc[0]);
       });
       double tot[1];
       cluster_total<1>(cl, acc, slot[0], sh, tot_sh, tot);
@@ -1074,10 +1141,10 @@ k_bi_cluster(IpDev D, int max_iter) {
     // t = A s, w = (t . s) / (t . t)
     {
       float acc[2] = {0.0f, 0.0f};
-      spmv_rows<true, 8>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
+      spmv_rows<true, 8, false>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
         t[i] = ti;
-        acc[0] += ti * ti;
-        acc[1] += ti * si;
+        acc[0] = __fmaf_rn(ti, ti, acc[0]);
+        acc[1] = __fmaf_rn(ti, si, acc[1]);
       });
       double tot[2];
       cluster_total<2>(cl, acc, slot[1], sh, tot_sh, tot);
@@ -1106,8 +1173,8 @@ k_bi_cluster(IpDev D, int max_iter) {
 
 // rhs == 0: Eigen sets x = 0; then the instances move to the solution
 // (InitialPlace::updateCoordi :380-385, float -> int truncation)
-__global__ void k_ip_move(IpDev D) {
-  const int i = blockIdx.x * kB + threadIdx.x;
+__device__ __forceinline__ void ip_move_body(const IpDev& D, int vb) {
+  const int i = vb * kB + threadIdx.x;
   if (i >= D.n_mov) return;
   const int n = D.n_mov;
   float x = D.x[i], y = D.x[n + i];
@@ -1119,8 +1186,8 @@ __global__ void k_ip_move(IpDev D) {
 // Start of one solve: the warm start is the instances' current centres
 // (instLocVecX_ = inst->cx(), src/initialPlace.cpp:211-218) and, as every
 // BiCGSTAB solve begins, p = v = 0.
-__global__ void k_ip_guess(IpDev D) {
-  const int i = blockIdx.x * kB + threadIdx.x;
+__device__ __forceinline__ void ip_guess_body(const IpDev& D, int vb) {
+  const int i = vb * kB + threadIdx.x;
   if (i >= D.n_mov) return;
   const int2 c = D.ctr[i];
   const int n = D.n_mov;
@@ -1130,12 +1197,80 @@ __global__ void k_ip_guess(IpDev D) {
   D.v[i] = D.v[n + i] = 0.0f;
 }
 
+__global__ void k_ip_move(const __grid_constant__ IpDev D) { ip_move_body(D, (int)blockIdx.x); }
+__global__ void k_ip_guess(const __grid_constant__ IpDev D) { ip_guess_body(D, (int)blockIdx.x); }
+
+// ------------------------------------------------------------ batched form
+// The phases of the kernel-per-phase solve for many jobs at once: block b of
+// a batched launch takes work item items[b] = (job, block of the job's own
+// launch, that launch's grid, axis) and runs the per-job kernel's body on
+// the job's tables, so every job computes exactly what its own launches
+// compute (the bodies spell their floating-point rounding out, so the
+// arithmetic does not depend on the kernel they are compiled into).
+enum IpPhase {
+  kIpPos = 0, kIpBound, kIpCount, kIpScanBlocks, kIpScanAdd, kIpRowptr, kIpFill, kIpRowsum, kIpGuess,
+  kIpResidualInit, kIpResidual, kIpP, kIpV, kIpS, kIpT, kIpXr, kIpMove
+};
+
+template <int Ph>
+__global__ void __launch_bounds__(kB, 4) k_ipb(const IpDev* __restrict__ Ds, const IpParams* __restrict__ Ps,
+                                            const int4* __restrict__ items) {
+  // the job's tables in shared memory (IpDev is a few hundred bytes)
+  __shared__ __align__(16) unsigned char raw[sizeof(IpDev)];
+  static_assert(sizeof(IpDev) % 4 == 0, "IpDev is copied as words");
+  const int4 it = items[blockIdx.x];
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(Ds + it.x);
+    unsigned* dst = reinterpret_cast<unsigned*>(raw);
+    for (int w = threadIdx.x; w < (int)(sizeof(IpDev) / 4); w += blockDim.x) dst[w] = src[w];
+  }
+  __syncthreads();
+  const IpDev& D = *reinterpret_cast<const IpDev*>(raw);
+  const int vb = it.y, vg = it.z, ax = it.w;
+  if constexpr (Ph == kIpPos) ip_pos_body(D, vb);
+  else if constexpr (Ph == kIpBound) ip_bound_body(D, vb);
+  else if constexpr (Ph == kIpCount) { const IpParams P = Ps[it.x]; ip_count_body(D, P, vb, vg, ax); }
+  else if constexpr (Ph == kIpScanBlocks) scan_blocks_body(D.cnt, D.slot_off, D.scan_part, D.n_mp, vb, vg, ax);
+  else if constexpr (Ph == kIpScanAdd) scan_add_body(D.slot_off, D.scan_part, D.n_mp, vb, vg, ax);
+  else if constexpr (Ph == kIpRowptr) ip_rowptr_body(D, vb, ax);
+  else if constexpr (Ph == kIpFill) { const IpParams P = Ps[it.x]; ip_fill_body(D, P, vb, vg, ax); }
+  else if constexpr (Ph == kIpRowsum) ip_rowsum_body(D, vb, ax);
+  else if constexpr (Ph == kIpGuess) ip_guess_body(D, vb);
+  else if constexpr (Ph == kIpResidualInit) bi_residual_body(D, 1, Ps[it.x].max_iter, vb, vg, ax);
+  else if constexpr (Ph == kIpResidual) bi_residual_body(D, 0, Ps[it.x].max_iter, vb, vg, ax);
+  else if constexpr (Ph == kIpP) bi_p_body(D, vb, vg, ax);
+  else if constexpr (Ph == kIpV) bi_v_body(D, vb, vg, ax);
+  else if constexpr (Ph == kIpS) bi_s_body(D, vb, vg, ax);
+  else if constexpr (Ph == kIpT) bi_t_body(D, vb, vg, ax);
+  else if constexpr (Ph == kIpXr) bi_xr_body(D, Ps[it.x].max_iter, vb, vg, ax);
+  else if constexpr (Ph == kIpMove) ip_move_body(D, vb);
+}
+
+// the scan of the block sums: one block of kScanT threads per (job, axis)
+__global__ void __launch_bounds__(kScanT) k_ipb_scan_parts(const IpDev* __restrict__ Ds,
+                                                           const int4* __restrict__ items) {
+  const int4 it = items[blockIdx.x];
+  const IpDev& D = Ds[it.x];
+  scan_parts_body(D.scan_part, it.z, D.slot_off, D.n_mp, it.w);
+}
+
+// both solver states of every job into one array (one copy to the host)
+__global__ void k_ipb_states(const IpDev* __restrict__ Ds, const int* __restrict__ jobs, int n, BiState* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < 2 * n) out[k] = Ds[jobs[k >> 1]].st[k & 1];
+}
+
 int blocks_for(int n) { return std::max(1, (n + kB - 1) / kB); }
 
 }  // namespace
 
-// Runs the initial place on the device; on return the host model's
-// instances (and pins) are at the solution.  stats may be null.
+// Rows per thread of the solver phases when the grid is not capped: four
+// rows give each warp four SpMV windows (the next one's row data fetched
+// while the current one is summed) and each thread four vector elements in
+// flight, and divide the blocks' fixed costs (work item, tables, FP64 block
+// reduction) by four.
+constexpr int kSolveRows = 4;
+
 struct IpSizes {
   size_t nnz_cap = 1, bytes = 0;
   int grid = 1;
@@ -1158,8 +1293,9 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
     if (deg > 1 && (int)deg < m.p.initial_place_max_fanout) nnz += 4 * deg - 6;
   }
   z.nnz_cap = std::max<size_t>(nnz, 1);
-  const int nb_mov = blocks_for((int)nP);
-  z.grid = std::max(1, std::min(nb_mov, grid_cap));
+  // kSolveRows rows per thread (and a window of kSolveRows rows per warp
+  // in flight in the SpMV), at most grid_cap blocks per axis
+  z.grid = std::max(1, std::min((int)((nP + (size_t)kB * kSolveRows - 1) / ((size_t)kB * kSolveRows)), grid_cap));
   const size_t scan_blocks = blocks_for((int)n_mp);
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
@@ -1178,16 +1314,47 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
 // (a cooperative grid has at most 8 blocks of kB threads per SM, 2 axes)
 size_t initial_place_bytes(const HostModel& m, int sm_count) { return ip_sizes(m, sm_count * 8).bytes; }
 
-int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& timer,
-                      void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev) {
+// One job's initial place on the device: its scratch, tables and solver
+// state (ip_setup), the rounds (run_initial_place's loop, or the batched
+// form's lockstep rounds), and the read-back (ip_finish).
+struct IpRun {
+  HostModel* m = nullptr;
+  cudaStream_t s = nullptr;
+  cudaMemPool_t pool = nullptr;
+  cudaEvent_t sync_ev = nullptr;
+  IpDev D;
+  IpParams P;
+  int nP = 0, nb_mov = 0, grid = 1, scan_blocks = 1;
+  bool cluster = false, coop = false;
+  int coop_attr = 0, per_sm = 0;
+  std::vector<int2> ctr;         // host centres (read back at the end)
+  BiState* st_h = nullptr;       // pinned solver states [2] (+ GridBar)
+  int rounds = 0, iters[2] = {0, 0}, coop_rounds = 0;
+  float err = 0.0f;
+  bool finished = false;         // the rounds are over (stop test or limit)
+  double t_start = 0.0;
+};
+
+namespace {
+double wall_now() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev,
+             IpRun& R) {
   static_assert(2 * sizeof(BiState) + sizeof(GridBar) <= sizeof(HostPinned::ip_state),
                 "pinned solver state too small");
+  R.m = &m;
+  R.s = s;
+  R.pool = pool;
+  R.sync_ev = sync_ev;
+  R.st_h = static_cast<BiState*>(pinned);
+  R.t_start = wall_now();
+  IpDev& D = R.D;
   const gpl_params& prm = m.p;
-  // verbose_level >= 2: wall time of the host preparation and of each round
-  const auto wall = [] { return std::chrono::duration<double, std::milli>(
-                             std::chrono::steady_clock::now().time_since_epoch()).count(); };
-  const double t_start = wall();
-  IpDev D;
+  const auto wall = wall_now;
+  const double t_start = R.t_start;
   D.n_mov = (int)m.place_insts.size();
   D.n_pins = m.n_pins;
   D.n_nets = m.n_nets;
@@ -1311,23 +1478,90 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     printf("[InitialPlace] host arrays %.2f ms, device scratch %.1f MB + uploads %.2f ms\n", t_host - t_start,
            z.bytes / 1e6, wall() - t_host);
   }
-  BiState* st_h = static_cast<BiState*>(pinned);
   if (rc) {
     set_error("initial place: upload failed");
     dev_free(D.mem, pool, s);
+    D.mem = nullptr;
     return rc;
   }
-  IpParams P;
+  IpParams& P = R.P;
   P.max_fanout = prm.initial_place_max_fanout;
   P.min_diff = prm.initial_place_min_diff_length;
   P.weight_scale = prm.initial_place_net_weight_scale;
   P.max_iter = prm.initial_place_max_solver_iter;
-  const dim3 g2(nb_mov, 2), gs(grid, 2);
+  R.nP = nP;
+  R.nb_mov = nb_mov;
+  R.grid = grid;
+  R.scan_blocks = scan_blocks;
+  R.cluster = cluster;
+  R.coop = coop;
+  R.coop_attr = coop_attr;
+  R.per_sm = per_sm;
+  R.ctr.assign(ctr.data(), ctr.data() + nP);
   if (prm.verbose_level >= 2)
     printf("[InitialPlace] setup %.2f ms (host arrays, scratch, upload)\n", wall() - t_start);
+  return GPL_OK;
+}
+
+// After the rounds: the solution's centres back to the host model (when a
+// round ran), the scratch released, the statistics.
+int ip_finish(IpRun& R, gpl_ip_stats* stats, int rc) {
+  HostModel& m = *R.m;
+  IpDev& D = R.D;
+  const double t_end = wall_now();
+  unsigned fill_overflow = 0;
+  if (!rc && D.mem) {
+    if (cudaMemcpyAsync(R.ctr.data(), D.ctr, R.nP * 8, cudaMemcpyDeviceToHost, R.s) != cudaSuccess ||
+        cudaMemcpyAsync(&fill_overflow, D.counters + kFillOverflow, sizeof(unsigned), cudaMemcpyDeviceToHost, R.s) !=
+            cudaSuccess ||
+        host_wait(R.s, R.sync_ev) != cudaSuccess) rc = GPL_ERR_CUDA;
+  }
+  if (D.mem) dev_free(D.mem, R.pool, R.s);
+  D.mem = nullptr;
+  if (rc) { set_error("initial place: CUDA error"); return rc; }
+  if (fill_overflow) { set_error("initial place: B2B entries exceeded their bound"); return GPL_ERR_CUDA; }
+  if (R.rounds > 0)
+    for (int k = 0; k < R.nP; k++) host_set_inst_center(m, m.place_insts[k], R.ctr[k].x, R.ctr[k].y);
+  if (m.p.verbose_level >= 2) printf("[InitialPlace] read-back and release %.2f ms\n", wall_now() - t_end);
+  if (stats) {
+    stats->iterations = R.rounds;
+    stats->last_error = R.err;
+    stats->last_hpwl = 0;
+    stats->solver_iters_x = R.iters[0];
+    stats->solver_iters_y = R.iters[1];
+    stats->cooperative_rounds = R.coop_rounds;
+  }
+  return GPL_OK;
+}
+
+// The round's end for one job: its solver states give the error
+// (solver.error() = sqrt(|r|^2 / |b|^2)) and the stop test
+// (src/initialPlace.cpp:93-99).
+void ip_round_done(IpRun& R, int round, const BiState* st) {
+  const float ex = st[0].rhs_sq > 0 ? (float)sqrt(st[0].rr / st[0].rhs_sq) : 0.0f;
+  const float ey = st[1].rhs_sq > 0 ? (float)sqrt(st[1].rr / st[1].rhs_sq) : 0.0f;
+  R.err = std::max(ex, ey);
+  R.iters[0] = st[0].i;
+  R.iters[1] = st[1].i;
+  R.rounds = round;
+  if ((R.err <= 1e-5 && round >= 5) || round >= R.m->p.initial_place_max_iter) R.finished = true;
+}
+
+int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* stats, Timer& timer,
+                      void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev) {
+  IpRun R;
+  int rc = ip_setup(m, s, sm_count, pinned, pool, sync_ev, R);
+  if (rc) return rc;
+  const gpl_params& prm = m.p;
+  IpDev& D = R.D;
+  const IpParams& P = R.P;
+  const int nP = R.nP, nb_mov = R.nb_mov, grid = R.grid, scan_blocks = R.scan_blocks;
+  bool cluster = R.cluster, coop = R.coop;
+  const int coop_attr = R.coop_attr, per_sm = R.per_sm, mode = prm.ip_solver;
+  BiState* st_h = R.st_h;
+  const dim3 g2(nb_mov, 2), gs(grid, 2);
+  const auto wall = wall_now;
   double t_round = wall();
-  float err = 0.0f;
-  int rounds = 0, iters[2] = {0, 0}, coop_rounds = 0;
   // The round's assembly (11 kernels) and a chunk of 8 solver iterations of
   // the phase form (48 kernels) have fixed arguments for the whole job, so
   // each is captured once as a CUDA graph and replayed (one launch instead
@@ -1389,7 +1623,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
       const cudaError_t ce = cudaGetLastError();
       if (ce == cudaSuccess) {
         solved = true;
-        coop_rounds++;
+        R.coop_rounds++;
       } else {
         // not launched (no room for the cluster): the grid forms below
         if (prm.verbose_level > 0)
@@ -1420,7 +1654,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
             host_wait(s, sync_ev) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
         if (bar_h->err == 0) {
           solved = true;
-          coop_rounds++;
+          R.coop_rounds++;
         } else {
           // a barrier wait ran out: solve this round again phase by phase
           coop = false;
@@ -1450,44 +1684,262 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     timer.count(1);
     if (cudaMemcpyAsync(st_h, D.st, 2 * sizeof(BiState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         host_wait(s, sync_ev) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
-    // solver.error() = sqrt(|r|^2 / |b|^2)
-    float ex = st_h[0].rhs_sq > 0 ? (float)sqrt(st_h[0].rr / st_h[0].rhs_sq) : 0.0f;
-    float ey = st_h[1].rhs_sq > 0 ? (float)sqrt(st_h[1].rr / st_h[1].rhs_sq) : 0.0f;
-    err = std::max(ex, ey);
-    iters[0] = st_h[0].i; iters[1] = st_h[1].i;
-    rounds = round;
+    ip_round_done(R, round, st_h);
     if (prm.verbose_level >= 2) {
       const double t = wall();
-      printf("[InitialPlace] Iter: %d error: %g solver iterations: %d %d (%.2f ms)\n", round, err, iters[0],
-             iters[1], t - t_round);
+      printf("[InitialPlace] Iter: %d error: %g solver iterations: %d %d (%.2f ms)\n", round, R.err, R.iters[0],
+             R.iters[1], t - t_round);
       t_round = t;
     }
-    if (err <= 1e-5 && round >= 5) break;
-  }
-  const double t_end = wall();
-  unsigned fill_overflow = 0;
-  if (!rc) {
-    if (cudaMemcpyAsync(ctr.data(), D.ctr, nP * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(&fill_overflow, D.counters + kFillOverflow, sizeof(unsigned), cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
-        host_wait(s, sync_ev) != cudaSuccess) rc = GPL_ERR_CUDA;
+    if (R.finished) break;
   }
   if (assembly_exec) cudaGraphExecDestroy(assembly_exec);
   if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
-  dev_free(D.mem, pool, s);
-  if (rc) { set_error("initial place: CUDA error"); return rc; }
-  if (fill_overflow) { set_error("initial place: B2B entries exceeded their bound"); return GPL_ERR_CUDA; }
-  if (rounds > 0)
-    for (int k = 0; k < nP; k++) host_set_inst_center(m, m.place_insts[k], ctr[k].x, ctr[k].y);
-  if (prm.verbose_level >= 2) printf("[InitialPlace] read-back and release %.2f ms\n", wall() - t_end);
-  if (stats) {
-    stats->iterations = rounds;
-    stats->last_error = err;
-    stats->last_hpwl = 0;
-    stats->solver_iters_x = iters[0];
-    stats->solver_iters_y = iters[1];
-    stats->cooperative_rounds = coop_rounds;
+  (void)nP;
+  return ip_finish(R, stats, rc);
+}
+
+// ------------------------------------------------------------ batched form
+// The rounds of many jobs in lockstep: every round, each member's assembly
+// phases run as one launch per phase over the work table, then chunks of
+// eight solver iterations (six launches each) until every member's two
+// solves are done (a member that finished early skips the later chunks'
+// blocks: every phase body returns at once on a finished solve, as it does
+// in the job's own chunks), then the move; then each member's error and stop
+// test as run_initial_place takes them.  A member leaves when its rounds
+// end.  Each membership's assembly and chunk are captured as CUDA graphs.
+namespace {
+
+enum IpTable { kTPos = 0, kTBound, kTScan, kTParts, kTRowptr, kTRowsum, kTMov, kTSolve, kTTables };
+
+// the work items of one member in each table
+void ip_items(const IpRun& R, int k, std::vector<int4> (&t)[kTTables]) {
+  const HostModel& m = *R.m;
+  for (int b = 0; b < blocks_for(m.n_pins); b++) t[kTPos].push_back(make_int4(k, b, 0, 0));
+  for (int b = 0; b < blocks_for(m.n_nets); b++) t[kTBound].push_back(make_int4(k, b, 0, 0));
+  for (int a = 0; a < 2; a++) {
+    for (int b = 0; b < R.scan_blocks; b++) t[kTScan].push_back(make_int4(k, b, R.scan_blocks, a));
+    t[kTParts].push_back(make_int4(k, 0, R.scan_blocks, a));
+    for (int b = 0; b < blocks_for(R.nP + 1); b++) t[kTRowptr].push_back(make_int4(k, b, 0, a));
+    for (int b = 0; b < R.nb_mov; b++) t[kTRowsum].push_back(make_int4(k, b, R.nb_mov, a));
+    for (int b = 0; b < R.grid; b++) t[kTSolve].push_back(make_int4(k, b, R.grid, a));
   }
+  for (int b = 0; b < R.nb_mov; b++) t[kTMov].push_back(make_int4(k, b, 0, 0));
+}
+
+size_t ip_item_count(const IpRun& R) {
+  const HostModel& m = *R.m;
+  return (size_t)blocks_for(m.n_pins) + blocks_for(m.n_nets) +
+         2 * ((size_t)R.scan_blocks + 1 + blocks_for(R.nP + 1) + R.nb_mov + R.grid) + R.nb_mov;
+}
+
+using IpBatchKernel = void (*)(const IpDev*, const IpParams*, const int4*);
+
+}  // namespace
+
+int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* launches) {
+  std::vector<IpRun> R(n);
+  std::vector<char> active(n, 0);
+  size_t max_items = 0;
+  bool verbose = false;
+  for (int k = 0; k < n; k++) verbose |= jobs[k].m->p.verbose_level >= 2;
+  const double t_start = wall_now();
+  for (int k = 0; k < n; k++) {
+    IpBatchJob& J = jobs[k];
+    J.status = GPL_OK;
+    if (J.m->p.initial_place_max_iter <= 0) continue;
+    J.status = ip_setup(*J.m, J.s, sm_count, J.pinned, J.pool, J.sync_ev, R[k]);
+    if (!J.status && host_wait(J.s, J.sync_ev) != cudaSuccess) J.status = ip_finish(R[k], nullptr, GPL_ERR_CUDA);
+    if (J.status) continue;
+    active[k] = 1;
+    max_items += ip_item_count(R[k]);
+  }
+  int rc = GPL_OK;
+  cudaStream_t bs = nullptr;
+  char* dmem = nullptr;
+  char* hmem = nullptr;
+  cudaGraphExec_t assembly_exec = nullptr, chunk_exec = nullptr;
+  long long nl = 0;
+  std::vector<int> mem;
+  for (int k = 0; k < n; k++)
+    if (active[k]) mem.push_back(k);
+  if (!mem.empty()) {
+    // device: the members' tables and parameters, the work items, the
+    // member list and the gathered solver states; pinned: items, list, states
+    const size_t b_ds = (size_t)n * sizeof(IpDev), b_ps = (size_t)n * sizeof(IpParams);
+    const size_t b_items = max_items * sizeof(int4), b_list = (size_t)n * sizeof(int),
+                 b_st = 2 * (size_t)n * sizeof(BiState);
+    auto rnd = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t o_ps = rnd(b_ds), o_items = o_ps + rnd(b_ps), o_list = o_items + rnd(b_items),
+                 o_st = o_list + rnd(b_list), total = o_st + rnd(b_st);
+    const size_t h_list = rnd(b_items), h_st = h_list + rnd(b_list), h_total = h_st + rnd(b_st);
+    std::vector<IpDev> ds(n);
+    std::vector<IpParams> ps(n);
+    int maxit = 0;
+    for (int k : mem) {
+      ds[k] = R[k].D;
+      ps[k] = R[k].P;
+      maxit = std::max(maxit, R[k].P.max_iter);
+    }
+    if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void**)&dmem, total) != cudaSuccess || cudaMallocHost((void**)&hmem, h_total) != cudaSuccess ||
+        cudaMemcpyAsync(dmem, ds.data(), b_ds, cudaMemcpyHostToDevice, bs) != cudaSuccess ||
+        cudaMemcpyAsync(dmem + o_ps, ps.data(), b_ps, cudaMemcpyHostToDevice, bs) != cudaSuccess ||
+        cudaStreamSynchronize(bs) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("batched initial place: setup failed");
+      rc = GPL_ERR_CUDA;
+    }
+    const IpDev* d_ds = reinterpret_cast<const IpDev*>(dmem);
+    const IpParams* d_ps = reinterpret_cast<const IpParams*>(dmem + o_ps);
+    const int4* d_items = reinterpret_cast<const int4*>(dmem + o_items);
+    const int* d_list = reinterpret_cast<const int*>(dmem + o_list);
+    BiState* d_st = reinterpret_cast<BiState*>(dmem + o_st);
+    int4* h_items = reinterpret_cast<int4*>(hmem);
+    int* h_lst = reinterpret_cast<int*>(hmem + h_list);
+    const BiState* h_states = reinterpret_cast<const BiState*>(hmem + h_st);
+    int off[kTTables] = {}, cnt[kTTables] = {};
+    int n_mem = 0;
+    auto L = [&](IpBatchKernel kern, int table, size_t smem) {
+      if (!cnt[table]) return;
+      kern<<<cnt[table], kB, smem, bs>>>(d_ds, d_ps, d_items + off[table]);
+      nl++;
+    };
+    auto gather = [&]() {
+      k_ipb_states<<<(2 * n_mem + 127) / 128, 128, 0, bs>>>(d_ds, d_list, n_mem, d_st);
+      nl++;
+      cudaMemcpyAsync(hmem + h_st, d_st, 2 * (size_t)n_mem * sizeof(BiState), cudaMemcpyDeviceToHost, bs);
+    };
+    auto assembly = [&]() {
+      L(k_ipb<kIpPos>, kTPos, 0);
+      L(k_ipb<kIpBound>, kTBound, 0);
+      L(k_ipb<kIpCount>, kTScan, 0);
+      L(k_ipb<kIpScanBlocks>, kTScan, 0);
+      if (cnt[kTParts]) {
+        k_ipb_scan_parts<<<cnt[kTParts], kScanT, 0, bs>>>(d_ds, d_items + off[kTParts]);
+        nl++;
+      }
+      L(k_ipb<kIpScanAdd>, kTScan, 0);
+      L(k_ipb<kIpRowptr>, kTRowptr, 0);
+      L(k_ipb<kIpFill>, kTScan, 0);
+      L(k_ipb<kIpRowsum>, kTRowsum, 0);
+      L(k_ipb<kIpGuess>, kTMov, 0);
+      L(k_ipb<kIpResidualInit>, kTSolve, stage_bytes(kB));
+    };
+    auto chunk = [&]() {
+      for (int k = 0; k < 8; k++) {
+        L(k_ipb<kIpResidual>, kTSolve, stage_bytes(kB));
+        L(k_ipb<kIpP>, kTSolve, 0);
+        L(k_ipb<kIpV>, kTSolve, stage_bytes(kB));
+        L(k_ipb<kIpS>, kTSolve, 0);
+        L(k_ipb<kIpT>, kTSolve, stage_bytes(kB));
+        L(k_ipb<kIpXr>, kTSolve, 0);
+      }
+      gather();
+    };
+    // a captured body launches its kernels once per replay: count them
+    // when replayed, not when captured
+    auto capture = [&](auto&& body, long long& per_replay) -> cudaGraphExec_t {
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t e = nullptr;
+      const long long before = nl;
+      if (cudaStreamBeginCapture(bs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      body();
+      if (cudaStreamEndCapture(bs, &g) != cudaSuccess || !g || cudaGraphInstantiate(&e, g, 0) != cudaSuccess)
+        e = nullptr;
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      per_replay = nl - before;
+      nl = before;
+      return e;
+    };
+    auto replay = [&](cudaGraphExec_t e, auto&& body, long long per_replay) {
+      if (e) {
+        if (cudaGraphLaunch(e, bs) != cudaSuccess) return false;
+        nl += per_replay;
+      } else {
+        body();
+      }
+      return cudaGetLastError() == cudaSuccess;
+    };
+    long long n_assembly = 0, n_chunk = 0;
+    bool layout_changed = true;
+    if (verbose) printf("[InitialPlace] batched: %d jobs set up in %.2f ms\n", (int)mem.size(), wall_now() - t_start);
+    for (int round = 1; !rc && !mem.empty(); round++) {
+      const double t_round = wall_now();
+      int chunks = 0;
+      if (layout_changed) {
+        // the members' work items and list (pinned), then up to the device
+        std::vector<int4> t[kTTables];
+        for (int q = 0; q < (int)mem.size(); q++) ip_items(R[mem[q]], mem[q], t);
+        int at = 0;
+        for (int tb = 0; tb < kTTables; tb++) {
+          off[tb] = at;
+          cnt[tb] = (int)t[tb].size();
+          std::copy(t[tb].begin(), t[tb].end(), h_items + at);
+          at += cnt[tb];
+        }
+        n_mem = (int)mem.size();
+        std::copy(mem.begin(), mem.end(), h_lst);
+        if (cudaMemcpyAsync(dmem + o_items, h_items, (size_t)at * sizeof(int4), cudaMemcpyHostToDevice, bs) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(dmem + o_list, h_lst, (size_t)n_mem * sizeof(int), cudaMemcpyHostToDevice, bs) !=
+                cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+        if (assembly_exec) cudaGraphExecDestroy(assembly_exec);
+        if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+        assembly_exec = capture(assembly, n_assembly);
+        chunk_exec = capture(chunk, n_chunk);
+        layout_changed = false;
+      }
+      if (!replay(assembly_exec, assembly, n_assembly)) { rc = GPL_ERR_CUDA; break; }
+      for (int it = 0; it <= 2 * maxit + 2; it += 8) {
+        if (!replay(chunk_exec, chunk, n_chunk) || cudaStreamSynchronize(bs) != cudaSuccess) {
+          rc = GPL_ERR_CUDA;
+          break;
+        }
+        chunks++;
+        bool all = true;
+        for (int q = 0; q < n_mem && all; q++) all = h_states[2 * q].done && h_states[2 * q + 1].done;
+        if (all) break;
+      }
+      if (rc) break;
+      L(k_ipb<kIpMove>, kTMov, 0);
+      gather();
+      if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(bs) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
+      std::vector<int> next;
+      for (int q = 0; q < n_mem; q++) {
+        IpRun& r = R[mem[q]];
+        ip_round_done(r, round, h_states + 2 * q);
+        if (r.m->p.verbose_level >= 2)
+          printf("[InitialPlace] Iter: %d error: %g solver iterations: %d %d (batched, %d jobs)\n", round, r.err,
+                 r.iters[0], r.iters[1], n_mem);
+        if (!r.finished) next.push_back(mem[q]);
+      }
+      if (verbose)
+        printf("[InitialPlace] batched round %d: %d jobs, %d chunks of 8 solver iterations, %.2f ms\n", round, n_mem,
+               chunks, wall_now() - t_round);
+      layout_changed = next.size() != mem.size();
+      mem.swap(next);
+    }
+    if (rc) {
+      cudaGetLastError();
+      set_error("batched initial place: CUDA error");
+    }
+  }
+  if (assembly_exec) cudaGraphExecDestroy(assembly_exec);
+  if (chunk_exec) cudaGraphExecDestroy(chunk_exec);
+  if (bs) cudaStreamSynchronize(bs);
+  if (dmem) cudaFree(dmem);
+  if (hmem) cudaFreeHost(hmem);
+  if (bs) cudaStreamDestroy(bs);
+  const double t_end = wall_now();
+  for (int k = 0; k < n; k++)
+    if (active[k]) jobs[k].status = ip_finish(R[k], jobs[k].stats, rc);
+  if (verbose) printf("[InitialPlace] batched: read-back of %d jobs %.2f ms\n", n, wall_now() - t_end);
+  if (launches) *launches = nl;
   return GPL_OK;
 }
 

@@ -1916,4 +1916,45 @@ gpl_status gpl_initial_place(gpl_job* j, gpl_ip_stats* st) {
                                        j->sync_ev);
 }
 
+gpl_status gpl_batch_initial_place(gpl_job* const* jobs, int32_t n_jobs, gpl_ip_stats* stats, gpl_status* status,
+                                   int64_t* kernel_launches) {
+  if (kernel_launches) *kernel_launches = 0;
+  if (!jobs || n_jobs <= 0) { set_error("gpl_batch_initial_place: no jobs"); return GPL_ERR_INVALID_ARG; }
+  for (int k = 0; k < n_jobs; k++) {
+    if (!jobs[k]) { set_error("gpl_batch_initial_place: null job"); return GPL_ERR_INVALID_ARG; }
+    if (jobs[k]->nb_ready) {
+      set_error("gpl_batch_initial_place: initial place must run before the Nesterov stage");
+      return GPL_ERR_BAD_STATE;
+    }
+    if (jobs[k]->device != jobs[0]->device) {
+      set_error("gpl_batch_initial_place: the jobs must be on one device");
+      return GPL_ERR_INVALID_ARG;
+    }
+    for (int q = 0; q < k; q++)
+      if (jobs[q] == jobs[k]) { set_error("gpl_batch_initial_place: a job is listed twice"); return GPL_ERR_INVALID_ARG; }
+  }
+  cudaSetDevice(jobs[0]->device);
+  int sm = 0;
+  GPL_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, jobs[0]->device));
+  // each job as gpl_initial_place prepares it: centred (unless incremental),
+  // its Nesterov setup's host part started on its worker thread
+  std::vector<IpBatchJob> b(n_jobs);
+  for (int k = 0; k < n_jobs; k++) {
+    gpl_job* j = jobs[k];
+    if (!j->m.p.incremental_place_mode) host_place_center(j->m);
+    if (stats) memset(&stats[k], 0, sizeof(stats[k]));
+    if (j->m.p.initial_place_max_iter > 0) start_static_prep(j);
+    b[k].m = &j->m;
+    b[k].s = j->stream;
+    b[k].pinned = j->pinned->ip_state;
+    b[k].pool = j->pool;
+    b[k].sync_ev = j->sync_ev;
+    b[k].stats = stats ? &stats[k] : nullptr;
+  }
+  const int rc = run_initial_place_batch(b.data(), n_jobs, sm, kernel_launches);
+  for (int k = 0; k < n_jobs; k++)
+    if (status) status[k] = (gpl_status)b[k].status;
+  return (gpl_status)rc;
+}
+
 }  // extern "C"

@@ -163,6 +163,22 @@ def batch_nesterov_run(placers, max_iters: int = 0):
     return list(stats), list(status), int(launches.value)
 
 
+def batch_initial_place(placers):
+    """gpl_batch_initial_place: the initial places of several jobs (Placer
+    objects before nesterov_init, one device) in lockstep rounds, one launch
+    per phase for all of them.  Returns ([IpStats], [status],
+    kernel_launches); every job's result equals initial_place on it alone
+    (kernel-per-phase solver)."""
+    lib = load()
+    n = len(placers)
+    handles = (C.c_void_p * n)(*[p.h.value for p in placers])
+    stats = (_abi.IpStats * n)()
+    status = (C.c_int32 * n)()
+    launches = C.c_int64(0)
+    check(lib.gpl_batch_initial_place(handles, n, stats, status, C.byref(launches)))
+    return list(stats), list(status), int(launches.value)
+
+
 def poisson_solve(density_dev_ptr: int, phi_dev_ptr: int, fx_dev_ptr: int, fy_dev_ptr: int,
                   nx: int, ny: int, bin_size_x: int, bin_size_y: int, stream: int = 0):
     """gpl_poisson_solve on device pointers (e.g. torch tensors' data_ptr())."""
