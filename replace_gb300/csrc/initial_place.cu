@@ -79,6 +79,8 @@ struct IpDev {
   BiState* st;             // [2]
   BiState* st_h;           // pinned mirror
   int parts = 0;
+  int rows_blk = 0;        // rows per block of the kernel-per-phase SpMV (a multiple of 32)
+  int2* win;               // [2][parts] x window (first index, length) of each SpMV block; length 0: none
   size_t nnz_cap = 0;
   char* mem = nullptr;
   size_t bytes = 0;
@@ -390,6 +392,40 @@ __device__ __forceinline__ void ip_rowsum_body(const IpDev& D, int vb, int axis)
   D.b[axis * D.n_mov + i] = rhs;
 }
 
+// The x window of SpMV block vb: its own rows and every column its rows'
+// entries read, as (first index, length), or length 0 when that is wider
+// than kXWin (the block then gathers from global memory).
+constexpr int kXWinMax = 5632;
+__device__ __forceinline__ void ip_window_body(const IpDev& D, int vb, int axis) {
+  __shared__ int sh[2][kB / 32];
+  const int n = D.n_mov;
+  const int r0 = vb * D.rows_blk, r1 = min(r0 + D.rows_blk, n);
+  int lo = r0, hi = r1;
+  if (r0 < r1) {
+    const int32_t* rp = D.rowptr + axis * (n + 1);
+    const int32_t* col = D.col + axis * D.nnz_cap;
+    const int k1 = (int)min((size_t)rp[r1], D.nnz_cap);
+    for (int k = rp[r0] + threadIdx.x; k < k1; k += blockDim.x) {
+      const int c = col[k];
+      lo = min(lo, c);
+      hi = max(hi, c + 1);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][wid] = lo; sh[1][wid] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kB / 32; w++) { lo = min(lo, sh[0][w]); hi = max(hi, sh[1][w]); }
+    const bool fits = r0 < r1 && hi - lo <= kXWinMax;
+    D.win[axis * D.parts + vb] = make_int2(fits ? lo : 0, fits ? hi - lo : 0);
+  }
+}
+
 // The per-job launches of the assembly phases (blockIdx.y = axis); the
 // batched form runs the same bodies from a work table.
 __global__ void k_ip_pos(const __grid_constant__ IpDev D) { ip_pos_body(D, (int)blockIdx.x); }
@@ -411,6 +447,7 @@ __global__ void k_ip_fill(const __grid_constant__ IpDev D, const __grid_constant
   ip_fill_body(D, P, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
 __global__ void k_ip_rowsum(const __grid_constant__ IpDev D) { ip_rowsum_body(D, (int)blockIdx.x, (int)blockIdx.y); }
+__global__ void k_ip_window(const __grid_constant__ IpDev D) { ip_window_body(D, (int)blockIdx.x, (int)blockIdx.y); }
 
 // ------------------------------------------------------------ solver
 // Sparse products: each warp takes windows of 32 consecutive rows (row
@@ -445,6 +482,16 @@ constexpr int kStage = 1024;   // floats of shared memory per warp
 // dynamic shared memory of a launch whose blocks have `threads` threads
 constexpr size_t stage_bytes(int threads) { return (size_t)(threads / 32) * kStage * sizeof(float); }
 
+// The kernel-per-phase SpMV gives each block a contiguous range of rows and
+// stages the slice of the multiplied vector that the range's entries read
+// (its x window: the lowest to the highest column, at most kXWin floats)
+// in shared memory after the warps' product stages, so that the gathers hit
+// shared memory instead of L1/L2.  A block whose window is wider reads the
+// vector from global memory.  Product stages (32 KB) and window (22 KB) fit
+// four blocks per SM, the occupancy the grid is sized for.
+constexpr int kXWin = kXWinMax;
+constexpr size_t spmv_bytes() { return stage_bytes(kB) + (size_t)kXWin * sizeof(float); }
+
 // Row data of one window, fetched a window ahead.
 struct RowFetch {
   int s, e;        // the lane's row entry range
@@ -475,12 +522,11 @@ __device__ __forceinline__ void prefetch_window(const int32_t* col, const float*
 }
 
 // One window: returns the lane's row product (valid lanes).
-template <bool kFromL2, int kBatch>
+template <bool kFromL2, int kBatch, class Ld>
 __device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, const float* __restrict__ val,
-                                             const float* xv, const RowFetch& f, bool valid, float* stage) {
+                                             Ld ld, const RowFetch& f, bool valid, float* stage) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  auto ld = [&](int j) { return kFromL2 ? __ldcg(xv + j) : xv[j]; };
   const int s = f.s, e = f.e;
   float acc = f.acc;
   const bool long_row = e - s > kLongRow;
@@ -535,24 +581,28 @@ __device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, co
   return acc;
 }
 
-// (A xv)_i for the warp's windows w0, w0 + step, ...; epi(i, value, aux[i])
-// for every row.  All 32 lanes call it together (w0 is warp-uniform).
-template <bool kFromL2 = false, int kBatch = 16, bool kPrefetch = true, class Epi>
+// (A xv)_i for the warp's windows w0, w0 + step, ... below n_end;
+// epi(i, value, aux[i]) for every row.  All 32 lanes call it together (w0 is
+// warp-uniform).  kWin: every xv[j] is read from xs[j - lo] (the block's x
+// window in shared memory, which holds every column the rows read).
+template <bool kFromL2 = false, int kBatch = 16, bool kPrefetch = true, bool kWin = false, class Epi>
 __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float* xv, const float* aux,
-                                          int w0, int step, float* stage, Epi epi) {
-  const int n = D.n_mov;
+                                          int w0, int step, float* stage, Epi epi, int n_end = -1,
+                                          const float* xs = nullptr, int lo = 0) {
+  const int n = n_end < 0 ? D.n_mov : n_end;
   const int lane = threadIdx.x & 31;
-  const int32_t* __restrict__ rp = D.rowptr + axis * (n + 1);
+  auto ld = [&](int j) { return kWin ? xs[j - lo] : (kFromL2 ? __ldcg(xv + j) : xv[j]); };
+  const int32_t* __restrict__ rp = D.rowptr + axis * (D.n_mov + 1);
   const int32_t* __restrict__ col = D.col + axis * D.nnz_cap;
   const float* __restrict__ val = D.val + axis * D.nnz_cap;
-  const float* __restrict__ dg = D.diag + axis * n;
+  const float* __restrict__ dg = D.diag + axis * D.n_mov;
   auto fetch = [&](int w) {
     RowFetch f{0, 0, 0.0f, 0.0f};
     const int i = w + lane;
     if (i < n) {
       f.s = rp[i];
       f.e = rp[i + 1];
-      f.acc = __fmul_rn(dg[i], kFromL2 ? __ldcg(xv + i) : xv[i]);
+      f.acc = __fmul_rn(dg[i], ld(i));
       f.aux = aux ? (kFromL2 ? __ldcg(aux + i) : aux[i]) : 0.0f;
     }
     return f;
@@ -564,7 +614,7 @@ __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float*
     if (kPrefetch) prefetch_window(col, val, next, w + step + lane < n);
     const RowFetch next2 = fetch(w + 2 * step);
     const int i = w + lane;
-    const float v = spmv_window<kFromL2, kBatch>(col, val, xv, cur, i < n, stage);
+    const float v = spmv_window<kFromL2, kBatch>(col, val, ld, cur, i < n, stage);
     if (i < n) epi(i, v, cur.aux);
     cur = next;
     next = next2;
@@ -646,6 +696,27 @@ __device__ __forceinline__ float* warp_stage() {
   return stage_all + (threadIdx.x >> 5) * kStage;
 }
 
+// The block's SpMV rows [r0, r1) and its x window: the window's slice of xv
+// copied to shared memory (after the product stages) by the whole block.
+struct BlockRows {
+  int r0, r1, lo, span;
+  const float* xs;
+};
+__device__ __forceinline__ BlockRows block_rows(const IpDev& D, const float* xv, int vb, int axis) {
+  extern __shared__ float stage_all[];
+  BlockRows b;
+  b.r0 = vb * D.rows_blk;
+  b.r1 = min(b.r0 + D.rows_blk, D.n_mov);
+  const int2 w = D.win[axis * D.parts + vb];
+  b.lo = w.x;
+  b.span = w.y;
+  float* xs = stage_all + (kB / 32) * kStage;
+  for (int k = threadIdx.x; k < b.span; k += blockDim.x) xs[k] = xv[b.lo + k];
+  __syncthreads();
+  b.xs = xs;
+  return b;
+}
+
 // block partial sums of up to 2 products, then the last block of this axis
 // runs `fin` with the totals (fixed-order reduction)
 template <int N, class Fin>
@@ -702,14 +773,17 @@ __device__ __forceinline__ void bi_residual_body(const IpDev& D, int init, int m
   float* r = D.r + axis * n;
   float* r0 = D.r0 + axis * n;
   float v[2] = {0.0f, 0.0f};
-  spmv_rows(D, axis, x, bb, vb * kB + (threadIdx.x & ~31), vgrid * kB, stage,
-            [&](int i, float ax, float bi) {
-              const float ri = bi - ax;
-              r[i] = ri;
-              r0[i] = ri;
-              v[0] = __fmaf_rn(ri, ri, v[0]);
-              v[1] = __fmaf_rn(bi, bi, v[1]);
-            });
+  const BlockRows br = block_rows(D, x, vb, axis);
+  auto epi = [&](int i, float ax, float bi) {
+    const float ri = bi - ax;
+    r[i] = ri;
+    r0[i] = ri;
+    v[0] = __fmaf_rn(ri, ri, v[0]);
+    v[1] = __fmaf_rn(bi, bi, v[1]);
+  };
+  const int w0 = br.r0 + (threadIdx.x & ~31);
+  if (br.span) spmv_rows<false, 8, true, true>(D, axis, x, bb, w0, kB, stage, epi, br.r1, br.xs, br.lo);
+  else spmv_rows<false, 8, true, false>(D, axis, x, bb, w0, kB, stage, epi, br.r1);
   reduce_and_finish<2>(D, 0, v, [&](BiState& s, const double* t) {
     if (init) {
       s.r0sq = t[0];
@@ -757,11 +831,14 @@ __device__ __forceinline__ void bi_v_body(const IpDev& D, int vb, int vgrid, int
   float* v = D.v + axis * n;
   const float* r0 = D.r0 + axis * n;
   float acc[1] = {0.0f};
-  spmv_rows(D, axis, p, r0, vb * kB + (threadIdx.x & ~31), vgrid * kB, stage,
-            [&](int i, float vi, float r0i) {
-              v[i] = vi;
-              acc[0] = __fmaf_rn(r0i, vi, acc[0]);
-            });
+  const BlockRows br = block_rows(D, p, vb, axis);
+  auto epi = [&](int i, float vi, float r0i) {
+    v[i] = vi;
+    acc[0] = __fmaf_rn(r0i, vi, acc[0]);
+  };
+  const int w0 = br.r0 + (threadIdx.x & ~31);
+  if (br.span) spmv_rows<false, 8, true, true>(D, axis, p, r0, w0, kB, stage, epi, br.r1, br.xs, br.lo);
+  else spmv_rows<false, 8, true, false>(D, axis, p, r0, w0, kB, stage, epi, br.r1);
   reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; }, vb, vgrid, axis);
 }
 
@@ -784,12 +861,15 @@ __device__ __forceinline__ void bi_t_body(const IpDev& D, int vb, int vgrid, int
   const float* s = D.s + axis * n;
   float* t = D.t + axis * n;
   float acc[2] = {0.0f, 0.0f};
-  spmv_rows(D, axis, s, s, vb * kB + (threadIdx.x & ~31), vgrid * kB, stage,
-            [&](int i, float ti, float si) {
-              t[i] = ti;
-              acc[0] = __fmaf_rn(ti, ti, acc[0]);
-              acc[1] = __fmaf_rn(ti, si, acc[1]);
-            });
+  const BlockRows br = block_rows(D, s, vb, axis);
+  auto epi = [&](int i, float ti, float si) {
+    t[i] = ti;
+    acc[0] = __fmaf_rn(ti, ti, acc[0]);
+    acc[1] = __fmaf_rn(ti, si, acc[1]);
+  };
+  const int w0 = br.r0 + (threadIdx.x & ~31);
+  if (br.span) spmv_rows<false, 8, true, true>(D, axis, s, s, w0, kB, stage, epi, br.r1, br.xs, br.lo);
+  else spmv_rows<false, 8, true, false>(D, axis, s, s, w0, kB, stage, epi, br.r1);
   reduce_and_finish<2>(D, 2, acc, [&](BiState& st, const double* tt) {
     st.w = tt[0] > 0.0 ? tt[1] / tt[0] : 0.0;
   }, vb, vgrid, axis);
@@ -818,19 +898,19 @@ __device__ __forceinline__ void bi_xr_body(const IpDev& D, int max_iter, int vb,
 }
 
 // The per-job launches of the solver phases (blockIdx.y = axis).
-__global__ void k_bi_residual(const __grid_constant__ IpDev D, int init, int max_iter) {
+__global__ void __launch_bounds__(kB, 4) k_bi_residual(const __grid_constant__ IpDev D, int init, int max_iter) {
   bi_residual_body(D, init, max_iter, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
 __global__ void k_bi_p(const __grid_constant__ IpDev D) {
   bi_p_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
-__global__ void k_bi_v(const __grid_constant__ IpDev D) {
+__global__ void __launch_bounds__(kB, 4) k_bi_v(const __grid_constant__ IpDev D) {
   bi_v_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
 __global__ void k_bi_s(const __grid_constant__ IpDev D) {
   bi_s_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
-__global__ void k_bi_t(const __grid_constant__ IpDev D) {
+__global__ void __launch_bounds__(kB, 4) k_bi_t(const __grid_constant__ IpDev D) {
   bi_t_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
 __global__ void k_bi_xr(const __grid_constant__ IpDev D, int max_iter) {
@@ -1209,7 +1289,7 @@ __global__ void k_ip_guess(const __grid_constant__ IpDev D) { ip_guess_body(D, (
 // arithmetic does not depend on the kernel they are compiled into).
 enum IpPhase {
   kIpPos = 0, kIpBound, kIpCount, kIpScanBlocks, kIpScanAdd, kIpRowptr, kIpFill, kIpRowsum, kIpGuess,
-  kIpResidualInit, kIpResidual, kIpP, kIpV, kIpS, kIpT, kIpXr, kIpMove
+  kIpResidualInit, kIpResidual, kIpP, kIpV, kIpS, kIpT, kIpXr, kIpMove, kIpWindow
 };
 
 template <int Ph>
@@ -1244,6 +1324,7 @@ __global__ void __launch_bounds__(kB, 4) k_ipb(const IpDev* __restrict__ Ds, con
   else if constexpr (Ph == kIpT) bi_t_body(D, vb, vg, ax);
   else if constexpr (Ph == kIpXr) bi_xr_body(D, Ps[it.x].max_iter, vb, vg, ax);
   else if constexpr (Ph == kIpMove) ip_move_body(D, vb);
+  else if constexpr (Ph == kIpWindow) ip_window_body(D, vb, ax);
 }
 
 // the scan of the block sums: one block of kScanT threads per (job, axis)
@@ -1274,6 +1355,7 @@ constexpr int kSolveRows = 4;
 struct IpSizes {
   size_t nnz_cap = 1, bytes = 0;
   int grid = 1;
+  int rows_blk = 32;
 };
 
 // Scratch layout of run_initial_place (the sizes its carving below takes).
@@ -1295,7 +1377,10 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   z.nnz_cap = std::max<size_t>(nnz, 1);
   // kSolveRows rows per thread (and a window of kSolveRows rows per warp
   // in flight in the SpMV), at most grid_cap blocks per axis
-  z.grid = std::max(1, std::min((int)((nP + (size_t)kB * kSolveRows - 1) / ((size_t)kB * kSolveRows)), grid_cap));
+  const int g0 = std::max(1, std::min((int)((nP + (size_t)kB * kSolveRows - 1) / ((size_t)kB * kSolveRows)), grid_cap));
+  // the SpMV's contiguous row ranges: whole windows of 32 rows per block
+  z.rows_blk = std::max(32, (int)((nP + g0 - 1) / g0 + 31) / 32 * 32);
+  z.grid = std::max(1, (int)((nP + z.rows_blk - 1) / z.rows_blk));
   const size_t scan_blocks = blocks_for((int)n_mp);
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
@@ -1306,6 +1391,7 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 4);
   for (int k = 0; k < 9; k++) add(2 * nP * 4);
   add(2 * 2 * (size_t)z.grid * 8); add(4 * 2 * 2 * (size_t)z.grid * 8); add(sizeof(GridBar));
+  add(2 * (size_t)z.grid * 8);
   add(16 * 4); add(2 * sizeof(BiState));
   z.bytes = bytes;
   return z;
@@ -1398,6 +1484,11 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bi_coop, kB, stage_bytes(kB));
   // the cluster solve's stages exceed the default dynamic shared-memory cap
   cudaFuncSetAttribute(k_bi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes(kClThreads));
+  // the SpMV phases' product stages and x window exceed the default cap too
+  for (const void* f : {(const void*)k_bi_residual, (const void*)k_bi_v, (const void*)k_bi_t,
+                        (const void*)k_ipb<kIpResidualInit>, (const void*)k_ipb<kIpResidual>,
+                        (const void*)k_ipb<kIpV>, (const void*)k_ipb<kIpT>})
+    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_bytes());
   cudaGetLastError();
   // ip_solver: 0 auto, 1 kernel per phase, 2 cooperative grid, 3 cluster per axis
   const int mode = prm.ip_solver;
@@ -1415,6 +1506,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   const int nb_mov = blocks_for(nP);
   const int grid = z.grid;
   D.parts = grid;
+  D.rows_blk = z.rows_blk;
   D.n_mp = (int)mp.size();
   const int scan_blocks = blocks_for(D.n_mp);
   const double t_host = wall();
@@ -1457,6 +1549,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   D.part = (double*)take(2 * 2 * (size_t)D.parts * 8);
   D.cpart = (double*)take(4 * 2 * 2 * (size_t)D.parts * 8);
   D.bar = (GridBar*)take(sizeof(GridBar));
+  D.win = (int2*)take(2 * (size_t)grid * 8);
   D.counters = (unsigned*)take(16 * 4);
   D.st = (BiState*)take(2 * sizeof(BiState));
   int rc = GPL_OK;
@@ -1562,7 +1655,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   const dim3 g2(nb_mov, 2), gs(grid, 2);
   const auto wall = wall_now;
   double t_round = wall();
-  // The round's assembly (11 kernels) and a chunk of 8 solver iterations of
+  // The round's assembly (12 kernels) and a chunk of 8 solver iterations of
   // the phase form (48 kernels) have fixed arguments for the whole job, so
   // each is captured once as a CUDA graph and replayed (one launch instead
   // of tens: small jobs are bound by launches).  Without graphs (use_graph 0,
@@ -1579,15 +1672,16 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     k_ip_fill<<<dim3(scan_blocks, 2), kB, 0, s>>>(D, P);
     k_ip_rowsum<<<g2, kB, 0, s>>>(D);
     k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
-    k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 1, P.max_iter);
+    k_ip_window<<<gs, kB, 0, s>>>(D);
+    k_bi_residual<<<gs, kB, spmv_bytes(), s>>>(D, 1, P.max_iter);
   };
   auto phase_chunk = [&]() {
     for (int k = 0; k < 8; k++) {
-      k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 0, P.max_iter);
+      k_bi_residual<<<gs, kB, spmv_bytes(), s>>>(D, 0, P.max_iter);
       k_bi_p<<<gs, kB, 0, s>>>(D);
-      k_bi_v<<<gs, kB, stage_bytes(kB), s>>>(D);
+      k_bi_v<<<gs, kB, spmv_bytes(), s>>>(D);
       k_bi_s<<<gs, kB, 0, s>>>(D);
-      k_bi_t<<<gs, kB, stage_bytes(kB), s>>>(D);
+      k_bi_t<<<gs, kB, spmv_bytes(), s>>>(D);
       k_bi_xr<<<gs, kB, 0, s>>>(D, P.max_iter);
     }
   };
@@ -1612,7 +1706,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
       assembly();
     }
     timer.end(kKOther);
-    timer.count(11);
+    timer.count(12);
     bool solved = false;
     if (cluster) {
       // the whole solve of each axis in one cluster
@@ -1659,7 +1753,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
           // a barrier wait ran out: solve this round again phase by phase
           coop = false;
           k_ip_guess<<<nb_mov, kB, 0, s>>>(D);
-          k_bi_residual<<<gs, kB, stage_bytes(kB), s>>>(D, 1, P.max_iter);
+          k_bi_residual<<<gs, kB, spmv_bytes(), s>>>(D, 1, P.max_iter);
           timer.count(2);
         }
       }
@@ -1824,15 +1918,16 @@ int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* laun
       L(k_ipb<kIpFill>, kTScan, 0);
       L(k_ipb<kIpRowsum>, kTRowsum, 0);
       L(k_ipb<kIpGuess>, kTMov, 0);
-      L(k_ipb<kIpResidualInit>, kTSolve, stage_bytes(kB));
+      L(k_ipb<kIpWindow>, kTSolve, 0);
+      L(k_ipb<kIpResidualInit>, kTSolve, spmv_bytes());
     };
     auto chunk = [&]() {
       for (int k = 0; k < 8; k++) {
-        L(k_ipb<kIpResidual>, kTSolve, stage_bytes(kB));
+        L(k_ipb<kIpResidual>, kTSolve, spmv_bytes());
         L(k_ipb<kIpP>, kTSolve, 0);
-        L(k_ipb<kIpV>, kTSolve, stage_bytes(kB));
+        L(k_ipb<kIpV>, kTSolve, spmv_bytes());
         L(k_ipb<kIpS>, kTSolve, 0);
-        L(k_ipb<kIpT>, kTSolve, stage_bytes(kB));
+        L(k_ipb<kIpT>, kTSolve, spmv_bytes());
         L(k_ipb<kIpXr>, kTSolve, 0);
       }
       gather();
