@@ -42,7 +42,8 @@ constexpr int kB = 256;
 struct BiState {
   double rho, rho_old, alpha, w, r0sq, rhs_sq, tol2, rr, dot_r0r;
   int i, restarts, done, need_restart, zero_x;
-  int pad[3];
+  int par;                 // kernel-per-phase form: which p / v buffer holds the current iterate
+  int pad[2];
 };
 
 struct IpDev {
@@ -71,7 +72,8 @@ struct IpDev {
   float* val;
   float* diag;             // [2][n_mov]
   float* b;                // [2][n_mov]
-  float *x, *r, *r0, *p, *v, *s, *t;   // [2][n_mov]
+  float *x, *r, *r0, *s, *t;   // [2][n_mov]
+  float *p, *v;            // [2 buffers][2][n_mov] (the grid and cluster forms use buffer 0)
   double* part;            // [2][slots][parts]
   double* cpart;           // cooperative solve: [4 phases][2 axes][2][parts]
   struct GridBar* bar;     // cooperative solve: grid barrier
@@ -581,17 +583,19 @@ __device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, co
   return acc;
 }
 
-// (A xv)_i for the warp's windows w0, w0 + step, ... below n_end;
-// epi(i, value, aux[i]) for every row.  All 32 lanes call it together (w0 is
-// warp-uniform).  kWin: every xv[j] is read from xs[j - lo] (the block's x
-// window in shared memory, which holds every column the rows read).
-template <bool kFromL2 = false, int kBatch = 16, bool kPrefetch = true, bool kWin = false, class Epi>
-__device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float* xv, const float* aux,
+// (A x)_i for the warp's windows w0, w0 + step, ... below n_end, x_j = gx(j);
+// epi(i, value, aux[i]) for every row (kAuxX: aux_i = x_i).  All 32 lanes
+// call it together (w0 is warp-uniform).  kWin: every x_j is read from
+// xs[j - lo] (the block's x window in shared memory, which holds every
+// column the rows read).
+template <bool kFromL2 = false, int kBatch = 16, bool kPrefetch = true, bool kWin = false, bool kAuxX = false,
+          class GX, class Epi>
+__device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, GX gx, const float* aux,
                                           int w0, int step, float* stage, Epi epi, int n_end = -1,
                                           const float* xs = nullptr, int lo = 0) {
   const int n = n_end < 0 ? D.n_mov : n_end;
   const int lane = threadIdx.x & 31;
-  auto ld = [&](int j) { return kWin ? xs[j - lo] : (kFromL2 ? __ldcg(xv + j) : xv[j]); };
+  auto ld = [&](int j) { return kWin ? xs[j - lo] : gx(j); };
   const int32_t* __restrict__ rp = D.rowptr + axis * (D.n_mov + 1);
   const int32_t* __restrict__ col = D.col + axis * D.nnz_cap;
   const float* __restrict__ val = D.val + axis * D.nnz_cap;
@@ -602,8 +606,9 @@ __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, const float*
     if (i < n) {
       f.s = rp[i];
       f.e = rp[i + 1];
-      f.acc = __fmul_rn(dg[i], ld(i));
-      f.aux = aux ? (kFromL2 ? __ldcg(aux + i) : aux[i]) : 0.0f;
+      const float xi = ld(i);
+      f.acc = __fmul_rn(dg[i], xi);
+      f.aux = kAuxX ? xi : (aux ? (kFromL2 ? __ldcg(aux + i) : aux[i]) : 0.0f);
     }
     return f;
   };
@@ -690,19 +695,27 @@ __device__ __forceinline__ void phase_xr(float* x, float* r, const float* p, con
   }
 }
 
+// a vector read through L2 only (other blocks wrote it in the same launch)
+struct L2Vec {
+  const float* v;
+  __device__ __forceinline__ float operator()(int j) const { return __ldcg(v + j); }
+};
+
 // the calling warp's stage in the launch's dynamic shared memory
 __device__ __forceinline__ float* warp_stage() {
   extern __shared__ float stage_all[];
   return stage_all + (threadIdx.x >> 5) * kStage;
 }
 
-// The block's SpMV rows [r0, r1) and its x window: the window's slice of xv
-// copied to shared memory (after the product stages) by the whole block.
+// The block's SpMV rows [r0, r1) and its x window: x_j = gx(j) over the
+// window, written to shared memory (after the product stages) by the whole
+// block.
 struct BlockRows {
   int r0, r1, lo, span;
   const float* xs;
 };
-__device__ __forceinline__ BlockRows block_rows(const IpDev& D, const float* xv, int vb, int axis) {
+template <class GX>
+__device__ __forceinline__ BlockRows block_rows(const IpDev& D, GX gx, int vb, int axis) {
   extern __shared__ float stage_all[];
   BlockRows b;
   b.r0 = vb * D.rows_blk;
@@ -711,10 +724,15 @@ __device__ __forceinline__ BlockRows block_rows(const IpDev& D, const float* xv,
   b.lo = w.x;
   b.span = w.y;
   float* xs = stage_all + (kB / 32) * kStage;
-  for (int k = threadIdx.x; k < b.span; k += blockDim.x) xs[k] = xv[b.lo + k];
+  for (int k = threadIdx.x; k < b.span; k += blockDim.x) xs[k] = gx(b.lo + k);
   __syncthreads();
   b.xs = xs;
   return b;
+}
+
+// buffer `par` of p or v (axis `axis`)
+__device__ __forceinline__ float* pv_buf(float* base, const IpDev& D, int par, int axis) {
+  return base + ((size_t)par * 2 + axis) * D.n_mov;
 }
 
 // block partial sums of up to 2 products, then the last block of this axis
@@ -773,7 +791,8 @@ __device__ __forceinline__ void bi_residual_body(const IpDev& D, int init, int m
   float* r = D.r + axis * n;
   float* r0 = D.r0 + axis * n;
   float v[2] = {0.0f, 0.0f};
-  const BlockRows br = block_rows(D, x, vb, axis);
+  auto gx = [&](int j) { return x[j]; };
+  const BlockRows br = block_rows(D, gx, vb, axis);
   auto epi = [&](int i, float ax, float bi) {
     const float ri = bi - ax;
     r[i] = ri;
@@ -782,8 +801,8 @@ __device__ __forceinline__ void bi_residual_body(const IpDev& D, int init, int m
     v[1] = __fmaf_rn(bi, bi, v[1]);
   };
   const int w0 = br.r0 + (threadIdx.x & ~31);
-  if (br.span) spmv_rows<false, 8, true, true>(D, axis, x, bb, w0, kB, stage, epi, br.r1, br.xs, br.lo);
-  else spmv_rows<false, 8, true, false>(D, axis, x, bb, w0, kB, stage, epi, br.r1);
+  if (br.span) spmv_rows<false, 8, true, true>(D, axis, gx, bb, w0, kB, stage, epi, br.r1, br.xs, br.lo);
+  else spmv_rows<false, 8, true, false>(D, axis, gx, bb, w0, kB, stage, epi, br.r1);
   reduce_and_finish<2>(D, 0, v, [&](BiState& s, const double* t) {
     if (init) {
       s.r0sq = t[0];
@@ -792,7 +811,7 @@ __device__ __forceinline__ void bi_residual_body(const IpDev& D, int init, int m
       s.rho = s.alpha = s.w = 1.0;
       s.dot_r0r = t[0];
       s.tol2 = 1.1920928955078125e-07 * 1.1920928955078125e-07 * t[1];
-      s.i = 0; s.restarts = 0; s.done = 0; s.need_restart = 0; s.zero_x = 0;
+      s.i = 0; s.restarts = 0; s.done = 0; s.need_restart = 0; s.zero_x = 0; s.par = 0;
       if (t[1] == 0.0) { s.zero_x = 1; s.done = 1; s.rr = 0.0; }
       else loop_head(s, max_iter);
     } else {
@@ -803,11 +822,18 @@ __device__ __forceinline__ void bi_residual_body(const IpDev& D, int init, int m
   }, vb, vgrid, axis);
 }
 
-__device__ __forceinline__ void bi_p_body(const IpDev& D, int vb, int vgrid, int axis) {
+// p = r + beta (p - w v) and v = A p, alpha = rho / (r0 . v): the new p is
+// computed where it is read (the block's x window, its own rows for Xr, the
+// gathers of a block without a window) from the previous p and v, which
+// therefore live in a second buffer (S.par selects the current one).
+// kWB: entries per lane in flight in the window path (load scheduling only:
+// the arithmetic does not depend on it).
+template <int kWB = 8>
+__device__ __forceinline__ void bi_pv_body(const IpDev& D, int vb, int vgrid, int axis) {
+  float* stage = warp_stage();
   const BiState& S = D.st[axis];
   if (S.done) return;
-  // beta once per block: FP64 division is slow on this part, and every
-  // thread would otherwise divide twice
+  // beta once per block: FP64 division is slow on this part
   __shared__ float sc[2];
   if (threadIdx.x == 0) {
     const double beta = (S.rho / S.rho_old) * (S.alpha / S.w);
@@ -815,61 +841,51 @@ __device__ __forceinline__ void bi_p_body(const IpDev& D, int vb, int vgrid, int
     sc[1] = (float)S.w;
   }
   __syncthreads();
-  const int n = D.n_mov;
-  float* p = D.p + axis * n;
-  const float* r = D.r + axis * n;
-  const float* v = D.v + axis * n;
-  phase_p(p, r, v, sc[0], sc[1], vb * kB + threadIdx.x, vgrid * kB, n);
-}
-
-// v = A p, alpha = rho / (r0 . v)
-__device__ __forceinline__ void bi_v_body(const IpDev& D, int vb, int vgrid, int axis) {
-  float* stage = warp_stage();
-  if (D.st[axis].done) return;
-  const int n = D.n_mov;
-  const float* p = D.p + axis * n;
-  float* v = D.v + axis * n;
-  const float* r0 = D.r0 + axis * n;
+  const float bf = sc[0], wf = sc[1];
+  const int par = S.par;
+  const float* po = pv_buf(D.p, D, par, axis);
+  const float* vo = pv_buf(D.v, D, par, axis);
+  float* pn = pv_buf(D.p, D, par ^ 1, axis);
+  float* vn = pv_buf(D.v, D, par ^ 1, axis);
+  const float* r = D.r + axis * D.n_mov;
+  const float* r0 = D.r0 + axis * D.n_mov;
+  auto gx = [&](int j) { return __fmaf_rn(bf, __fmaf_rn(-wf, vo[j], po[j]), r[j]); };
+  const BlockRows br = block_rows(D, gx, vb, axis);
+  for (int i = br.r0 + threadIdx.x; i < br.r1; i += blockDim.x) pn[i] = br.span ? br.xs[i - br.lo] : gx(i);
   float acc[1] = {0.0f};
-  const BlockRows br = block_rows(D, p, vb, axis);
   auto epi = [&](int i, float vi, float r0i) {
-    v[i] = vi;
+    vn[i] = vi;
     acc[0] = __fmaf_rn(r0i, vi, acc[0]);
   };
   const int w0 = br.r0 + (threadIdx.x & ~31);
-  if (br.span) spmv_rows<false, 8, true, true>(D, axis, p, r0, w0, kB, stage, epi, br.r1, br.xs, br.lo);
-  else spmv_rows<false, 8, true, false>(D, axis, p, r0, w0, kB, stage, epi, br.r1);
+  if (br.span) spmv_rows<false, kWB, true, true>(D, axis, gx, r0, w0, kB, stage, epi, br.r1, br.xs, br.lo);
+  else spmv_rows<false, 4, true, false>(D, axis, gx, r0, w0, kB, stage, epi, br.r1);   // 3 gathers an entry
   reduce_and_finish<1>(D, 1, acc, [&](BiState& s, const double* t) { s.alpha = s.rho / t[0]; }, vb, vgrid, axis);
 }
 
-__device__ __forceinline__ void bi_s_body(const IpDev& D, int vb, int vgrid, int axis) {
+// s = r - alpha v and t = A s, omega = (t . s) / (t . t): s computed where it
+// is read, as p in bi_pv_body; the block writes its own rows' s for Xr.
+__device__ __forceinline__ void bi_st_body(const IpDev& D, int vb, int vgrid, int axis) {
+  float* stage = warp_stage();
   const BiState& S = D.st[axis];
   if (S.done) return;
-  const int n = D.n_mov;
-  const float* r = D.r + axis * n;
-  const float* v = D.v + axis * n;
-  float* s = D.s + axis * n;
   const float af = (float)S.alpha;
-  phase_s(s, r, v, af, vb * kB + threadIdx.x, vgrid * kB, n);
-}
-
-// t = A s, omega = (t . s) / (t . t)
-__device__ __forceinline__ void bi_t_body(const IpDev& D, int vb, int vgrid, int axis) {
-  float* stage = warp_stage();
-  if (D.st[axis].done) return;
-  const int n = D.n_mov;
-  const float* s = D.s + axis * n;
-  float* t = D.t + axis * n;
+  const float* vn = pv_buf(D.v, D, S.par ^ 1, axis);
+  const float* r = D.r + axis * D.n_mov;
+  float* s = D.s + axis * D.n_mov;
+  float* t = D.t + axis * D.n_mov;
+  auto gx = [&](int j) { return __fmaf_rn(-af, vn[j], r[j]); };
+  const BlockRows br = block_rows(D, gx, vb, axis);
+  for (int i = br.r0 + threadIdx.x; i < br.r1; i += blockDim.x) s[i] = br.span ? br.xs[i - br.lo] : gx(i);
   float acc[2] = {0.0f, 0.0f};
-  const BlockRows br = block_rows(D, s, vb, axis);
   auto epi = [&](int i, float ti, float si) {
     t[i] = ti;
     acc[0] = __fmaf_rn(ti, ti, acc[0]);
     acc[1] = __fmaf_rn(ti, si, acc[1]);
   };
   const int w0 = br.r0 + (threadIdx.x & ~31);
-  if (br.span) spmv_rows<false, 8, true, true>(D, axis, s, s, w0, kB, stage, epi, br.r1, br.xs, br.lo);
-  else spmv_rows<false, 8, true, false>(D, axis, s, s, w0, kB, stage, epi, br.r1);
+  if (br.span) spmv_rows<false, 8, true, true, true>(D, axis, gx, nullptr, w0, kB, stage, epi, br.r1, br.xs, br.lo);
+  else spmv_rows<false, 4, true, false, true>(D, axis, gx, nullptr, w0, kB, stage, epi, br.r1);
   reduce_and_finish<2>(D, 2, acc, [&](BiState& st, const double* tt) {
     st.w = tt[0] > 0.0 ? tt[1] / tt[0] : 0.0;
   }, vb, vgrid, axis);
@@ -882,7 +898,7 @@ __device__ __forceinline__ void bi_xr_body(const IpDev& D, int max_iter, int vb,
   const int n = D.n_mov;
   float* x = D.x + axis * n;
   float* r = D.r + axis * n;
-  const float* p = D.p + axis * n;
+  const float* p = pv_buf(D.p, D, S.par ^ 1, axis);
   const float* s = D.s + axis * n;
   const float* t = D.t + axis * n;
   const float* r0 = D.r0 + axis * n;
@@ -893,6 +909,7 @@ __device__ __forceinline__ void bi_xr_body(const IpDev& D, int max_iter, int vb,
     st.rr = tt[0];
     st.dot_r0r = tt[1];
     st.i++;
+    st.par ^= 1;
     loop_head(st, max_iter);
   }, vb, vgrid, axis);
 }
@@ -901,17 +918,11 @@ __device__ __forceinline__ void bi_xr_body(const IpDev& D, int max_iter, int vb,
 __global__ void __launch_bounds__(kB, 4) k_bi_residual(const __grid_constant__ IpDev D, int init, int max_iter) {
   bi_residual_body(D, init, max_iter, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
-__global__ void k_bi_p(const __grid_constant__ IpDev D) {
-  bi_p_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+__global__ void __launch_bounds__(kB, 4) k_bi_pv(const __grid_constant__ IpDev D) {
+  bi_pv_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
-__global__ void __launch_bounds__(kB, 4) k_bi_v(const __grid_constant__ IpDev D) {
-  bi_v_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
-}
-__global__ void k_bi_s(const __grid_constant__ IpDev D) {
-  bi_s_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
-}
-__global__ void __launch_bounds__(kB, 4) k_bi_t(const __grid_constant__ IpDev D) {
-  bi_t_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
+__global__ void __launch_bounds__(kB, 4) k_bi_st(const __grid_constant__ IpDev D) {
+  bi_st_body(D, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
 }
 __global__ void k_bi_xr(const __grid_constant__ IpDev D, int max_iter) {
   bi_xr_body(D, max_iter, (int)blockIdx.x, (int)gridDim.x, (int)blockIdx.y);
@@ -1020,7 +1031,7 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     if ((!S[0].done && S[0].need_restart) || (!S[1].done && S[1].need_restart)) {
       float acc[2] = {0.0f, 0.0f};
       if (!S[axis].done && S[axis].need_restart)
-        spmv_rows<true, 4>(D, axis, x, bb, w0, step, stage, [&](int i, float ax, float bi) {
+        spmv_rows<true, 4>(D, axis, L2Vec{x}, bb, w0, step, stage, [&](int i, float ax, float bi) {
           const float ri = bi - ax;
           r[i] = ri;
           r0[i] = ri;
@@ -1053,7 +1064,7 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     {
       float acc[1] = {0.0f};
       if (live)
-        spmv_rows<true, 4>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
+        spmv_rows<true, 4>(D, axis, L2Vec{p}, r0, w0, step, stage, [&](int i, float vi, float r0i) {
           v[i] = vi;
           acc[0] = __fmaf_rn(r0i, vi, acc[0]);
         });
@@ -1076,7 +1087,7 @@ __global__ void __launch_bounds__(kB, 4) k_bi_coop(IpDev D, int max_iter) {
     {
       float acc[2] = {0.0f, 0.0f};
       if (live)
-        spmv_rows<true, 4>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
+        spmv_rows<true, 4>(D, axis, L2Vec{sv}, sv, w0, step, stage, [&](int i, float ti, float si) {
           t[i] = ti;
           acc[0] = __fmaf_rn(ti, ti, acc[0]);
           acc[1] = __fmaf_rn(ti, si, acc[1]);
@@ -1177,7 +1188,7 @@ k_bi_cluster(IpDev D, int max_iter) {
     // restart: r = r0 = b - A x
     if (S.need_restart) {
       float acc[2] = {0.0f, 0.0f};
-      spmv_rows<true, 8, false>(D, axis, x, bb, w0, step, stage, [&](int i, float ax, float bi) {
+      spmv_rows<true, 8, false>(D, axis, L2Vec{x}, bb, w0, step, stage, [&](int i, float ax, float bi) {
         const float ri = bi - ax;
         r[i] = ri;
         r0[i] = ri;
@@ -1203,7 +1214,7 @@ k_bi_cluster(IpDev D, int max_iter) {
     // v = A p, alpha = rho / (r0 . v)
     {
       float acc[1] = {0.0f};
-      spmv_rows<true, 8, false>(D, axis, p, r0, w0, step, stage, [&](int i, float vi, float r0i) {
+      spmv_rows<true, 8, false>(D, axis, L2Vec{p}, r0, w0, step, stage, [&](int i, float vi, float r0i) {
         v[i] = vi;
         acc[0] = __fmaf_rn(r0i, vi, acc[0]);
       });
@@ -1221,7 +1232,7 @@ k_bi_cluster(IpDev D, int max_iter) {
     // t = A s, w = (t . s) / (t . t)
     {
       float acc[2] = {0.0f, 0.0f};
-      spmv_rows<true, 8, false>(D, axis, sv, sv, w0, step, stage, [&](int i, float ti, float si) {
+      spmv_rows<true, 8, false>(D, axis, L2Vec{sv}, sv, w0, step, stage, [&](int i, float ti, float si) {
         t[i] = ti;
         acc[0] = __fmaf_rn(ti, ti, acc[0]);
         acc[1] = __fmaf_rn(ti, si, acc[1]);
@@ -1289,7 +1300,7 @@ __global__ void k_ip_guess(const __grid_constant__ IpDev D) { ip_guess_body(D, (
 // arithmetic does not depend on the kernel they are compiled into).
 enum IpPhase {
   kIpPos = 0, kIpBound, kIpCount, kIpScanBlocks, kIpScanAdd, kIpRowptr, kIpFill, kIpRowsum, kIpGuess,
-  kIpResidualInit, kIpResidual, kIpP, kIpV, kIpS, kIpT, kIpXr, kIpMove, kIpWindow
+  kIpResidualInit, kIpResidual, kIpPV, kIpST, kIpXr, kIpMove, kIpWindow
 };
 
 template <int Ph>
@@ -1318,10 +1329,8 @@ __global__ void __launch_bounds__(kB, 4) k_ipb(const IpDev* __restrict__ Ds, con
   else if constexpr (Ph == kIpGuess) ip_guess_body(D, vb);
   else if constexpr (Ph == kIpResidualInit) bi_residual_body(D, 1, Ps[it.x].max_iter, vb, vg, ax);
   else if constexpr (Ph == kIpResidual) bi_residual_body(D, 0, Ps[it.x].max_iter, vb, vg, ax);
-  else if constexpr (Ph == kIpP) bi_p_body(D, vb, vg, ax);
-  else if constexpr (Ph == kIpV) bi_v_body(D, vb, vg, ax);
-  else if constexpr (Ph == kIpS) bi_s_body(D, vb, vg, ax);
-  else if constexpr (Ph == kIpT) bi_t_body(D, vb, vg, ax);
+  else if constexpr (Ph == kIpPV) bi_pv_body<4>(D, vb, vg, ax);   // 4: no spills with the tables in shared memory
+  else if constexpr (Ph == kIpST) bi_st_body(D, vb, vg, ax);
   else if constexpr (Ph == kIpXr) bi_xr_body(D, Ps[it.x].max_iter, vb, vg, ax);
   else if constexpr (Ph == kIpMove) ip_move_body(D, vb);
   else if constexpr (Ph == kIpWindow) ip_window_body(D, vb, ax);
@@ -1389,7 +1398,8 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   add(nP * 8); add(m.n_pins * 8); add(m.n_nets * 16); add(2 * n_mp * 4); add(2 * (n_mp + 1) * 4);
   add(2 * n_mp * 4); add(2 * n_mp * 4); add(2 * (nP + 1) * 4);
   add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 4);
-  for (int k = 0; k < 9; k++) add(2 * nP * 4);
+  for (int k = 0; k < 7; k++) add(2 * nP * 4);
+  for (int k = 0; k < 2; k++) add(2 * 2 * nP * 4);
   add(2 * 2 * (size_t)z.grid * 8); add(4 * 2 * 2 * (size_t)z.grid * 8); add(sizeof(GridBar));
   add(2 * (size_t)z.grid * 8);
   add(16 * 4); add(2 * sizeof(BiState));
@@ -1485,9 +1495,9 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   // the cluster solve's stages exceed the default dynamic shared-memory cap
   cudaFuncSetAttribute(k_bi_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_bytes(kClThreads));
   // the SpMV phases' product stages and x window exceed the default cap too
-  for (const void* f : {(const void*)k_bi_residual, (const void*)k_bi_v, (const void*)k_bi_t,
+  for (const void* f : {(const void*)k_bi_residual, (const void*)k_bi_pv, (const void*)k_bi_st,
                         (const void*)k_ipb<kIpResidualInit>, (const void*)k_ipb<kIpResidual>,
-                        (const void*)k_ipb<kIpV>, (const void*)k_ipb<kIpT>})
+                        (const void*)k_ipb<kIpPV>, (const void*)k_ipb<kIpST>})
     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spmv_bytes());
   cudaGetLastError();
   // ip_solver: 0 auto, 1 kernel per phase, 2 cooperative grid, 3 cluster per axis
@@ -1542,8 +1552,8 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   D.x = (float*)take(2 * nP * 4);
   D.r = (float*)take(2 * nP * 4);
   D.r0 = (float*)take(2 * nP * 4);
-  D.p = (float*)take(2 * nP * 4);
-  D.v = (float*)take(2 * nP * 4);
+  D.p = (float*)take(2 * 2 * nP * 4);
+  D.v = (float*)take(2 * 2 * nP * 4);
   D.s = (float*)take(2 * nP * 4);
   D.t = (float*)take(2 * nP * 4);
   D.part = (double*)take(2 * 2 * (size_t)D.parts * 8);
@@ -1656,7 +1666,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   const auto wall = wall_now;
   double t_round = wall();
   // The round's assembly (12 kernels) and a chunk of 8 solver iterations of
-  // the phase form (48 kernels) have fixed arguments for the whole job, so
+  // the phase form (32 kernels) have fixed arguments for the whole job, so
   // each is captured once as a CUDA graph and replayed (one launch instead
   // of tens: small jobs are bound by launches).  Without graphs (use_graph 0,
   // kernel timing, or a failed capture) the same kernels are launched one
@@ -1678,10 +1688,8 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   auto phase_chunk = [&]() {
     for (int k = 0; k < 8; k++) {
       k_bi_residual<<<gs, kB, spmv_bytes(), s>>>(D, 0, P.max_iter);
-      k_bi_p<<<gs, kB, 0, s>>>(D);
-      k_bi_v<<<gs, kB, spmv_bytes(), s>>>(D);
-      k_bi_s<<<gs, kB, 0, s>>>(D);
-      k_bi_t<<<gs, kB, spmv_bytes(), s>>>(D);
+      k_bi_pv<<<gs, kB, spmv_bytes(), s>>>(D);
+      k_bi_st<<<gs, kB, spmv_bytes(), s>>>(D);
       k_bi_xr<<<gs, kB, 0, s>>>(D, P.max_iter);
     }
   };
@@ -1767,7 +1775,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
         phase_chunk();
       }
       timer.end(kKOther);
-      timer.count(48);
+      timer.count(32);
       if (cudaGetLastError() != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
       if (cudaMemcpyAsync(st_h, D.st, 2 * sizeof(BiState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
           host_wait(s, sync_ev) != cudaSuccess) { rc = GPL_ERR_CUDA; break; }
@@ -1796,7 +1804,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
 // ------------------------------------------------------------ batched form
 // The rounds of many jobs in lockstep: every round, each member's assembly
 // phases run as one launch per phase over the work table, then chunks of
-// eight solver iterations (six launches each) until every member's two
+// eight solver iterations (four launches each) until every member's two
 // solves are done (a member that finished early skips the later chunks'
 // blocks: every phase body returns at once on a finished solve, as it does
 // in the job's own chunks), then the move; then each member's error and stop
@@ -1924,10 +1932,8 @@ int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* laun
     auto chunk = [&]() {
       for (int k = 0; k < 8; k++) {
         L(k_ipb<kIpResidual>, kTSolve, spmv_bytes());
-        L(k_ipb<kIpP>, kTSolve, 0);
-        L(k_ipb<kIpV>, kTSolve, spmv_bytes());
-        L(k_ipb<kIpS>, kTSolve, 0);
-        L(k_ipb<kIpT>, kTSolve, spmv_bytes());
+        L(k_ipb<kIpPV>, kTSolve, spmv_bytes());
+        L(k_ipb<kIpST>, kTSolve, spmv_bytes());
         L(k_ipb<kIpXr>, kTSolve, 0);
       }
       gather();
