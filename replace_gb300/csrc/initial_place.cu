@@ -1354,16 +1354,21 @@ int blocks_for(int n) { return std::max(1, (n + kB - 1) / kB); }
 
 }  // namespace
 
-// Rows per thread of the solver phases when the grid is not capped: four
-// rows give each warp four SpMV windows (the next one's row data fetched
-// while the current one is summed) and each thread four vector elements in
-// flight, and divide the blocks' fixed costs (work item, tables, FP64 block
-// reduction) by four.
-constexpr int kSolveRows = 4;
+// Rows per thread of the SpMV phases when the grid is not capped.  Small
+// systems (up to kSmallRows rows, latency-bound alone) take one row per
+// thread: one SpMV window per warp, the shortest kernel; larger ones four
+// (four windows per warp, the next one's row data fetched while the current
+// one is summed).  The x + r phase of a small system runs on a quarter of
+// the SpMV grid (four vector elements per thread, all in flight at once:
+// no longer alone, and a quarter of the blocks' FP64 block reductions when
+// many jobs run batched).
+constexpr int kSmallRows = 65536;
+int solve_rows(size_t n) { return n <= (size_t)kSmallRows ? 1 : 4; }
 
 struct IpSizes {
   size_t nnz_cap = 1, bytes = 0;
-  int grid = 1;
+  int grid = 1;        // SpMV blocks per axis
+  int xr_grid = 1;     // x + r blocks per axis
   int rows_blk = 32;
 };
 
@@ -1384,12 +1389,13 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
     if (deg > 1 && (int)deg < m.p.initial_place_max_fanout) nnz += 4 * deg - 6;
   }
   z.nnz_cap = std::max<size_t>(nnz, 1);
-  // kSolveRows rows per thread (and a window of kSolveRows rows per warp
-  // in flight in the SpMV), at most grid_cap blocks per axis
-  const int g0 = std::max(1, std::min((int)((nP + (size_t)kB * kSolveRows - 1) / ((size_t)kB * kSolveRows)), grid_cap));
+  // solve_rows rows per thread, at most grid_cap blocks per axis
+  const size_t rows_per_block = (size_t)kB * solve_rows(nP);
+  const int g0 = std::max(1, std::min((int)((nP + rows_per_block - 1) / rows_per_block), grid_cap));
   // the SpMV's contiguous row ranges: whole windows of 32 rows per block
   z.rows_blk = std::max(32, (int)((nP + g0 - 1) / g0 + 31) / 32 * 32);
   z.grid = std::max(1, (int)((nP + z.rows_blk - 1) / z.rows_blk));
+  z.xr_grid = nP <= (size_t)kSmallRows ? (z.grid + 3) / 4 : z.grid;
   const size_t scan_blocks = blocks_for((int)n_mp);
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
@@ -1420,7 +1426,7 @@ struct IpRun {
   cudaEvent_t sync_ev = nullptr;
   IpDev D;
   IpParams P;
-  int nP = 0, nb_mov = 0, grid = 1, scan_blocks = 1;
+  int nP = 0, nb_mov = 0, grid = 1, xr_grid = 1, scan_blocks = 1;
   bool cluster = false, coop = false;
   int coop_attr = 0, per_sm = 0;
   std::vector<int2> ctr;         // host centres (read back at the end)
@@ -1595,6 +1601,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   R.nP = nP;
   R.nb_mov = nb_mov;
   R.grid = grid;
+  R.xr_grid = z.xr_grid;
   R.scan_blocks = scan_blocks;
   R.cluster = cluster;
   R.coop = coop;
@@ -1662,7 +1669,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
   bool cluster = R.cluster, coop = R.coop;
   const int coop_attr = R.coop_attr, per_sm = R.per_sm, mode = prm.ip_solver;
   BiState* st_h = R.st_h;
-  const dim3 g2(nb_mov, 2), gs(grid, 2);
+  const dim3 g2(nb_mov, 2), gs(grid, 2), gx(R.xr_grid, 2);
   const auto wall = wall_now;
   double t_round = wall();
   // The round's assembly (12 kernels) and a chunk of 8 solver iterations of
@@ -1690,7 +1697,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
       k_bi_residual<<<gs, kB, spmv_bytes(), s>>>(D, 0, P.max_iter);
       k_bi_pv<<<gs, kB, spmv_bytes(), s>>>(D);
       k_bi_st<<<gs, kB, spmv_bytes(), s>>>(D);
-      k_bi_xr<<<gs, kB, 0, s>>>(D, P.max_iter);
+      k_bi_xr<<<gx, kB, 0, s>>>(D, P.max_iter);
     }
   };
   auto capture = [&](auto&& body) -> cudaGraphExec_t {
@@ -1812,7 +1819,7 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
 // end.  Each membership's assembly and chunk are captured as CUDA graphs.
 namespace {
 
-enum IpTable { kTPos = 0, kTBound, kTScan, kTParts, kTRowptr, kTRowsum, kTMov, kTSolve, kTTables };
+enum IpTable { kTPos = 0, kTBound, kTScan, kTParts, kTRowptr, kTRowsum, kTMov, kTSolve, kTVec, kTTables };
 
 // the work items of one member in each table
 void ip_items(const IpRun& R, int k, std::vector<int4> (&t)[kTTables]) {
@@ -1825,6 +1832,7 @@ void ip_items(const IpRun& R, int k, std::vector<int4> (&t)[kTTables]) {
     for (int b = 0; b < blocks_for(R.nP + 1); b++) t[kTRowptr].push_back(make_int4(k, b, 0, a));
     for (int b = 0; b < R.nb_mov; b++) t[kTRowsum].push_back(make_int4(k, b, R.nb_mov, a));
     for (int b = 0; b < R.grid; b++) t[kTSolve].push_back(make_int4(k, b, R.grid, a));
+    for (int b = 0; b < R.xr_grid; b++) t[kTVec].push_back(make_int4(k, b, R.xr_grid, a));
   }
   for (int b = 0; b < R.nb_mov; b++) t[kTMov].push_back(make_int4(k, b, 0, 0));
 }
@@ -1832,7 +1840,7 @@ void ip_items(const IpRun& R, int k, std::vector<int4> (&t)[kTTables]) {
 size_t ip_item_count(const IpRun& R) {
   const HostModel& m = *R.m;
   return (size_t)blocks_for(m.n_pins) + blocks_for(m.n_nets) +
-         2 * ((size_t)R.scan_blocks + 1 + blocks_for(R.nP + 1) + R.nb_mov + R.grid) + R.nb_mov;
+         2 * ((size_t)R.scan_blocks + 1 + blocks_for(R.nP + 1) + R.nb_mov + R.grid + R.xr_grid) + R.nb_mov;
 }
 
 using IpBatchKernel = void (*)(const IpDev*, const IpParams*, const int4*);
@@ -1934,7 +1942,7 @@ int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* laun
         L(k_ipb<kIpResidual>, kTSolve, spmv_bytes());
         L(k_ipb<kIpPV>, kTSolve, spmv_bytes());
         L(k_ipb<kIpST>, kTSolve, spmv_bytes());
-        L(k_ipb<kIpXr>, kTSolve, 0);
+        L(k_ipb<kIpXr>, kTVec, 0);
       }
       gather();
     };
