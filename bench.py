@@ -199,8 +199,8 @@ def cpu_baseline_sample(nl, td, bins, warmup=CPU_WARMUP, steps=CPU_STEPS):
     return steps / (t2 - t1), evals, t2 - t0
 
 
-def cpu_sample_text(steps, warmup, evals, seconds):
-    return (f"{steps} Nesterov iterations ({evals:.2f} evaluations each) of the same 1M-cell job "
+def cpu_sample_text(steps, warmup, evals, seconds, workload=WORKLOAD):
+    return (f"{steps} Nesterov iterations ({evals:.2f} evaluations each) of the same {workload} job "
             f"after setup, init and {warmup} warm-up iterations, from the centred placement "
             f"({seconds:.1f} s of single-threaded CPU work; the oracle restatement of the "
             "reference's path, which has no threads: its initial place alone would take minutes "
@@ -326,6 +326,21 @@ def batched_form(n_jobs, slots, device):
                            "p99_latency_s": float(np.percentile(lat, 99)),
                            "same_result_as_one_at_a_time": bool(same_srv)},
     }
+
+
+def batched_ip_only(n_jobs, device=0):
+    """The batched initial place of the batched form's job set, alone: one
+    JSON line with its wall time, rounds and kernel launches (the case the
+    batched kernels are profiled on)."""
+    from replace_gb300 import Placer, batch_initial_place, netlist as N
+    ps = [Placer(nl, target_density=td, device=device, poisson_path=1) for nl, td in N.job_batch(n_jobs, seed=4)]
+    t0 = time.perf_counter()
+    st, status, launches = batch_initial_place(ps)
+    t = time.perf_counter() - t0
+    for p in ps:
+        p.close()
+    print(json.dumps({"batched_initial_place": {"jobs": n_jobs, "seconds": t, "rounds": int(sum(s.iterations for s in st)),
+                                                "kernel_launches": launches, "ok": all(s == 0 for s in status)}}))
 
 
 def serving_stream(n_jobs, slots, device, rate_scale=1.0, arms=("server", "one_at_a_time")):
@@ -464,7 +479,7 @@ def run_reference(args):
     if rank != 0:
         return
     from replace_gb300 import netlist as N
-    nl, td, bins = N.generate_workload(WORKLOAD, seed=1)
+    nl, td, bins = N.generate_workload(args.workload, seed=1)
     from oracle import oracle as O
     O.build()
     # Each CPU iteration of the 1M-cell job takes about a second: the arm
@@ -477,12 +492,12 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1000 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded generator, 1M cells)",
-        "config": {"workload": WORKLOAD, "cells": 1_000_000, "nets": 1_050_000, "bins": "1024x1024",
-                   "target_density": td, "parallelism": "single-threaded CPU"},
+        "data": "synthetic (seeded generator, %d movable cells)" % int((nl.inst_kind == 0).sum()),
+        "config": {"workload": args.workload, "cells": int((nl.inst_kind == 0).sum()), "nets": nl.n_nets,
+                   "bins": f"{bins}x{bins}", "target_density": td, "parallelism": "single-threaded CPU"},
         "cpu_baseline": {"value": v, "unit": "iters/s", "cores": 1, "kind": "port",
                          "host": host_cpu(),
-                         "sample": cpu_sample_text(steps, warm, evals, secs) +
+                         "sample": cpu_sample_text(steps, warm, evals, secs, args.workload) +
                                    "; the reference's own build needs the reference sources, "
                                    "OpenDB and Eigen, none of which is on this host"},
         "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -517,10 +532,14 @@ def main():
                     help="BiCGSTAB form of the initial place: 0 auto, 1 phase kernels, 2 cooperative grid, 3 cluster")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the tensor-core Poisson (precision) form beside the timed job")
+    ap.add_argument("--only-batched-ip", action="store_true",
+                    help="time only the batched initial place of the --batch-jobs job set (profiling case)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_batched_ip:
+        return batched_ip_only(args.batch_jobs)
 
     import torch
     rank, local_rank, world = dist_env()
@@ -599,7 +618,9 @@ def main():
                                           bin_grid_cnt_y=bins, device=local_rank))
         q.initial_place()
         q.nesterov_init()
-        rc2, st2, _ = q.nesterov_run(args.e2e_iters)
+        # a workload on which the reference itself diverges (the 200k-cell /
+        # 40-macro one: REPL-4) ends with that code here too; it is reported
+        rc2, st2, _ = q.nesterov_run(args.e2e_iters, allow_divergence=True)
         lx, ly = q.inst_locations()
         t1 = time.perf_counter()
         q.close()
@@ -610,7 +631,7 @@ def main():
                     "note": f"one step = a whole placement job through the C ABI from host arrays: "
                             "netlist upload, host setup, initial place, Nesterov loop to its stop "
                             f"rule ({e2e_iters} iterations), location read-back",
-                    "job_seconds": t1 - t0, "finished": bool(st2.finished),
+                    "job_seconds": t1 - t0, "status": int(rc2), "finished": bool(st2.finished),
                     "final_overflow": float(st2.overflow), "final_hpwl": int(st2.hpwl)}
     clk = clocks.stop()
     parity = None
@@ -630,7 +651,7 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         v_cpu, ev_cpu, t_cpu = cpu_baseline_sample(nl, td, bins)
         cpu = {"value": v_cpu, "unit": "iters/s", "cores": 1, "kind": "port", "host": host_cpu(),
-               "sample": cpu_sample_text(CPU_STEPS, CPU_WARMUP, ev_cpu, t_cpu)}
+               "sample": cpu_sample_text(CPU_STEPS, CPU_WARMUP, ev_cpu, t_cpu, args.workload)}
 
     if rank == 0:
         line = {
