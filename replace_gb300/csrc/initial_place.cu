@@ -1369,6 +1369,7 @@ struct IpSizes {
   size_t nnz_cap = 1, bytes = 0;
   int grid = 1;        // SpMV blocks per axis
   int xr_grid = 1;     // x + r blocks per axis
+  int parts = 1;       // block partials per axis and value (the larger grid)
   int rows_blk = 32;
 };
 
@@ -1395,7 +1396,10 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   // the SpMV's contiguous row ranges: whole windows of 32 rows per block
   z.rows_blk = std::max(32, (int)((nP + g0 - 1) / g0 + 31) / 32 * 32);
   z.grid = std::max(1, (int)((nP + z.rows_blk - 1) / z.rows_blk));
+  // x + r of a small system: four elements per thread, all in flight at
+  // once (a larger grid for the capped large systems measured slower)
   z.xr_grid = nP <= (size_t)kSmallRows ? (z.grid + 3) / 4 : z.grid;
+  z.parts = std::max(z.grid, z.xr_grid);
   const size_t scan_blocks = blocks_for((int)n_mp);
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += (b + 255) / 256 * 256 + 256; };
@@ -1406,8 +1410,8 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 4);
   for (int k = 0; k < 7; k++) add(2 * nP * 4);
   for (int k = 0; k < 2; k++) add(2 * 2 * nP * 4);
-  add(2 * 2 * (size_t)z.grid * 8); add(4 * 2 * 2 * (size_t)z.grid * 8); add(sizeof(GridBar));
-  add(2 * (size_t)z.grid * 8);
+  add(2 * 2 * (size_t)z.parts * 8); add(4 * 2 * 2 * (size_t)z.parts * 8); add(sizeof(GridBar));
+  add(2 * (size_t)z.parts * 8);
   add(16 * 4); add(2 * sizeof(BiState));
   z.bytes = bytes;
   return z;
@@ -1521,7 +1525,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   D.nnz_cap = z.nnz_cap;
   const int nb_mov = blocks_for(nP);
   const int grid = z.grid;
-  D.parts = grid;
+  D.parts = z.parts;
   D.rows_blk = z.rows_blk;
   D.n_mp = (int)mp.size();
   const int scan_blocks = blocks_for(D.n_mp);
@@ -1565,7 +1569,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   D.part = (double*)take(2 * 2 * (size_t)D.parts * 8);
   D.cpart = (double*)take(4 * 2 * 2 * (size_t)D.parts * 8);
   D.bar = (GridBar*)take(sizeof(GridBar));
-  D.win = (int2*)take(2 * (size_t)grid * 8);
+  D.win = (int2*)take(2 * (size_t)D.parts * 8);
   D.counters = (unsigned*)take(16 * 4);
   D.st = (BiState*)take(2 * sizeof(BiState));
   int rc = GPL_OK;
