@@ -69,6 +69,7 @@ struct IpDev {
   int32_t* rowptr;         // [2][n_mov + 1]
   int32_t* scan_part;      // block sums of the scan
   int32_t* col;            // [2][nnz_cap]
+  uint16_t* col16;         // [2][nnz_cap] column - the block's x window start (blocks with a window)
   float* val;
   float* diag;             // [2][n_mov]
   float* b;                // [2][n_mov]
@@ -396,7 +397,8 @@ __device__ __forceinline__ void ip_rowsum_body(const IpDev& D, int vb, int axis)
 
 // The x window of SpMV block vb: its own rows and every column its rows'
 // entries read, as (first index, length), or length 0 when that is wider
-// than kXWin (the block then gathers from global memory).
+// than kXWin (the block then gathers from global memory); for a block with
+// a window, its entries' columns relative to the window start in 16 bits.
 constexpr int kXWinMax = 5632;
 __device__ __forceinline__ void ip_window_body(const IpDev& D, int vb, int axis) {
   __shared__ int sh[2][kB / 32];
@@ -421,10 +423,22 @@ __device__ __forceinline__ void ip_window_body(const IpDev& D, int vb, int axis)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) { sh[0][wid] = lo; sh[1][wid] = hi; }
   __syncthreads();
+  __shared__ int s_lo;
   if (threadIdx.x == 0) {
     for (int w = 1; w < kB / 32; w++) { lo = min(lo, sh[0][w]); hi = max(hi, sh[1][w]); }
     const bool fits = r0 < r1 && hi - lo <= kXWinMax;
     D.win[axis * D.parts + vb] = make_int2(fits ? lo : 0, fits ? hi - lo : 0);
+    s_lo = fits ? lo : -1;
+  }
+  __syncthreads();
+  // the window-relative columns the SpMV reads (2 bytes an entry instead of 4)
+  const int base = s_lo;
+  if (base >= 0) {
+    const int32_t* rp = D.rowptr + axis * (n + 1);
+    const int32_t* col = D.col + axis * D.nnz_cap;
+    uint16_t* col16 = D.col16 + axis * D.nnz_cap;
+    const int k1 = (int)min((size_t)rp[r1], D.nnz_cap);
+    for (int k = rp[r0] + threadIdx.x; k < k1; k += blockDim.x) col16[k] = (uint16_t)(col[k] - base);
   }
 }
 
@@ -505,8 +519,8 @@ struct RowFetch {
 // from DRAM into L2 while the warp works on the window before it: one bulk
 // L2 prefetch per array, issued by lane 0, the range widened to 16-byte
 // boundaries (it stays inside the arrays' 256-byte padding).
-__device__ __forceinline__ void prefetch_window(const int32_t* col, const float* val, const RowFetch& f,
-                                                bool valid) {
+template <class C>
+__device__ __forceinline__ void prefetch_window(const C* col, const float* val, const RowFetch& f, bool valid) {
   const unsigned full = 0xffffffffu;
   const unsigned m = __ballot_sync(full, valid);
   if (!m) return;
@@ -524,8 +538,8 @@ __device__ __forceinline__ void prefetch_window(const int32_t* col, const float*
 }
 
 // One window: returns the lane's row product (valid lanes).
-template <bool kFromL2, int kBatch, class Ld>
-__device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, const float* __restrict__ val,
+template <bool kFromL2, int kBatch, class C, class Ld>
+__device__ __forceinline__ float spmv_window(const C* __restrict__ col, const float* __restrict__ val,
                                              Ld ld, const RowFetch& f, bool valid, float* stage) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -544,7 +558,7 @@ __device__ __forceinline__ float spmv_window(const int32_t* __restrict__ col, co
 #pragma unroll
       for (int b = 0; b < kBatch; b++) {
         const int k = c0 + 32 * b + lane;
-        cj[b] = k < total ? __ldg(col + base + k) : 0;
+        cj[b] = k < total ? (int)__ldg(col + base + k) : 0;
         vj[b] = k < total ? __ldg(val + base + k) : 0.0f;
       }
 #pragma unroll
@@ -595,9 +609,13 @@ __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, GX gx, const
                                           const float* xs = nullptr, int lo = 0) {
   const int n = n_end < 0 ? D.n_mov : n_end;
   const int lane = threadIdx.x & 31;
+  // entry columns: window-relative 16-bit in window mode, absolute otherwise
+  auto ldc = [&](int c) { return kWin ? xs[c] : gx(c); };
+  // the rows' own operands (absolute row index)
   auto ld = [&](int j) { return kWin ? xs[j - lo] : gx(j); };
   const int32_t* __restrict__ rp = D.rowptr + axis * (D.n_mov + 1);
   const int32_t* __restrict__ col = D.col + axis * D.nnz_cap;
+  const uint16_t* __restrict__ col16 = D.col16 + axis * D.nnz_cap;
   const float* __restrict__ val = D.val + axis * D.nnz_cap;
   const float* __restrict__ dg = D.diag + axis * D.n_mov;
   auto fetch = [&](int w) {
@@ -616,10 +634,15 @@ __device__ __forceinline__ void spmv_rows(const IpDev& D, int axis, GX gx, const
   RowFetch cur = fetch(w0);
   RowFetch next = fetch(w0 + step);
   for (int w = w0; w < n; w += step) {
-    if (kPrefetch) prefetch_window(col, val, next, w + step + lane < n);
+    if constexpr (kPrefetch) {
+      if constexpr (kWin) prefetch_window(col16, val, next, w + step + lane < n);
+      else prefetch_window(col, val, next, w + step + lane < n);
+    }
     const RowFetch next2 = fetch(w + 2 * step);
     const int i = w + lane;
-    const float v = spmv_window<kFromL2, kBatch>(col, val, ld, cur, i < n, stage);
+    float v;
+    if constexpr (kWin) v = spmv_window<kFromL2, kBatch>(col16, val, ldc, cur, i < n, stage);
+    else v = spmv_window<kFromL2, kBatch>(col, val, ldc, cur, i < n, stage);
     if (i < n) epi(i, v, cur.aux);
     cur = next;
     next = next2;
@@ -1407,7 +1430,7 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   add(m.n_pins * 8); add(m.n_pins * 8); add((nP + 1) * 4); add(n_mp * 4);
   add(nP * 8); add(m.n_pins * 8); add(m.n_nets * 16); add(2 * n_mp * 4); add(2 * (n_mp + 1) * 4);
   add(2 * n_mp * 4); add(2 * n_mp * 4); add(2 * (nP + 1) * 4);
-  add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 4);
+  add(2 * scan_blocks * 4); add(2 * z.nnz_cap * 4); add(2 * z.nnz_cap * 2); add(2 * z.nnz_cap * 4);
   for (int k = 0; k < 7; k++) add(2 * nP * 4);
   for (int k = 0; k < 2; k++) add(2 * 2 * nP * 4);
   add(2 * 2 * (size_t)z.parts * 8); add(4 * 2 * 2 * (size_t)z.parts * 8); add(sizeof(GridBar));
@@ -1556,6 +1579,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   D.rowptr = (int32_t*)take(2 * (nP + 1) * 4);
   D.scan_part = (int32_t*)take(2 * scan_blocks * 4);
   D.col = (int32_t*)take(2 * D.nnz_cap * 4);
+  D.col16 = (uint16_t*)take(2 * D.nnz_cap * 2);
   D.val = (float*)take(2 * D.nnz_cap * 4);
   D.diag = (float*)take(2 * nP * 4);
   D.b = (float*)take(2 * nP * 4);
