@@ -79,6 +79,7 @@ struct IpDev {
   double* cpart;           // cooperative solve: [4 phases][2 axes][2][parts]
   struct GridBar* bar;     // cooperative solve: grid barrier
   unsigned* counters;      // [2][8]
+  struct IpLoop* loop;     // the device loop's state (kernel-per-phase form)
   BiState* st;             // [2]
   BiState* st_h;           // pinned mirror
   int parts = 0;
@@ -1373,6 +1374,54 @@ __global__ void k_ipb_states(const IpDev* __restrict__ Ds, const int* __restrict
   if (k < 2 * n) out[k] = Ds[jobs[k >> 1]].st[k & 1];
 }
 
+// ------------------------------------------------------------ device loop
+// The rounds of the kernel-per-phase form as one CUDA graph: WHILE (rounds
+// go on) { assembly; WHILE (a solve goes on) { 8 iterations; chunk tail };
+// move; round tail }.  The one-thread tails take the decisions the host loop
+// takes between its chunks and rounds (same tests, same values), so the host
+// waits once per initial place instead of once per chunk.
+struct IpLoop {
+  int round, chunks, max_rounds, iter_limit;   // iter_limit: the host loop's 2 * max_iter + 2
+  int finished, iters_x, iters_y;
+  float err;
+};
+
+__global__ void k_ip_loop_head(IpLoop* L, int max_rounds, int iter_limit, cudaGraphConditionalHandle h_round) {
+  IpLoop l{};
+  l.max_rounds = max_rounds;
+  l.iter_limit = iter_limit;
+  *L = l;
+  cudaGraphSetConditional(h_round, max_rounds > 0 ? 1u : 0u);
+}
+
+__global__ void k_ip_chunk_head(IpLoop* L, cudaGraphConditionalHandle h_chunk) {
+  L->chunks = 0;
+  cudaGraphSetConditional(h_chunk, 1u);
+}
+
+// after a chunk: another one while a solve goes on and the host loop's
+// iteration bound allows (it counts 8 per chunk from 0)
+__global__ void k_ip_chunk_tail(const BiState* st, IpLoop* L, cudaGraphConditionalHandle h_chunk) {
+  const int n = ++L->chunks;
+  const bool done = st[0].done && st[1].done;
+  cudaGraphSetConditional(h_chunk, (!done && 8 * n <= L->iter_limit) ? 1u : 0u);
+}
+
+// after the move: the round's error (solver.error() = sqrt(|r|^2 / |b|^2),
+// in double as on the host) and the stop test (src/initialPlace.cpp:93-99)
+__global__ void k_ip_round_tail(const BiState* st, IpLoop* L, cudaGraphConditionalHandle h_round) {
+  IpLoop l = *L;
+  l.round++;
+  const float ex = st[0].rhs_sq > 0 ? (float)sqrt(st[0].rr / st[0].rhs_sq) : 0.0f;
+  const float ey = st[1].rhs_sq > 0 ? (float)sqrt(st[1].rr / st[1].rhs_sq) : 0.0f;
+  l.err = ex < ey ? ey : ex;
+  l.iters_x = st[0].i;
+  l.iters_y = st[1].i;
+  l.finished = ((l.err <= 1e-5 && l.round >= 5) || l.round >= l.max_rounds) ? 1 : 0;
+  *L = l;
+  cudaGraphSetConditional(h_round, l.finished ? 0u : 1u);
+}
+
 int blocks_for(int n) { return std::max(1, (n + kB - 1) / kB); }
 
 }  // namespace
@@ -1435,7 +1484,7 @@ IpSizes ip_sizes(const HostModel& m, int grid_cap) {
   for (int k = 0; k < 2; k++) add(2 * 2 * nP * 4);
   add(2 * 2 * (size_t)z.parts * 8); add(4 * 2 * 2 * (size_t)z.parts * 8); add(sizeof(GridBar));
   add(2 * (size_t)z.parts * 8);
-  add(16 * 4); add(2 * sizeof(BiState));
+  add(16 * 4); add(sizeof(IpLoop)); add(2 * sizeof(BiState));
   z.bytes = bytes;
   return z;
 }
@@ -1446,6 +1495,9 @@ size_t initial_place_bytes(const HostModel& m, int sm_count) { return ip_sizes(m
 // One job's initial place on the device: its scratch, tables and solver
 // state (ip_setup), the rounds (run_initial_place's loop, or the batched
 // form's lockstep rounds), and the read-back (ip_finish).
+// offset of the device loop's state copy in the job's pinned ip_state block
+constexpr size_t kIpLoopPinned = 512;
+
 struct IpRun {
   HostModel* m = nullptr;
   cudaStream_t s = nullptr;
@@ -1472,7 +1524,8 @@ double wall_now() {
 
 int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPool_t pool, cudaEvent_t sync_ev,
              IpRun& R) {
-  static_assert(2 * sizeof(BiState) + sizeof(GridBar) <= sizeof(HostPinned::ip_state),
+  static_assert(2 * sizeof(BiState) + sizeof(GridBar) <= kIpLoopPinned &&
+                    kIpLoopPinned + sizeof(IpLoop) <= sizeof(HostPinned::ip_state),
                 "pinned solver state too small");
   R.m = &m;
   R.s = s;
@@ -1595,6 +1648,7 @@ int ip_setup(HostModel& m, cudaStream_t s, int sm_count, void* pinned, cudaMemPo
   D.bar = (GridBar*)take(sizeof(GridBar));
   D.win = (int2*)take(2 * (size_t)D.parts * 8);
   D.counters = (unsigned*)take(16 * 4);
+  D.loop = (IpLoop*)take(sizeof(IpLoop));
   D.st = (BiState*)take(2 * sizeof(BiState));
   int rc = GPL_OK;
   auto up = [&](void* dst, const void* src, size_t b) {
@@ -1739,6 +1793,94 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     cudaGetLastError();
     return e;
   };
+  // The whole initial place as one graph with conditional nodes (the phase
+  // form with graphs, no kernel timing, no per-round printing): one launch
+  // and one wait.  Any failure to build it leaves the host loop below.
+  if (!cluster && !coop && prm.use_graph && !timer.enabled && prm.verbose_level < 2 &&
+      prm.initial_place_max_iter > 0) {
+    // the unique node without dependents of a graph captured from one stream
+    auto tail_of = [](cudaGraph_t gr) -> cudaGraphNode_t {
+      size_t n = 0;
+      if (cudaGraphGetNodes(gr, nullptr, &n) != cudaSuccess || n == 0) return nullptr;
+      std::vector<cudaGraphNode_t> nodes(n);
+      if (cudaGraphGetNodes(gr, nodes.data(), &n) != cudaSuccess) return nullptr;
+      cudaGraphNode_t t = nullptr;
+      int tails = 0;
+      for (cudaGraphNode_t nd : nodes) {
+        size_t k = 0;
+        if (cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &k) != cudaSuccess) return nullptr;
+        if (k == 0) { t = nd; tails++; }
+      }
+      return tails == 1 ? t : nullptr;
+    };
+    auto into = [&](cudaGraph_t gr, const cudaGraphNode_t* dep, auto&& body) {
+      cudaGraph_t cap = nullptr;
+      if (cudaStreamBeginCaptureToGraph(s, gr, dep, nullptr, dep ? 1 : 0, cudaStreamCaptureModeThreadLocal) !=
+          cudaSuccess)
+        return false;
+      body();
+      return cudaStreamEndCapture(s, &cap) == cudaSuccess;
+    };
+    auto add_while = [](cudaGraph_t gr, cudaGraphNode_t dep, cudaGraphConditionalHandle h, cudaGraphNode_t* node,
+                        cudaGraph_t* body) {
+      cudaGraphNodeParams wp = {cudaGraphNodeTypeConditional};
+      wp.conditional.handle = h;
+      wp.conditional.type = cudaGraphCondTypeWhile;
+      wp.conditional.size = 1;
+      if (cudaGraphAddNode(node, gr, &dep, nullptr, 1, &wp) != cudaSuccess) return false;
+      *body = wp.conditional.phGraph_out[0];
+      return true;
+    };
+    IpLoop* L_h = reinterpret_cast<IpLoop*>(reinterpret_cast<unsigned char*>(st_h) + kIpLoopPinned);
+    cudaGraph_t g = nullptr, body_r = nullptr, body_c = nullptr;
+    cudaGraphNode_t head = nullptr, wr = nullptr, wc = nullptr, a_tail = nullptr;
+    cudaGraphConditionalHandle h_round = 0, h_chunk = 0;
+    cudaGraphExec_t loop_exec = nullptr;
+    const int iter_limit = 2 * P.max_iter + 2;
+    bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+    ok = ok && cudaGraphConditionalHandleCreate(&h_round, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+    ok = ok && cudaGraphConditionalHandleCreate(&h_chunk, g, 0, cudaGraphCondAssignDefault) == cudaSuccess;
+    ok = ok && into(g, nullptr, [&] {
+      k_ip_loop_head<<<1, 1, 0, s>>>(D.loop, prm.initial_place_max_iter, iter_limit, h_round);
+    });
+    ok = ok && (head = tail_of(g)) != nullptr;
+    ok = ok && add_while(g, head, h_round, &wr, &body_r);
+    ok = ok && into(body_r, nullptr, [&] {
+      assembly();
+      k_ip_chunk_head<<<1, 1, 0, s>>>(D.loop, h_chunk);
+    });
+    ok = ok && (a_tail = tail_of(body_r)) != nullptr;
+    ok = ok && add_while(body_r, a_tail, h_chunk, &wc, &body_c);
+    ok = ok && into(body_c, nullptr, [&] {
+      phase_chunk();
+      k_ip_chunk_tail<<<1, 1, 0, s>>>(D.st, D.loop, h_chunk);
+    });
+    ok = ok && into(body_r, &wc, [&] {
+      k_ip_move<<<nb_mov, kB, 0, s>>>(D);
+      k_ip_round_tail<<<1, 1, 0, s>>>(D.st, D.loop, h_round);
+    });
+    ok = ok && into(g, &wr, [&] {
+      cudaMemcpyAsync(L_h, D.loop, sizeof(IpLoop), cudaMemcpyDeviceToHost, s);
+    });
+    ok = ok && cudaGraphInstantiate(&loop_exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (ok) {
+      if (cudaGraphLaunch(loop_exec, s) != cudaSuccess || host_wait(s, sync_ev) != cudaSuccess) {
+        rc = GPL_ERR_CUDA;
+      } else {
+        R.rounds = L_h->round;
+        R.err = L_h->err;
+        R.iters[0] = L_h->iters_x;
+        R.iters[1] = L_h->iters_y;
+        R.finished = L_h->finished != 0;
+      }
+      cudaGraphExecDestroy(loop_exec);
+      return ip_finish(R, stats, rc);
+    }
+    if (loop_exec) cudaGraphExecDestroy(loop_exec);
+    if (prm.verbose_level > 0) printf("[InitialPlace] device loop not built: the host drives the rounds\n");
+  }
   cudaGraphExec_t assembly_exec = capture(assembly);
   cudaGraphExec_t chunk_exec = (!cluster && !coop) ? capture(phase_chunk) : nullptr;
   for (int round = 1; round <= prm.initial_place_max_iter && !rc; round++) {
