@@ -136,7 +136,7 @@ def algorithmic_bytes(kind, ng, npins, nn, nb):
 # run under ncu.
 NCU_TRAFFIC = {
     "1m_cells_1024bins": {
-        "wa_wirelength": 101.6e6, "gcell_gradient": 131.0e6, "density_scatter": 64.7e6,
+        "wa_wirelength": 100.9e6, "gcell_gradient": 109.1e6, "density_scatter": 39.5e6,
         "poisson_rows_dct": 29.4e6, "poisson_cols_solve": 4.3e6, "poisson_rows_inverse": 8.5e6,
     },
 }
@@ -532,6 +532,10 @@ def main():
                     help="BiCGSTAB form of the initial place: 0 auto, 1 phase kernels, 2 cooperative grid, 3 cluster")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the tensor-core Poisson (precision) form beside the timed job")
+    ap.add_argument("--scatter-tile", type=int, default=0, choices=[0, 16, 32, 64],
+                    help="scatter tile side in bins (0: chosen by timing at init; pin it for profiling runs)")
+    ap.add_argument("--scatter-chunk", type=int, default=0, choices=[0, 1024, 2048],
+                    help="gcells per scatter block (0: chosen with the tile)")
     ap.add_argument("--only-batched-ip", action="store_true",
                     help="time only the batched initial place of the --batch-jobs job set (profiling case)")
     args = ap.parse_args()
@@ -556,7 +560,8 @@ def main():
     # loop; the timed iterations start after the warm-up ones
     params = _abi.default_params(target_density=td, bin_grid_cnt_x=bins, bin_grid_cnt_y=bins,
                                  device=local_rank, stream=stream.cuda_stream,
-                                 poisson_path=args.poisson_path, ip_solver=args.ip_solver)
+                                 poisson_path=args.poisson_path, ip_solver=args.ip_solver,
+                                 scatter_tile=args.scatter_tile, scatter_chunk=args.scatter_chunk)
     p = Placer(nl, params)
     ip_stats = p.initial_place()
     p.nesterov_init()
@@ -665,6 +670,7 @@ def main():
                        "pins": nl.n_pins, "target_density": td,
                        "evals_per_iter": round((st.evaluations) / max(st.iterations, 1), 3),
                        "poisson_form": {1: "shared-memory FFT", 2: "tensor-core GEMM"}.get(info.poisson_path),
+                       "scatter_shape": f"{info.scatter_tile} bins / {info.scatter_chunk} gcells",
                        # the autotuner's timings (None: not timed; auto mode
                        # skips the GEMM form above 512 bins per axis)
                        "poisson_fft_us": round(info.poisson_fft_us, 1) or None,

@@ -141,10 +141,13 @@ typedef struct gpl_params {
   int32_t scatter_chunk;                   /* gcells per scatter block (1024 or 2048); 0 = chosen
                                               by timing (with the tile) */
   int32_t device_loop;                     /* 0 = the host drives the Nesterov loop, one
-                                              evaluation graph at a time (default); 1 = the loop
-                                              runs on the device (a CUDA graph with a conditional
-                                              WHILE node: evaluation, then a one-thread control
-                                              kernel).  Same control arithmetic and results. */
+                                              evaluation graph at a time, and the initial
+                                              place's rounds, one chunk of solver iterations
+                                              at a time (default); 1 = both run on the device
+                                              (CUDA graphs with conditional WHILE nodes and
+                                              one-thread control kernels).  Same control
+                                              arithmetic and results; the host-driven form
+                                              interleaves better with other jobs' work. */
 } gpl_params;
 
 /* Counts and grid chosen by the job (NesterovBase / BinGrid). */

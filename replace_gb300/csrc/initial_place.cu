@@ -1793,10 +1793,13 @@ int run_initial_place(HostModel& m, cudaStream_t s, int sm_count, gpl_ip_stats* 
     cudaGetLastError();
     return e;
   };
-  // The whole initial place as one graph with conditional nodes (the phase
-  // form with graphs, no kernel timing, no per-round printing): one launch
-  // and one wait.  Any failure to build it leaves the host loop below.
-  if (!cluster && !coop && prm.use_graph && !timer.enabled && prm.verbose_level < 2 &&
+  // The whole initial place as one graph with conditional nodes (device_loop
+  // 1; the phase form with graphs, no kernel timing, no per-round
+  // printing): one launch and one wait.  Under the placement server the
+  // host-driven rounds interleave better with the other jobs' kernels (64
+  // small jobs: 0.96 s against 1.28 s), so it is not the default.  Any
+  // failure to build it leaves the host loop below.
+  if (!cluster && !coop && prm.use_graph && prm.device_loop && !timer.enabled && prm.verbose_level < 2 &&
       prm.initial_place_max_iter > 0) {
     // the unique node without dependents of a graph captured from one stream
     auto tail_of = [](cudaGraph_t gr) -> cudaGraphNode_t {

@@ -103,3 +103,21 @@ def test_cluster_solve_agrees_with_grid_solve(gpu_lib):
     assert a.iterations == b.iterations and a.cooperative_rounds == a.iterations
     assert abs(ha - hb) <= 1e-3 * hb
     assert a.last_error < 3 * b.last_error and b.last_error < 3 * a.last_error
+
+
+@pytest.mark.parametrize("name", ["simple03", "syn10k_b128"])
+def test_device_loop_matches_host_loop(gpu_lib, name):
+    """The rounds as one CUDA graph with conditional nodes (device_loop 1)
+    take the host loop's decisions on the device: identical rounds, error,
+    iteration counts and locations."""
+    from replace_gb300 import Placer
+    nl, _ = case(name)
+    out = []
+    for dl in (0, 1):
+        p = Placer(nl, target_density=0.7, initial_place_max_iter=20, device_loop=dl)
+        st = p.initial_place()
+        out.append((st.iterations, st.last_error, st.solver_iters_x, st.solver_iters_y,
+                    *p.inst_locations()))
+        p.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
