@@ -20,7 +20,10 @@
 // Solver.  Vectors are FP32 (as the reference's float Eigen vectors); inner
 // products and the rho / alpha / omega scalars are FP64.  Both axes run in
 // the same launches (blockIdx.y = axis).  The scalar steps are done by the
-// last block of each reduction kernel, so the host only polls a done flag.
+// last block of each reduction kernel, so the host only polls a done flag
+// (or, with device_loop, one-thread kernels take the host's decisions
+// inside one graph).  The batched form runs the same block bodies for many
+// jobs from a work table (run_initial_place_batch).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -954,12 +957,14 @@ __global__ void k_bi_xr(const __grid_constant__ IpDev D, int max_iter) {
 
 // ---------------------------------------------------- cooperative solve
 // The whole BiCGSTAB solve of both axes as one cooperative launch: the
-// phases of k_bi_residual .. k_bi_xr run in the same order with the same
-// block partials, separated by grid barriers instead of kernel boundaries,
-// so the iterates are the same as the kernel-per-phase loop's with the same
-// grid.  Every block reduces the partials of both axes itself (same fixed
-// order), so every block holds the same solver scalars and the loop ends in
-// step across the grid.
+// phases of the kernel-per-phase loop (with the p and s updates as phases
+// of their own) run in the same order, separated by grid barriers instead
+// of kernel boundaries, on the same grid; the rows are strided over the
+// blocks (the phase form's SpMV gives each block a contiguous range), so
+// the dot products sum in another order and the iterates agree to rounding.
+// Every block reduces the partials of both axes itself (same fixed order),
+// so every block holds the same solver scalars and the loop ends in step
+// across the grid.
 
 struct GridBar {
   unsigned count, gen;
