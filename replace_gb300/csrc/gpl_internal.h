@@ -412,6 +412,8 @@ struct IpBatchJob {
 // The initial place of n jobs in lockstep rounds, one launch per phase over
 // all jobs (initial_place.cu); each job's result is bit-identical to
 // run_initial_place's kernel-per-phase form.  *launches: kernels launched.
+// Returns GPL_OK, or the error that stopped the batch as a whole (each
+// job's status is in jobs[k].status either way).
 int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* launches);
 
 // A job's host model without a stream or staging (a server binds those when

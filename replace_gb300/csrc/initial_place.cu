@@ -2227,7 +2227,9 @@ int run_initial_place_batch(IpBatchJob* jobs, int n, int sm_count, int64_t* laun
     if (active[k]) jobs[k].status = ip_finish(R[k], jobs[k].stats, rc);
   if (verbose) printf("[InitialPlace] batched: read-back of %d jobs %.2f ms\n", n, wall_now() - t_end);
   if (launches) *launches = nl;
-  return GPL_OK;
+  // a failure of the batch itself (its tables, stream or kernels) is also
+  // the call's status; every job's own status says what happened to it
+  return rc;
 }
 
 }  // namespace gpl
