@@ -696,7 +696,7 @@ __global__ void __launch_bounds__(256) k_poisson_dens(PassAArgs A) {
   float ovf = 0.0f;
 #pragma unroll 4
   for (int b = blockIdx.x * 256 + threadIdx.x; b < nb; b += gridDim.x * 256) {
-    const int j = b / A.nx, i = b - j * A.nx;
+    const int j = b >> A.logn, i = b & (A.nx - 1);     // bin grids are powers of 2
     const int blx = A.core_lx + i * A.size_x, bux = min(blx + A.size_x, A.core_ux);
     const int bly = A.core_ly + j * A.size_y, buy = min(bly + A.size_y, A.core_uy);
     const long long bin_area = (long long)(bux - blx) * (long long)(buy - bly);
