@@ -169,3 +169,19 @@ def test_large_netlist_checks_run_in_parallel_ranges():
         job = C.c_void_p()
         assert lib.gpl_create(C.byref(h.desc), C.byref(_abi.default_params()), C.byref(job)) == \
             _abi.GPL_ERR_NO_DEVICE
+
+
+def test_batched_calls_validate_their_job_lists_on_the_host():
+    """The batched entry points reject an empty or null job list before any
+    device work (gpl_batch_initial_place, gpl_batch_nesterov_run)."""
+    from replace_gb300 import load
+    lib = load()
+    launches = C.c_int64(-1)
+    assert lib.gpl_batch_initial_place(None, 0, None, None, C.byref(launches)) == _abi.GPL_ERR_INVALID_ARG
+    assert launches.value == 0
+    assert b"no jobs" in lib.gpl_last_error()
+    null_jobs = (C.c_void_p * 2)(None, None)
+    assert lib.gpl_batch_initial_place(null_jobs, 2, None, None, None) == _abi.GPL_ERR_INVALID_ARG
+    assert b"null job" in lib.gpl_last_error()
+    assert lib.gpl_batch_nesterov_run(None, 0, 0, None, None, None) == _abi.GPL_ERR_INVALID_ARG
+    assert lib.gpl_batch_nesterov_run(null_jobs, 2, 0, None, None, None) == _abi.GPL_ERR_INVALID_ARG
